@@ -1,0 +1,236 @@
+/*
+ * pfgpu.h -- C ABI of the GB300-native coupled platelet / fibrin / lattice-
+ * Boltzmann step (libpfgpu.so).
+ *
+ * Two layers are exported:
+ *
+ *  1. Drop-in names with the reference's signatures (semLB.cu / GPUDefines.h):
+ *     fluid_*GPUKernel, sem_*GPUKernel, fiber_*GPUKernel.  They take the same
+ *     host array layouts as the reference driver (gpuSEM_LB.c) and return
+ *     nothing, like the reference; a failure is recorded and can be read with
+ *     pfgpu_last_error().  The gsl_rng* arguments of the reference are
+ *     replaced by an opaque uniform source (pfgpu_uniform_source, may be NULL).
+ *
+ *  2. pfgpu_* functions that return a status code: the scene-based job API
+ *     used by tests, the benchmark and the batch/serving layer.
+ *
+ * All pointers are host pointers unless a name says otherwise; every call is
+ * synchronous with respect to the host buffers it reads or writes.
+ */
+#ifndef PFGPU_H
+#define PFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status */
+typedef enum pfgpu_status {
+  PFGPU_OK = 0,
+  PFGPU_ERR_INVALID = 1,      /* bad argument / inconsistent sizes */
+  PFGPU_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  PFGPU_ERR_NOMEM = 3,        /* device allocation failed or budget exceeded */
+  PFGPU_ERR_UNSUPPORTED = 4,  /* valid input the GPU path does not implement */
+  PFGPU_ERR_DEVICE = 5,       /* a kernel reported an error status */
+  PFGPU_DONE = 6              /* the platelet detached (reference semLB.cu:451-455) */
+} pfgpu_status;
+
+/* ------------------------------------------------------------ scene */
+enum { PF_BC_PERIODIC = 0, PF_BC_BOUNCEBACK = 1, PF_BC_ZOUHE_SHEAR = 2 };
+enum { PF_PREC_FP64 = 0, PF_PREC_FP32 = 1, PF_PREC_FP16 = 2 };
+enum { PF_BOND_BELL = 0, PF_BOND_CONSTANT = 1 };
+enum { PF_FIB_HOOKE = 0, PF_FIB_WLC = 1 };
+enum { PF_MEM_SPRING = 1, PF_MEM_WALL = 2, PF_MEM_AREAVOL = 4, PF_MEM_BEND = 8, PF_MEM_ALL = 15 };
+
+/* Indices into pf_scene.params: the reference's model parameter table
+ * (sem_kernel.cu:58-76, filled at gpuSEM_LB.c:1206-1233). */
+enum {
+  PF_P_NUMRECEPTORS = 0, PF_P_SEED = 1, PF_P_KSPRING = 2, PF_P_KF0 = 3, PF_P_KR0 = 4,
+  PF_P_SHEAR = 5, PF_P_RHO0 = 6, PF_P_L0 = 7, PF_P_T0 = 8, PF_P_M0 = 9, PF_P_F0 = 10,
+  PF_P_UMAX = 11, PF_P_NU = 12, PF_P_TAU = 13, PF_P_P0 = 14, PF_P_CL = 15,
+  PF_P_UNIT = 16, PF_P_KS = 17, PF_P_KV = 18, PF_P_KBEND = 19
+};
+
+/* Everything one coupled simulation needs.  Array layouts: lattice arrays are
+ * [..][nz][ny][nx] (x fastest, the reference's dense host layout); platelet
+ * arrays are platelet-major [n_platelets][...].  The triangulated membrane
+ * topology is one template shared by all platelets: elements
+ * 0..n_membrane-1 of each platelet are the mesh vertices, the rest are
+ * cytoplasm elements. */
+typedef struct pf_scene {
+  /* lattice */
+  int nx, ny, nz;
+  float dx, dt;                 /* micron, second (float like the reference) */
+  float params[100];            /* reference parameter table, PF_P_* */
+  int bc[3];                    /* per axis: PF_BC_* (ZOUHE_SHEAR only on z) */
+  int ibm_wrap[3];              /* per axis: 1 = IBM stencils and positions periodic */
+  double body_force[3];         /* force added at every lattice node, reference force units */
+  const double *f_init;         /* [19][nz][ny][nx] or NULL: equilibrium of rho=1, u_init */
+  const double *u_init;         /* [3][nz][ny][nx] (units of UMAX) or NULL: reference shear profile
+                                   gpuSEM_LB.c:1234-1243 when bc[2]==ZOUHE_SHEAR, else rest */
+  const double *F_init;         /* [3][nz][ny][nx] lattice force of the step before the first, or NULL */
+  const double *rho_init;       /* [nz][ny][nx] density the first collision uses (with u_init), or NULL.
+                                   The reference's first collision reads the host rho/u arrays
+                                   (fluid_initGPUKernel, semLB.cu:154-233), not moments of fIN. */
+
+  /* platelets (SEM elements) */
+  int n_platelets, n_elem, n_membrane, n_tri, n_node;
+  const int *tri;               /* [n_tri][6]: 3 vertices, 3 edge-midpoint nodes (gpuSEM_LB.c:846-880) */
+  const int *node_ntri;         /* [n_node] triangles sharing each node (node_nbrElemNum) */
+  const int *ring;              /* [n_membrane][10] ring-ordered neighbour vertices (node_nbr_nodes) */
+  const int *spring_ptr;        /* [n_elem+1] CSR of membrane springs (dense bondLengths > 1e-6) */
+  const int *spring_nbr;        /* [spring_ptr[n_elem]] neighbour element, ascending per row */
+  const double *spring_L0;      /* [spring_ptr[n_elem]] rest length */
+  const double *S0;             /* [n_platelets][n_tri] rest triangle areas */
+  const double *S0_all;         /* [n_platelets] rest membrane area */
+  const double *V0;             /* [n_platelets] rest volume */
+  const double *X, *Y, *RY, *Z; /* [n_platelets][n_elem] initial positions (Y wrapped, RY unwrapped) */
+  int membrane_forces;          /* PF_MEM_* bitmask */
+
+  /* receptors (GPIb-alpha) and vWF wall sites */
+  int n_rec;                    /* receptors per platelet */
+  const int *rec_tri;           /* [n_platelets][n_rec] triangle of each receptor */
+  const float *rec_r1, *rec_r2; /* [n_platelets][n_rec] barycentric parameters */
+  const int *rec_state;         /* [n_platelets][n_rec][3] (site i, site j, bonds) or NULL = unbound */
+  const int *vwf;               /* [4][ny][nx] slot owners (-1 free) or NULL = all free */
+  int bond_model;               /* PF_BOND_* */
+  double p_on, p_off;           /* per-draw probabilities for PF_BOND_CONSTANT */
+
+  /* Morse pair forces between elements (within and between platelets) */
+  int morse;                    /* 0 = off */
+  double morse_intra[4];        /* U0, rho, r_eq, cutoff (same platelet) */
+  double morse_inter[4];        /* U0, rho, r_eq, cutoff (different platelets) */
+
+  /* fibrin network */
+  int n_fib;
+  const double *fib_X, *fib_Y, *fib_Z; /* [n_fib] */
+  const int *fib_fixed;         /* [n_fib] 1 = node does not move (fiber.cpp:380-384) */
+  const int *fib_ptr;           /* [n_fib+1] CSR of links at each node (Link_at_Node) */
+  const int *fib_nbr;           /* other end node of each link slot */
+  const double *fib_L0;         /* rest length of each link slot */
+  int fib_law;                  /* PF_FIB_* */
+  double fib_k;                 /* Hookean stiffness (nN/um) or WLC modulus */
+  double fib_mass;              /* WLC mass divisor (fiber.cpp:730) */
+
+  /* injected uniform stream and detachment */
+  uint64_t seed;                /* Philox-4x32-10 key of the receptor/detach uniforms */
+  double detach_rate;           /* gama of semLB.cu:451 (0 = never detach) */
+} pf_scene;
+
+/* ------------------------------------------------------------ job API */
+typedef struct pfgpu_job pfgpu_job;
+
+/* Creates a device-resident simulation on the current CUDA device.
+ * precision: PF_PREC_*; fp16_scale: population scale for PF_PREC_FP16
+ * (ignored otherwise). */
+int pfgpu_job_create(const pf_scene *scene, int precision, double fp16_scale, pfgpu_job **out);
+/* Runs nsteps coupled steps (SEM+Morse+fibrin forces, bonds, IBM spreading,
+ * fused collide-stream, moments, IBM interpolation, position update).
+ * Returns PFGPU_DONE if the platelet detached. */
+int pfgpu_job_step(pfgpu_job *job, int nsteps);
+/* Same, captured once in a CUDA graph and replayed (no host work per step). */
+int pfgpu_job_step_graph(pfgpu_job *job, int nsteps);
+int pfgpu_job_sync(pfgpu_job *job);
+/* Copies state back in scene layouts; any pointer may be NULL. */
+int pfgpu_job_get_lattice(pfgpu_job *job, double *fIN, double *fOUT, double *rho, double *u /*[3][N]*/,
+                          double *F /*[3][N]*/);
+int pfgpu_job_get_elements(pfgpu_job *job, double *X, double *Y, double *RY, double *Z,
+                           double *V /*[3][P*E]*/, double *F /*[3][P*E]*/);
+int pfgpu_job_get_bonds(pfgpu_job *job, int *rec_state /*[P][n_rec][3]*/, int *vwf /*[4][ny][nx]*/,
+                        int *total_bond);
+int pfgpu_job_get_fibrin(pfgpu_job *job, double *X, double *Y, double *Z, double *V /*[3][M]*/,
+                         double *F /*[3][M]*/);
+/* Per-platelet FP64 reductions of the last force pass: [P][2] (S_all, V) and
+ * the membrane vertex mean curvature km [P][n_membrane]. */
+int pfgpu_job_get_membrane(pfgpu_job *job, double *S_V, double *km);
+/* FP64 conservation sums over the lattice: mass and x/y/z momentum. */
+int pfgpu_job_conservation(pfgpu_job *job, double out[4]);
+int64_t pfgpu_job_step_count(const pfgpu_job *job);
+size_t pfgpu_job_device_bytes(const pfgpu_job *job);
+/* Kernel launches one coupled step issues (graph nodes). */
+int pfgpu_job_launches_per_step(const pfgpu_job *job);
+void pfgpu_job_destroy(pfgpu_job *job);
+
+/* Device bytes a job with this scene and precision would allocate. */
+size_t pfgpu_scene_device_bytes(const pf_scene *scene, int precision);
+
+/* ------------------------------------------------------------ batch API */
+/* Many independent jobs advanced together by one persistent kernel per phase
+ * over an offset table (continuous batching).  Jobs may join and leave
+ * between steps. */
+typedef struct pfgpu_batch pfgpu_batch;
+int pfgpu_batch_create(size_t hbm_budget_bytes, pfgpu_batch **out);
+/* Admits a job if it fits the budget; returns PFGPU_ERR_NOMEM otherwise.
+ * *slot receives the job's id within the batch. */
+int pfgpu_batch_admit(pfgpu_batch *b, const pf_scene *scene, int precision, double fp16_scale, int *slot);
+int pfgpu_batch_step(pfgpu_batch *b, int nsteps);
+int pfgpu_batch_retire(pfgpu_batch *b, int slot);
+pfgpu_job *pfgpu_batch_job(pfgpu_batch *b, int slot);
+size_t pfgpu_batch_bytes_in_use(const pfgpu_batch *b);
+int pfgpu_batch_num_jobs(const pfgpu_batch *b);
+void pfgpu_batch_destroy(pfgpu_batch *b);
+
+/* ------------------------------------------------------------ misc */
+const char *pfgpu_last_error(void);
+int pfgpu_version(void);
+/* Philox-4x32-10 uniforms of the receptor stream (step, receptor) -> (u1, u2),
+ * the same values the device draws; for tests and drivers. */
+void pfgpu_receptor_uniforms(uint64_t seed, int64_t step, int64_t receptor, double out[2]);
+double pfgpu_detach_uniform(uint64_t seed, int64_t step);
+
+/* Opaque replacement for the reference's gsl_rng* arguments. */
+typedef struct pfgpu_uniform_source {
+  uint64_t seed;
+} pfgpu_uniform_source;
+
+/* ------------------------------------------------------------ drop-in names
+ * Signatures of semLB.cu:111, :154, :303, :534, :562, :597, :667, :705, :749,
+ * :865, :441, :979, :1005 (host array layouts of gpuSEM_LB.c). */
+void *fluid_allocGPUKernel(void *model, float dt, float dx, int width, int height, int depth);
+void fluid_initGPUKernel(void *model, void *g, int aFlag, float *hostParameters, void **fIN, void **fOUT,
+                         void *ux, void *uy, void *uz, void *rho, void *obstacle, void *Fx, void *Fy,
+                         void *Fz, void *vWFbond);
+void fluid_invokeGPUKernel(void *model, void *g, void *g_SEM, double *randNum, void *r, int timeSteps);
+void fluid_releaseGPUKernel(void *model, void *g);
+
+void *sem_allocGPUKernel(void *model, int maxCells, int maxElements, int SurfElem, int newnode,
+                         int numReceptorsPerElem, float dt, double S0_all, float *hostSEMparameters);
+void sem_initGPUKernel(void *model, void *g, int numOfCells, int *numOfElements, int SurfElem,
+                       int numReceptorsPerElem, void *hostX_Ref, void *hostY_Ref, void *hostZ_Ref,
+                       void *hostX, void *hostY, void *hostRY, void *hostZ, void *hostVX, void *hostVY,
+                       void *hostVZ, void *hostFX, void *hostFY, void *hostFZ, void *hostType,
+                       void *hostBonds, void *triElem, void *receptor_r1, void *receptor_r2,
+                       void *node_share_Elem, void *N, void *node_nbrElemNum, void *node_nbr_nodes,
+                       void *S0, double V0, void *receptBond, void *randNum);
+void sem_invokeGPUKernel_Force(void *model, void *g, int timeSteps, int *done, int *totalT, void *r,
+                               double gama);
+void sem_copyGPUKernel(void *model, void *g, void *hostX, void *hostY, void *hostRY, void *hostZ,
+                       void *hostVX, void *hostVY, void *hostVZ, void *hostFX, void *hostFY,
+                       void *hostFZ, int timeSteps);
+void sem_releaseGPUKernel(void *model, void *g);
+
+void *fiber_allocGPUKernel(void *model, int maxNodes, int maxLinks, int max_N_conn_at_Node, double dt,
+                           double *hostParameters);
+void fiber_init_GPUKernel(void *model, void *fg, void *NodeType, void *N_Conn_at_Node, void *Link_at_Node,
+                          void *lAdjVer, void *linkLengths, void *linkLengths0, void *linkThick, void *X,
+                          void *V_X, void *X0, void *F_X, void *Y, void *Y0, void *V_Y, void *F_Y, void *Z,
+                          void *Z0, void *V_Z, void *F_Z);
+void fiber_copy_GPUKernel(void *model, void *fg, void *X, void *V_X, void *X0, void *F_X, void *Y, void *Y0,
+                          void *V_Y, void *F_Y, void *Z, void *Z0, void *V_Z, void *F_Z);
+void fiber_release_GPUKernel(void *model, void *fg);
+
+/* Additions to the drop-in layer (no reference counterpart): couple a fibrin
+ * handle to a fluid handle so fluid_invokeGPUKernel spreads its spring forces
+ * and advects its nodes; select the fibrin force law. */
+int pfgpu_fluid_attach_fiber(void *g, void *fg, int law, double k, double mass);
+/* Precision of fluid handles created by later fluid_allocGPUKernel calls
+ * (default PF_PREC_FP64, the reference's arithmetic). */
+int pfgpu_set_default_precision(int precision, double fp16_scale);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

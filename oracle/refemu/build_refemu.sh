@@ -1,0 +1,19 @@
+#!/bin/sh
+# Builds oracle/_ref/librefemu.so: the reference's own kernel sources
+# (LB_kernel.cu, which includes sem_kernel.cu) compiled with g++ through the
+# serial CUDA emulation header, plus the step-loop harness refemu.cpp.
+# Oracle test infrastructure: it reads the reference tree, so it only builds
+# where that tree is present (REF_DIR, default /root/reference).
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF_DIR=${REF_DIR:-/root/reference}
+OUT="$HERE/../_ref"
+if [ ! -f "$REF_DIR/LB_kernel.cu" ]; then
+  echo "reference tree not found at $REF_DIR; skipping refemu build" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+g++ -O2 -std=c++17 -fPIC -shared -w -fno-fast-math -ffp-contract=off \
+    -x c++ -I"$HERE/stub" -I"$HERE" -I"$REF_DIR" \
+    "$HERE/refemu.cpp" -o "$OUT/librefemu.so"
+echo "built $OUT/librefemu.so"

@@ -1,0 +1,273 @@
+"""Seeded synthetic workloads.
+
+* `reference_case`   -- the reference's own setting at test size: one
+  triangulated platelet, Bell-model receptor bonds, Zou/He shear walls on z,
+  periodic x/y lattice, IBM periodic in y only (LB_kernel.cu:1483-1518).
+* `plain_small`      -- 64x32x32 body-force Poiseuille channel with half-way
+  bounce-back walls on y and z, one platelet of 400 membrane + 200 cytoplasm
+  elements, Morse pairs, a 200-node / 400-link Hookean fibrin mesh.
+* `single_large`     -- 256x128x128 shear channel (1000 1/s through the
+  reference's unit chain), 50 platelets x 600 elements placed by seeded
+  dart-throwing Poisson-disk sampling, a 20k-node / 40k-link fibrin mesh on
+  the bottom wall, 200 receptors per platelet with constant per-step bond
+  probabilities 1e-2 / 1e-3.
+* `mixed_small`      -- a scaled-down single_large for GPU parity tests.
+
+Lengths are in microns with the reference's lattice spacing dx = 0.2 um
+(Input/parameter.dat DELTA_X); the platelet ellipsoid has semi-axes
+1.0 x 1.0 x 0.5 um.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import mesh as M
+from .scene import (BC_BOUNCEBACK, BC_PERIODIC, BC_ZOUHE_SHEAR, BOND_BELL, BOND_CONSTANT, FIB_HOOKE,
+                    MEM_ALL, P_KF0, P_KR0, P_NUMRECEPTORS, Scene, force_to_lattice, reference_params)
+
+REF_DX = 0.2
+REF_DT = 1e-8
+
+
+class PlateletTemplate:
+    """One platelet in local coordinates: mesh vertices first, cytoplasm after."""
+
+    def __init__(self, verts, tris, n_cyto: int, seed: int, axes):
+        self.verts = np.asarray(verts, dtype=np.float64)
+        self.tris = np.asarray(tris, dtype=np.int32)
+        self.n_membrane = len(self.verts)
+        rng = np.random.default_rng(seed)
+        pts = []
+        a = np.asarray(axes, dtype=np.float64) * 0.85
+        while len(pts) < n_cyto:
+            q = rng.uniform(-1, 1, size=3)
+            if q @ q <= 1.0:
+                pts.append(q * a)
+        self.cyto = np.array(pts, dtype=np.float64).reshape(-1, 3)
+        self.n_elem = self.n_membrane + len(self.cyto)
+        self.local = np.vstack([self.verts, self.cyto]) if len(self.cyto) else self.verts.copy()
+        self.sp_ptr, self.sp_nbr, self.sp_L0 = M.edge_rest_lengths(self.verts, self.tris, self.n_elem)
+        self.mean_bond = M.mean_bond_length(self.sp_L0, self.sp_ptr, self.sp_nbr)
+
+
+def _place(scene: Scene, tpl: PlateletTemplate, centers: np.ndarray, ly_um: float):
+    P = len(centers)
+    E = tpl.n_elem
+    X = np.zeros((P, E))
+    Y = np.zeros((P, E))
+    Z = np.zeros((P, E))
+    for p, c in enumerate(centers):
+        X[p] = tpl.local[:, 0] + c[0]
+        Y[p] = tpl.local[:, 1] + c[1]
+        Z[p] = tpl.local[:, 2] + c[2]
+    RY = Y.copy()
+    if scene.ibm_wrap[1]:
+        Y = np.where(Y > ly_um, Y - ly_um, Y)
+        Y = np.where(Y < 0, Y + ly_um, Y)
+    topo = M.build_topology(tpl.tris, tpl.n_membrane, np.stack([X[0], RY[0], Z[0]], 1))
+    S0 = np.zeros((P, len(tpl.tris)))
+    S0_all = np.zeros(P)
+    V0 = np.zeros(P)
+    for p in range(P):
+        S0[p], S0_all[p], V0[p] = M.rest_area_volume(tpl.tris, np.stack([X[p], RY[p], Z[p]], 1))
+    scene.n_platelets, scene.n_elem, scene.n_membrane = P, E, tpl.n_membrane
+    scene.tri, scene.node_ntri, scene.ring = topo.tri6, topo.node_ntri, topo.ring
+    scene.spring_ptr, scene.spring_nbr, scene.spring_L0 = tpl.sp_ptr, tpl.sp_nbr, tpl.sp_L0
+    scene.S0, scene.S0_all, scene.V0 = S0, S0_all, V0
+    scene.X, scene.Y, scene.RY, scene.Z = X, Y, RY, Z
+    scene.meta["topology"] = topo
+    return topo
+
+
+def _receptors_per_triangle(scene: Scene, R: int, rng):
+    """R receptors on every triangle, tri-major (the reference's
+    [SurfElem][numReceptorsPerElem] layout, gpuSEM_LB.c:732-747)."""
+    T = scene.n_tri
+    P = scene.n_platelets
+    scene.n_rec = T * R
+    scene.rec_tri = np.tile(np.repeat(np.arange(T, dtype=np.int32), R), (P, 1))
+    scene.rec_r1 = rng.uniform(size=(P, T * R)).astype(np.float32)
+    scene.rec_r2 = rng.uniform(size=(P, T * R)).astype(np.float32)
+
+
+def _receptors_random(scene: Scene, n_rec: int, rng):
+    P, T = scene.n_platelets, scene.n_tri
+    scene.n_rec = n_rec
+    tri = rng.integers(0, T, size=(P, n_rec)).astype(np.int32)
+    scene.rec_tri = np.sort(tri, axis=1)
+    scene.rec_r1 = rng.uniform(size=(P, n_rec)).astype(np.float32)
+    scene.rec_r2 = rng.uniform(size=(P, n_rec)).astype(np.float32)
+
+
+def _fibrin(scene: Scene, n_nodes: int, n_links: int, slab: float, rng, k: float):
+    """Nodes uniform in the wall slab z in [0, slab); links by nearest-neighbour
+    pairing (the n_links shortest distinct pairs among each node's 6 nearest
+    neighbours); rest length = initial length; nodes within one dx of the
+    wall are fixed (the rule of fiber.cpp:380-384 on the wall-normal axis)."""
+    from scipy.spatial import cKDTree
+
+    if n_nodes == 0:
+        scene.n_fib = 0
+        return
+    Lx, Ly = scene.nx * scene.dx, scene.ny * scene.dx
+    pts = np.stack([rng.uniform(0, Lx, n_nodes), rng.uniform(0, Ly, n_nodes),
+                    rng.uniform(0, slab, n_nodes)], 1)
+    tree = cKDTree(pts)
+    kk = min(7, n_nodes)
+    d, idx = tree.query(pts, k=kk)
+    pairs = {}
+    for i in range(n_nodes):
+        for q in range(1, kk):
+            j = int(idx[i, q])
+            key = (min(i, j), max(i, j))
+            if key not in pairs:
+                pairs[key] = float(d[i, q])
+    items = sorted(pairs.items(), key=lambda t: (t[1], t[0]))[:n_links]
+    links = np.array([p for p, _ in items], dtype=np.int32).reshape(-1, 2)
+    nbr = [[] for _ in range(n_nodes)]
+    for a, b in links:
+        nbr[a].append(int(b))
+        nbr[b].append(int(a))
+    ptr = np.zeros(n_nodes + 1, dtype=np.int32)
+    cols, L0 = [], []
+    for i in range(n_nodes):
+        ptr[i + 1] = ptr[i] + len(nbr[i])
+        for j in nbr[i]:
+            cols.append(j)
+            dd = pts[i] - pts[j]
+            L0.append(float(np.sqrt(dd @ dd)))
+    scene.n_fib = n_nodes
+    scene.fib_X, scene.fib_Y, scene.fib_Z = pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy()
+    scene.fib_fixed = (pts[:, 2] < scene.dx).astype(np.int32)
+    scene.fib_ptr = ptr
+    scene.fib_nbr = np.array(cols, dtype=np.int32)
+    scene.fib_L0 = np.array(L0, dtype=np.float64)
+    scene.fib_law = FIB_HOOKE
+    scene.fib_k = k
+    scene.meta["fib_links"] = links
+
+
+def poisson_disk(n: int, lo, hi, rmin: float, rng, fixed_z=None, n_fixed=0, max_tries=200000):
+    """Dart-throwing Poisson-disk sampling of `n` centres in the box [lo, hi)
+    with pairwise distance >= rmin; the first `n_fixed` darts have z=fixed_z."""
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    pts = []
+    tries = 0
+    while len(pts) < n:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("poisson_disk: domain too small for the requested count")
+        c = rng.uniform(lo, hi)
+        if len(pts) < n_fixed:
+            c[2] = fixed_z
+        if all(np.linalg.norm(c - q) >= rmin for q in pts):
+            pts.append(c)
+    return np.array(pts)
+
+
+# ---------------------------------------------------------------- workloads
+def reference_case(seed: int = 7, nx=16, ny=20, nz=10, level=1, R=2, center=None,
+                   kf0=3.0e4, kr0=1.5e4) -> Scene:
+    """The reference's own path at test size (bond rates stressed so that
+    binding happens within tens of steps)."""
+    rng = np.random.default_rng(seed)
+    v, t = M.ellipsoid_icosphere(level, axes=(0.6, 0.6, 0.3))
+    tpl = PlateletTemplate(v, t, 0, seed, (0.6, 0.6, 0.3))
+    T = len(t)
+    params = reference_params(dx=REF_DX, dt=REF_DT, nz=nz, shear=300.0, receptors=2 * R * T,
+                              mean_bond=tpl.mean_bond, kf0=kf0, kr0=kr0)
+    sc = Scene(nx=nx, ny=ny, nz=nz, dx=REF_DX, dt=REF_DT, params=params,
+               bc=(BC_PERIODIC, BC_PERIODIC, BC_ZOUHE_SHEAR), ibm_wrap=(0, 1, 0))
+    if center is None:
+        center = (nx * REF_DX / 2, ny * REF_DX / 2, 0.3 + 0.05)
+    _place(sc, tpl, np.array([center]), ny * REF_DX)
+    _receptors_per_triangle(sc, R, rng)
+    sc.bond_model = BOND_BELL
+    sc.membrane_forces = MEM_ALL
+    sc.seed = seed
+    sc.meta["R"] = R
+    return sc
+
+
+def plain_small(seed: int = 1, n_membrane=400, n_cyto=200, n_fib=200, n_links=400,
+                nx=64, ny=32, nz=32, g_lattice=2e-5) -> Scene:
+    rng = np.random.default_rng(seed)
+    axes = (1.0, 1.0, 0.5)
+    v, t = M.ellipsoid_fibonacci(n_membrane, axes, seed)
+    tpl = PlateletTemplate(v, t, n_cyto, seed, axes)
+    tau = 0.8
+    nu = 1.2e6 / 1.0239
+    dt = float(np.float32((tau - 0.5) * REF_DX * REF_DX / (3 * nu)))
+    umax = float(np.float32(REF_DX) / np.float32(dt))
+    params = reference_params(dx=REF_DX, dt=dt, nz=nz, shear=0.0, mean_bond=tpl.mean_bond, umax=umax,
+                              tau=tau, receptors=0.0)
+    sc = Scene(nx=nx, ny=ny, nz=nz, dx=REF_DX, dt=dt, params=params,
+               bc=(BC_PERIODIC, BC_BOUNCEBACK, BC_BOUNCEBACK), ibm_wrap=(1, 0, 0))
+    fx = g_lattice / force_to_lattice(params, REF_DX, dt)
+    sc.body_force = (fx, 0.0, 0.0)
+    _place(sc, tpl, np.array([(nx * REF_DX / 2, ny * REF_DX / 2, nz * REF_DX / 2)]), ny * REF_DX)
+    sc.morse = 1
+    sc.n_rec = 0
+    _fibrin(sc, n_fib, n_links, 3 * REF_DX, rng, 0.5)
+    sc.seed = seed
+    sc.meta.update(workload="plain_small", tau=tau, g_lattice=g_lattice)
+    return sc
+
+
+def single_large(seed: int = 2, nx=256, ny=128, nz=128, n_platelets=50, n_membrane=400, n_cyto=200,
+                 n_fib=20000, n_links=40000, n_rec=200, shear=1000.0, n_wall=10) -> Scene:
+    rng = np.random.default_rng(seed)
+    axes = (1.0, 1.0, 0.5)
+    v, t = M.ellipsoid_fibonacci(n_membrane, axes, seed)
+    tpl = PlateletTemplate(v, t, n_cyto, seed, axes)
+    params = reference_params(dx=REF_DX, dt=REF_DT, nz=nz, shear=shear, mean_bond=tpl.mean_bond)
+    sc = Scene(nx=nx, ny=ny, nz=nz, dx=REF_DX, dt=REF_DT, params=params,
+               bc=(BC_PERIODIC, BC_PERIODIC, BC_ZOUHE_SHEAR), ibm_wrap=(1, 1, 0))
+    L = np.array([nx, ny, nz]) * REF_DX
+    rmin = 2 * axes[0] + 2 * REF_DX
+    centers = poisson_disk(n_platelets, (axes[0], axes[1], axes[2] + 0.05),
+                           (L[0] - axes[0], L[1] - axes[1], L[2] - axes[2] - 0.6), rmin, rng,
+                           fixed_z=axes[2] + 0.05, n_fixed=min(n_wall, n_platelets))
+    _place(sc, tpl, centers, L[1])
+    _receptors_random(sc, n_rec, rng)
+    sc.params[P_NUMRECEPTORS] = n_rec * n_platelets
+    sc.bond_model = BOND_CONSTANT
+    sc.p_on, sc.p_off = 1e-2, 1e-3
+    sc.morse = 1
+    _fibrin(sc, n_fib, n_links, 3 * REF_DX, rng, 0.5)
+    sc.seed = seed
+    sc.meta.update(workload="single_large", shear=shear)
+    return sc
+
+
+def mixed_small(seed: int = 3, nx=40, ny=32, nz=20, n_platelets=3, level=1, n_cyto=12, n_fib=300,
+                n_links=600, n_rec=40, bell=False) -> Scene:
+    """Every feature of single_large on a lattice the oracle steps in seconds."""
+    rng = np.random.default_rng(seed)
+    axes = (0.6, 0.6, 0.3)
+    v, t = M.ellipsoid_icosphere(level, axes)
+    tpl = PlateletTemplate(v, t, n_cyto, seed, axes)
+    params = reference_params(dx=REF_DX, dt=REF_DT, nz=nz, shear=1000.0, mean_bond=tpl.mean_bond,
+                              kf0=3.0e4 if bell else None, kr0=1.5e4 if bell else 3.21,
+                              receptors=float(n_rec * n_platelets))
+    sc = Scene(nx=nx, ny=ny, nz=nz, dx=REF_DX, dt=REF_DT, params=params,
+               bc=(BC_PERIODIC, BC_PERIODIC, BC_ZOUHE_SHEAR), ibm_wrap=(1, 1, 0))
+    L = np.array([nx, ny, nz]) * REF_DX
+    centers = poisson_disk(n_platelets, (axes[0], axes[1], axes[2] + 0.05),
+                           (L[0] - axes[0], L[1] - axes[1], L[2] - axes[2] - 0.3), 2 * axes[0] + 2 * REF_DX,
+                           rng, fixed_z=axes[2] + 0.05, n_fixed=min(2, n_platelets))
+    _place(sc, tpl, centers, L[1])
+    _receptors_random(sc, n_rec, rng)
+    if bell:
+        sc.bond_model = BOND_BELL
+    else:
+        sc.bond_model = BOND_CONSTANT
+        sc.p_on, sc.p_off = 0.2, 0.05
+    sc.morse = 1
+    sc.morse_intra = (1.0, 2.0, 0.3, 0.6)
+    sc.morse_inter = (1.0, 2.0, 0.3, 0.6)
+    _fibrin(sc, n_fib, n_links, 3 * REF_DX, rng, 0.5)
+    sc.seed = seed
+    sc.meta.update(workload="mixed_small")
+    return sc
