@@ -1,0 +1,122 @@
+// pf_common.cuh -- shared device definitions of the coupled step.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pfgpu.h"
+
+namespace pf {
+
+// D3Q19 in the reference's ordering (LB_kernel.cu:40-47): the ordering is
+// the fIN[19] layout at the boundary.
+constexpr int Q = 19;
+__host__ __device__ constexpr int cx(int d) {
+  constexpr int v[Q] = {0, 1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0};
+  return v[d];
+}
+__host__ __device__ constexpr int cy(int d) {
+  constexpr int v[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1};
+  return v[d];
+}
+__host__ __device__ constexpr int cz(int d) {
+  constexpr int v[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1};
+  return v[d];
+}
+__host__ __device__ constexpr double wgt(int d) {
+  return d == 0 ? 1.0 / 3.0 : (d < 7 ? 1.0 / 18.0 : 1.0 / 36.0);
+}
+__host__ __device__ constexpr int opp(int d) {
+  constexpr int v[Q] = {0, 2, 1, 4, 3, 6, 5, 12, 11, 14, 13, 8, 7, 10, 9, 18, 17, 16, 15};
+  return v[d];
+}
+
+constexpr double kPi = 3.141592653589793;  // GPUDefines.h:36
+constexpr int kBrickX = 128;               // lattice brick = one CTA of the LBM kernel
+constexpr int kBinCap = 1024;              // Morse cell-bin capacity
+constexpr double kFixScale = 1099511627776.0;  // 2^40: fixed-point force accumulation
+
+// Device error bits (set instead of trapping; the host reads them after a step)
+enum : uint32_t {
+  ERR_BIN_OVERFLOW = 1u,
+  ERR_BOND_OVERFLOW = 2u,
+  ERR_NONFINITE = 4u,
+  ERR_MEMBRANE_SIZE = 8u,
+};
+
+// Per-job device-resident control block: written by kernels, read by the host
+// between steps.  Graph replays read the step counter from here.
+struct Control {
+  long long step;         // coupled steps completed
+  int done;               // platelet detached (semLB.cu:451-455)
+  int first;              // next LBM step is the first after an upload
+  int total_bond;         // sum of bond counts of the last bond pass
+  unsigned int err;       // ERR_* bits
+  int active_count[2];    // active-brick list lengths per force buffer
+  int nops;               // bond slot operations emitted this step
+  int pad;
+  double sv[2];           // unused spare
+};
+
+// ------------------------------------------------------------- Philox
+// Philox-4x32-10 (Salmon et al., SC'11): published multipliers and Weyl
+// constants, ten rounds.
+__host__ __device__ inline void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+    uint32_t n1 = (uint32_t)p1;
+    uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    uint32_t n3 = (uint32_t)p0;
+    c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+__host__ __device__ inline double u53(uint32_t a, uint32_t b) {
+  return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+// Two uniforms of receptor `rid` at coupled step `step`.
+__host__ __device__ inline void receptor_uniforms(uint64_t seed, long long step, long long rid, double& u1,
+                                                  double& u2) {
+  uint32_t c[4] = {(uint32_t)step, (uint32_t)((uint64_t)step >> 32), (uint32_t)rid,
+                   (uint32_t)((uint64_t)rid >> 32) ^ 0x52454350u};
+  philox4x32(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  u1 = u53(c[0], c[1]);
+  u2 = u53(c[2], c[3]);
+}
+__host__ __device__ inline double detach_uniform(uint64_t seed, long long step) {
+  uint32_t c[4] = {(uint32_t)step, (uint32_t)((uint64_t)step >> 32), 0xFFFFFFFFu, 0x44455443u};
+  philox4x32(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  return u53(c[0], c[1]);
+}
+
+// ------------------------------------------------------------- storage
+// Populations are stored shifted, g = f - w (FP16: q = g / (w * scale)).
+template <class S>
+struct StoreTraits;
+template <>
+struct StoreTraits<double> {
+  __device__ static double load(const double* p, int, double) { return __ldg(p); }
+  __device__ static void store(double* p, double v, int, double) { *p = v; }
+};
+template <>
+struct StoreTraits<float> {
+  __device__ static float load(const float* p, int, float) { return __ldg(p); }
+  __device__ static void store(float* p, float v, int, float) { *p = v; }
+};
+template <>
+struct StoreTraits<__half> {
+  __device__ static float load(const __half* p, int, float s) { return __half2float(__ldg(p)) * s; }
+  __device__ static void store(__half* p, float v, int, float inv_s) { *p = __float2half_rn(v * inv_s); }
+};
+
+__device__ inline int wrapi(int a, int n) {
+  int r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+}  // namespace pf

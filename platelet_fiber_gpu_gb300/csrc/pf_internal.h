@@ -1,0 +1,149 @@
+// pf_internal.h -- device-resident state of one coupled simulation and the
+// launchers of its kernels.
+//
+// Layout in HBM (one job):
+//   populations   2 x Store[19][N]      ping-pong, shifted g = f - w, SoA
+//   lattice force 2 x Real4[N]          reference force units, only bricks
+//                                       flagged active are read or non-zero
+//   brick flags   2 x uint32[nbricks]   + active-brick lists (one brick =
+//                                       128 x-nodes of one (y,z) row)
+//   u buffer      Real4[N]              (rho, u/C) at active bricks; before
+//                                       the first step: the initial rho, u
+//   elements      double X,Y,RY,Z,V,F   positions stay FP64
+//   membrane/Morse/bond/fibrin forces   one buffer each (concurrent kernels)
+//   Morse cell bins int[ncells][1024]
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "pf_common.cuh"
+
+namespace pf {
+
+struct alignas(32) D4 {
+  double x, y, z, w;
+};
+template <class R>
+struct R4T;
+template <>
+struct R4T<float> {
+  using type = float4;
+};
+template <>
+struct R4T<double> {
+  using type = D4;
+};
+template <class R>
+using R4 = typename R4T<R>::type;
+
+// ------------------------------------------------------------------ lattice
+struct LatticeConst {
+  int nx, ny, nz, nbx, nbricks;
+  long long N;
+  int bc[3];
+  int ibm_wrap[3];
+  float dxf, dtf;
+  double C;           // float-rounded dx/dt/UMAX
+  double omega;       // 1/tau
+  double kcoll;       // F0/rho0/UMAX*UNIT (double chain) * dt / C
+  double kmom;        // F0/rho0/UMAX*UNIT (float chain) * dt / C
+  double body[3];     // body force, reference units
+  double uw;          // top-wall velocity / C
+  double fp16_scale;  // sigma of the FP16 store
+  float dtT;          // dt / T0 (float, sem_kernel.cu:2106): position update factor
+};
+
+struct Lattice {
+  int precision = PF_PREC_FP64;
+  LatticeConst k{};
+  void* g[2] = {nullptr, nullptr};
+  void* F[2] = {nullptr, nullptr};
+  void* ubuf = nullptr;
+  unsigned* flags[2] = {nullptr, nullptr};
+  int* list[2] = {nullptr, nullptr};
+  size_t bytes = 0;
+};
+
+// ------------------------------------------------------------------ markers
+struct PlateletConst {
+  int P, E, Em, T, NN, nrec;
+  int mask;
+  float kspring, ks, kv, kbend, f0, kf0, kr0, numrec;
+  double dxd, dtd;
+  float dxf, dtf, dtT;
+  int bond_model;
+  double p_on, p_off;
+  uint64_t seed;
+  int morse;
+  double morse_intra[4], morse_inter[4];
+  int ncell[3];
+  double cs[3];
+  double L[3];
+  int wrap[3];
+  int nx, ny, nz;
+};
+
+struct Platelets {
+  PlateletConst k{};
+  // state (FP64)
+  double *X = nullptr, *Y = nullptr, *RY = nullptr, *Z = nullptr;
+  double* V = nullptr;     // [3][PE]
+  double* Ftot = nullptr;  // [3][PE] total element force of the last step
+  void* Fmem = nullptr;    // Real[3][PE] membrane forces
+  double* Fmorse = nullptr;  // [3][PE]
+  void* Fbond = nullptr;   // Real[3][PE]
+  // topology (template)
+  int *tri = nullptr, *node_ntri = nullptr, *node_tri = nullptr, *vert_local = nullptr, *ring = nullptr;
+  int *sp_ptr = nullptr, *sp_nbr = nullptr;
+  double *sp_L0 = nullptr, *S0 = nullptr, *S0_all = nullptr, *V0 = nullptr;
+  // membrane scratch (Real)
+  void *nN = nullptr, *nelem = nullptr, *S = nullptr, *km = nullptr;
+  double* SV = nullptr;  // [P][2]
+  // receptors
+  int *rec_tri = nullptr, *rec_state = nullptr, *vwf = nullptr;
+  float *r1 = nullptr, *r2 = nullptr;
+  void* rec_tmp = nullptr;  // per-receptor scratch of the bond pass
+  // Morse bins
+  int *bin_count = nullptr, *bin = nullptr;
+  int ncells = 0;
+  size_t bytes = 0;
+};
+
+struct Fibrin {
+  int M = 0;
+  int law = PF_FIB_HOOKE;
+  double k = 0.5, mass = 1.0;
+  double *X = nullptr, *Y = nullptr, *Z = nullptr, *V = nullptr, *F = nullptr;
+  int *fixed = nullptr, *ptr = nullptr, *nbr = nullptr;
+  double* L0 = nullptr;
+  size_t bytes = 0;
+};
+
+// ------------------------------------------------------------------ launchers
+// All launchers enqueue on `st` and return the launch error.
+cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_dev, const double* ru_dev,
+                           Control* ctl, cudaStream_t st);
+cudaError_t lattice_step(Lattice& L, Control* ctl, cudaStream_t st);
+cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
+// fIN [19][N], fOUT [19][N], rho [N], u [3][N], F [3][N] (double, device)
+cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* fIN, double* fOUT, double* rho,
+                             double* u, double* F, cudaStream_t st);
+cudaError_t lattice_conservation(Lattice& L, long long step, double* out4_dev, cudaStream_t st);
+
+cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
+cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
+cudaError_t fibrin_forces(Fibrin& Fb, int precision, Control* ctl, cudaStream_t st);
+cudaError_t bond_pass(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
+cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st);
+cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, double detach_rate,
+                           uint64_t seed, unsigned* done_blocks, cudaStream_t st);
+cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st);
+cudaError_t lattice_step_binned(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st);
+size_t bond_scratch_bytes(int NR);
+
+int membrane_threads();
+
+}  // namespace pf

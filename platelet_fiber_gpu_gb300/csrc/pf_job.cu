@@ -1,0 +1,731 @@
+// pf_job.cu -- job API of pfgpu.h: device-resident simulations built from a
+// pf_scene, stepped by direct launches or by a captured CUDA graph.
+//
+// One coupled step (the reference's sem_invokeGPUKernel_Force followed by
+// fluid_invokeGPUKernel, semLB.cu:303-531) is issued as:
+//   fork  -> membrane forces | Morse forces | fibrin forces | receptor bonds
+//   join  -> IBM spreading -> fused collide-stream -> moments of the active
+//            bricks -> IBM interpolation + position update + cell binning
+// The four force kernels write separate buffers, so they run concurrently.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pf_internal.h"
+
+namespace pf {
+size_t bond_scratch_bytes(int NR);
+}
+
+using namespace pf;
+
+static thread_local std::string g_last_error;
+static std::mutex g_err_mu;
+static std::string g_last_error_global;
+
+static int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_last_error_global = msg;
+  return code;
+}
+
+#define CK(call)                                                                               \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return set_error(e_ == cudaErrorMemoryAllocation ? PFGPU_ERR_NOMEM : PFGPU_ERR_CUDA,     \
+                       std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+  } while (0)
+
+struct pfgpu_job {
+  int precision = PF_PREC_FP64;
+  Lattice L;
+  Platelets Pl;
+  Fibrin Fb;
+  bool has_pl = false, has_fb = false;
+  Control* ctl = nullptr;
+  unsigned* done_blocks = nullptr;
+  double* scratch4 = nullptr;
+  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  double detach_rate = 0;
+  uint64_t seed = 0;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+  int launches_per_step = 0;
+};
+
+template <class T>
+static cudaError_t dalloc(pfgpu_job* j, T** p, size_t count) {
+  size_t bytes = count * sizeof(T);
+  if (bytes == 0) bytes = sizeof(T);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e == cudaSuccess) {
+    j->allocs.push_back(*p);
+    j->bytes += bytes;
+    cudaMemset(*p, 0, bytes);
+  }
+  return e;
+}
+template <class T>
+static cudaError_t dupload(pfgpu_job* j, T** p, const T* src, size_t count) {
+  cudaError_t e = dalloc(j, p, count);
+  if (e == cudaSuccess && src && count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
+  return e;
+}
+
+static void destroy(pfgpu_job* j) {
+  if (!j) return;
+  if (j->graph) cudaGraphExecDestroy(j->graph);
+  for (void* p : j->allocs) cudaFree(p);
+  cudaStream_t ss[4] = {j->s0, j->s1, j->s2, j->s3};
+  for (cudaStream_t s : ss)
+    if (s) cudaStreamDestroy(s);
+  cudaEvent_t ee[4] = {j->ev_fork, j->ev1, j->ev2, j->ev3};
+  for (cudaEvent_t e : ee)
+    if (e) cudaEventDestroy(e);
+  delete j;
+}
+
+static size_t store_bytes(int precision) {
+  return precision == PF_PREC_FP64 ? 8 : (precision == PF_PREC_FP32 ? 4 : 2);
+}
+static size_t real_bytes(int precision) { return precision == PF_PREC_FP64 ? 8 : 4; }
+
+// lattice constants from the reference parameter table (float arithmetic where
+// the reference does it in float)
+static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int precision) {
+  LatticeConst k{};
+  k.nx = s->nx; k.ny = s->ny; k.nz = s->nz;
+  k.nbx = (s->nx + kBrickX - 1) / kBrickX;
+  k.nbricks = k.nbx * s->ny * s->nz;
+  k.N = (long long)s->nx * s->ny * s->nz;
+  for (int a = 0; a < 3; ++a) { k.bc[a] = s->bc[a]; k.ibm_wrap[a] = s->ibm_wrap[a]; }
+  k.ibm_wrap[2] = 0;
+  k.dxf = s->dx; k.dtf = s->dt;
+  const float* mp = s->params;
+  float c = s->dx / s->dt;
+  c = c / mp[PF_P_UMAX];
+  k.C = (double)c;
+  k.omega = 1.0 / (double)mp[PF_P_TAU];
+  const double Kd = (double)mp[PF_P_F0] / (double)mp[PF_P_RHO0] / (double)mp[PF_P_UMAX] * (double)mp[PF_P_UNIT];
+  float kf = mp[PF_P_F0] / mp[PF_P_RHO0];
+  kf = kf / mp[PF_P_UMAX];
+  kf = kf * mp[PF_P_UNIT];
+  k.kcoll = Kd * (double)s->dt / k.C;
+  k.kmom = (double)kf * (double)s->dt / k.C;
+  for (int a = 0; a < 3; ++a) k.body[a] = s->body_force[a];
+  float uw = mp[PF_P_SHEAR] * (float)(s->nz - 1);
+  uw = uw * s->dx;
+  uw = uw / mp[PF_P_UMAX];
+  k.uw = (double)uw / k.C;
+  k.fp16_scale = precision == PF_PREC_FP16 ? fp16_scale : 1.0;
+  k.dtT = s->dt / mp[PF_P_T0];
+  return k;
+}
+
+static int validate(const pf_scene* s, int precision) {
+  if (!s) return set_error(PFGPU_ERR_INVALID, "scene is NULL");
+  if (s->nx < 1 || s->ny < 1 || s->nz < 1 || s->ny > 65535 || s->nz > 65535)
+    return set_error(PFGPU_ERR_INVALID, "lattice dimensions out of range");
+  if (precision < PF_PREC_FP64 || precision > PF_PREC_FP16) return set_error(PFGPU_ERR_INVALID, "bad precision");
+  if (s->bc[0] == PF_BC_ZOUHE_SHEAR || s->bc[1] == PF_BC_ZOUHE_SHEAR)
+    return set_error(PFGPU_ERR_UNSUPPORTED, "Zou/He shear walls are only supported on z");
+  if (s->bc[2] == PF_BC_ZOUHE_SHEAR && (s->bc[0] == PF_BC_BOUNCEBACK || s->bc[1] == PF_BC_BOUNCEBACK))
+    return set_error(PFGPU_ERR_UNSUPPORTED, "Zou/He z walls need periodic x and y");
+  if (s->n_platelets < 0 || s->n_elem < 0 || s->n_fib < 0 || s->n_rec < 0)
+    return set_error(PFGPU_ERR_INVALID, "negative count");
+  if (s->n_platelets > 0) {
+    if (!s->X || !s->Y || !s->RY || !s->Z) return set_error(PFGPU_ERR_INVALID, "element positions missing");
+    if (s->n_membrane > s->n_elem) return set_error(PFGPU_ERR_INVALID, "n_membrane > n_elem");
+    if (s->n_tri > 0 && (!s->tri || !s->node_ntri || !s->ring || !s->S0 || !s->S0_all || !s->V0))
+      return set_error(PFGPU_ERR_INVALID, "membrane topology missing");
+    if (s->n_rec > 0 && (!s->rec_tri || !s->rec_r1 || !s->rec_r2 || s->n_tri == 0))
+      return set_error(PFGPU_ERR_INVALID, "receptor arrays missing");
+    if ((long long)s->n_platelets * s->n_rec > (1LL << 30)) return set_error(PFGPU_ERR_INVALID, "too many receptors");
+  }
+  if (s->n_fib > 0 && (!s->fib_X || !s->fib_Y || !s->fib_Z || !s->fib_fixed || !s->fib_ptr))
+    return set_error(PFGPU_ERR_INVALID, "fibrin arrays missing");
+  // every index a kernel dereferences is checked here, on the host
+  if (s->n_platelets > 0 && s->n_elem > 0) {
+    const int E = s->n_elem, Em = s->n_membrane, T = s->n_tri, NN = s->n_node;
+    for (int t = 0; t < T; ++t)
+      for (int i = 0; i < 6; ++i) {
+        const int q = s->tri[6 * t + i];
+        if (q < 0 || q >= NN || (i < 3 && q >= Em))
+          return set_error(PFGPU_ERR_INVALID, "triangle index out of range");
+      }
+    for (int q = 0; q < NN; ++q)
+      if (s->node_ntri[q] < 0 || s->node_ntri[q] > 10) return set_error(PFGPU_ERR_INVALID, "node_ntri out of range");
+    if (T > 0)
+      for (int v = 0; v < Em; ++v)
+        for (int a = 0; a < s->node_ntri[v]; ++a) {
+          const int r = s->ring[10 * v + a];
+          if (r < 0 || r >= Em) return set_error(PFGPU_ERR_INVALID, "ring index out of range");
+        }
+    if (s->spring_ptr) {
+      if (s->spring_ptr[0] != 0) return set_error(PFGPU_ERR_INVALID, "spring_ptr[0] != 0");
+      for (int e = 0; e < E; ++e) {
+        if (s->spring_ptr[e + 1] < s->spring_ptr[e]) return set_error(PFGPU_ERR_INVALID, "spring_ptr not monotone");
+        for (int q = s->spring_ptr[e]; q < s->spring_ptr[e + 1]; ++q)
+          if (s->spring_nbr[q] < 0 || s->spring_nbr[q] >= E)
+            return set_error(PFGPU_ERR_INVALID, "spring neighbour out of range");
+      }
+    }
+    const long long NR = (long long)s->n_platelets * s->n_rec;
+    for (long long r = 0; r < NR; ++r)
+      if (s->rec_tri[r] < 0 || s->rec_tri[r] >= T) return set_error(PFGPU_ERR_INVALID, "receptor triangle out of range");
+  }
+  if (s->n_fib > 0) {
+    const int M = s->n_fib;
+    if (s->fib_ptr[0] != 0) return set_error(PFGPU_ERR_INVALID, "fib_ptr[0] != 0");
+    for (int m = 0; m < M; ++m) {
+      if (s->fib_ptr[m + 1] < s->fib_ptr[m]) return set_error(PFGPU_ERR_INVALID, "fib_ptr not monotone");
+      for (int q = s->fib_ptr[m]; q < s->fib_ptr[m + 1]; ++q)
+        if (s->fib_nbr[q] < 0 || s->fib_nbr[q] >= M) return set_error(PFGPU_ERR_INVALID, "fibrin link out of range");
+    }
+  }
+  return PFGPU_OK;
+}
+
+// Initial populations and the (rho, u) of the first collision, in the
+// reference's host conventions (gpuSEM_LB.c:1206-1258 and
+// fluid_initGPUKernel, semLB.cu:154-233).
+static void initial_lattice(const pf_scene* s, std::vector<double>& f, std::vector<double>& ru) {
+  const size_t N = (size_t)s->nx * s->ny * s->nz;
+  const int zh = s->bc[2] == PF_BC_ZOUHE_SHEAR;
+  const float* mp = s->params;
+  const bool have_ru = s->rho_init && s->u_init;
+  ru.assign(4 * N, 0.0);
+  if (s->f_init) {
+    f.assign(s->f_init, s->f_init + 19 * N);
+  } else {
+    f.assign(19 * N, 0.0);
+    const double shear = (double)mp[PF_P_SHEAR];
+    const double umax_d = shear > 0 ? shear * (s->nz - 1) * (double)s->dx : (double)mp[PF_P_UMAX];
+    const float dxdt = s->dx / s->dt;
+    const double C0 = (double)dxdt / umax_d, C02 = C0 * C0;
+    for (int k = 0; k < s->nz; ++k)
+      for (int j = 0; j < s->ny; ++j)
+        for (int i = 0; i < s->nx; ++i) {
+          const size_t n = (size_t)i + (size_t)s->nx * (j + (size_t)s->ny * k);
+          double u[3] = {0, 0, 0}, r = 1.0;
+          if (s->u_init) {
+            u[0] = s->u_init[n]; u[1] = s->u_init[N + n]; u[2] = s->u_init[2 * N + n];
+          } else if (zh) {
+            u[1] = shear * k * (double)s->dx / umax_d;
+          }
+          if (s->rho_init) r = s->rho_init[n];
+          for (int d = 0; d < 19; ++d) {
+            const double cu = 3.0 * (cx(d) * u[0] + cy(d) * u[1] + cz(d) * u[2]);
+            f[d * N + n] = r * wgt(d) * (1.0 + cu / C0 + 0.5 * cu * cu / C02 -
+                                         1.5 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) / C02);
+          }
+          ru[n] = r; ru[N + n] = u[0]; ru[2 * N + n] = u[1]; ru[3 * N + n] = u[2];
+        }
+  }
+  if (have_ru) {
+    for (size_t n = 0; n < N; ++n) {
+      ru[n] = s->rho_init[n];
+      ru[N + n] = s->u_init[n];
+      ru[2 * N + n] = s->u_init[N + n];
+      ru[3 * N + n] = s->u_init[2 * N + n];
+    }
+  } else if (s->f_init) {
+    float c = s->dx / s->dt;
+    c = c / mp[PF_P_UMAX];
+    const double C = (double)c;
+    float fq = mp[PF_P_F0] / mp[PF_P_RHO0];
+    fq = fq / mp[PF_P_UMAX];
+    fq = fq * mp[PF_P_UNIT];
+    const double Fo = (double)fq;
+    float uwf = mp[PF_P_SHEAR] * (float)(s->nz - 1);
+    uwf = uwf * s->dx;
+    uwf = uwf / mp[PF_P_UMAX];
+    for (size_t n = 0; n < N; ++n) {
+      double r = 0, a = 0, b = 0, cc = 0;
+      for (int d = 0; d < 19; ++d) {
+        const double v = f[d * N + n];
+        r += v; a += cx(d) * v; b += cy(d) * v; cc += cz(d) * v;
+      }
+      const double Fx = s->F_init ? s->F_init[n] : 0, Fy = s->F_init ? s->F_init[N + n] : 0,
+                   Fz = s->F_init ? s->F_init[2 * N + n] : 0;
+      ru[n] = r;
+      ru[N + n] = (a * C + 0.5 * Fo * Fx * (double)s->dt) / r;
+      ru[2 * N + n] = (b * C + 0.5 * Fo * Fy * (double)s->dt) / r;
+      ru[3 * N + n] = (cc * C + 0.5 * Fo * Fz * (double)s->dt) / r;
+      const int k = (int)(n / ((size_t)s->nx * s->ny));
+      if (zh && (k == 0 || k == s->nz - 1)) {
+        ru[N + n] = 0; ru[3 * N + n] = 0;
+        ru[2 * N + n] = k == 0 ? 0.0 : (double)uwf;
+      }
+    }
+  }
+}
+
+static int build_platelets(pfgpu_job* j, const pf_scene* s) {
+  Platelets& P = j->Pl;
+  PlateletConst& k = P.k;
+  k.P = s->n_platelets; k.E = s->n_elem; k.Em = s->n_membrane; k.T = s->n_tri; k.NN = s->n_node;
+  k.nrec = s->n_rec;
+  k.mask = s->membrane_forces;
+  const float* mp = s->params;
+  k.kspring = mp[PF_P_KSPRING]; k.ks = mp[PF_P_KS]; k.kv = mp[PF_P_KV]; k.kbend = mp[PF_P_KBEND] * 1;
+  k.f0 = mp[PF_P_F0]; k.kf0 = mp[PF_P_KF0]; k.kr0 = mp[PF_P_KR0]; k.numrec = mp[PF_P_NUMRECEPTORS];
+  k.dxd = (double)s->dx; k.dtd = (double)s->dt; k.dxf = s->dx; k.dtf = s->dt; k.dtT = s->dt / mp[PF_P_T0];
+  k.bond_model = s->bond_model; k.p_on = s->p_on; k.p_off = s->p_off; k.seed = s->seed;
+  k.morse = s->morse;
+  for (int a = 0; a < 4; ++a) { k.morse_intra[a] = s->morse_intra[a]; k.morse_inter[a] = s->morse_inter[a]; }
+  k.nx = s->nx; k.ny = s->ny; k.nz = s->nz;
+  const int n3[3] = {s->nx, s->ny, s->nz};
+  const double rc = s->morse_intra[3] > s->morse_inter[3] ? s->morse_intra[3] : s->morse_inter[3];
+  for (int a = 0; a < 3; ++a) {
+    const double L = n3[a] * (double)s->dx;
+    int nc = rc > 0 ? (int)std::floor(L / rc) : 1;
+    if (nc < 1) nc = 1;
+    k.ncell[a] = nc;
+    k.cs[a] = L / nc;
+    k.L[a] = L;
+    k.wrap[a] = a < 2 ? s->ibm_wrap[a] : 0;
+  }
+  const size_t PE = (size_t)k.P * k.E;
+  const size_t rb = real_bytes(j->precision);
+  CK(dupload(j, &P.X, s->X, PE));
+  CK(dupload(j, &P.Y, s->Y, PE));
+  CK(dupload(j, &P.RY, s->RY, PE));
+  CK(dupload(j, &P.Z, s->Z, PE));
+  CK(dalloc(j, &P.V, 3 * PE));
+  CK(dalloc(j, &P.Ftot, 3 * PE));
+  CK(dalloc(j, (char**)&P.Fmem, 3 * PE * rb));
+  CK(dalloc(j, &P.Fmorse, 3 * PE));
+  CK(dalloc(j, (char**)&P.Fbond, 3 * PE * rb));
+  // topology: triangles of each node in ascending order, and each vertex's
+  // local index in them (gathers replace the reference's atomics)
+  std::vector<int> node_tri((size_t)k.NN * 10, -1), vert_local((size_t)k.Em * 10, -1), fill(k.NN, 0);
+  for (int t = 0; t < k.T; ++t)
+    for (int i = 0; i < 6; ++i) {
+      const int q = s->tri[6 * t + i];
+      if (q < 0 || q >= k.NN) return set_error(PFGPU_ERR_INVALID, "triangle node index out of range");
+      if (fill[q] >= 10) return set_error(PFGPU_ERR_INVALID, "more than 10 triangles share a node");
+      node_tri[(size_t)q * 10 + fill[q]] = t;
+      if (q < k.Em) vert_local[(size_t)q * 10 + fill[q]] = i;
+      fill[q]++;
+    }
+  for (int q = 0; q < k.NN; ++q)
+    if (fill[q] != s->node_ntri[q]) return set_error(PFGPU_ERR_INVALID, "node_ntri inconsistent with tri");
+  CK(dupload(j, &P.tri, s->tri, (size_t)k.T * 6));
+  CK(dupload(j, &P.node_ntri, s->node_ntri, (size_t)k.NN));
+  CK(dupload(j, &P.node_tri, node_tri.data(), node_tri.size()));
+  CK(dupload(j, &P.vert_local, vert_local.data(), vert_local.size()));
+  CK(dupload(j, &P.ring, s->ring, (size_t)k.Em * 10));
+  std::vector<int> sp_ptr(k.E + 1, 0);
+  if (s->spring_ptr) sp_ptr.assign(s->spring_ptr, s->spring_ptr + k.E + 1);
+  const int nsp = sp_ptr[k.E];
+  CK(dupload(j, &P.sp_ptr, sp_ptr.data(), sp_ptr.size()));
+  CK(dupload(j, &P.sp_nbr, s->spring_nbr, (size_t)nsp));
+  CK(dupload(j, &P.sp_L0, s->spring_L0, (size_t)nsp));
+  CK(dupload(j, &P.S0, s->S0, (size_t)k.P * k.T));
+  CK(dupload(j, &P.S0_all, s->S0_all, (size_t)k.P));
+  CK(dupload(j, &P.V0, s->V0, (size_t)k.P));
+  CK(dalloc(j, (char**)&P.nN, (size_t)k.P * k.NN * 3 * rb));
+  CK(dalloc(j, (char**)&P.nelem, (size_t)k.P * k.T * 3 * rb));
+  CK(dalloc(j, (char**)&P.S, (size_t)k.P * k.T * rb));
+  CK(dalloc(j, (char**)&P.km, (size_t)k.P * k.Em * rb));
+  CK(dalloc(j, &P.SV, (size_t)k.P * 2));
+  // receptors and wall sites
+  const size_t NR = (size_t)k.P * k.nrec;
+  CK(dupload(j, &P.rec_tri, s->rec_tri, NR));
+  CK(dupload(j, &P.r1, s->rec_r1, NR));
+  CK(dupload(j, &P.r2, s->rec_r2, NR));
+  std::vector<int> st(3 * NR, -1);
+  if (s->rec_state) st.assign(s->rec_state, s->rec_state + 3 * NR);
+  CK(dupload(j, &P.rec_state, st.data(), st.size()));
+  std::vector<int> vw((size_t)4 * s->nx * s->ny, -1);
+  if (s->vwf) vw.assign(s->vwf, s->vwf + vw.size());
+  CK(dupload(j, &P.vwf, vw.data(), vw.size()));
+  if (NR) CK(dalloc(j, (char**)&P.rec_tmp, bond_scratch_bytes((int)NR)));
+  if (k.morse) {
+    P.ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
+    CK(dalloc(j, &P.bin_count, (size_t)P.ncells));
+    CK(dalloc(j, &P.bin, (size_t)P.ncells * kBinCap));
+  }
+  return PFGPU_OK;
+}
+
+static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
+  Fibrin& F = j->Fb;
+  F.M = s->n_fib;
+  F.law = s->fib_law;
+  F.k = s->fib_k;
+  F.mass = s->fib_mass;
+  const size_t M = (size_t)F.M;
+  const int nl = s->fib_ptr[M];
+  CK(dupload(j, &F.X, s->fib_X, M));
+  CK(dupload(j, &F.Y, s->fib_Y, M));
+  CK(dupload(j, &F.Z, s->fib_Z, M));
+  CK(dalloc(j, &F.V, 3 * M));
+  CK(dalloc(j, &F.F, 3 * M));
+  CK(dupload(j, &F.fixed, s->fib_fixed, M));
+  CK(dupload(j, &F.ptr, s->fib_ptr, M + 1));
+  CK(dupload(j, &F.nbr, s->fib_nbr, (size_t)nl));
+  CK(dupload(j, &F.L0, s->fib_L0, (size_t)nl));
+  return PFGPU_OK;
+}
+
+static int enqueue_step(pfgpu_job* j) {
+  Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
+  Fibrin* Fb = j->has_fb ? &j->Fb : nullptr;
+  int launches = 0;
+  CK(cudaEventRecord(j->ev_fork, j->s0));
+  CK(cudaStreamWaitEvent(j->s1, j->ev_fork, 0));
+  CK(cudaStreamWaitEvent(j->s2, j->ev_fork, 0));
+  CK(cudaStreamWaitEvent(j->s3, j->ev_fork, 0));
+  if (Pl) {
+    CK(membrane_forces(*Pl, j->precision, j->ctl, j->s1));
+    launches++;
+    if (Pl->k.morse && Pl->k.P * Pl->k.E) {
+      CK(morse_forces(*Pl, j->precision, j->ctl, j->s2));
+      launches++;
+    }
+    if (Pl->k.nrec) {
+      CK(bond_pass(*Pl, j->precision, j->ctl, j->s0));
+      launches++;
+    }
+  }
+  if (Fb) {
+    CK(fibrin_forces(*Fb, j->precision, j->ctl, j->s3));
+    launches++;
+  }
+  CK(cudaEventRecord(j->ev1, j->s1));
+  CK(cudaEventRecord(j->ev2, j->s2));
+  CK(cudaEventRecord(j->ev3, j->s3));
+  CK(cudaStreamWaitEvent(j->s0, j->ev1, 0));
+  CK(cudaStreamWaitEvent(j->s0, j->ev2, 0));
+  CK(cudaStreamWaitEvent(j->s0, j->ev3, 0));
+  if (Pl || Fb) {
+    CK(spread_markers(j->L, Pl, Fb, j->ctl, j->s0));
+    launches++;
+  }
+  CK(lattice_step_binned(j->L, j->ctl, Pl && Pl->k.morse ? Pl->bin_count : nullptr, Pl ? Pl->ncells : 0, j->s0));
+  launches++;
+  if (Pl || Fb) {
+    CK(lattice_moments_active(j->L, j->ctl, j->s0));
+    launches++;
+  }
+  CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
+  launches++;
+  j->launches_per_step = launches;
+  return PFGPU_OK;
+}
+
+static int check_control(pfgpu_job* j) {
+  Control c;
+  CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+  if (c.err) {
+    char buf[128];
+    snprintf(buf, sizeof buf, "device error bits 0x%x", c.err);
+    return set_error(PFGPU_ERR_DEVICE, buf);
+  }
+  return c.done ? PFGPU_DONE : PFGPU_OK;
+}
+
+extern "C" {
+
+size_t pfgpu_scene_device_bytes(const pf_scene* s, int precision) {
+  if (!s) return 0;
+  const size_t N = (size_t)s->nx * s->ny * s->nz;
+  const size_t sb = store_bytes(precision), rb = real_bytes(precision);
+  const size_t nbricks = (size_t)((s->nx + kBrickX - 1) / kBrickX) * s->ny * s->nz;
+  size_t b = 2 * 19 * N * sb + 3 * N * 4 * rb + 4 * nbricks * 4;
+  const size_t PE = (size_t)s->n_platelets * s->n_elem;
+  b += PE * (4 * 8 + 6 * 8 + 3 * 8 + 6 * rb);
+  b += (size_t)s->n_platelets * ((size_t)s->n_node * 3 + (size_t)s->n_tri * 4 + s->n_membrane) * rb;
+  const size_t NR = (size_t)s->n_platelets * s->n_rec;
+  b += NR * 64 + 4 * (size_t)s->nx * s->ny * 4;
+  if (s->morse) {
+    const double rc = s->morse_intra[3] > s->morse_inter[3] ? s->morse_intra[3] : s->morse_inter[3];
+    size_t nc = 1;
+    const int n3[3] = {s->nx, s->ny, s->nz};
+    for (int a = 0; a < 3; ++a) {
+      int c = rc > 0 ? (int)std::floor(n3[a] * (double)s->dx / rc) : 1;
+      nc *= (size_t)(c < 1 ? 1 : c);
+    }
+    b += nc * (kBinCap + 1) * 4;
+  }
+  b += (size_t)s->n_fib * 14 * 8;
+  b += 19 * N * 8 + 4 * N * 8 + 3 * N * 8;  // transient upload staging
+  return b;
+}
+
+int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_job** out) {
+  if (!out) return set_error(PFGPU_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate(s, precision);
+  if (rc) return rc;
+  if (precision == PF_PREC_FP16 && !(fp16_scale > 0)) return set_error(PFGPU_ERR_INVALID, "fp16_scale must be > 0");
+  pfgpu_job* j = new pfgpu_job();
+  j->precision = precision;
+  j->detach_rate = s->detach_rate;
+  j->seed = s->seed;
+  auto fail = [&](int code) { destroy(j); return code; };
+#define CKJ(call)                                                                               \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      set_error(e_ == cudaErrorMemoryAllocation ? PFGPU_ERR_NOMEM : PFGPU_ERR_CUDA,             \
+                std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+      return fail(e_ == cudaErrorMemoryAllocation ? PFGPU_ERR_NOMEM : PFGPU_ERR_CUDA);          \
+    }                                                                                           \
+  } while (0)
+  CKJ(cudaStreamCreateWithFlags(&j->s0, cudaStreamNonBlocking));
+  CKJ(cudaStreamCreateWithFlags(&j->s1, cudaStreamNonBlocking));
+  CKJ(cudaStreamCreateWithFlags(&j->s2, cudaStreamNonBlocking));
+  CKJ(cudaStreamCreateWithFlags(&j->s3, cudaStreamNonBlocking));
+  CKJ(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
+  CKJ(cudaEventCreateWithFlags(&j->ev1, cudaEventDisableTiming));
+  CKJ(cudaEventCreateWithFlags(&j->ev2, cudaEventDisableTiming));
+  CKJ(cudaEventCreateWithFlags(&j->ev3, cudaEventDisableTiming));
+  // lattice
+  Lattice& L = j->L;
+  L.precision = precision;
+  L.k = lattice_const(s, fp16_scale, precision);
+  const size_t N = (size_t)L.k.N;
+  const size_t sb = store_bytes(precision), rb = real_bytes(precision);
+  CKJ(dalloc(j, (char**)&L.g[0], 19 * N * sb));
+  CKJ(dalloc(j, (char**)&L.g[1], 19 * N * sb));
+  CKJ(dalloc(j, (char**)&L.F[0], 4 * N * rb));
+  CKJ(dalloc(j, (char**)&L.F[1], 4 * N * rb));
+  CKJ(dalloc(j, (char**)&L.ubuf, 4 * N * rb));
+  CKJ(dalloc(j, &L.flags[0], (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.flags[1], (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.list[0], (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.list[1], (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &j->ctl, 1));
+  CKJ(dalloc(j, &j->done_blocks, 1));
+  CKJ(dalloc(j, &j->scratch4, 4));
+  {
+    std::vector<double> f, ru;
+    initial_lattice(s, f, ru);
+    double *df = nullptr, *dF = nullptr, *dru = nullptr;
+    CKJ(cudaMalloc(&df, f.size() * sizeof(double)));
+    cudaError_t e = cudaMemcpy(df, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&dru, ru.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(dru, ru.data(), ru.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && s->F_init) {
+      e = cudaMalloc(&dF, 3 * N * sizeof(double));
+      if (e == cudaSuccess) e = cudaMemcpy(dF, s->F_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = lattice_upload(L, df, dF, dru, j->ctl, j->s0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(j->s0);
+    cudaFree(df);
+    cudaFree(dF);
+    cudaFree(dru);
+    CKJ(e);
+  }
+  Control c{};
+  c.step = 0;
+  c.done = 0;
+  c.first = 1;
+  c.total_bond = 1;  // sem_initGPUKernel, semLB.cu:880
+  CKJ(cudaMemcpy(j->ctl, &c, sizeof c, cudaMemcpyHostToDevice));
+  if (s->n_platelets > 0 && s->n_elem > 0) {
+    j->has_pl = true;
+    rc = build_platelets(j, s);
+    if (rc) return fail(rc);
+    CKJ(bin_elements(j->Pl, j->ctl, j->s0));
+  }
+  if (s->n_fib > 0) {
+    j->has_fb = true;
+    rc = build_fibrin(j, s);
+    if (rc) return fail(rc);
+  }
+  CKJ(cudaStreamSynchronize(j->s0));
+  *out = j;
+  return PFGPU_OK;
+}
+
+int pfgpu_job_step(pfgpu_job* j, int nsteps) {
+  if (!j || nsteps < 0) return set_error(PFGPU_ERR_INVALID, "bad job or step count");
+  for (int i = 0; i < nsteps; ++i) {
+    int rc = enqueue_step(j);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(j->s0));
+  return check_control(j);
+}
+
+int pfgpu_job_step_graph(pfgpu_job* j, int nsteps) {
+  if (!j || nsteps < 0) return set_error(PFGPU_ERR_INVALID, "bad job or step count");
+  if (!j->graph) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(j->s0, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(j);
+    cudaError_t e = cudaStreamEndCapture(j->s0, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    CK(e);
+    e = cudaGraphInstantiate(&j->graph, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+  }
+  for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(j->graph, j->s0));
+  CK(cudaStreamSynchronize(j->s0));
+  return check_control(j);
+}
+
+int pfgpu_job_enqueue(pfgpu_job* j, int nsteps, cudaStream_t) {
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  if (!j->graph) {
+    int rc = pfgpu_job_step_graph(j, 0);
+    if (rc) return rc;
+  }
+  for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(j->graph, j->s0));
+  return PFGPU_OK;
+}
+
+int pfgpu_job_sync(pfgpu_job* j) {
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  CK(cudaStreamSynchronize(j->s0));
+  return check_control(j);
+}
+
+int64_t pfgpu_job_step_count(const pfgpu_job* j) {
+  if (!j) return -1;
+  Control c;
+  if (cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return c.step;
+}
+
+int pfgpu_job_get_lattice(pfgpu_job* j, double* fIN, double* fOUT, double* rho, double* u, double* F) {
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  CK(cudaStreamSynchronize(j->s0));
+  const size_t N = (size_t)j->L.k.N;
+  Control c;
+  CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+  double *dfi = nullptr, *dfo = nullptr, *dr = nullptr, *du = nullptr, *dF = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (fIN) e = cudaMalloc(&dfi, 19 * N * sizeof(double));
+  if (e == cudaSuccess && fOUT) e = cudaMalloc(&dfo, 19 * N * sizeof(double));
+  if (e == cudaSuccess && rho) e = cudaMalloc(&dr, N * sizeof(double));
+  if (e == cudaSuccess && u) e = cudaMalloc(&du, 3 * N * sizeof(double));
+  if (e == cudaSuccess && F) e = cudaMalloc(&dF, 3 * N * sizeof(double));
+  if (e == cudaSuccess) e = lattice_download(j->L, j->ctl, c.step, dfi, dfo, dr, du, dF, j->s0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(j->s0);
+  if (e == cudaSuccess && fIN) e = cudaMemcpy(fIN, dfi, 19 * N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && fOUT) e = cudaMemcpy(fOUT, dfo, 19 * N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && rho) e = cudaMemcpy(rho, dr, N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && u) e = cudaMemcpy(u, du, 3 * N * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && F) e = cudaMemcpy(F, dF, 3 * N * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(dfi); cudaFree(dfo); cudaFree(dr); cudaFree(du); cudaFree(dF);
+  CK(e);
+  return PFGPU_OK;
+}
+
+int pfgpu_job_get_elements(pfgpu_job* j, double* X, double* Y, double* RY, double* Z, double* V, double* F) {
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  CK(cudaStreamSynchronize(j->s0));
+  if (!j->has_pl) return PFGPU_OK;
+  const size_t PE = (size_t)j->Pl.k.P * j->Pl.k.E;
+  if (X) CK(cudaMemcpy(X, j->Pl.X, PE * 8, cudaMemcpyDeviceToHost));
+  if (Y) CK(cudaMemcpy(Y, j->Pl.Y, PE * 8, cudaMemcpyDeviceToHost));
+  if (RY) CK(cudaMemcpy(RY, j->Pl.RY, PE * 8, cudaMemcpyDeviceToHost));
+  if (Z) CK(cudaMemcpy(Z, j->Pl.Z, PE * 8, cudaMemcpyDeviceToHost));
+  if (V) CK(cudaMemcpy(V, j->Pl.V, 3 * PE * 8, cudaMemcpyDeviceToHost));
+  if (F) CK(cudaMemcpy(F, j->Pl.Ftot, 3 * PE * 8, cudaMemcpyDeviceToHost));
+  return PFGPU_OK;
+}
+
+int pfgpu_job_get_bonds(pfgpu_job* j, int* rec_state, int* vwf, int* total_bond) {
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  CK(cudaStreamSynchronize(j->s0));
+  if (total_bond) {
+    Control c;
+    CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+    *total_bond = c.total_bond;
+  }
+  if (!j->has_pl) return PFGPU_OK;
+  const size_t NR = (size_t)j->Pl.k.P * j->Pl.k.nrec;
+  if (rec_state && NR) CK(cudaMemcpy(rec_state, j->Pl.rec_state, 3 * NR * 4, cudaMemcpyDeviceToHost));
+  if (vwf) CK(cudaMemcpy(vwf, j->Pl.vwf, (size_t)4 * j->L.k.nx * j->L.k.ny * 4, cudaMemcpyDeviceToHost));
+  return PFGPU_OK;
+}
+
+int pfgpu_job_get_fibrin(pfgpu_job* j, double* X, double* Y, double* Z, double* V, double* F) {
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  CK(cudaStreamSynchronize(j->s0));
+  if (!j->has_fb) return PFGPU_OK;
+  const size_t M = (size_t)j->Fb.M;
+  if (X) CK(cudaMemcpy(X, j->Fb.X, M * 8, cudaMemcpyDeviceToHost));
+  if (Y) CK(cudaMemcpy(Y, j->Fb.Y, M * 8, cudaMemcpyDeviceToHost));
+  if (Z) CK(cudaMemcpy(Z, j->Fb.Z, M * 8, cudaMemcpyDeviceToHost));
+  if (V) CK(cudaMemcpy(V, j->Fb.V, 3 * M * 8, cudaMemcpyDeviceToHost));
+  if (F) CK(cudaMemcpy(F, j->Fb.F, 3 * M * 8, cudaMemcpyDeviceToHost));
+  return PFGPU_OK;
+}
+
+int pfgpu_job_get_membrane(pfgpu_job* j, double* S_V, double* km) {
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  CK(cudaStreamSynchronize(j->s0));
+  if (!j->has_pl) return PFGPU_OK;
+  const PlateletConst& k = j->Pl.k;
+  if (S_V) CK(cudaMemcpy(S_V, j->Pl.SV, (size_t)k.P * 2 * 8, cudaMemcpyDeviceToHost));
+  if (km) {
+    const size_t n = (size_t)k.P * k.Em;
+    if (j->precision == PF_PREC_FP64) {
+      CK(cudaMemcpy(km, j->Pl.km, n * 8, cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<float> tmp(n);
+      CK(cudaMemcpy(tmp.data(), j->Pl.km, n * 4, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < n; ++i) km[i] = tmp[i];
+    }
+  }
+  return PFGPU_OK;
+}
+
+int pfgpu_job_conservation(pfgpu_job* j, double out[4]) {
+  if (!j || !out) return set_error(PFGPU_ERR_INVALID, "bad arguments");
+  CK(cudaStreamSynchronize(j->s0));
+  Control c;
+  CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+  CK(lattice_conservation(j->L, c.step, j->scratch4, j->s0));
+  CK(cudaMemcpyAsync(out, j->scratch4, 4 * sizeof(double), cudaMemcpyDeviceToHost, j->s0));
+  CK(cudaStreamSynchronize(j->s0));
+  return PFGPU_OK;
+}
+
+size_t pfgpu_job_device_bytes(const pfgpu_job* j) { return j ? j->bytes : 0; }
+int pfgpu_job_launches_per_step(const pfgpu_job* j) { return j ? j->launches_per_step : 0; }
+void pfgpu_job_destroy(pfgpu_job* j) {
+  if (j && j->s0) cudaStreamSynchronize(j->s0);
+  destroy(j);
+}
+
+const char* pfgpu_last_error(void) {
+  if (!g_last_error.empty()) return g_last_error.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_last_error_global.c_str();
+}
+int pfgpu_version(void) { return 100; }
+
+void pfgpu_receptor_uniforms(uint64_t seed, int64_t step, int64_t receptor, double out[2]) {
+  receptor_uniforms(seed, step, receptor, out[0], out[1]);
+}
+double pfgpu_detach_uniform(uint64_t seed, int64_t step) { return detach_uniform(seed, step); }
+
+// internal accessors for the batch and drop-in layers
+cudaStream_t pfgpu_job_stream_(pfgpu_job* j) { return j->s0; }
+int pfgpu_job_control_(pfgpu_job* j, Control* out) {
+  CK(cudaMemcpy(out, j->ctl, sizeof *out, cudaMemcpyDeviceToHost));
+  return PFGPU_OK;
+}
+
+}  // extern "C"
+
+int pfgpu_set_error_(int code, const char* msg) { return set_error(code, msg); }

@@ -1,0 +1,490 @@
+// pf_lattice.cu -- D3Q19 lattice kernels: the fused pull-scheme
+// collide-stream step with boundary conditions, moments on active bricks,
+// upload (un-streaming) and download.
+//
+// Reference semantics kept (LB_kernel.cu): the collision of step t uses the
+// density/velocity of step t-1 (moments of fIN with the half force of step
+// t-1, :1108-1199) and the force of step t (:1203-1304); streaming is
+// periodic on every axis (:1312-1359) and the Zou/He planes then overwrite
+// the five unknown populations (:395-780), where density and velocity are the
+// boundary values (those planes are obstacle nodes for the moments kernel).
+// Arithmetic is in lattice units on shifted populations g = f - w:
+//   geq_d = w_d (drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u.u))
+//   S_d   = w_d (1 - omega/2) (3 c.F + 9 (c.u)(c.F) - 3 u.F)
+// which is the reference's Guo forcing with u -> u/C and F -> F*K*dt/C.
+#include "pf_internal.h"
+
+namespace pf {
+
+namespace {
+
+template <class S, class R>
+struct Lat {
+  static __device__ __forceinline__ R scale(int d, R sigma) { return (R)wgt(d) * sigma; }
+};
+
+template <class S, class R>
+__device__ __forceinline__ R ld(const S* p, int d, R sigma) {
+  return (R)StoreTraits<S>::load(p, d, (decltype(StoreTraits<S>::load(p, 0, R(0))))(wgt(d) * sigma));
+}
+
+template <class R>
+__device__ __forceinline__ void ld_force(const R4<R>* F, size_t n, R& fx, R& fy, R& fz);
+template <>
+__device__ __forceinline__ void ld_force<float>(const float4* F, size_t n, float& fx, float& fy, float& fz) {
+  float4 v = __ldcg(F + n);
+  fx += v.x; fy += v.y; fz += v.z;
+}
+template <>
+__device__ __forceinline__ void ld_force<double>(const D4* F, size_t n, double& fx, double& fy, double& fz) {
+  const double2* p = reinterpret_cast<const double2*>(F + n);
+  double2 a = __ldcg(p), b = __ldcg(p + 1);
+  fx += a.x; fy += a.y; fz += b.x;
+}
+template <class R>
+__device__ __forceinline__ void zero_force(R4<R>* F, size_t n);
+template <>
+__device__ __forceinline__ void zero_force<float>(float4* F, size_t n) { F[n] = make_float4(0, 0, 0, 0); }
+template <>
+__device__ __forceinline__ void zero_force<double>(D4* F, size_t n) { F[n] = D4{0, 0, 0, 0}; }
+
+template <class R>
+__device__ __forceinline__ void st_u(R4<R>* U, size_t n, R a, R b, R c, R d);
+template <>
+__device__ __forceinline__ void st_u<float>(float4* U, size_t n, float a, float b, float c, float d) {
+  U[n] = make_float4(a, b, c, d);
+}
+template <>
+__device__ __forceinline__ void st_u<double>(D4* U, size_t n, double a, double b, double c, double d) {
+  U[n] = D4{a, b, c, d};
+}
+template <class R>
+__device__ __forceinline__ void ld_u(const R4<R>* U, size_t n, R& a, R& b, R& c, R& d);
+template <>
+__device__ __forceinline__ void ld_u<float>(const float4* U, size_t n, float& a, float& b, float& c, float& d) {
+  float4 v = U[n];
+  a = v.x; b = v.y; c = v.z; d = v.w;
+}
+template <>
+__device__ __forceinline__ void ld_u<double>(const D4* U, size_t n, double& a, double& b, double& c, double& d) {
+  D4 v = U[n];
+  a = v.x; b = v.y; c = v.z; d = v.w;
+}
+
+// Pull the 19 post-stream populations of node (x,y,z) from the post-collision
+// buffer: periodic on periodic and Zou/He axes (the reference streams
+// periodically first), half-way bounce-back through faces of bounce-back axes.
+template <class S, class R>
+__device__ __forceinline__ void gather(const LatticeConst& k, const S* __restrict__ gin, int x, int y, int z,
+                                       R g[Q]) {
+  const int nx = k.nx, ny = k.ny, nz = k.nz;
+  const size_t N = (size_t)k.N;
+  const R sigma = (R)k.fp16_scale;
+  int xm = x - 1, xp = x + 1, ym = y - 1, yp = y + 1, zm = z - 1, zp = z + 1;
+  bool oxm = false, oxp = false, oym = false, oyp = false, ozm = false, ozp = false;
+  if (xm < 0) { if (k.bc[0] == PF_BC_BOUNCEBACK) oxm = true; else xm = nx - 1; }
+  if (xp >= nx) { if (k.bc[0] == PF_BC_BOUNCEBACK) oxp = true; else xp = 0; }
+  if (ym < 0) { if (k.bc[1] == PF_BC_BOUNCEBACK) oym = true; else ym = ny - 1; }
+  if (yp >= ny) { if (k.bc[1] == PF_BC_BOUNCEBACK) oyp = true; else yp = 0; }
+  if (zm < 0) { if (k.bc[2] == PF_BC_BOUNCEBACK) ozm = true; else zm = nz - 1; }
+  if (zp >= nz) { if (k.bc[2] == PF_BC_BOUNCEBACK) ozp = true; else zp = 0; }
+  const size_t n = (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z);
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    const int sx = cx(d) == 1 ? xm : (cx(d) == -1 ? xp : x);
+    const int sy = cy(d) == 1 ? ym : (cy(d) == -1 ? yp : y);
+    const int sz = cz(d) == 1 ? zm : (cz(d) == -1 ? zp : z);
+    const bool out = (cx(d) == 1 && oxm) || (cx(d) == -1 && oxp) || (cy(d) == 1 && oym) ||
+                     (cy(d) == -1 && oyp) || (cz(d) == 1 && ozm) || (cz(d) == -1 && ozp);
+    if (out) {
+      g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
+    } else {
+      g[d] = ld<S, R>(gin + (size_t)d * N + (size_t)sx + (size_t)nx * ((size_t)sy + (size_t)ny * sz), d, sigma);
+    }
+  }
+}
+
+// Zou/He planes: z=0 no-slip (LB_kernel.cu:395-600) and z=nz-1 moving plate
+// (:602-780, where C, Nzx, Nzy are float).  Writes the unknowns, returns the
+// boundary density; velocity is the wall's.
+template <class R>
+__device__ __forceinline__ R zouhe_bottom(R g[Q]) {
+  const R rho = (R)1 + (g[1] + g[2] + g[3] + g[4] + g[7] + g[8] + g[11] + g[12] + g[0] +
+                        (R)2 * (g[6] + g[10] + g[14] + g[16] + g[18]));
+  const R Nzx = (R)0.5 * (g[1] + g[7] + g[8] - g[2] - g[11] - g[12]);
+  const R Nzy = (R)0.5 * (g[3] + g[7] + g[11] - g[4] - g[8] - g[12]);
+  g[5] = g[6];
+  g[9] = g[14] - Nzx;
+  g[13] = g[10] + Nzx;
+  g[15] = g[18] - Nzy;
+  g[17] = g[16] + Nzy;
+  return rho;
+}
+template <class R>
+__device__ __forceinline__ R zouhe_top(R g[Q], R uw) {
+  const R rho = (R)1 + (g[1] + g[2] + g[3] + g[4] + g[7] + g[11] + g[12] + g[8] + g[0] +
+                        (R)2 * (g[5] + g[9] + g[13] + g[15] + g[17]));
+  const R Nzx = (R)(float)((R)0.5 * (g[1] + g[7] + g[8] - g[2] - g[11] - g[12]));
+  const R Nzy = (R)(float)((R)0.5 * (g[3] + g[7] + g[11] - g[4] - g[8] - g[12]) - (R)(1.0 / 3.0) * rho * uw);
+  g[6] = g[5];
+  g[10] = g[13] - Nzx;
+  g[14] = g[9] + Nzx;
+  g[16] = g[17] + (R)(1.0 / 6.0) * rho * uw - Nzy;
+  g[18] = g[15] + (R)(1.0 / 6.0) * rho * (-uw) + Nzy;
+  return rho;
+}
+
+template <class R>
+__device__ __forceinline__ void moments(const R g[Q], R& drho, R& jx, R& jy, R& jz) {
+  drho = 0; jx = 0; jy = 0; jz = 0;
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    drho += g[d];
+    if (cx(d)) jx += cx(d) * g[d];
+    if (cy(d)) jy += cy(d) * g[d];
+    if (cz(d)) jz += cz(d) * g[d];
+  }
+}
+
+// density and lattice velocity of a post-stream node (boundary values on the
+// Zou/He planes, half-force corrected moments elsewhere)
+template <class R>
+__device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z, bool apply_bc, R Fx, R Fy,
+                                           R Fz, R& rho, R& ux, R& uy, R& uz) {
+  if (apply_bc && k.bc[2] == PF_BC_ZOUHE_SHEAR && z == 0) {
+    rho = zouhe_bottom(g);
+    ux = 0; uy = 0; uz = 0;
+    return;
+  }
+  if (apply_bc && k.bc[2] == PF_BC_ZOUHE_SHEAR && z == k.nz - 1) {
+    rho = zouhe_top(g, (R)k.uw);
+    ux = 0; uy = (R)k.uw; uz = 0;
+    return;
+  }
+  R drho, jx, jy, jz;
+  moments(g, drho, jx, jy, jz);
+  rho = (R)1 + drho;
+  const R hk = (R)0.5 * (R)k.kmom;
+  ux = (jx + hk * Fx) / rho;
+  uy = (jy + hk * Fy) / rho;
+  uz = (jz + hk * Fz) / rho;
+}
+
+template <class S, class R>
+__global__ void __launch_bounds__(kBrickX) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                                      R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                                      int ncells, Control* ctl) {
+  if (ctl->done) return;
+  const long long step = ctl->step;
+  const int par = (int)(step & 1);
+  const S* __restrict__ gin = par ? gB : gA;
+  S* __restrict__ gout = par ? gA : gB;
+  R4<R>* Fc = par ? FB : FA;
+  R4<R>* Fp = par ? FA : FB;
+  unsigned* flp = par ? flA : flB;
+  const unsigned* flc = par ? flB : flA;
+  const int first = ctl->first;
+  const int x = blockIdx.x * kBrickX + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  const int brick = blockIdx.x + k.nbx * (y + k.ny * z);
+  const unsigned fc = flc[brick], fp = flp[brick];
+  if (x < k.nx) {
+    const size_t N = (size_t)k.N;
+    const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
+    R g[Q];
+    gather<S, R>(k, gin, x, y, z, g);
+    R rho, ux, uy, uz;
+    if (first) {
+      ld_u<R>(ubuf, n, rho, ux, uy, uz);
+      if (k.bc[2] == PF_BC_ZOUHE_SHEAR) { /* the first collision streams without the BC */ }
+    } else {
+      R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
+      if (fp) ld_force<R>(Fp, n, px, py, pz);
+      node_state<R>(k, g, z, true, px, py, pz, rho, ux, uy, uz);
+    }
+    R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+    if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
+    const R kc = (R)k.kcoll;
+    Fx *= kc; Fy *= kc; Fz *= kc;
+    const R om = (R)k.omega;
+    const R drho = rho - (R)1;
+    const R usq = ux * ux + uy * uy + uz * uz;
+    const R uF = ux * Fx + uy * Fy + uz * Fz;
+    const R sf = (R)1 - (R)0.5 * om;
+    const R sigma = (R)k.fp16_scale;
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
+      const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
+      const R w = (R)wgt(d);
+      const R geq = w * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq));
+      const R src = w * sf * ((R)3 * cF + (R)9 * cu * cF - (R)3 * uF);
+      const R gn = g[d] - om * (g[d] - geq) + src;
+      StoreTraits<S>::store(gout + (size_t)d * N + n, gn, d,
+                            (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+    }
+    if (fp) zero_force<R>(Fp, n);
+    (void)fc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && fp) flp[brick] = 0;
+  if (bin_count) {
+    const size_t tid = (((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * blockDim.x +
+                       threadIdx.x;
+    const size_t tot = (size_t)gridDim.x * gridDim.y * gridDim.z * blockDim.x;
+    for (size_t c = tid; c < (size_t)ncells; c += tot) bin_count[c] = 0;
+  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0) ctl->active_count[par ^ 1] = 0;
+}
+
+// (rho, u/C) of the nodes of the active bricks after this step's stream and
+// boundary conditions, with this step's force: input of the IBM interpolation
+// (the reference's velocity_density, LB_kernel.cu:1108-1199).
+template <class S, class R>
+__global__ void __launch_bounds__(kBrickX) moments_active_k(LatticeConst k, const S* gA, const S* gB,
+                                                            const R4<R>* FA, const R4<R>* FB, R4<R>* ubuf,
+                                                            const int* lA, const int* lB, const Control* ctl) {
+  if (ctl->done) return;
+  const int par = (int)(ctl->step & 1);
+  const S* gnew = par ? gA : gB;
+  const R4<R>* Fc = par ? FB : FA;
+  const int* list = par ? lB : lA;
+  const unsigned* fl = nullptr;
+  (void)fl;
+  const int cnt = ctl->active_count[par];
+  for (int b = blockIdx.x; b < cnt; b += gridDim.x) {
+    const int brick = list[b];
+    const int bx = brick % k.nbx;
+    const int y = (brick / k.nbx) % k.ny;
+    const int z = brick / (k.nbx * k.ny);
+    const int x = bx * kBrickX + threadIdx.x;
+    if (x >= k.nx) continue;
+    const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
+    R g[Q];
+    gather<S, R>(k, gnew, x, y, z, g);
+    R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+    ld_force<R>(Fc, n, Fx, Fy, Fz);
+    R rho, ux, uy, uz;
+    node_state<R>(k, g, z, true, Fx, Fy, Fz, rho, ux, uy, uz);
+    st_u<R>(ubuf, n, rho, ux, uy, uz);
+  }
+}
+
+// Full-lattice post-stream state in the reference's host layouts (double).
+template <class S, class R>
+__global__ void download_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, const R4<R>* ubuf, int apply_bc,
+                           int use_ubuf, double* fIN, double* fOUT, double* rho_o, double* u_o, double* F_o) {
+  const size_t N = (size_t)k.N;
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int x = (int)(n % k.nx), y = (int)((n / k.nx) % k.ny), z = (int)(n / ((size_t)k.nx * k.ny));
+  R g[Q];
+  gather<S, R>(k, gsrc, x, y, z, g);
+  R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+  ld_force<R>(Fsrc, n, Fx, Fy, Fz);
+  R rho, ux, uy, uz;
+  if (use_ubuf) {
+    ld_u<R>(ubuf, n, rho, ux, uy, uz);
+  } else {
+    node_state<R>(k, g, z, apply_bc != 0, Fx, Fy, Fz, rho, ux, uy, uz);
+  }
+  const R sigma = (R)k.fp16_scale;
+  for (int d = 0; d < Q; ++d) {
+    if (fIN) fIN[(size_t)d * N + n] = (double)g[d] + wgt(d);
+    if (fOUT) fOUT[(size_t)d * N + n] = (double)ld<S, R>(gsrc + (size_t)d * N + n, d, sigma) + wgt(d);
+  }
+  if (rho_o) rho_o[n] = (double)rho;
+  if (u_o) {
+    u_o[n] = (double)ux * k.C;
+    u_o[N + n] = (double)uy * k.C;
+    u_o[2 * N + n] = (double)uz * k.C;
+  }
+  if (F_o) {
+    F_o[n] = (double)Fx;
+    F_o[N + n] = (double)Fy;
+    F_o[2 * N + n] = (double)Fz;
+  }
+}
+
+// f*_d(x) = fIN_d(x + c_d) so that the first pull reproduces fIN; through a
+// bounce-back face f*_d(x) = fIN_opp(d)(x).  Also loads the initial force of
+// the step before the first (flags its bricks) and (rho, u/C) for the first
+// collision.
+template <class S, class R>
+__global__ void upload_k(LatticeConst k, S* g, const double* fIN, R4<R>* Fprev, unsigned* flprev, const double* F,
+                         R4<R>* ubuf, const double* ru) {
+  const size_t N = (size_t)k.N;
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int x = (int)(n % k.nx), y = (int)((n / k.nx) % k.ny), z = (int)(n / ((size_t)k.nx * k.ny));
+  const R sigma = (R)k.fp16_scale;
+  for (int d = 0; d < Q; ++d) {
+    int tx = x + cx(d), ty = y + cy(d), tz = z + cz(d);
+    bool out = false;
+    if (tx < 0 || tx >= k.nx) { if (k.bc[0] == PF_BC_BOUNCEBACK) out = true; else tx = (tx + k.nx) % k.nx; }
+    if (ty < 0 || ty >= k.ny) { if (k.bc[1] == PF_BC_BOUNCEBACK) out = true; else ty = (ty + k.ny) % k.ny; }
+    if (tz < 0 || tz >= k.nz) { if (k.bc[2] == PF_BC_BOUNCEBACK) out = true; else tz = (tz + k.nz) % k.nz; }
+    double f = out ? fIN[(size_t)opp(d) * N + n]
+                   : fIN[(size_t)d * N + (size_t)tx + (size_t)k.nx * ((size_t)ty + (size_t)k.ny * tz)];
+    StoreTraits<S>::store(g + (size_t)d * N + n, (R)(f - wgt(d)), d,
+                          (decltype(StoreTraits<S>::load(g, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+  }
+  R fx = 0, fy = 0, fz = 0;
+  if (F) { fx = (R)F[n]; fy = (R)F[N + n]; fz = (R)F[2 * N + n]; }
+  if (fx != 0 || fy != 0 || fz != 0) {
+    const int brick = x / kBrickX + k.nbx * (y + k.ny * z);
+    flprev[brick] = 1u;
+  }
+  R4<R> v;
+  v.x = fx; v.y = fy; v.z = fz; v.w = 0;
+  Fprev[n] = v;
+  st_u<R>(ubuf, n, (R)ru[n], (R)(ru[N + n] / k.C), (R)(ru[2 * N + n] / k.C), (R)(ru[3 * N + n] / k.C));
+}
+
+template <class S, class R>
+__global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
+  const size_t N = (size_t)k.N;
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = 0, a = 0, b = 0, c = 0;
+  if (n < N) {
+    const int x = (int)(n % k.nx), y = (int)((n / k.nx) % k.ny), z = (int)(n / ((size_t)k.nx * k.ny));
+    R g[Q];
+    gather<S, R>(k, gsrc, x, y, z, g);
+    if (k.bc[2] == PF_BC_ZOUHE_SHEAR && (z == 0 || z == k.nz - 1)) {
+      if (z == 0) zouhe_bottom(g);
+      else zouhe_top(g, (R)k.uw);
+    }
+    for (int d = 0; d < Q; ++d) {
+      double f = (double)g[d] + wgt(d);
+      m += f; a += cx(d) * f; b += cy(d) * f; c += cz(d) * f;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m += __shfl_xor_sync(0xffffffffu, m, o);
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, m); atomicAdd(out + 1, a); atomicAdd(out + 2, b); atomicAdd(out + 3, c);
+  }
+}
+
+template <class S, class R>
+cudaError_t step_impl(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st) {
+  dim3 grid(L.k.nbx, L.k.ny, L.k.nz);
+  lbm_step_k<S, R><<<grid, kBrickX, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
+                                              (R4<R>*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells, ctl);
+  return cudaGetLastError();
+}
+template <class S, class R>
+cudaError_t moments_impl(Lattice& L, Control* ctl, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = sms * 8;
+  if (grid > L.k.nbricks) grid = L.k.nbricks;
+  moments_active_k<S, R><<<grid, kBrickX, 0, st>>>(L.k, (const S*)L.g[0], (const S*)L.g[1],
+                                                    (const R4<R>*)L.F[0], (const R4<R>*)L.F[1], (R4<R>*)L.ubuf,
+                                                    L.list[0], L.list[1], ctl);
+  return cudaGetLastError();
+}
+template <class S, class R>
+cudaError_t upload_impl(Lattice& L, const double* fIN, const double* F, const double* ru, cudaStream_t st) {
+  const size_t N = (size_t)L.k.N;
+  upload_k<S, R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(L.k, (S*)L.g[0], fIN, (R4<R>*)L.F[1], L.flags[1], F,
+                                                              (R4<R>*)L.ubuf, ru);
+  return cudaGetLastError();
+}
+template <class S, class R>
+cudaError_t download_impl(Lattice& L, long long step, double* fIN, double* fOUT, double* rho, double* u, double* F,
+                          cudaStream_t st) {
+  const size_t N = (size_t)L.k.N;
+  // latest post-collision buffer and force of the last step; before any
+  // step: the uploaded state (no boundary pass yet, initial rho/u)
+  const void* gsrc;
+  const void* Fs;
+  int apply_bc = 1, use_ubuf = 0;
+  if (step == 0) {
+    gsrc = L.g[0];
+    Fs = L.F[1];
+    apply_bc = 0;
+    use_ubuf = 1;
+  } else {
+    const int last = (int)((step - 1) & 1);
+    gsrc = last ? L.g[0] : L.g[1];
+    Fs = L.F[last];
+  }
+  download_k<S, R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(L.k, (const S*)gsrc, (const R4<R>*)Fs,
+                                                                (const R4<R>*)L.ubuf, apply_bc, use_ubuf, fIN,
+                                                                fOUT, rho, u, F);
+  return cudaGetLastError();
+}
+template <class S, class R>
+cudaError_t conservation_impl(Lattice& L, long long step, double* out, cudaStream_t st) {
+  const size_t N = (size_t)L.k.N;
+  const void* gsrc = step == 0 ? L.g[0] : (((step - 1) & 1) ? L.g[0] : L.g[1]);
+  cudaMemsetAsync(out, 0, 4 * sizeof(double), st);
+  conservation_k<S, R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(L.k, (const S*)gsrc, out);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+#define PF_DISPATCH(L, CALL)                              \
+  switch ((L).precision) {                                \
+    case PF_PREC_FP64: return CALL<double, double>;       \
+    case PF_PREC_FP32: return CALL<float, float>;         \
+    case PF_PREC_FP16: return CALL<__half, float>;        \
+    default: return cudaErrorInvalidValue;                \
+  }
+
+cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_dev, const double* ru_dev,
+                           Control* ctl, cudaStream_t st) {
+  (void)ctl;
+  switch (L.precision) {
+    case PF_PREC_FP64: return upload_impl<double, double>(L, fIN_dev, F_dev, ru_dev, st);
+    case PF_PREC_FP32: return upload_impl<float, float>(L, fIN_dev, F_dev, ru_dev, st);
+    case PF_PREC_FP16: return upload_impl<__half, float>(L, fIN_dev, F_dev, ru_dev, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t lattice_step_binned(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st) {
+  switch (L.precision) {
+    case PF_PREC_FP64: return step_impl<double, double>(L, ctl, bin_count, ncells, st);
+    case PF_PREC_FP32: return step_impl<float, float>(L, ctl, bin_count, ncells, st);
+    case PF_PREC_FP16: return step_impl<__half, float>(L, ctl, bin_count, ncells, st);
+  }
+  return cudaErrorInvalidValue;
+}
+cudaError_t lattice_step(Lattice& L, Control* ctl, cudaStream_t st) {
+  return lattice_step_binned(L, ctl, nullptr, 0, st);
+}
+cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st) {
+  switch (L.precision) {
+    case PF_PREC_FP64: return moments_impl<double, double>(L, ctl, st);
+    case PF_PREC_FP32: return moments_impl<float, float>(L, ctl, st);
+    case PF_PREC_FP16: return moments_impl<__half, float>(L, ctl, st);
+  }
+  return cudaErrorInvalidValue;
+}
+cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* fIN, double* fOUT, double* rho,
+                             double* u, double* F, cudaStream_t st) {
+  (void)ctl;
+  switch (L.precision) {
+    case PF_PREC_FP64: return download_impl<double, double>(L, step, fIN, fOUT, rho, u, F, st);
+    case PF_PREC_FP32: return download_impl<float, float>(L, step, fIN, fOUT, rho, u, F, st);
+    case PF_PREC_FP16: return download_impl<__half, float>(L, step, fIN, fOUT, rho, u, F, st);
+  }
+  return cudaErrorInvalidValue;
+}
+cudaError_t lattice_conservation(Lattice& L, long long step, double* out, cudaStream_t st) {
+  switch (L.precision) {
+    case PF_PREC_FP64: return conservation_impl<double, double>(L, step, out, st);
+    case PF_PREC_FP32: return conservation_impl<float, float>(L, step, out, st);
+    case PF_PREC_FP16: return conservation_impl<__half, float>(L, step, out, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace pf

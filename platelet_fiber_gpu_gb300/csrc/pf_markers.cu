@@ -1,0 +1,950 @@
+// pf_markers.cu -- kernels on immersed markers (platelet elements and fibrin
+// nodes): IBM spreading and interpolation (LB_kernel.cu:1419-1642, restated
+// element-centric over the 4x4x4 stencil), position update
+// (sem_kernel.cu:2087-2148), the per-platelet membrane force pass
+// (sem_kernel.cu:320-1749), Morse pair forces over cell bins, fibrin link
+// forces (fiber.cpp:647-733) and the receptor-bond pass
+// (sem_kernel.cu:1750-2083).
+#include "pf_internal.h"
+
+namespace pf {
+
+namespace {
+
+__device__ __forceinline__ void atomic_add3(float4* F, size_t n, float x, float y, float z) {
+  atomicAdd(F + n, make_float4(x, y, z, 0.f));
+}
+__device__ __forceinline__ void atomic_add3(D4* F, size_t n, double x, double y, double z) {
+  double* p = reinterpret_cast<double*>(F + n);
+  atomicAdd(p, x);
+  atomicAdd(p + 1, y);
+  atomicAdd(p + 2, z);
+}
+
+template <class R>
+__device__ __forceinline__ R phi(double r);
+template <>
+__device__ __forceinline__ double phi<double>(double r) {
+  return 0.25 * (1.0 + cos(0.5 * kPi * r));
+}
+template <>
+__device__ __forceinline__ float phi<float>(double r) {
+  return 0.25f * (1.f + cospif(0.5f * (float)r));
+}
+
+// Nodes of one axis within 2 dx of x, with weights.  spread=1 forms node
+// coordinates as int*float (LB_kernel.cu:1474), spread=0 as int*double
+// (:1581), like the reference's two IBM kernels.
+template <class R>
+__device__ __forceinline__ int axis_stencil(double x, float dxf, int n, int wrap, int spread, int node[5],
+                                            int raw[5], R w[5]) {
+  const double dxd = (double)dxf;
+  const double thr = (double)(2.0f * dxf);
+  const int base = (int)floor(x / dxd);
+  int cnt = 0;
+#pragma unroll
+  for (int ii = base - 2; ii <= base + 2; ++ii) {
+    const double xn = spread ? (double)((float)ii * dxf) : (double)ii * dxd;
+    const double dd = x - xn;
+    if (fabs(dd) >= (spread ? thr : 2.0 * dxd)) continue;
+    int nd = ii;
+    if (ii < 0 || ii >= n) {
+      if (!wrap) continue;
+      nd = wrapi(ii, n);
+    }
+    node[cnt] = nd;
+    raw[cnt] = ii;
+    w[cnt] = phi<R>(dd / dxd);
+    cnt++;
+  }
+  return cnt;
+}
+
+// ---------------------------------------------------------------- spreading
+template <class R>
+__global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R>* FB, unsigned* flA,
+                                                unsigned* flB, int* lA, int* lB, int PE, const double* X,
+                                                const double* Y, const double* Z, const R* Fmem,
+                                                const double* Fmorse, const R* Fbond, double* Ftot, int M,
+                                                const double* fX, const double* fY, const double* fZ,
+                                                const double* fF, double F0, Control* ctl) {
+  if (ctl->done) return;
+  const int par = (int)(ctl->step & 1);
+  R4<R>* Fc = par ? FB : FA;
+  unsigned* fl = par ? flB : flA;
+  int* list = par ? lB : lA;
+  int* counter = &ctl->active_count[par];
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  double x, y, z, fx, fy, fz;
+  if (idx < PE) {
+    x = X[idx]; y = Y[idx]; z = Z[idx];
+    fx = (double)Fmem[idx]; fy = (double)Fmem[PE + idx]; fz = (double)Fmem[2 * PE + idx];
+    if (Fmorse) { fx += Fmorse[idx]; fy += Fmorse[PE + idx]; fz += Fmorse[2 * PE + idx]; }
+    if (Fbond) { fx += (double)Fbond[idx]; fy += (double)Fbond[PE + idx]; fz += (double)Fbond[2 * PE + idx]; }
+    Ftot[idx] = fx; Ftot[PE + idx] = fy; Ftot[2 * PE + idx] = fz;
+  } else if (idx < PE + M) {
+    const int m = idx - PE;
+    x = fX[m]; y = fY[m]; z = fZ[m];
+    fx = fF[m] / F0; fy = fF[M + m] / F0; fz = fF[2 * M + m] / F0;
+  } else {
+    return;
+  }
+  int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
+  R wx[5], wy[5], wz[5];
+  const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 1, nxa, rx, wx);
+  const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 1, nya, ry, wy);
+  const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 1, nza, rz, wz);
+  const R Fx = (R)fx, Fy = (R)fy, Fz = (R)fz;
+  for (int c = 0; c < czn; ++c)
+    for (int b = 0; b < cyn; ++b) {
+      int last_brick = -1;
+      for (int a = 0; a < cxn; ++a) {
+        const int brick = nxa[a] / kBrickX + lk.nbx * (nya[b] + lk.ny * nza[c]);
+        if (brick != last_brick) {
+          last_brick = brick;
+          if (fl[brick] == 0u && atomicExch(fl + brick, 1u) == 0u) list[atomicAdd(counter, 1)] = brick;
+        }
+        const R delta = wx[a] * wy[b] * wz[c];
+        const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
+        atomic_add3(Fc, n, Fx * delta, Fy * delta, Fz * delta);
+      }
+    }
+}
+
+// ------------------------------------------------------- interp + advance
+__device__ __forceinline__ int cell_of(const PlateletConst& k, double x, double y, double z) {
+  const double p[3] = {x, y, z};
+  int c[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double v = p[a];
+    if (k.wrap[a]) v -= k.L[a] * floor(v / k.L[a]);
+    int ci = (int)floor(v / k.cs[a]);
+    if (ci < 0) ci = 0;
+    if (ci >= k.ncell[a]) ci = k.ncell[a] - 1;
+    c[a] = ci;
+  }
+  return c[0] + k.ncell[0] * (c[1] + k.ncell[1] * c[2]);
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, PlateletConst pk, const R4<R>* ubuf,
+                                                        int PE, double* X, double* Y, double* RY, double* Z,
+                                                        double* V, int M, double* fX, double* fY, double* fZ,
+                                                        double* fV, const int* ffix, int* bin_count, int* bin,
+                                                        Control* ctl, unsigned* done_blocks, double detach_rate,
+                                                        uint64_t seed) {
+  if (ctl->done) return;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < PE + M) {
+    const bool el = idx < PE;
+    const int m = idx - PE;
+    double x = el ? X[idx] : fX[m], y = el ? Y[idx] : fY[m], z = el ? Z[idx] : fZ[m];
+    int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
+    R wx[5], wy[5], wz[5];
+    const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 0, nxa, rx, wx);
+    const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 0, nya, ry, wy);
+    const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 0, nza, rz, wz);
+    R ax = 0, ay = 0, az = 0;
+    for (int c = 0; c < czn; ++c)
+      for (int b = 0; b < cyn; ++b)
+        for (int a = 0; a < cxn; ++a) {
+          const R delta = wx[a] * wy[b] * wz[c];
+          const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
+          const R4<R> u = ubuf[n];
+          ax += u.y * delta; ay += u.z * delta; az += u.w * delta;
+        }
+    const double vx = (double)ax * lk.C, vy = (double)ay * lk.C, vz = (double)az * lk.C;
+    const float dtT = lk.dtT;
+    const double Lx = (double)lk.nx * (double)lk.dxf, Ly = (double)lk.ny * (double)lk.dxf;
+    if (el) {
+      V[idx] = vx; V[PE + idx] = vy; V[2 * PE + idx] = vz;
+      x += vx * dtT;
+      if (lk.ibm_wrap[0]) { if (x > Lx) x -= Lx; else if (x < 0) x += Lx; }
+      y += vy * dtT;
+      if (lk.ibm_wrap[1]) { if (y > Ly) y -= Ly; else if (y < 0) y += Ly; }
+      RY[idx] += vy * dtT;
+      z += vz * dtT;
+      X[idx] = x; Y[idx] = y; Z[idx] = z;
+      if (bin) {
+        const int c = cell_of(pk, x, y, z);
+        const int slot = atomicAdd(bin_count + c, 1);
+        if (slot < kBinCap) bin[(size_t)c * kBinCap + slot] = idx;
+        else atomicOr(&ctl->err, ERR_BIN_OVERFLOW);
+      }
+    } else {
+      fV[m] = vx; fV[M + m] = vy; fV[2 * M + m] = vz;
+      if (!ffix[m]) {
+        x += vx * dtT;
+        if (lk.ibm_wrap[0]) { if (x > Lx) x -= Lx; else if (x < 0) x += Lx; }
+        y += vy * dtT;
+        if (lk.ibm_wrap[1]) { if (y > Ly) y -= Ly; else if (y < 0) y += Ly; }
+        z += vz * dtT;
+        fX[m] = x; fY[m] = y; fZ[m] = z;
+      }
+    }
+  }
+  // the last block to finish closes the step: counter, first flag, and the
+  // detach test of the next step (semLB.cu:451-455)
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(done_blocks, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      const long long s = ctl->step + 1;
+      ctl->step = s;
+      ctl->first = 0;
+      if (detach_rate > 0 && ctl->total_bond == 0 && detach_uniform(seed, s) < detach_rate) ctl->done = 1;
+      *done_blocks = 0u;
+    }
+  }
+}
+
+__global__ void bin_elements_k(PlateletConst pk, int PE, const double* X, const double* Y, const double* Z,
+                               int* bin_count, int* bin, Control* ctl) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= PE) return;
+  const int c = cell_of(pk, X[g], Y[g], Z[g]);
+  const int slot = atomicAdd(bin_count + c, 1);
+  if (slot < kBinCap) bin[(size_t)c * kBinCap + slot] = g;
+  else atomicOr(&ctl->err, ERR_BIN_OVERFLOW);
+}
+
+// ---------------------------------------------------------------- membrane
+// Gaussian elimination with partial pivoting on [3][4], normalising pivot
+// rows (sem_kernel.cu:249-284), and the row solve of :286-311.
+template <class R>
+__device__ __forceinline__ void gauss34(R g[3][4]) {
+  int i = 0, j = 0;
+  while (i < 3 && j < 3) {
+    int maxi = i;
+    for (int k = i + 1; k < 3; ++k)
+      if (fabs(g[k][j]) > fabs(g[maxi][j])) maxi = k;
+    if (g[maxi][j] != 0) {
+      R piv = 0;
+      for (int k = j; k < 4; ++k) {
+        R t = g[i][k];
+        g[i][k] = g[maxi][k];
+        g[maxi][k] = t;
+        if (k == j) piv = g[i][j];
+        g[i][k] /= piv;
+      }
+      for (int k = i + 1; k < 3; ++k) {
+        R f = g[k][j];
+        for (int l = j; l < 4; ++l) g[k][l] -= f * g[i][l];
+      }
+      i++;
+    }
+    j++;
+  }
+}
+
+template <class R>
+__device__ __forceinline__ R nrm3(R a, R b, R c) {
+  return sqrt(a * a + b * b + c * c);
+}
+
+// One CTA per platelet: springs + wall, triangle areas/normals and the global
+// area/volume (FP64 sums), nodal normals, curvature tensor and mean
+// curvature at the vertices, area/volume penalty and bending forces.  Every
+// accumulation is a gather in ascending triangle order, so the result does
+// not depend on scheduling.
+template <class R>
+__global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double* X, const double* Y,
+                                                  const double* RY, const double* Z, const int* tri,
+                                                  const int* node_ntri, const int* node_tri,
+                                                  const int* vert_local, const int* ring, const int* sp_ptr,
+                                                  const int* sp_nbr, const double* sp_L0, const double* S0,
+                                                  const double* S0_all, const double* V0, R* nN, R* nelem, R* S,
+                                                  R* kmv, double* SV, R* Fmem, Control* ctl) {
+  if (ctl->done) return;
+  const int p = blockIdx.x;
+  const int E = k.E, Em = k.Em, T = k.T, NN = k.NN, PE = k.P * k.E;
+  const int base = p * E;
+  const R F0 = (R)k.f0;
+  // geometry relative to a platelet origin in the single-precision build
+  const bool rel = sizeof(R) == 4;
+  const double ox = rel ? X[base] : 0.0, oy = rel ? Y[base] : 0.0, oz = rel ? Z[base] : 0.0;
+  auto P3 = [&](int e, R out[3]) {
+    out[0] = (R)(X[base + e] - ox);
+    out[1] = (R)(Y[base + e] - oy);
+    out[2] = (R)(Z[base + e] - oz);
+  };
+  R* nNp = nN + (size_t)p * NN * 3;
+  R* nep = nelem + (size_t)p * T * 3;
+  R* Sp = S + (size_t)p * T;
+  R* kmp = kmv + (size_t)p * Em;
+  __shared__ double s_a[256], s_b[256];
+  __shared__ int s_i[256];
+  __shared__ double s_Sall, s_V;
+  __shared__ int s_wall_idx;
+  __shared__ double s_wall_f;
+
+  // lowest element (sem_kernel.cu:409-430): first index attaining the minimum
+  {
+    double zmin = 1e300;
+    int imin = 0x7fffffff;
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const double zz = Z[base + e];
+      if (zz < zmin || (zz == zmin && e < imin)) { zmin = zz; imin = e; }
+    }
+    s_a[threadIdx.x] = zmin;
+    s_i[threadIdx.x] = imin;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        const double z2 = s_a[threadIdx.x + s];
+        const int i2 = s_i[threadIdx.x + s];
+        if (z2 < s_a[threadIdx.x] || (z2 == s_a[threadIdx.x] && i2 < s_i[threadIdx.x])) {
+          s_a[threadIdx.x] = z2;
+          s_i[threadIdx.x] = i2;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      s_wall_idx = -1;
+      s_wall_f = 0;
+      const double dmin = s_a[0];
+      if ((k.mask & PF_MEM_WALL) && E > 0 && dmin <= 0.02) {
+        s_wall_idx = s_i[0];
+        s_wall_f = 5e-4 * 2000 * exp(-2000 * dmin) / (1 - exp(-2000 * dmin)) / (double)k.f0;
+      }
+    }
+    __syncthreads();
+  }
+  // springs on RY (sem_kernel.cu:355-389) plus the wall force
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    R fx = 0, fy = 0, fz = 0;
+    if (e == s_wall_idx && e != 0) fz = (R)s_wall_f;
+    if (k.mask & PF_MEM_SPRING)
+      for (int q = sp_ptr[e]; q < sp_ptr[e + 1]; ++q) {
+        const int nb = sp_nbr[q];
+        const R d1 = (R)(X[base + nb] - X[base + e]);
+        const R d2 = (R)(RY[base + nb] - RY[base + e]);
+        const R d3 = (R)(Z[base + nb] - Z[base + e]);
+        const R r = nrm3(d1, d2, d3);
+        const R w = r - (R)sp_L0[q];
+        const R fc = (R)k.kspring * w / r;
+        fx += fc * d1 / (R)1.0 / F0;
+        fy += fc * d2 / (R)1.0 / F0;
+        fz += fc * d3 / (R)1.0 / F0;
+      }
+    if (e == s_wall_idx && e == 0) fz += (R)s_wall_f;
+    Fmem[base + e] = fx;
+    Fmem[PE + base + e] = fy;
+    Fmem[2 * PE + base + e] = fz;
+  }
+  if (!(k.mask & (PF_MEM_AREAVOL | PF_MEM_BEND))) {
+    if (threadIdx.x == 0) { SV[2 * p] = 0; SV[2 * p + 1] = 0; }
+    return;
+  }
+  // triangle areas, normals, global area and volume
+  double pa = 0, pv = 0;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    const int* nd = tri + 6 * t;
+    R c0[3], c1[3], c2[3];
+    P3(nd[0], c0); P3(nd[1], c1); P3(nd[2], c2);
+    R e12[3], e13[3], n[3], cc[3];
+    for (int i = 0; i < 3; ++i) {
+      cc[i] = (R)(1 / 3.0) * (c0[i] + c1[i] + c2[i]);
+      e12[i] = c1[i] - c0[i];
+      e13[i] = c2[i] - c0[i];
+    }
+    n[0] = e12[1] * e13[2] - e12[2] * e13[1];
+    n[1] = e12[2] * e13[0] - e12[0] * e13[2];
+    n[2] = e12[0] * e13[1] - e12[1] * e13[0];
+    const R nn = nrm3(n[0], n[1], n[2]);
+    n[0] /= -nn; n[1] /= -nn; n[2] /= -nn;
+    const R St = (R)0.5 * nn;
+    Sp[t] = St;
+    nep[3 * t] = n[0]; nep[3 * t + 1] = n[1]; nep[3 * t + 2] = n[2];
+    pa += (double)St;
+    pv += (double)((R)(1 / 3.0) * (cc[0] * n[0] + cc[1] * n[1] + cc[2] * n[2]) * St);
+  }
+  s_a[threadIdx.x] = pa;
+  s_b[threadIdx.x] = pv;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s_a[threadIdx.x] += s_a[threadIdx.x + s];
+      s_b[threadIdx.x] += s_b[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    s_Sall = s_a[0];
+    s_V = s_b[0];
+    SV[2 * p] = s_a[0];
+    SV[2 * p + 1] = s_b[0];
+  }
+  __syncthreads();
+  // nodal normals: mean of the element normals of the node's triangles
+  for (int q = threadIdx.x; q < NN; q += blockDim.x) {
+    const int cnt = node_ntri[q];
+    R a0 = 0, a1 = 0, a2 = 0;
+    for (int j = 0; j < cnt; ++j) {
+      const int t = node_tri[10 * q + j];
+      a0 += nep[3 * t]; a1 += nep[3 * t + 1]; a2 += nep[3 * t + 2];
+    }
+    if (cnt > 0) {
+      a0 /= (R)cnt; a1 /= (R)cnt; a2 /= (R)cnt;
+      const R nn = nrm3(a0, a1, a2);
+      a0 /= nn; a1 /= nn; a2 /= nn;
+    }
+    nNp[3 * q] = a0; nNp[3 * q + 1] = a1; nNp[3 * q + 2] = a2;
+  }
+  __syncthreads();
+  // curvature tensor at each vertex from its triangles (6-node element),
+  // mean curvature km = tr/2 of the node average
+  for (int v = threadIdx.x; v < Em; v += blockDim.x) {
+    const int cnt = node_ntri[v];
+    R K[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < cnt; ++j) {
+      const int t = node_tri[10 * v + j];
+      const int li = vert_local[10 * v + j];
+      const int* nd = tri + 6 * t;
+      R c[6][3], nv[6][3];
+      P3(nd[0], c[0]); P3(nd[1], c[1]); P3(nd[2], c[2]);
+      for (int i = 0; i < 3; ++i) {
+        c[3][i] = (R)0.5 * (c[0][i] + c[1][i]);
+        c[4][i] = (R)0.5 * (c[0][i] + c[2][i]);
+        c[5][i] = (R)0.5 * (c[1][i] + c[2][i]);
+      }
+      for (int i = 0; i < 6; ++i)
+        for (int d = 0; d < 3; ++d) nv[i][d] = nNp[3 * nd[i] + d];
+      const R s_ = li == 1 ? (R)1 : (R)0, t_ = li == 2 ? (R)1 : (R)0;
+      const R gs[6] = {4 * s_ + 4 * t_ - 3, 4 * s_ - 1, 0, -8 * s_ - 4 * t_ + 4, -4 * t_, 4 * t_};
+      const R gt[6] = {4 * t_ + 4 * s_ - 3, 0, 4 * t_ - 1, -4 * s_, -8 * t_ - 4 * s_ + 4, 4 * s_};
+      R a1[3], a2[3], a3[3], a4[3];
+      for (int d = 0; d < 3; ++d) {
+        a1[d] = c[0][d] * gs[0] + c[1][d] * gs[1] + c[2][d] * gs[2] + c[3][d] * gs[3] + c[4][d] * gs[4] +
+                c[5][d] * gs[5];
+        a2[d] = nv[0][d] * gs[0] + nv[1][d] * gs[1] + nv[2][d] * gs[2] + nv[3][d] * gs[3] + nv[4][d] * gs[4] +
+                nv[5][d] * gs[5];
+        a3[d] = c[0][d] * gt[0] + c[1][d] * gt[1] + c[2][d] * gt[2] + c[3][d] * gt[3] + c[4][d] * gt[4] +
+                c[5][d] * gt[5];
+        a4[d] = nv[0][d] * gt[0] + nv[1][d] * gt[1] + nv[2][d] * gt[2] + nv[3][d] * gt[3] + nv[4][d] * gt[4] +
+                nv[5][d] * gt[5];
+      }
+      R A[3][3];
+      for (int i = 0; i < 3; ++i) {
+        R g[3][4];
+        for (int d = 0; d < 3; ++d) { g[0][d] = a1[d]; g[1][d] = a3[d]; g[2][d] = nv[li][d]; }
+        g[0][3] = a2[i]; g[1][3] = a4[i]; g[2][3] = 0;
+        gauss34<R>(g);
+        A[i][2] = g[2][3];
+        A[i][1] = g[1][3] - A[i][2] * g[1][2];
+        A[i][0] = g[0][3] - A[i][2] * g[0][2] - A[i][1] * g[0][1];
+      }
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) K[a * 3 + b] += A[b][a];
+    }
+    R km = 0;
+    if (cnt > 0) km = (R)0.5 * (K[0] / (R)cnt + K[4] / (R)cnt + K[8] / (R)cnt);
+    kmp[v] = km;
+  }
+  __syncthreads();
+  // area/volume penalty (sem_kernel.cu:1640-1749) and bending
+  // (:1499-1638) at each vertex
+  const double Sall = s_Sall, Vol = s_V;
+  for (int v = threadIdx.x; v < Em; v += blockDim.x) {
+    R fx = Fmem[base + v], fy = Fmem[PE + base + v], fz = Fmem[2 * PE + base + v];
+    const int cnt = node_ntri[v];
+    if (k.mask & PF_MEM_AREAVOL) {
+      const R Ks = (R)k.ks, Kv = (R)k.kv;
+      const R sglob = (R)((Sall - S0_all[p]) / S0_all[p]);
+      const R vglob = (R)((Vol - V0[p]) / V0[p]);
+      for (int j = 0; j < cnt; ++j) {
+        const int t = node_tri[10 * v + j];
+        const int i = vert_local[10 * v + j];
+        const int* nd = tri + 6 * t;
+        R c[3][3], L[3][3], cc[3], n[3];
+        P3(nd[0], c[0]); P3(nd[1], c[1]); P3(nd[2], c[2]);
+        for (int d = 0; d < 3; ++d) {
+          L[0][d] = c[1][d] - c[2][d];
+          L[1][d] = c[2][d] - c[0][d];
+          L[2][d] = c[0][d] - c[1][d];
+          cc[d] = (R)(1 / 3.0) * (c[0][d] + c[1][d] + c[2][d]);
+          n[d] = nep[3 * t + d];
+        }
+        const R S0e = (R)S0[(size_t)p * T + t], Se = Sp[t];
+        R dS[3];
+        dS[0] = (R)-0.5 * (L[i][1] * n[2] - L[i][2] * n[1]);
+        dS[1] = (R)-0.5 * (L[i][2] * n[0] - L[i][0] * n[2]);
+        dS[2] = (R)-0.5 * (L[i][0] * n[1] - L[i][1] * n[0]);
+        const R fa = -Ks * ((Se - S0e) / S0e + sglob);
+        fx += fa * dS[0] / F0;
+        fy += fa * dS[1] / F0;
+        fz += fa * dS[2] / F0;
+        R dV[3];
+        const R t0 = -L[1][1] * L[0][2] / (R)3.0 + L[1][2] * L[0][1] / (R)3.0;
+        const R t1 = -L[1][2] * L[0][0] / (R)3.0 + L[1][0] * L[0][2] / (R)3.0;
+        const R t2 = -L[1][0] * L[0][1] / (R)3.0 + L[1][1] * L[0][0] / (R)3.0;
+        dV[0] = t0 - L[i][2] * cc[1] + L[i][1] * cc[2];
+        dV[1] = t1 + L[i][2] * cc[0] - L[i][0] * cc[2];
+        dV[2] = t2 - L[i][1] * cc[0] + L[i][0] * cc[1];
+        const R fv = -Kv * vglob;
+        fx += fv * dV[0] / (R)6.0 / F0;
+        fy += fv * dV[1] / (R)6.0 / F0;
+        fz += fv * dV[2] / (R)6.0 / F0;
+      }
+    }
+    if (k.mask & PF_MEM_BEND) {
+      const int* rg = ring + 10 * v;
+      R xi[3], ni[3] = {nNp[3 * v], nNp[3 * v + 1], nNp[3 * v + 2]};
+      P3(v, xi);
+      R Ai = 0, sum = 0;
+      const R kmi = kmp[v];
+      for (int a = 0; a < cnt; ++a) {
+        const int jn = rg[a], jp = rg[a == 0 ? cnt - 1 : a - 1], jx = rg[a == cnt - 1 ? 0 : a + 1];
+        R xj[3], x1[3], x2[3];
+        P3(jn, xj); P3(jp, x1); P3(jx, x2);
+        R ri1[3], r1j[3], rij[3], ri2[3], r2j[3], cij[3], ci2[3], c2j[3], ce[3];
+        for (int d = 0; d < 3; ++d) {
+          ri1[d] = xi[d] - x1[d]; r1j[d] = x1[d] - xj[d]; rij[d] = xi[d] - xj[d];
+          ri2[d] = xi[d] - x2[d]; r2j[d] = x2[d] - xj[d];
+          cij[d] = (R)0.5 * (xi[d] + xj[d]); ci2[d] = (R)0.5 * (xi[d] + x2[d]); c2j[d] = (R)0.5 * (x2[d] + xj[d]);
+        }
+        const R ai = rij[0] * ri2[0] + rij[1] * ri2[1] + rij[2] * ri2[2];
+        const R a2 = -(ri2[0] * r2j[0] + ri2[1] * r2j[1] + ri2[2] * r2j[2]);
+        const R aj = rij[0] * r2j[0] + rij[1] * r2j[1] + rij[2] * r2j[2];
+        const R a1 = -(r1j[0] * ri1[0] + r1j[1] * ri1[1] + r1j[2] * ri1[2]);
+        if (ai < 0) {
+          for (int d = 0; d < 3; ++d) ce[d] = c2j[d];
+        } else if (a2 < 0) {
+          for (int d = 0; d < 3; ++d) ce[d] = cij[d];
+        } else if (aj < 0) {
+          for (int d = 0; d < 3; ++d) ce[d] = ci2[d];
+        } else {
+          R g[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
+          for (int d = 0; d < 3; ++d) {
+            g[0][d] = rij[d]; g[1][d] = ri2[d];
+            g[0][3] += cij[d] * rij[d]; g[1][3] += ci2[d] * ri2[d];
+          }
+          g[2][0] = (xj[1] - xi[1]) * (x2[2] - xi[2]) - (xj[2] - xi[2]) * (x2[1] - xi[1]);
+          g[2][1] = (xj[2] - xi[2]) * (x2[0] - xi[0]) - (xj[0] - xi[0]) * (x2[2] - xi[2]);
+          g[2][2] = (xj[0] - xi[0]) * (x2[1] - xi[1]) - (xj[1] - xi[1]) * (x2[0] - xi[0]);
+          g[2][3] = g[2][0] * xi[0] + g[2][1] * xi[1] + g[2][2] * xi[2];
+          gauss34<R>(g);
+          ce[2] = g[2][3];
+          ce[1] = g[1][3] - ce[2] * g[1][2];
+          ce[0] = g[0][3] - ce[2] * g[0][2] - ce[1] * g[0][1];
+        }
+        R L1 = nrm3(xi[0] - cij[0], xi[1] - cij[1], xi[2] - cij[2]);
+        R L2 = nrm3(ce[0] - cij[0], ce[1] - cij[1], ce[2] - cij[2]);
+        const R L3 = nrm3(xi[0] - ce[0], xi[1] - ce[1], xi[2] - ce[2]);
+        R Pe = (R)0.5 * (L1 + L2 + L3);
+        Ai += sqrt(Pe * (Pe - L1) * (Pe - L2) * (Pe - L3));
+        L1 = nrm3(xi[0] - ci2[0], xi[1] - ci2[1], xi[2] - ci2[2]);
+        L2 = nrm3(ce[0] - ci2[0], ce[1] - ci2[1], ce[2] - ci2[2]);
+        Pe = (R)0.5 * (L1 + L2 + L3);
+        Ai += sqrt(Pe * (Pe - L1) * (Pe - L2) * (Pe - L3));
+        const R alpha = (R)1 / tan(acos(a1 / (nrm3(xi[0] - x1[0], xi[1] - x1[1], xi[2] - x1[2]) *
+                                             nrm3(x1[0] - xj[0], x1[1] - xj[1], x1[2] - xj[2]))));
+        const R beta = (R)1 / tan(acos(a2 / (nrm3(xi[0] - x2[0], xi[1] - x2[1], xi[2] - x2[2]) *
+                                            nrm3(x2[0] - xj[0], x2[1] - xj[1], x2[2] - xj[2]))));
+        sum += (R)0.5 * (alpha + beta) * (kmp[jn] - kmi);
+      }
+      const R Kb = (R)k.kbend;
+      fx += Kb / Ai * sum * ni[0] / F0;
+      fy += Kb / Ai * sum * ni[1] / F0;
+      fz += Kb / Ai * sum * ni[2] / F0;
+    }
+    Fmem[base + v] = fx;
+    Fmem[PE + base + v] = fy;
+    Fmem[2 * PE + base + v] = fz;
+  }
+}
+
+// ---------------------------------------------------------------- Morse
+template <class R>
+__global__ void __launch_bounds__(128) morse_k(PlateletConst k, const double* X, const double* Y, const double* Z,
+                                               const int* bin_count, const int* bin, double* Fm, Control* ctl) {
+  if (ctl->done) return;
+  const int PE = k.P * k.E;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= PE) return;
+  const double xi = X[g], yi = Y[g], zi = Z[g];
+  const int cid = cell_of(k, xi, yi, zi);
+  const int c0 = cid % k.ncell[0], c1 = (cid / k.ncell[0]) % k.ncell[1], c2 = cid / (k.ncell[0] * k.ncell[1]);
+  const int pg = g / k.E;
+  long long ax = 0, ay = 0, az = 0;
+  int seen[27], nseen = 0;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        int cc[3] = {c0 + dx, c1 + dy, c2 + dz};
+        bool ok = true;
+        for (int a = 0; a < 3; ++a)
+          if (cc[a] < 0 || cc[a] >= k.ncell[a]) {
+            if (k.wrap[a]) cc[a] = (cc[a] + k.ncell[a]) % k.ncell[a];
+            else ok = false;
+          }
+        if (!ok) continue;
+        const int nc = cc[0] + k.ncell[0] * (cc[1] + k.ncell[1] * cc[2]);
+        bool dup = false;
+        for (int q = 0; q < nseen; ++q) dup |= (seen[q] == nc);
+        if (dup) continue;
+        seen[nseen++] = nc;
+        int cnt = bin_count[nc];
+        if (cnt > kBinCap) cnt = kBinCap;
+        const int* members = bin + (size_t)nc * kBinCap;
+        for (int q = 0; q < cnt; ++q) {
+          const int h = members[q];
+          if (h == g) continue;
+          double d[3] = {xi - X[h], yi - Y[h], zi - Z[h]};
+          for (int a = 0; a < 3; ++a)
+            if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
+          const double* mp = (h / k.E == pg) ? k.morse_intra : k.morse_inter;
+          const R r = nrm3((R)d[0], (R)d[1], (R)d[2]);
+          if (!(r < (R)mp[3]) || r <= 0) continue;
+          const R ex = exp((R)mp[1] * ((R)mp[2] - r));
+          const R f = (R)2.0 * (R)mp[1] * (R)mp[0] * (ex * ex - ex) / r;
+          ax += __double2ll_rn((double)(f * (R)d[0]) * kFixScale);
+          ay += __double2ll_rn((double)(f * (R)d[1]) * kFixScale);
+          az += __double2ll_rn((double)(f * (R)d[2]) * kFixScale);
+        }
+      }
+  const double s = 1.0 / kFixScale / (double)k.f0;
+  Fm[g] = (double)ax * s;
+  Fm[PE + g] = (double)ay * s;
+  Fm[2 * PE + g] = (double)az * s;
+}
+
+// ---------------------------------------------------------------- fibrin
+__global__ void fibrin_k(int M, int law, double kk, double mass, const double* X, const double* Y, const double* Z,
+                         const int* ptr, const int* nbr, const double* L0, double* F, const Control* ctl) {
+  if (ctl->done) return;
+  const int ni = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ni >= M) return;
+  double fx = 0, fy = 0, fz = 0;
+  for (int q = ptr[ni]; q < ptr[ni + 1]; ++q) {
+    const int o = nbr[q];
+    const double d0 = X[ni] - X[o], d1 = Y[ni] - Y[o], d2 = Z[ni] - Z[o];
+    const double len = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    if (len < 1.0e-13) continue;
+    double wf;
+    if (law == PF_FIB_WLC) {
+      const double En = 1.3806503 * 1e-8 * 10;
+      const double CC = En / L0[q];
+      const double tl = 1.0 - (len - L0[q]) / L0[q];
+      const double IP1 = 0.25 * 1.0 / (tl * tl) - 0.25 + (len - L0[q]) / L0[q];
+      wf = -CC * IP1 / mass;
+    } else {
+      wf = kk * (len - L0[q]);
+    }
+    fx -= wf * d0 / len;
+    fy -= wf * d1 / len;
+    fz -= wf * d2 / len;
+  }
+  F[ni] = fx;
+  F[M + ni] = fy;
+  F[2 * M + ni] = fz;
+}
+
+// ---------------------------------------------------------------- bonds
+struct RecTmp {
+  double rx, ry, rz;
+  int active, bond0, si, sj, ci, cj;
+  int kind[2];  // 0 none, 1 claim, 2 release
+  int ok[2];
+};
+
+__device__ __forceinline__ unsigned long long op_key(int site, int rid, int opi) {
+  return ((unsigned long long)(unsigned)site << 32) | ((unsigned long long)(unsigned)rid << 1) |
+         (unsigned long long)opi;
+}
+
+// Single CTA.  Receptors are independent except through the vWF slots of a
+// site; slot operations are therefore grouped by site and applied in
+// ascending (receptor id, operation) order, which is the outcome of a serial
+// schedule of the reference kernel.  Every receptor reads totalBond before any
+// addition (avaiBond = NUMOFRECEPTORS).
+template <class R>
+__global__ void __launch_bounds__(1024) bonds_k(PlateletConst k, const double* X, const double* Y, const double* Z,
+                                                const int* tri, const int* rec_tri, const float* r1a,
+                                                const float* r2a, int* rec_state, int* vwf, RecTmp* tmp,
+                                                unsigned long long* ops, int ops_cap, R* Fbond, Control* ctl) {
+  if (ctl->done) return;
+  const int PE = k.P * k.E;
+  const int NR = k.P * k.nrec;
+  __shared__ int s_nops;
+  __shared__ long long s_tot[32];
+  for (int i = threadIdx.x; i < 3 * PE; i += blockDim.x) Fbond[i] = 0;
+  if (threadIdx.x == 0) s_nops = 0;
+  __syncthreads();
+  const long long step = ctl->step;
+  const double dx = k.dxd, dt = k.dtd;
+  const int avai = (int)(k.numrec - 0);
+  // phase A: geometry, decisions, slot operations
+  for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+    RecTmp t;
+    t.kind[0] = t.kind[1] = 0;
+    t.ok[0] = t.ok[1] = 0;
+    t.active = 0;
+    const int p = r / k.nrec;
+    const int eo = p * k.E;
+    const int* nd = tri + 6 * rec_tri[r];
+    int* st = rec_state + 3 * r;
+    const float r1 = r1a[r], r2 = r2a[r];
+    const float wa = 1 - r1, wb = r1 * (1 - r2), wc = r1 * r2;
+    const double rz = wa * Z[eo + nd[0]] + wb * Z[eo + nd[1]] + wc * Z[eo + nd[2]];
+    const int bond = st[2] > -1 ? st[2] : 0;
+    if (!(rz > 0.078 && bond == 0)) {
+      const double rx = wa * X[eo + nd[0]] + wb * X[eo + nd[1]] + wc * X[eo + nd[2]];
+      const double ry = wa * Y[eo + nd[0]] + wb * Y[eo + nd[1]] + wc * Y[eo + nd[2]];
+      t.active = 1;
+      t.rx = rx; t.ry = ry; t.rz = rz;
+      t.bond0 = bond;
+      t.si = st[0]; t.sj = st[1];
+      int si = bond ? st[0] : (int)(rx / dx + 0.5), sj = bond ? st[1] : (int)(ry / dx + 0.5);
+      t.ci = (int)(rx / dx + 0.5);
+      t.cj = (int)(ry / dx + 0.5);
+      const double d1 = rx - si * dx, d2 = ry - sj * dx, d3 = rz;
+      const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
+      const double w = fabs(0.078 - dr);
+      const double fc = 10.0 * w;
+      double aon, aoff;
+      if (k.bond_model == PF_BOND_BELL) {
+        const double Kf = (double)k.kf0 * exp(fc * (0.00071 - 0.5 * w) / 4.05) * avai;
+        const double Kr = (double)k.kr0 * exp(0.00071 * fc / 4.05) * avai;
+        aon = 1 - exp(-Kf * dt);
+        aoff = 1 - exp(-Kr * dt);
+      } else {
+        aon = k.p_on;
+        aoff = k.p_off;
+      }
+      double u1, u2;
+      receptor_uniforms(k.seed, step, r, u1, u2);
+      if (bond == 0) {
+        if (u1 < aon) t.kind[0] = 1;
+        if (u2 < aon) t.kind[1] = 1;
+      } else if (bond == 1) {
+        if (u1 < aoff) {
+          t.kind[0] = 2;
+          if (u2 < aon && rz < 0.078) t.kind[1] = 1;
+        } else if (u2 < aoff && rz < 0.078) {
+          t.kind[0] = 2;
+        }
+      } else if (bond == 2) {
+        if (u1 < aoff) t.kind[0] = 2;
+        if (u2 < aoff) t.kind[1] = 2;
+      }
+      for (int o = 0; o < 2; ++o) {
+        if (!t.kind[o]) continue;
+        const int ii = t.kind[o] == 1 ? t.ci : t.si, jj = t.kind[o] == 1 ? t.cj : t.sj;
+        const int site = wrapi(jj, k.ny) * k.nx + wrapi(ii, k.nx);
+        const int slot = atomicAdd(&s_nops, 1);
+        if (slot < ops_cap) ops[slot] = op_key(site, r, o);
+        else atomicOr(&ctl->err, ERR_BOND_OVERFLOW);
+      }
+    }
+    tmp[r] = t;
+  }
+  __syncthreads();
+  const int nops = min(s_nops, ops_cap);
+  // phase B: bitonic sort of the operation keys, then one pass per site
+  int pow2 = 1;
+  while (pow2 < nops) pow2 <<= 1;
+  for (int i = nops + threadIdx.x; i < pow2; i += blockDim.x) ops[i] = ~0ull;
+  __syncthreads();
+  for (int size = 2; size <= pow2; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < pow2; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const unsigned long long a = ops[i], b = ops[j];
+          if ((a > b) == up) { ops[i] = b; ops[j] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  const int plane = k.nx * k.ny;
+  for (int i = threadIdx.x; i < nops; i += blockDim.x) {
+    const unsigned site = (unsigned)(ops[i] >> 32);
+    if (i > 0 && (unsigned)(ops[i - 1] >> 32) == site) continue;
+    for (int j = i; j < nops && (unsigned)(ops[j] >> 32) == site; ++j) {
+      const int rid = (int)((ops[j] >> 1) & 0x7fffffffu);
+      const int o = (int)(ops[j] & 1u);
+      const int kind = tmp[rid].kind[o];
+      int ok = 0;
+      for (int kk = 0; kk < 4; ++kk) {
+        int* slot = vwf + (size_t)kk * plane + site;
+        if (kind == 1 && *slot == -1) { *slot = rid; ok = 1; break; }
+        if (kind == 2 && *slot == rid) { *slot = -1; ok = 1; break; }
+      }
+      tmp[rid].ok[o] = ok;
+    }
+  }
+  __syncthreads();
+  // phase C: bond counts, sites, forces on the triangle's vertices
+  long long tot = 0;
+  for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+    const RecTmp t = tmp[r];
+    if (!t.active) continue;
+    int bond = t.bond0, si = t.bond0 ? t.si : -1, sj = t.bond0 ? t.sj : -1;
+    for (int o = 0; o < 2; ++o) {
+      if (!t.kind[o] || !t.ok[o]) continue;
+      if (t.kind[o] == 1) { bond++; si = t.ci; sj = t.cj; }
+      else { bond--; if (bond == 0) { si = -1; sj = -1; } }
+    }
+    int* st = rec_state + 3 * r;
+    st[0] = si; st[1] = sj;
+    if (bond) {
+      const int p = r / k.nrec;
+      const int eo = p * k.E;
+      const int* nd = tri + 6 * rec_tri[r];
+      const double d1 = t.rx - si * dx, d2 = t.ry - sj * dx, d3 = t.rz;
+      const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
+      const double fcb = 10.0 * (0.078 - dr) * bond / dr;
+      const double fX = fcb * d1, fY = fcb * d2, fZ = fcb * d3;
+      double drv[3];
+      for (int m = 0; m < 3; ++m) {
+        const double a = t.rx - X[eo + nd[m]], b = t.ry - Y[eo + nd[m]], c = t.rz - Z[eo + nd[m]];
+        drv[m] = sqrt(a * a + b * b + c * c);
+      }
+      const double sum = 1.0 / drv[0] + 1.0 / drv[1] + 1.0 / drv[2];
+      for (int m = 0; m < 3; ++m) {
+        const int e = eo + nd[m];
+        atomicAdd(Fbond + e, (R)(fX * 1.0 / drv[m] / sum / (double)k.f0));
+        atomicAdd(Fbond + PE + e, (R)(fY * 1.0 / drv[m] / sum / (double)k.f0));
+        atomicAdd(Fbond + 2 * PE + e, (R)(fZ * 1.0 / drv[m] / sum / (double)k.f0));
+      }
+      st[2] = bond;
+      tot += bond;
+    } else {
+      st[2] = -1;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if ((threadIdx.x & 31) == 0) s_tot[threadIdx.x >> 5] = tot;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long s = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += s_tot[w];
+    ctl->total_bond = (int)s;
+    ctl->nops = nops;
+  }
+}
+
+}  // namespace
+
+int membrane_threads() { return 256; }
+
+cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st) {
+  const PlateletConst& k = Pl.k;
+  if (k.P == 0) return cudaSuccess;
+  if (precision == PF_PREC_FP64)
+    membrane_k<double><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
+                                            Pl.vert_local, Pl.ring, Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0,
+                                            Pl.S0_all, Pl.V0, (double*)Pl.nN, (double*)Pl.nelem, (double*)Pl.S,
+                                            (double*)Pl.km, Pl.SV, (double*)Pl.Fmem, ctl);
+  else
+    membrane_k<float><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
+                                           Pl.vert_local, Pl.ring, Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0,
+                                           Pl.S0_all, Pl.V0, (float*)Pl.nN, (float*)Pl.nelem, (float*)Pl.S,
+                                           (float*)Pl.km, Pl.SV, (float*)Pl.Fmem, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st) {
+  const PlateletConst& k = Pl.k;
+  const int PE = k.P * k.E;
+  if (!k.morse || PE == 0) return cudaSuccess;
+  const unsigned grid = (PE + 127) / 128;
+  if (precision == PF_PREC_FP64)
+    morse_k<double><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, Pl.bin, Pl.Fmorse, ctl);
+  else
+    morse_k<float><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, Pl.bin, Pl.Fmorse, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t fibrin_forces(Fibrin& Fb, int precision, Control* ctl, cudaStream_t st) {
+  (void)precision;
+  if (Fb.M == 0) return cudaSuccess;
+  fibrin_k<<<(Fb.M + 255) / 256, 256, 0, st>>>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr, Fb.nbr,
+                                                Fb.L0, Fb.F, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t bond_pass(Platelets& Pl, int precision, Control* ctl, cudaStream_t st) {
+  const PlateletConst& k = Pl.k;
+  const int NR = k.P * k.nrec;
+  if (NR == 0) return cudaSuccess;
+  RecTmp* tmp = (RecTmp*)Pl.rec_tmp;
+  unsigned long long* ops = (unsigned long long*)(tmp + NR);
+  const int cap = 2 * NR;
+  if (precision == PF_PREC_FP64)
+    bonds_k<double><<<1, 1024, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.r1, Pl.r2, Pl.rec_state,
+                                        Pl.vwf, tmp, ops, cap, (double*)Pl.Fbond, ctl);
+  else
+    bonds_k<float><<<1, 1024, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.r1, Pl.r2, Pl.rec_state,
+                                       Pl.vwf, tmp, ops, cap, (float*)Pl.Fbond, ctl);
+  return cudaGetLastError();
+}
+
+size_t bond_scratch_bytes(int NR) {
+  size_t ops = 1;
+  while (ops < (size_t)2 * NR) ops <<= 1;
+  return (size_t)NR * sizeof(RecTmp) + ops * sizeof(unsigned long long) + 64;
+}
+
+cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st) {
+  const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
+  const int M = Fb ? Fb->M : 0;
+  if (PE + M == 0) return cudaSuccess;
+  const unsigned grid = (PE + M + 127) / 128;
+  const double F0 = Pl ? (double)Pl->k.f0 : 1.0;
+  if (L.precision == PF_PREC_FP64)
+    spread_k<double><<<grid, 128, 0, st>>>(
+        L.k, (D4*)L.F[0], (D4*)L.F[1], L.flags[0], L.flags[1], L.list[0], L.list[1], PE, Pl ? Pl->X : nullptr,
+        Pl ? Pl->Y : nullptr, Pl ? Pl->Z : nullptr, Pl ? (double*)Pl->Fmem : nullptr,
+        (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr, (Pl && Pl->k.nrec) ? (double*)Pl->Fbond : nullptr,
+        Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr,
+        Fb ? Fb->F : nullptr, F0, ctl);
+  else
+    spread_k<float><<<grid, 128, 0, st>>>(
+        L.k, (float4*)L.F[0], (float4*)L.F[1], L.flags[0], L.flags[1], L.list[0], L.list[1], PE,
+        Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->Z : nullptr, Pl ? (float*)Pl->Fmem : nullptr,
+        (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr, (Pl && Pl->k.nrec) ? (float*)Pl->Fbond : nullptr,
+        Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr,
+        Fb ? Fb->F : nullptr, F0, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, double detach_rate,
+                           uint64_t seed, unsigned* done_blocks, cudaStream_t st) {
+  const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
+  const int M = Fb ? Fb->M : 0;
+  const unsigned grid = (PE + M + 127) / 128 > 0 ? (PE + M + 127) / 128 : 1;
+  PlateletConst pk{};
+  if (Pl) pk = Pl->k;
+  int* bc = (Pl && Pl->k.morse) ? Pl->bin_count : nullptr;
+  int* bn = (Pl && Pl->k.morse) ? Pl->bin : nullptr;
+  if (L.precision == PF_PREC_FP64)
+    interp_advance_k<double><<<grid, 128, 0, st>>>(
+        L.k, pk, (const D4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
+        Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
+        Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, ctl, done_blocks,
+        detach_rate, seed);
+  else
+    interp_advance_k<float><<<grid, 128, 0, st>>>(
+        L.k, pk, (const float4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
+        Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
+        Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, ctl, done_blocks,
+        detach_rate, seed);
+  return cudaGetLastError();
+}
+
+cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st) {
+  const int PE = Pl.k.P * Pl.k.E;
+  if (!Pl.k.morse || PE == 0) return cudaSuccess;
+  cudaMemsetAsync(Pl.bin_count, 0, sizeof(int) * (size_t)Pl.ncells, st);
+  bin_elements_k<<<(PE + 127) / 128, 128, 0, st>>>(Pl.k, PE, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, Pl.bin, ctl);
+  return cudaGetLastError();
+}
+
+}  // namespace pf

@@ -1,0 +1,155 @@
+"""ctypes binding of libpfgpu.so (the CUDA library).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .scene import Scene
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpfgpu.so"
+
+PFGPU_OK, PFGPU_DONE = 0, 6
+_STATUS = {1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "UNSUPPORTED", 5: "DEVICE", 6: "DONE"}
+
+_lib = None
+
+
+class PfgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"pfgpu error {_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is not built; run platelet_fiber_gpu_gb300.build.build()")
+        L = C.CDLL(str(LIB_PATH))
+        vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+        L.pfgpu_job_create.argtypes = [vp, C.c_int, C.c_double, C.POINTER(vp)]
+        L.pfgpu_job_step.argtypes = [vp, C.c_int]
+        L.pfgpu_job_step_graph.argtypes = [vp, C.c_int]
+        L.pfgpu_job_sync.argtypes = [vp]
+        L.pfgpu_job_get_lattice.argtypes = [vp, dp, dp, dp, dp, dp]
+        L.pfgpu_job_get_elements.argtypes = [vp, dp, dp, dp, dp, dp, dp]
+        L.pfgpu_job_get_bonds.argtypes = [vp, ip, ip, ip]
+        L.pfgpu_job_get_fibrin.argtypes = [vp, dp, dp, dp, dp, dp]
+        L.pfgpu_job_get_membrane.argtypes = [vp, dp, dp]
+        L.pfgpu_job_conservation.argtypes = [vp, dp]
+        L.pfgpu_job_step_count.restype = C.c_int64
+        L.pfgpu_job_step_count.argtypes = [vp]
+        L.pfgpu_job_device_bytes.restype = C.c_size_t
+        L.pfgpu_job_device_bytes.argtypes = [vp]
+        L.pfgpu_job_launches_per_step.argtypes = [vp]
+        L.pfgpu_job_destroy.argtypes = [vp]
+        L.pfgpu_scene_device_bytes.restype = C.c_size_t
+        L.pfgpu_scene_device_bytes.argtypes = [vp, C.c_int]
+        L.pfgpu_last_error.restype = C.c_char_p
+        L.pfgpu_receptor_uniforms.argtypes = [C.c_uint64, C.c_int64, C.c_int64, dp]
+        L.pfgpu_detach_uniform.restype = C.c_double
+        L.pfgpu_detach_uniform.argtypes = [C.c_uint64, C.c_int64]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=C.c_double):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+def check(code: int, allow_done: bool = False) -> int:
+    if code == PFGPU_OK or (allow_done and code == PFGPU_DONE):
+        return code
+    raise PfgpuError(code, lib().pfgpu_last_error().decode(errors="replace"))
+
+
+def scene_device_bytes(scene: Scene, precision: int) -> int:
+    c = scene.to_c()
+    return lib().pfgpu_scene_device_bytes(C.byref(c), precision)
+
+
+class Job:
+    """A device-resident coupled simulation (pfgpu_job)."""
+
+    def __init__(self, scene: Scene, precision: int = 1, fp16_scale: float = 0.0):
+        self.scene = scene
+        self.precision = precision
+        self._c = scene.to_c()
+        h = C.c_void_p()
+        check(lib().pfgpu_job_create(C.byref(self._c), precision, fp16_scale, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pfgpu_job_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n: int = 1, graph: bool = True) -> int:
+        f = lib().pfgpu_job_step_graph if graph else lib().pfgpu_job_step
+        return check(f(self.h, int(n)), allow_done=True)
+
+    @property
+    def steps(self) -> int:
+        return int(lib().pfgpu_job_step_count(self.h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().pfgpu_job_device_bytes(self.h))
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(lib().pfgpu_job_launches_per_step(self.h))
+
+    def lattice(self, fIN=True, fOUT=False):
+        N = self.scene.n_nodes
+        a = np.zeros((19, N)) if fIN else None
+        b = np.zeros((19, N)) if fOUT else None
+        rho, u, F = np.zeros(N), np.zeros((3, N)), np.zeros((3, N))
+        check(lib().pfgpu_job_get_lattice(self.h, _p(a), _p(b), _p(rho), _p(u), _p(F)))
+        return dict(fIN=a, fOUT=b, rho=rho, u=u, F=F)
+
+    def elements(self):
+        PE = self.scene.n_platelets * self.scene.n_elem
+        X, Y, RY, Z = (np.zeros(PE) for _ in range(4))
+        V, F = np.zeros((3, PE)), np.zeros((3, PE))
+        check(lib().pfgpu_job_get_elements(self.h, _p(X), _p(Y), _p(RY), _p(Z), _p(V), _p(F)))
+        return dict(X=X, Y=Y, RY=RY, Z=Z, V=V, F=F)
+
+    def bonds(self):
+        sc = self.scene
+        st = np.zeros((sc.n_platelets, sc.n_rec, 3), dtype=np.int32)
+        vwf = np.zeros((4, sc.ny, sc.nx), dtype=np.int32)
+        tot = C.c_int(0)
+        check(lib().pfgpu_job_get_bonds(self.h, _p(st, C.c_int), _p(vwf, C.c_int), C.byref(tot)))
+        return dict(rec_state=st, vwf=vwf, total=tot.value)
+
+    def fibrin(self):
+        M = self.scene.n_fib
+        X, Y, Z = np.zeros(M), np.zeros(M), np.zeros(M)
+        V, F = np.zeros((3, M)), np.zeros((3, M))
+        check(lib().pfgpu_job_get_fibrin(self.h, _p(X), _p(Y), _p(Z), _p(V), _p(F)))
+        return dict(X=X, Y=Y, Z=Z, V=V, F=F)
+
+    def membrane(self):
+        sc = self.scene
+        SV = np.zeros((sc.n_platelets, 2))
+        km = np.zeros((sc.n_platelets, sc.n_membrane))
+        check(lib().pfgpu_job_get_membrane(self.h, _p(SV), _p(km)))
+        return dict(S_V=SV, km=km)
+
+    def conservation(self):
+        out = np.zeros(4)
+        check(lib().pfgpu_job_conservation(self.h, _p(out)))
+        return out
