@@ -33,8 +33,9 @@ __host__ __device__ constexpr int opp(int d) {
 }
 
 constexpr double kPi = 3.141592653589793;  // GPUDefines.h:36
-constexpr int kBrickX = 128;               // lattice brick = one CTA of the LBM kernel
-constexpr int kBinCap = 1024;              // Morse cell-bin capacity
+constexpr int kBrickX = 32;                // force brick = 32 x-nodes of one row (one warp)
+constexpr int kLbmBlock = 128;             // threads of an LBM CTA (4 bricks)
+constexpr int kBinCap = 512;               // Morse cell-bin capacity
 constexpr double kFixScale = 1099511627776.0;  // 2^40: fixed-point force accumulation
 
 // Device error bits (set instead of trapping; the host reads them after a step)
@@ -54,9 +55,10 @@ struct Control {
   int total_bond;         // sum of bond counts of the last bond pass
   unsigned int err;       // ERR_* bits
   int active_count[2];    // active-brick list lengths per force buffer
-  int nops;               // bond slot operations emitted this step
+  int nops;               // bond slot operations of the last bond pass
   int pad;
-  double sv[2];           // unused spare
+  int nops_active[2];     // bond pass counters: operations, active receptors
+  int occupied;           // Morse cells holding at least one element
 };
 
 // ------------------------------------------------------------- Philox

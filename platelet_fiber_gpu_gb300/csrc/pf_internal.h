@@ -7,11 +7,11 @@
 //                                       flagged active are read or non-zero
 //   brick flags   2 x uint32[nbricks]   + active-brick lists (one brick =
 //                                       128 x-nodes of one (y,z) row)
-//   u buffer      Real4[N]              (rho, u/C) at active bricks; before
-//                                       the first step: the initial rho, u
+//   u buffer      Real4[N]              (rho-1, u/C) at active bricks; before
+//                                       the first step: the initial rho-1, u/C
 //   elements      double X,Y,RY,Z,V,F   positions stay FP64
 //   membrane/Morse/bond/fibrin forces   one buffer each (concurrent kernels)
-//   Morse cell bins int[ncells][1024]
+//   Morse cell bins float4[ncells][512] (cell-relative position, id)
 #pragma once
 
 #include <cuda_runtime.h>
@@ -107,7 +107,8 @@ struct Platelets {
   float *r1 = nullptr, *r2 = nullptr;
   void* rec_tmp = nullptr;  // per-receptor scratch of the bond pass
   // Morse bins
-  int *bin_count = nullptr, *bin = nullptr;
+  int* bin_count = nullptr;
+  void* bin = nullptr;  // float4 [ncells][kBinCap]: cell-relative position, element id
   int ncells = 0;
   size_t bytes = 0;
 };

@@ -352,7 +352,7 @@ static int build_platelets(pfgpu_job* j, const pf_scene* s) {
   if (k.morse) {
     P.ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
     CK(dalloc(j, &P.bin_count, (size_t)P.ncells));
-    CK(dalloc(j, &P.bin, (size_t)P.ncells * kBinCap));
+    CK(dalloc(j, (char**)&P.bin, (size_t)P.ncells * kBinCap * sizeof(float4) + (size_t)P.ncells * sizeof(int)));
   }
   return PFGPU_OK;
 }
@@ -390,11 +390,11 @@ static int enqueue_step(pfgpu_job* j) {
     launches++;
     if (Pl->k.morse && Pl->k.P * Pl->k.E) {
       CK(morse_forces(*Pl, j->precision, j->ctl, j->s2));
-      launches++;
+      launches += 2;
     }
     if (Pl->k.nrec) {
       CK(bond_pass(*Pl, j->precision, j->ctl, j->s0));
-      launches++;
+      launches += 2;
     }
   }
   if (Fb) {
@@ -455,7 +455,7 @@ size_t pfgpu_scene_device_bytes(const pf_scene* s, int precision) {
       int c = rc > 0 ? (int)std::floor(n3[a] * (double)s->dx / rc) : 1;
       nc *= (size_t)(c < 1 ? 1 : c);
     }
-    b += nc * (kBinCap + 1) * 4;
+    b += nc * (kBinCap * 16 + 4);
   }
   b += (size_t)s->n_fib * 14 * 8;
   b += 19 * N * 8 + 4 * N * 8 + 3 * N * 8;  // transient upload staging

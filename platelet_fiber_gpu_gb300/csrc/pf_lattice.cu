@@ -107,10 +107,12 @@ __device__ __forceinline__ void gather(const LatticeConst& k, const S* __restric
 // Zou/He planes: z=0 no-slip (LB_kernel.cu:395-600) and z=nz-1 moving plate
 // (:602-780, where C, Nzx, Nzy are float).  Writes the unknowns, returns the
 // boundary density; velocity is the wall's.
+// Both return drho = rho - 1: in shifted form the weights of the summed
+// populations add up to one.
 template <class R>
 __device__ __forceinline__ R zouhe_bottom(R g[Q]) {
-  const R rho = (R)1 + (g[1] + g[2] + g[3] + g[4] + g[7] + g[8] + g[11] + g[12] + g[0] +
-                        (R)2 * (g[6] + g[10] + g[14] + g[16] + g[18]));
+  const R drho = (g[1] + g[2] + g[3] + g[4] + g[7] + g[8] + g[11] + g[12] + g[0] +
+                  (R)2 * (g[6] + g[10] + g[14] + g[16] + g[18]));
   const R Nzx = (R)0.5 * (g[1] + g[7] + g[8] - g[2] - g[11] - g[12]);
   const R Nzy = (R)0.5 * (g[3] + g[7] + g[11] - g[4] - g[8] - g[12]);
   g[5] = g[6];
@@ -118,12 +120,13 @@ __device__ __forceinline__ R zouhe_bottom(R g[Q]) {
   g[13] = g[10] + Nzx;
   g[15] = g[18] - Nzy;
   g[17] = g[16] + Nzy;
-  return rho;
+  return drho;
 }
 template <class R>
 __device__ __forceinline__ R zouhe_top(R g[Q], R uw) {
-  const R rho = (R)1 + (g[1] + g[2] + g[3] + g[4] + g[7] + g[11] + g[12] + g[8] + g[0] +
-                        (R)2 * (g[5] + g[9] + g[13] + g[15] + g[17]));
+  const R drho = (g[1] + g[2] + g[3] + g[4] + g[7] + g[11] + g[12] + g[8] + g[0] +
+                  (R)2 * (g[5] + g[9] + g[13] + g[15] + g[17]));
+  const R rho = (R)1 + drho;
   const R Nzx = (R)(float)((R)0.5 * (g[1] + g[7] + g[8] - g[2] - g[11] - g[12]));
   const R Nzy = (R)(float)((R)0.5 * (g[3] + g[7] + g[11] - g[4] - g[8] - g[12]) - (R)(1.0 / 3.0) * rho * uw);
   g[6] = g[5];
@@ -131,7 +134,7 @@ __device__ __forceinline__ R zouhe_top(R g[Q], R uw) {
   g[14] = g[9] + Nzx;
   g[16] = g[17] + (R)(1.0 / 6.0) * rho * uw - Nzy;
   g[18] = g[15] + (R)(1.0 / 6.0) * rho * (-uw) + Nzy;
-  return rho;
+  return drho;
 }
 
 template <class R>
@@ -146,24 +149,26 @@ __device__ __forceinline__ void moments(const R g[Q], R& drho, R& jx, R& jy, R& 
   }
 }
 
-// density and lattice velocity of a post-stream node (boundary values on the
-// Zou/He planes, half-force corrected moments elsewhere)
+// density deviation drho = rho - 1 and lattice velocity of a post-stream node
+// (boundary values on the Zou/He planes, half-force corrected moments
+// elsewhere).  drho is carried separately: rounding 1 + drho in FP32 would
+// put ~6e-8 of noise into the density every step.
 template <class R>
 __device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z, bool apply_bc, R Fx, R Fy,
-                                           R Fz, R& rho, R& ux, R& uy, R& uz) {
+                                           R Fz, R& drho, R& ux, R& uy, R& uz) {
   if (apply_bc && k.bc[2] == PF_BC_ZOUHE_SHEAR && z == 0) {
-    rho = zouhe_bottom(g);
+    drho = zouhe_bottom(g);
     ux = 0; uy = 0; uz = 0;
     return;
   }
   if (apply_bc && k.bc[2] == PF_BC_ZOUHE_SHEAR && z == k.nz - 1) {
-    rho = zouhe_top(g, (R)k.uw);
+    drho = zouhe_top(g, (R)k.uw);
     ux = 0; uy = (R)k.uw; uz = 0;
     return;
   }
-  R drho, jx, jy, jz;
+  R jx, jy, jz;
   moments(g, drho, jx, jy, jz);
-  rho = (R)1 + drho;
+  const R rho = (R)1 + drho;
   const R hk = (R)0.5 * (R)k.kmom;
   ux = (jx + hk * Fx) / rho;
   uy = (jy + hk * Fy) / rho;
@@ -171,9 +176,9 @@ __device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z,
 }
 
 template <class S, class R>
-__global__ void __launch_bounds__(kBrickX) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
-                                                      R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
-                                                      int ncells, Control* ctl) {
+__global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                                        R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                                        int ncells, Control* ctl) {
   if (ctl->done) return;
   const long long step = ctl->step;
   const int par = (int)(step & 1);
@@ -184,29 +189,33 @@ __global__ void __launch_bounds__(kBrickX) lbm_step_k(LatticeConst k, S* gA, S* 
   unsigned* flp = par ? flA : flB;
   const unsigned* flc = par ? flB : flA;
   const int first = ctl->first;
-  const int x = blockIdx.x * kBrickX + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-  const int brick = blockIdx.x + k.nbx * (y + k.ny * z);
-  const unsigned fc = flc[brick], fp = flp[brick];
+  const int x = blockIdx.x * kLbmBlock + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  // one force brick per warp
+  const int bxw = x / kBrickX;
+  const bool row_ok = bxw < k.nbx;
+  const int brick = bxw + k.nbx * (y + k.ny * z);
+  const unsigned fc = row_ok ? flc[brick] : 0u, fp = row_ok ? flp[brick] : 0u;
   if (x < k.nx) {
     const size_t N = (size_t)k.N;
     const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
     R g[Q];
     gather<S, R>(k, gin, x, y, z, g);
-    R rho, ux, uy, uz;
+    R drho, ux, uy, uz;
     if (first) {
-      ld_u<R>(ubuf, n, rho, ux, uy, uz);
-      if (k.bc[2] == PF_BC_ZOUHE_SHEAR) { /* the first collision streams without the BC */ }
+      // the first collision after an upload uses the uploaded density and
+      // velocity, and its populations are the uploaded fIN (no boundary pass)
+      ld_u<R>(ubuf, n, drho, ux, uy, uz);
     } else {
       R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
       if (fp) ld_force<R>(Fp, n, px, py, pz);
-      node_state<R>(k, g, z, true, px, py, pz, rho, ux, uy, uz);
+      node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
     }
     R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
     if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
     const R kc = (R)k.kcoll;
     Fx *= kc; Fy *= kc; Fz *= kc;
     const R om = (R)k.omega;
-    const R drho = rho - (R)1;
+    const R rho = (R)1 + drho;
     const R usq = ux * ux + uy * uy + uz * uz;
     const R uF = ux * Fx + uy * Fy + uz * Fz;
     const R sf = (R)1 - (R)0.5 * om;
@@ -223,15 +232,15 @@ __global__ void __launch_bounds__(kBrickX) lbm_step_k(LatticeConst k, S* gA, S* 
                             (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
     }
     if (fp) zero_force<R>(Fp, n);
-    (void)fc;
   }
-  __syncthreads();
-  if (threadIdx.x == 0 && fp) flp[brick] = 0;
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0 && fp) flp[brick] = 0;
   if (bin_count) {
     const size_t tid = (((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * blockDim.x +
                        threadIdx.x;
     const size_t tot = (size_t)gridDim.x * gridDim.y * gridDim.z * blockDim.x;
     for (size_t c = tid; c < (size_t)ncells; c += tot) bin_count[c] = 0;
+    if (tid == 0) ctl->occupied = 0;
   }
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0) ctl->active_count[par ^ 1] = 0;
 }
@@ -240,32 +249,32 @@ __global__ void __launch_bounds__(kBrickX) lbm_step_k(LatticeConst k, S* gA, S* 
 // boundary conditions, with this step's force: input of the IBM interpolation
 // (the reference's velocity_density, LB_kernel.cu:1108-1199).
 template <class S, class R>
-__global__ void __launch_bounds__(kBrickX) moments_active_k(LatticeConst k, const S* gA, const S* gB,
-                                                            const R4<R>* FA, const R4<R>* FB, R4<R>* ubuf,
-                                                            const int* lA, const int* lB, const Control* ctl) {
+__global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, const S* gA, const S* gB,
+                                                              const R4<R>* FA, const R4<R>* FB, R4<R>* ubuf,
+                                                              const int* lA, const int* lB, const Control* ctl) {
   if (ctl->done) return;
   const int par = (int)(ctl->step & 1);
   const S* gnew = par ? gA : gB;
   const R4<R>* Fc = par ? FB : FA;
   const int* list = par ? lB : lA;
-  const unsigned* fl = nullptr;
-  (void)fl;
   const int cnt = ctl->active_count[par];
-  for (int b = blockIdx.x; b < cnt; b += gridDim.x) {
+  const int warps = kLbmBlock / 32;
+  const int lane = threadIdx.x & 31;
+  for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < cnt; b += gridDim.x * warps) {
     const int brick = list[b];
     const int bx = brick % k.nbx;
     const int y = (brick / k.nbx) % k.ny;
     const int z = brick / (k.nbx * k.ny);
-    const int x = bx * kBrickX + threadIdx.x;
+    const int x = bx * kBrickX + lane;
     if (x >= k.nx) continue;
     const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
     R g[Q];
     gather<S, R>(k, gnew, x, y, z, g);
     R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
     ld_force<R>(Fc, n, Fx, Fy, Fz);
-    R rho, ux, uy, uz;
-    node_state<R>(k, g, z, true, Fx, Fy, Fz, rho, ux, uy, uz);
-    st_u<R>(ubuf, n, rho, ux, uy, uz);
+    R drho, ux, uy, uz;
+    node_state<R>(k, g, z, true, Fx, Fy, Fz, drho, ux, uy, uz);
+    st_u<R>(ubuf, n, drho, ux, uy, uz);
   }
 }
 
@@ -281,18 +290,18 @@ __global__ void download_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, con
   gather<S, R>(k, gsrc, x, y, z, g);
   R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
   ld_force<R>(Fsrc, n, Fx, Fy, Fz);
-  R rho, ux, uy, uz;
+  R drho, ux, uy, uz;
   if (use_ubuf) {
-    ld_u<R>(ubuf, n, rho, ux, uy, uz);
+    ld_u<R>(ubuf, n, drho, ux, uy, uz);
   } else {
-    node_state<R>(k, g, z, apply_bc != 0, Fx, Fy, Fz, rho, ux, uy, uz);
+    node_state<R>(k, g, z, apply_bc != 0, Fx, Fy, Fz, drho, ux, uy, uz);
   }
   const R sigma = (R)k.fp16_scale;
   for (int d = 0; d < Q; ++d) {
     if (fIN) fIN[(size_t)d * N + n] = (double)g[d] + wgt(d);
     if (fOUT) fOUT[(size_t)d * N + n] = (double)ld<S, R>(gsrc + (size_t)d * N + n, d, sigma) + wgt(d);
   }
-  if (rho_o) rho_o[n] = (double)rho;
+  if (rho_o) rho_o[n] = 1.0 + (double)drho;
   if (u_o) {
     u_o[n] = (double)ux * k.C;
     u_o[N + n] = (double)uy * k.C;
@@ -337,7 +346,7 @@ __global__ void upload_k(LatticeConst k, S* g, const double* fIN, R4<R>* Fprev, 
   R4<R> v;
   v.x = fx; v.y = fy; v.z = fz; v.w = 0;
   Fprev[n] = v;
-  st_u<R>(ubuf, n, (R)ru[n], (R)(ru[N + n] / k.C), (R)(ru[2 * N + n] / k.C), (R)(ru[3 * N + n] / k.C));
+  st_u<R>(ubuf, n, (R)(ru[n] - 1.0), (R)(ru[N + n] / k.C), (R)(ru[2 * N + n] / k.C), (R)(ru[3 * N + n] / k.C));
 }
 
 template <class S, class R>
@@ -371,8 +380,8 @@ __global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
 
 template <class S, class R>
 cudaError_t step_impl(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st) {
-  dim3 grid(L.k.nbx, L.k.ny, L.k.nz);
-  lbm_step_k<S, R><<<grid, kBrickX, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
+  dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);
+  lbm_step_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
                                               (R4<R>*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells, ctl);
   return cudaGetLastError();
 }
@@ -382,8 +391,9 @@ cudaError_t moments_impl(Lattice& L, Control* ctl, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int grid = sms * 8;
-  if (grid > L.k.nbricks) grid = L.k.nbricks;
-  moments_active_k<S, R><<<grid, kBrickX, 0, st>>>(L.k, (const S*)L.g[0], (const S*)L.g[1],
+  const int need = (L.k.nbricks + kLbmBlock / 32 - 1) / (kLbmBlock / 32);
+  if (grid > need) grid = need;
+  moments_active_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (const S*)L.g[0], (const S*)L.g[1],
                                                     (const R4<R>*)L.F[0], (const R4<R>*)L.F[1], (R4<R>*)L.ubuf,
                                                     L.list[0], L.list[1], ctl);
   return cudaGetLastError();

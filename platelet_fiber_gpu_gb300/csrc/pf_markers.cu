@@ -5,6 +5,8 @@
 // (sem_kernel.cu:320-1749), Morse pair forces over cell bins, fibrin link
 // forces (fiber.cpp:647-733) and the receptor-bond pass
 // (sem_kernel.cu:1750-2083).
+#include <algorithm>
+
 #include "pf_internal.h"
 
 namespace pf {
@@ -21,43 +23,68 @@ __device__ __forceinline__ void atomic_add3(D4* F, size_t n, double x, double y,
   atomicAdd(p + 2, z);
 }
 
+// Nodes of one axis within 2 dx of x, with weights.
+// FP64 build: the reference's arithmetic -- spreading forms node coordinates
+// as int*float (LB_kernel.cu:1474), interpolation as int*double (:1581), and
+// the support test is |x - x_i| < 2 dx in microns.
+// FP32 build: one FP64 multiply to lattice units, then FP32 offsets (both
+// IBM directions share one stencil).
 template <class R>
-__device__ __forceinline__ R phi(double r);
+struct Stencil;
 template <>
-__device__ __forceinline__ double phi<double>(double r) {
-  return 0.25 * (1.0 + cos(0.5 * kPi * r));
-}
-template <>
-__device__ __forceinline__ float phi<float>(double r) {
-  return 0.25f * (1.f + cospif(0.5f * (float)r));
-}
-
-// Nodes of one axis within 2 dx of x, with weights.  spread=1 forms node
-// coordinates as int*float (LB_kernel.cu:1474), spread=0 as int*double
-// (:1581), like the reference's two IBM kernels.
-template <class R>
-__device__ __forceinline__ int axis_stencil(double x, float dxf, int n, int wrap, int spread, int node[5],
-                                            int raw[5], R w[5]) {
-  const double dxd = (double)dxf;
-  const double thr = (double)(2.0f * dxf);
-  const int base = (int)floor(x / dxd);
-  int cnt = 0;
+struct Stencil<double> {
+  static __device__ __forceinline__ int axis(double x, float dxf, double, int n, int wrap, int spread, int node[5],
+                                             double w[5]) {
+    const double dxd = (double)dxf;
+    const double thr = spread ? (double)(2.0f * dxf) : 2.0 * dxd;
+    const int base = (int)floor(x / dxd);
+    int cnt = 0;
 #pragma unroll
-  for (int ii = base - 2; ii <= base + 2; ++ii) {
-    const double xn = spread ? (double)((float)ii * dxf) : (double)ii * dxd;
-    const double dd = x - xn;
-    if (fabs(dd) >= (spread ? thr : 2.0 * dxd)) continue;
-    int nd = ii;
-    if (ii < 0 || ii >= n) {
-      if (!wrap) continue;
-      nd = wrapi(ii, n);
+    for (int ii = base - 2; ii <= base + 2; ++ii) {
+      const double xn = spread ? (double)((float)ii * dxf) : (double)ii * dxd;
+      const double dd = x - xn;
+      if (fabs(dd) >= thr) continue;
+      int nd = ii;
+      if (ii < 0 || ii >= n) {
+        if (!wrap) continue;
+        nd = wrapi(ii, n);
+      }
+      node[cnt] = nd;
+      w[cnt] = 0.25 * (1.0 + cos(0.5 * kPi * dd / dxd));
+      cnt++;
     }
-    node[cnt] = nd;
-    raw[cnt] = ii;
-    w[cnt] = phi<R>(dd / dxd);
-    cnt++;
+    return cnt;
   }
-  return cnt;
+};
+template <>
+struct Stencil<float> {
+  static __device__ __forceinline__ int axis(double x, float, double inv_dx, int n, int wrap, int, int node[5],
+                                             float w[5]) {
+    const double r = x * inv_dx;
+    const double fb = floor(r);
+    const int base = (int)fb;
+    const float fr = (float)(r - fb);
+    int cnt = 0;
+#pragma unroll
+    for (int o = -1; o <= 2; ++o) {
+      const float dd = fr - (float)o;
+      if (!(fabsf(dd) < 2.f)) continue;
+      int nd = base + o;
+      if (nd < 0 || nd >= n) {
+        if (!wrap) continue;
+        nd = wrapi(nd, n);
+      }
+      node[cnt] = nd;
+      w[cnt] = 0.25f * (1.f + cospif(0.5f * dd));
+      cnt++;
+    }
+    return cnt;
+  }
+};
+template <class R>
+__device__ __forceinline__ int axis_stencil(double x, float dxf, int n, int wrap, int spread, int node[5], int*,
+                                            R w[5]) {
+  return Stencil<R>::axis(x, dxf, 1.0 / (double)dxf, n, wrap, spread, node, w);
 }
 
 // ---------------------------------------------------------------- spreading
@@ -95,14 +122,46 @@ __global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R
   const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 1, nya, ry, wy);
   const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 1, nza, rz, wz);
   const R Fx = (R)fx, Fy = (R)fy, Fz = (R)fz;
+  const bool ref_nodes = sizeof(R) == 8;
+  if (ref_nodes) {
+    // the FP64 build's spreading and interpolation stencils can differ at the
+    // support edge (int*float vs int*double node coordinates): flag the bricks
+    // of every candidate node so the interpolation always finds fresh moments
+    const double inv = 1.0 / (double)lk.dxf;
+    const int bx = (int)floor(x * inv), by = (int)floor(y * inv), bz = (int)floor(z * inv);
+    for (int iz = bz - 2; iz <= bz + 2; ++iz) {
+      if (iz < 0 || iz >= lk.nz) continue;
+      for (int iy0 = by - 2; iy0 <= by + 2; ++iy0) {
+        int iy = iy0;
+        if (iy < 0 || iy >= lk.ny) {
+          if (!lk.ibm_wrap[1]) continue;
+          iy = wrapi(iy, lk.ny);
+        }
+        int last = -1;
+        for (int ix0 = bx - 2; ix0 <= bx + 2; ++ix0) {
+          int ix = ix0;
+          if (ix < 0 || ix >= lk.nx) {
+            if (!lk.ibm_wrap[0]) continue;
+            ix = wrapi(ix, lk.nx);
+          }
+          const int brick = ix / kBrickX + lk.nbx * (iy + lk.ny * iz);
+          if (brick == last) continue;
+          last = brick;
+          if (fl[brick] == 0u && atomicExch(fl + brick, 1u) == 0u) list[atomicAdd(counter, 1)] = brick;
+        }
+      }
+    }
+  }
   for (int c = 0; c < czn; ++c)
     for (int b = 0; b < cyn; ++b) {
       int last_brick = -1;
       for (int a = 0; a < cxn; ++a) {
-        const int brick = nxa[a] / kBrickX + lk.nbx * (nya[b] + lk.ny * nza[c]);
-        if (brick != last_brick) {
-          last_brick = brick;
-          if (fl[brick] == 0u && atomicExch(fl + brick, 1u) == 0u) list[atomicAdd(counter, 1)] = brick;
+        if (!ref_nodes) {
+          const int brick = nxa[a] / kBrickX + lk.nbx * (nya[b] + lk.ny * nza[c]);
+          if (brick != last_brick) {
+            last_brick = brick;
+            if (fl[brick] == 0u && atomicExch(fl + brick, 1u) == 0u) list[atomicAdd(counter, 1)] = brick;
+          }
         }
         const R delta = wx[a] * wy[b] * wz[c];
         const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
@@ -112,7 +171,10 @@ __global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R
 }
 
 // ------------------------------------------------------- interp + advance
-__device__ __forceinline__ int cell_of(const PlateletConst& k, double x, double y, double z) {
+// Morse cell of a position and the position relative to the cell's corner
+// (periodic axes wrapped first), the same rule as the oracle's cell list.
+__device__ __forceinline__ int cell_of(const PlateletConst& k, double x, double y, double z, float rel[3] = nullptr,
+                                       int cc[3] = nullptr) {
   const double p[3] = {x, y, z};
   int c[3];
 #pragma unroll
@@ -123,15 +185,31 @@ __device__ __forceinline__ int cell_of(const PlateletConst& k, double x, double 
     if (ci < 0) ci = 0;
     if (ci >= k.ncell[a]) ci = k.ncell[a] - 1;
     c[a] = ci;
+    if (rel) rel[a] = (float)(v - ci * k.cs[a]);
+    if (cc) cc[a] = ci;
   }
   return c[0] + k.ncell[0] * (c[1] + k.ncell[1] * c[2]);
+}
+__device__ __forceinline__ void bin_put(const PlateletConst& k, double x, double y, double z, int g, int* bin_count,
+                                        float4* bin, Control* ctl) {
+  float rel[3];
+  const int c = cell_of(k, x, y, z, rel);
+  const int slot = atomicAdd(bin_count + c, 1);
+  // the first element of a cell lists the cell as occupied (the list sits
+  // after the bins: occupied[ncells])
+  if (slot == 0) {
+    int* occ = reinterpret_cast<int*>(bin + (size_t)k.ncell[0] * k.ncell[1] * k.ncell[2] * kBinCap);
+    occ[atomicAdd(&ctl->occupied, 1)] = c;
+  }
+  if (slot < kBinCap) bin[(size_t)c * kBinCap + slot] = make_float4(rel[0], rel[1], rel[2], __int_as_float(g));
+  else atomicOr(&ctl->err, ERR_BIN_OVERFLOW);
 }
 
 template <class R>
 __global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, PlateletConst pk, const R4<R>* ubuf,
                                                         int PE, double* X, double* Y, double* RY, double* Z,
                                                         double* V, int M, double* fX, double* fY, double* fZ,
-                                                        double* fV, const int* ffix, int* bin_count, int* bin,
+                                                        double* fV, const int* ffix, int* bin_count, float4* bin,
                                                         Control* ctl, unsigned* done_blocks, double detach_rate,
                                                         uint64_t seed) {
   if (ctl->done) return;
@@ -166,12 +244,7 @@ __global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, Platele
       RY[idx] += vy * dtT;
       z += vz * dtT;
       X[idx] = x; Y[idx] = y; Z[idx] = z;
-      if (bin) {
-        const int c = cell_of(pk, x, y, z);
-        const int slot = atomicAdd(bin_count + c, 1);
-        if (slot < kBinCap) bin[(size_t)c * kBinCap + slot] = idx;
-        else atomicOr(&ctl->err, ERR_BIN_OVERFLOW);
-      }
+      if (bin) bin_put(pk, x, y, z, idx, bin_count, bin, ctl);
     } else {
       fV[m] = vx; fV[M + m] = vy; fV[2 * M + m] = vz;
       if (!ffix[m]) {
@@ -202,13 +275,10 @@ __global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, Platele
 }
 
 __global__ void bin_elements_k(PlateletConst pk, int PE, const double* X, const double* Y, const double* Z,
-                               int* bin_count, int* bin, Control* ctl) {
+                               int* bin_count, float4* bin, Control* ctl) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= PE) return;
-  const int c = cell_of(pk, X[g], Y[g], Z[g]);
-  const int slot = atomicAdd(bin_count + c, 1);
-  if (slot < kBinCap) bin[(size_t)c * kBinCap + slot] = g;
-  else atomicOr(&ctl->err, ERR_BIN_OVERFLOW);
+  bin_put(pk, X[g], Y[g], Z[g], g, bin_count, bin, ctl);
 }
 
 // ---------------------------------------------------------------- membrane
@@ -240,6 +310,34 @@ __device__ __forceinline__ void gauss34(R g[3][4]) {
   }
 }
 
+// The same elimination on [A | b1 b2 b3]: pivots depend on A only, so each
+// right-hand side sees exactly the operations of a separate 3x4 solve.
+template <class R>
+__device__ __forceinline__ void gauss36(R g[3][6]) {
+  int i = 0, j = 0;
+  while (i < 3 && j < 3) {
+    int maxi = i;
+    for (int k = i + 1; k < 3; ++k)
+      if (fabs(g[k][j]) > fabs(g[maxi][j])) maxi = k;
+    if (g[maxi][j] != 0) {
+      R piv = 0;
+      for (int k = j; k < 6; ++k) {
+        R t = g[i][k];
+        g[i][k] = g[maxi][k];
+        g[maxi][k] = t;
+        if (k == j) piv = g[i][j];
+        g[i][k] /= piv;
+      }
+      for (int k = i + 1; k < 3; ++k) {
+        R f = g[k][j];
+        for (int l = j; l < 6; ++l) g[k][l] -= f * g[i][l];
+      }
+      i++;
+    }
+    j++;
+  }
+}
+
 template <class R>
 __device__ __forceinline__ R nrm3(R a, R b, R c) {
   return sqrt(a * a + b * b + c * c);
@@ -251,7 +349,7 @@ __device__ __forceinline__ R nrm3(R a, R b, R c) {
 // accumulation is a gather in ascending triangle order, so the result does
 // not depend on scheduling.
 template <class R>
-__global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double* X, const double* Y,
+__global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double* X, const double* Y,
                                                   const double* RY, const double* Z, const int* tri,
                                                   const int* node_ntri, const int* node_tri,
                                                   const int* vert_local, const int* ring, const int* sp_ptr,
@@ -263,20 +361,35 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
   const int E = k.E, Em = k.Em, T = k.T, NN = k.NN, PE = k.P * k.E;
   const int base = p * E;
   const R F0 = (R)k.f0;
-  // geometry relative to a platelet origin in the single-precision build
-  const bool rel = sizeof(R) == 4;
+  // FP32 build: positions relative to the platelet's first element, cached
+  // once in shared memory (x, y, z, ry); FP64 build: absolute FP64 positions
+  // as the reference uses them
+  constexpr bool rel = sizeof(R) == 4;
+  extern __shared__ float s_pos[];
   const double ox = rel ? X[base] : 0.0, oy = rel ? Y[base] : 0.0, oz = rel ? Z[base] : 0.0;
+  const double ory = rel ? RY[base] : 0.0;
+  if constexpr (rel) {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      s_pos[4 * e] = (float)(X[base + e] - ox);
+      s_pos[4 * e + 1] = (float)(Y[base + e] - oy);
+      s_pos[4 * e + 2] = (float)(Z[base + e] - oz);
+      s_pos[4 * e + 3] = (float)(RY[base + e] - ory);
+    }
+    __syncthreads();
+  }
   auto P3 = [&](int e, R out[3]) {
-    out[0] = (R)(X[base + e] - ox);
-    out[1] = (R)(Y[base + e] - oy);
-    out[2] = (R)(Z[base + e] - oz);
+    if constexpr (rel) {
+      out[0] = (R)s_pos[4 * e]; out[1] = (R)s_pos[4 * e + 1]; out[2] = (R)s_pos[4 * e + 2];
+    } else {
+      out[0] = (R)X[base + e]; out[1] = (R)Y[base + e]; out[2] = (R)Z[base + e];
+    }
   };
   R* nNp = nN + (size_t)p * NN * 3;
   R* nep = nelem + (size_t)p * T * 3;
   R* Sp = S + (size_t)p * T;
   R* kmp = kmv + (size_t)p * Em;
-  __shared__ double s_a[256], s_b[256];
-  __shared__ int s_i[256];
+  __shared__ double s_a[512], s_b[512];
+  __shared__ int s_i[512];
   __shared__ double s_Sall, s_V;
   __shared__ int s_wall_idx;
   __shared__ double s_wall_f;
@@ -321,9 +434,16 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
     if (k.mask & PF_MEM_SPRING)
       for (int q = sp_ptr[e]; q < sp_ptr[e + 1]; ++q) {
         const int nb = sp_nbr[q];
-        const R d1 = (R)(X[base + nb] - X[base + e]);
-        const R d2 = (R)(RY[base + nb] - RY[base + e]);
-        const R d3 = (R)(Z[base + nb] - Z[base + e]);
+        R d1, d2, d3;
+        if constexpr (rel) {
+          d1 = s_pos[4 * nb] - s_pos[4 * e];
+          d2 = s_pos[4 * nb + 3] - s_pos[4 * e + 3];
+          d3 = s_pos[4 * nb + 2] - s_pos[4 * e + 2];
+        } else {
+          d1 = X[base + nb] - X[base + e];
+          d2 = RY[base + nb] - RY[base + e];
+          d3 = Z[base + nb] - Z[base + e];
+        }
         const R r = nrm3(d1, d2, d3);
         const R w = r - (R)sp_L0[q];
         const R fc = (R)k.kspring * w / r;
@@ -340,7 +460,8 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
     if (threadIdx.x == 0) { SV[2 * p] = 0; SV[2 * p + 1] = 0; }
     return;
   }
-  // triangle areas, normals, global area and volume
+  // triangle areas, normals; the global area and volume are summed in FP64;
+  // the local strain (Se - S0e)/S0e is kept for the area force
   double pa = 0, pv = 0;
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
     const int* nd = tri + 6 * t;
@@ -358,7 +479,8 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
     const R nn = nrm3(n[0], n[1], n[2]);
     n[0] /= -nn; n[1] /= -nn; n[2] /= -nn;
     const R St = (R)0.5 * nn;
-    Sp[t] = St;
+    const R S0e = (R)S0[(size_t)p * T + t];
+    Sp[t] = (St - S0e) / S0e;
     nep[3 * t] = n[0]; nep[3 * t + 1] = n[1]; nep[3 * t + 2] = n[2];
     pa += (double)St;
     pv += (double)((R)(1 / 3.0) * (cc[0] * n[0] + cc[1] * n[1] + cc[2] * n[2]) * St);
@@ -429,14 +551,16 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
                 nv[5][d] * gt[5];
       }
       R A[3][3];
-      for (int i = 0; i < 3; ++i) {
-        R g[3][4];
+      {
+        R g[3][6];
         for (int d = 0; d < 3; ++d) { g[0][d] = a1[d]; g[1][d] = a3[d]; g[2][d] = nv[li][d]; }
-        g[0][3] = a2[i]; g[1][3] = a4[i]; g[2][3] = 0;
-        gauss34<R>(g);
-        A[i][2] = g[2][3];
-        A[i][1] = g[1][3] - A[i][2] * g[1][2];
-        A[i][0] = g[0][3] - A[i][2] * g[0][2] - A[i][1] * g[0][1];
+        for (int i = 0; i < 3; ++i) { g[0][3 + i] = a2[i]; g[1][3 + i] = a4[i]; g[2][3 + i] = 0; }
+        gauss36<R>(g);
+        for (int i = 0; i < 3; ++i) {
+          A[i][2] = g[2][3 + i];
+          A[i][1] = g[1][3 + i] - A[i][2] * g[1][2];
+          A[i][0] = g[0][3 + i] - A[i][2] * g[0][2] - A[i][1] * g[0][1];
+        }
       }
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) K[a * 3 + b] += A[b][a];
@@ -469,12 +593,11 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
           cc[d] = (R)(1 / 3.0) * (c[0][d] + c[1][d] + c[2][d]);
           n[d] = nep[3 * t + d];
         }
-        const R S0e = (R)S0[(size_t)p * T + t], Se = Sp[t];
         R dS[3];
         dS[0] = (R)-0.5 * (L[i][1] * n[2] - L[i][2] * n[1]);
         dS[1] = (R)-0.5 * (L[i][2] * n[0] - L[i][0] * n[2]);
         dS[2] = (R)-0.5 * (L[i][0] * n[1] - L[i][1] * n[0]);
-        const R fa = -Ks * ((Se - S0e) / S0e + sglob);
+        const R fa = -Ks * (Sp[t] + sglob);
         fx += fa * dS[0] / F0;
         fy += fa * dS[1] / F0;
         fz += fa * dS[2] / F0;
@@ -541,10 +664,18 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
         L2 = nrm3(ce[0] - ci2[0], ce[1] - ci2[1], ce[2] - ci2[2]);
         Pe = (R)0.5 * (L1 + L2 + L3);
         Ai += sqrt(Pe * (Pe - L1) * (Pe - L2) * (Pe - L3));
-        const R alpha = (R)1 / tan(acos(a1 / (nrm3(xi[0] - x1[0], xi[1] - x1[1], xi[2] - x1[2]) *
-                                             nrm3(x1[0] - xj[0], x1[1] - xj[1], x1[2] - xj[2]))));
-        const R beta = (R)1 / tan(acos(a2 / (nrm3(xi[0] - x2[0], xi[1] - x2[1], xi[2] - x2[2]) *
-                                            nrm3(x2[0] - xj[0], x2[1] - xj[1], x2[2] - xj[2]))));
+        const R ca = a1 / (nrm3(xi[0] - x1[0], xi[1] - x1[1], xi[2] - x1[2]) *
+                           nrm3(x1[0] - xj[0], x1[1] - xj[1], x1[2] - xj[2]));
+        const R cb = a2 / (nrm3(xi[0] - x2[0], xi[1] - x2[1], xi[2] - x2[2]) *
+                           nrm3(x2[0] - xj[0], x2[1] - xj[1], x2[2] - xj[2]));
+        R alpha, beta;
+        if constexpr (sizeof(R) == 8) {
+          alpha = (R)1 / tan(acos(ca));  // sem_kernel.cu:1624-1625
+          beta = (R)1 / tan(acos(cb));
+        } else {
+          alpha = ca * rsqrtf(1.f - ca * ca);  // cot(acos(c)) = c / sqrt(1 - c^2)
+          beta = cb * rsqrtf(1.f - cb * cb);
+        }
         sum += (R)0.5 * (alpha + beta) * (kmp[jn] - kmi);
       }
       const R Kb = (R)k.kbend;
@@ -559,95 +690,180 @@ __global__ void __launch_bounds__(256) membrane_k(PlateletConst k, const double*
 }
 
 // ---------------------------------------------------------------- Morse
-template <class R>
+// Cell bins are sorted by element id after binning, so a cell list is the
+// same set in the same order as the oracle's counting sort, and the pair sums
+// below run in a fixed order.
+__global__ void __launch_bounds__(256) sort_bins_k(int ncells, const int* bin_count, float4* bin,
+                                                   const Control* ctl) {
+  if (ctl->done) return;
+  const int* occ = reinterpret_cast<const int*>(bin + (size_t)ncells * kBinCap);
+  const int nocc = ctl->occupied;
+  __shared__ float4 s_b[kBinCap];
+  for (int oc = blockIdx.x; oc < nocc; oc += gridDim.x) {
+    const int c = occ[oc];
+    const int cnt = min(bin_count[c], kBinCap);
+    int pow2 = 1;
+    while (pow2 < cnt) pow2 <<= 1;
+    float4* b = bin + (size_t)c * kBinCap;
+    for (int i = threadIdx.x; i < pow2; i += blockDim.x)
+      s_b[i] = i < cnt ? b[i] : make_float4(0, 0, 0, __int_as_float(0x7fffffff));
+    __syncthreads();
+    for (int size = 2; size <= pow2; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int i = threadIdx.x; i < pow2; i += blockDim.x) {
+          const int j = i ^ stride;
+          if (j > i) {
+            const bool up = (i & size) == 0;
+            const float4 a = s_b[i], e = s_b[j];
+            if ((__float_as_int(a.w) > __float_as_int(e.w)) == up) { s_b[i] = e; s_b[j] = a; }
+          }
+        }
+        __syncthreads();
+      }
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) b[i] = s_b[i];
+    __syncthreads();
+  }
+}
+
+// F_i = sum_j 2 rho U0 [e^{2 rho (req - r)} - e^{rho (req - r)}] (x_i - x_j)/r
+// for 0 < r < cutoff (intra- or inter-platelet parameters), over the 27
+// neighbouring cells in a fixed order.  One CTA per occupied cell: the cell's
+// elements are the threads; each neighbour cell's members are staged through
+// shared memory and read by broadcast.  FP32 build: cell-relative float
+// coordinates from the bins (no FP64 in the pair loop).  FP64 build, or a
+// periodic axis with fewer than three cells: FP64 positions, minimum image,
+// neighbour cells de-duplicated.
+template <class R, bool FAST>
 __global__ void __launch_bounds__(128) morse_k(PlateletConst k, const double* X, const double* Y, const double* Z,
-                                               const int* bin_count, const int* bin, double* Fm, Control* ctl) {
+                                               const int* bin_count, const float4* bin, double* Fm, Control* ctl) {
   if (ctl->done) return;
   const int PE = k.P * k.E;
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= PE) return;
-  const double xi = X[g], yi = Y[g], zi = Z[g];
-  const int cid = cell_of(k, xi, yi, zi);
-  const int c0 = cid % k.ncell[0], c1 = (cid / k.ncell[0]) % k.ncell[1], c2 = cid / (k.ncell[0] * k.ncell[1]);
-  const int pg = g / k.E;
-  long long ax = 0, ay = 0, az = 0;
-  int seen[27], nseen = 0;
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        int cc[3] = {c0 + dx, c1 + dy, c2 + dz};
-        bool ok = true;
-        for (int a = 0; a < 3; ++a)
-          if (cc[a] < 0 || cc[a] >= k.ncell[a]) {
-            if (k.wrap[a]) cc[a] = (cc[a] + k.ncell[a]) % k.ncell[a];
-            else ok = false;
+  const int ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
+  const int* occ = reinterpret_cast<const int*>(bin + (size_t)ncells * kBinCap);
+  const int nocc = ctl->occupied;
+  __shared__ float4 s_m[128];
+  const R U0a = (R)k.morse_intra[0], rhoa = (R)k.morse_intra[1], reqa = (R)k.morse_intra[2], rca = (R)k.morse_intra[3];
+  const R U0b = (R)k.morse_inter[0], rhob = (R)k.morse_inter[1], reqb = (R)k.morse_inter[2], rcb = (R)k.morse_inter[3];
+  const R rc2a = rca * rca, rc2b = rcb * rcb;
+  const float cs0 = (float)k.cs[0], cs1 = (float)k.cs[1], cs2 = (float)k.cs[2];
+  for (int oc = blockIdx.x; oc < nocc; oc += gridDim.x) {
+    const int c = occ[oc];
+    const int cnt = min(bin_count[c], kBinCap);
+    const int c0 = c % k.ncell[0], c1 = (c / k.ncell[0]) % k.ncell[1], c2 = c / (k.ncell[0] * k.ncell[1]);
+    for (int q0 = 0; q0 < cnt; q0 += blockDim.x) {
+      const int q = q0 + threadIdx.x;
+      const bool valid = q < cnt;
+      const float4 own = valid ? bin[(size_t)c * kBinCap + q] : make_float4(0, 0, 0, __int_as_float(-1));
+      const int g = __float_as_int(own.w);
+      const int pbase = valid ? (g / k.E) * k.E : 0;
+      double xi = 0, yi = 0, zi = 0;
+      if (!FAST && valid) { xi = X[g]; yi = Y[g]; zi = Z[g]; }
+      R ax = 0, ay = 0, az = 0;
+      int seen[FAST ? 1 : 27];
+      int nseen = 0;
+      for (int nb = 0; nb < 27; ++nb) {
+        const int dx = nb % 3 - 1, dy = (nb / 3) % 3 - 1, dz = nb / 9 - 1;
+        int cc0 = c0 + dx, cc1 = c1 + dy, cc2 = c2 + dz;
+        if (cc0 < 0 || cc0 >= k.ncell[0]) { if (!k.wrap[0]) continue; cc0 = (cc0 + k.ncell[0]) % k.ncell[0]; }
+        if (cc1 < 0 || cc1 >= k.ncell[1]) { if (!k.wrap[1]) continue; cc1 = (cc1 + k.ncell[1]) % k.ncell[1]; }
+        if (cc2 < 0 || cc2 >= k.ncell[2]) { if (!k.wrap[2]) continue; cc2 = (cc2 + k.ncell[2]) % k.ncell[2]; }
+        const int nc = cc0 + k.ncell[0] * (cc1 + k.ncell[1] * cc2);
+        if (!FAST) {
+          bool dup = false;
+          for (int t = 0; t < nseen; ++t) dup |= (seen[t] == nc);
+          if (dup) continue;
+          seen[nseen++] = nc;
+        }
+        const int ncnt = min(bin_count[nc], kBinCap);
+        const float ox = own.x - dx * cs0, oy = own.y - dy * cs1, oz = own.z - dz * cs2;
+        for (int m0 = 0; m0 < ncnt; m0 += 128) {
+          __syncthreads();
+          if (m0 + threadIdx.x < ncnt) s_m[threadIdx.x] = bin[(size_t)nc * kBinCap + m0 + threadIdx.x];
+          __syncthreads();
+          const int mm = min(128, ncnt - m0);
+          if (!valid) continue;
+#pragma unroll 4
+          for (int j = 0; j < mm; ++j) {
+            const float4 mb = s_m[j];
+            const int h = __float_as_int(mb.w);
+            const bool intra = (unsigned)(h - pbase) < (unsigned)k.E;
+            R d0, d1, d2;
+            if (FAST) {
+              d0 = (R)(ox - mb.x); d1 = (R)(oy - mb.y); d2 = (R)(oz - mb.z);
+            } else {
+              double e0 = xi - X[h], e1 = yi - Y[h], e2 = zi - Z[h];
+              if (k.wrap[0]) e0 -= k.L[0] * floor(e0 / k.L[0] + 0.5);
+              if (k.wrap[1]) e1 -= k.L[1] * floor(e1 / k.L[1] + 0.5);
+              if (k.wrap[2]) e2 -= k.L[2] * floor(e2 / k.L[2] + 0.5);
+              d0 = (R)e0; d1 = (R)e1; d2 = (R)e2;
+            }
+            const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
+            if (!(r2 < (intra ? rc2a : rc2b)) || !(r2 > (R)0)) continue;
+            const R U0 = intra ? U0a : U0b, rho = intra ? rhoa : rhob, req = intra ? reqa : reqb;
+            R fr;
+            if (sizeof(R) == 4) {
+              const float rinv = rsqrtf((float)r2);
+              const float r = (float)r2 * rinv;
+              const float ex = __expf((float)rho * ((float)req - r));
+              fr = (R)(2.0f * (float)rho * (float)U0 * (ex * ex - ex) * rinv);
+            } else {
+              const R r = sqrt(r2);
+              if (!(r < (intra ? rca : rcb))) continue;
+              const R ex = exp(rho * (req - r));
+              fr = (R)2.0 * rho * U0 * (ex * ex - ex) / r;
+            }
+            ax += fr * d0; ay += fr * d1; az += fr * d2;
           }
-        if (!ok) continue;
-        const int nc = cc[0] + k.ncell[0] * (cc[1] + k.ncell[1] * cc[2]);
-        bool dup = false;
-        for (int q = 0; q < nseen; ++q) dup |= (seen[q] == nc);
-        if (dup) continue;
-        seen[nseen++] = nc;
-        int cnt = bin_count[nc];
-        if (cnt > kBinCap) cnt = kBinCap;
-        const int* members = bin + (size_t)nc * kBinCap;
-        for (int q = 0; q < cnt; ++q) {
-          const int h = members[q];
-          if (h == g) continue;
-          double d[3] = {xi - X[h], yi - Y[h], zi - Z[h]};
-          for (int a = 0; a < 3; ++a)
-            if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
-          const double* mp = (h / k.E == pg) ? k.morse_intra : k.morse_inter;
-          const R r = nrm3((R)d[0], (R)d[1], (R)d[2]);
-          if (!(r < (R)mp[3]) || r <= 0) continue;
-          const R ex = exp((R)mp[1] * ((R)mp[2] - r));
-          const R f = (R)2.0 * (R)mp[1] * (R)mp[0] * (ex * ex - ex) / r;
-          ax += __double2ll_rn((double)(f * (R)d[0]) * kFixScale);
-          ay += __double2ll_rn((double)(f * (R)d[1]) * kFixScale);
-          az += __double2ll_rn((double)(f * (R)d[2]) * kFixScale);
         }
       }
-  const double s = 1.0 / kFixScale / (double)k.f0;
-  Fm[g] = (double)ax * s;
-  Fm[PE + g] = (double)ay * s;
-  Fm[2 * PE + g] = (double)az * s;
+      if (valid && g >= 0 && g < PE) {
+        const double sc = 1.0 / (double)k.f0;
+        Fm[g] = (double)ax * sc;
+        Fm[PE + g] = (double)ay * sc;
+        Fm[2 * PE + g] = (double)az * sc;
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------- fibrin
+template <class R>
 __global__ void fibrin_k(int M, int law, double kk, double mass, const double* X, const double* Y, const double* Z,
                          const int* ptr, const int* nbr, const double* L0, double* F, const Control* ctl) {
   if (ctl->done) return;
   const int ni = blockIdx.x * blockDim.x + threadIdx.x;
   if (ni >= M) return;
-  double fx = 0, fy = 0, fz = 0;
+  R fx = 0, fy = 0, fz = 0;
+  const double xi = X[ni], yi = Y[ni], zi = Z[ni];
   for (int q = ptr[ni]; q < ptr[ni + 1]; ++q) {
     const int o = nbr[q];
-    const double d0 = X[ni] - X[o], d1 = Y[ni] - Y[o], d2 = Z[ni] - Z[o];
-    const double len = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-    if (len < 1.0e-13) continue;
-    double wf;
+    const R d0 = (R)(xi - X[o]), d1 = (R)(yi - Y[o]), d2 = (R)(zi - Z[o]);
+    const R len = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    if (len < (R)1.0e-13) continue;
+    const R l0 = (R)L0[q];
+    R wf;
     if (law == PF_FIB_WLC) {
-      const double En = 1.3806503 * 1e-8 * 10;
-      const double CC = En / L0[q];
-      const double tl = 1.0 - (len - L0[q]) / L0[q];
-      const double IP1 = 0.25 * 1.0 / (tl * tl) - 0.25 + (len - L0[q]) / L0[q];
-      wf = -CC * IP1 / mass;
+      const R En = (R)(1.3806503 * 1e-8 * 10);
+      const R CC = En / l0;
+      const R tl = (R)1.0 - (len - l0) / l0;
+      const R IP1 = (R)0.25 * (R)1.0 / (tl * tl) - (R)0.25 + (len - l0) / l0;
+      wf = -CC * IP1 / (R)mass;
     } else {
-      wf = kk * (len - L0[q]);
+      wf = (R)kk * (len - l0);
     }
     fx -= wf * d0 / len;
     fy -= wf * d1 / len;
     fz -= wf * d2 / len;
   }
-  F[ni] = fx;
-  F[M + ni] = fy;
-  F[2 * M + ni] = fz;
+  F[ni] = (double)fx;
+  F[M + ni] = (double)fy;
+  F[2 * M + ni] = (double)fz;
 }
 
 // ---------------------------------------------------------------- bonds
 struct RecTmp {
   double rx, ry, rz;
-  int active, bond0, si, sj, ci, cj;
+  int bond0, si, sj, ci, cj;
   int kind[2];  // 0 none, 1 claim, 2 release
   int ok[2];
 };
@@ -657,95 +873,103 @@ __device__ __forceinline__ unsigned long long op_key(int site, int rid, int opi)
          (unsigned long long)opi;
 }
 
-// Single CTA.  Receptors are independent except through the vWF slots of a
-// site; slot operations are therefore grouped by site and applied in
-// ascending (receptor id, operation) order, which is the outcome of a serial
-// schedule of the reference kernel.  Every receptor reads totalBond before any
-// addition (avaiBond = NUMOFRECEPTORS).
-template <class R>
-__global__ void __launch_bounds__(1024) bonds_k(PlateletConst k, const double* X, const double* Y, const double* Z,
-                                                const int* tri, const int* rec_tri, const float* r1a,
-                                                const float* r2a, int* rec_state, int* vwf, RecTmp* tmp,
-                                                unsigned long long* ops, int ops_cap, R* Fbond, Control* ctl) {
+// Bond pass, part 1 (all receptors, many CTAs): receptor positions, Bell or
+// constant probabilities, decisions from the two injected uniforms, and the
+// slot operations they imply.  Receptors on the triangle above the bond
+// range and unbound do nothing (sem_kernel.cu:1812).  Every receptor reads
+// totalBond before any addition: avaiBond = NUMOFRECEPTORS.
+__global__ void bonds_prepare_k(PlateletConst k, const double* X, const double* Y, const double* Z,
+                                const int* tri, const int* rec_tri, const float* r1a, const float* r2a,
+                                const int* rec_state, RecTmp* tmp, int* active, unsigned long long* ops, int ops_cap,
+                                void* Fbond, int fbond_bytes, Control* ctl) {
   if (ctl->done) return;
   const int PE = k.P * k.E;
   const int NR = k.P * k.nrec;
-  __shared__ int s_nops;
-  __shared__ long long s_tot[32];
-  for (int i = threadIdx.x; i < 3 * PE; i += blockDim.x) Fbond[i] = 0;
-  if (threadIdx.x == 0) s_nops = 0;
-  __syncthreads();
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gsz = gridDim.x * blockDim.x;
+  for (int i = gid; i < 3 * PE * fbond_bytes / 4; i += gsz) ((int*)Fbond)[i] = 0;
+  const int r = gid;
+  if (r >= NR) return;
   const long long step = ctl->step;
   const double dx = k.dxd, dt = k.dtd;
   const int avai = (int)(k.numrec - 0);
-  // phase A: geometry, decisions, slot operations
-  for (int r = threadIdx.x; r < NR; r += blockDim.x) {
-    RecTmp t;
-    t.kind[0] = t.kind[1] = 0;
-    t.ok[0] = t.ok[1] = 0;
-    t.active = 0;
-    const int p = r / k.nrec;
-    const int eo = p * k.E;
-    const int* nd = tri + 6 * rec_tri[r];
-    int* st = rec_state + 3 * r;
-    const float r1 = r1a[r], r2 = r2a[r];
-    const float wa = 1 - r1, wb = r1 * (1 - r2), wc = r1 * r2;
-    const double rz = wa * Z[eo + nd[0]] + wb * Z[eo + nd[1]] + wc * Z[eo + nd[2]];
-    const int bond = st[2] > -1 ? st[2] : 0;
-    if (!(rz > 0.078 && bond == 0)) {
-      const double rx = wa * X[eo + nd[0]] + wb * X[eo + nd[1]] + wc * X[eo + nd[2]];
-      const double ry = wa * Y[eo + nd[0]] + wb * Y[eo + nd[1]] + wc * Y[eo + nd[2]];
-      t.active = 1;
-      t.rx = rx; t.ry = ry; t.rz = rz;
-      t.bond0 = bond;
-      t.si = st[0]; t.sj = st[1];
-      int si = bond ? st[0] : (int)(rx / dx + 0.5), sj = bond ? st[1] : (int)(ry / dx + 0.5);
-      t.ci = (int)(rx / dx + 0.5);
-      t.cj = (int)(ry / dx + 0.5);
-      const double d1 = rx - si * dx, d2 = ry - sj * dx, d3 = rz;
-      const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
-      const double w = fabs(0.078 - dr);
-      const double fc = 10.0 * w;
-      double aon, aoff;
-      if (k.bond_model == PF_BOND_BELL) {
-        const double Kf = (double)k.kf0 * exp(fc * (0.00071 - 0.5 * w) / 4.05) * avai;
-        const double Kr = (double)k.kr0 * exp(0.00071 * fc / 4.05) * avai;
-        aon = 1 - exp(-Kf * dt);
-        aoff = 1 - exp(-Kr * dt);
-      } else {
-        aon = k.p_on;
-        aoff = k.p_off;
-      }
-      double u1, u2;
-      receptor_uniforms(k.seed, step, r, u1, u2);
-      if (bond == 0) {
-        if (u1 < aon) t.kind[0] = 1;
-        if (u2 < aon) t.kind[1] = 1;
-      } else if (bond == 1) {
-        if (u1 < aoff) {
-          t.kind[0] = 2;
-          if (u2 < aon && rz < 0.078) t.kind[1] = 1;
-        } else if (u2 < aoff && rz < 0.078) {
-          t.kind[0] = 2;
-        }
-      } else if (bond == 2) {
-        if (u1 < aoff) t.kind[0] = 2;
-        if (u2 < aoff) t.kind[1] = 2;
-      }
-      for (int o = 0; o < 2; ++o) {
-        if (!t.kind[o]) continue;
-        const int ii = t.kind[o] == 1 ? t.ci : t.si, jj = t.kind[o] == 1 ? t.cj : t.sj;
-        const int site = wrapi(jj, k.ny) * k.nx + wrapi(ii, k.nx);
-        const int slot = atomicAdd(&s_nops, 1);
-        if (slot < ops_cap) ops[slot] = op_key(site, r, o);
-        else atomicOr(&ctl->err, ERR_BOND_OVERFLOW);
-      }
-    }
-    tmp[r] = t;
+  const int p = r / k.nrec;
+  const int eo = p * k.E;
+  const int* nd = tri + 6 * rec_tri[r];
+  const int* st = rec_state + 3 * r;
+  const float r1 = r1a[r], r2 = r2a[r];
+  const float wa = 1 - r1, wb = r1 * (1 - r2), wc = r1 * r2;
+  const double rz = wa * Z[eo + nd[0]] + wb * Z[eo + nd[1]] + wc * Z[eo + nd[2]];
+  const int bond = st[2] > -1 ? st[2] : 0;
+  if (rz > 0.078 && bond == 0) return;
+  RecTmp t;
+  t.kind[0] = t.kind[1] = 0;
+  t.ok[0] = t.ok[1] = 0;
+  const double rx = wa * X[eo + nd[0]] + wb * X[eo + nd[1]] + wc * X[eo + nd[2]];
+  const double ry = wa * Y[eo + nd[0]] + wb * Y[eo + nd[1]] + wc * Y[eo + nd[2]];
+  t.rx = rx; t.ry = ry; t.rz = rz;
+  t.bond0 = bond;
+  t.si = st[0]; t.sj = st[1];
+  const int si = bond ? st[0] : (int)(rx / dx + 0.5), sj = bond ? st[1] : (int)(ry / dx + 0.5);
+  t.ci = (int)(rx / dx + 0.5);
+  t.cj = (int)(ry / dx + 0.5);
+  const double d1 = rx - si * dx, d2 = ry - sj * dx, d3 = rz;
+  const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
+  const double w = fabs(0.078 - dr);
+  const double fc = 10.0 * w;
+  double aon, aoff;
+  if (k.bond_model == PF_BOND_BELL) {
+    const double Kf = (double)k.kf0 * exp(fc * (0.00071 - 0.5 * w) / 4.05) * avai;
+    const double Kr = (double)k.kr0 * exp(0.00071 * fc / 4.05) * avai;
+    aon = 1 - exp(-Kf * dt);
+    aoff = 1 - exp(-Kr * dt);
+  } else {
+    aon = k.p_on;
+    aoff = k.p_off;
   }
-  __syncthreads();
-  const int nops = min(s_nops, ops_cap);
-  // phase B: bitonic sort of the operation keys, then one pass per site
+  double u1, u2;
+  receptor_uniforms(k.seed, step, r, u1, u2);
+  if (bond == 0) {
+    if (u1 < aon) t.kind[0] = 1;
+    if (u2 < aon) t.kind[1] = 1;
+  } else if (bond == 1) {
+    if (u1 < aoff) {
+      t.kind[0] = 2;
+      if (u2 < aon && rz < 0.078) t.kind[1] = 1;
+    } else if (u2 < aoff && rz < 0.078) {
+      t.kind[0] = 2;
+    }
+  } else if (bond == 2) {
+    if (u1 < aoff) t.kind[0] = 2;
+    if (u2 < aoff) t.kind[1] = 2;
+  }
+  tmp[r] = t;
+  active[atomicAdd(&ctl->nops_active[1], 1)] = r;
+  for (int o = 0; o < 2; ++o) {
+    if (!t.kind[o]) continue;
+    const int ii = t.kind[o] == 1 ? t.ci : t.si, jj = t.kind[o] == 1 ? t.cj : t.sj;
+    const int site = wrapi(jj, k.ny) * k.nx + wrapi(ii, k.nx);
+    const int slot = atomicAdd(&ctl->nops_active[0], 1);
+    if (slot < ops_cap) ops[slot] = op_key(site, r, o);
+    else atomicOr(&ctl->err, ERR_BOND_OVERFLOW);
+  }
+}
+
+// Bond pass, part 2 (one CTA): slot operations sorted by (site, receptor,
+// operation) and applied site by site in that order -- the outcome of a serial
+// schedule of sem_kernel.cu:1750-2083 -- then bond counts, stored sites and
+// the bond spring force on the triangle's vertices.
+template <class R>
+__global__ void __launch_bounds__(1024) bonds_resolve_k(PlateletConst k, const double* X, const double* Y,
+                                                        const double* Z, const int* tri, const int* rec_tri,
+                                                        int* rec_state, int* vwf, RecTmp* tmp, const int* active,
+                                                        unsigned long long* ops, int ops_cap, R* Fbond,
+                                                        Control* ctl) {
+  if (ctl->done) return;
+  const int PE = k.P * k.E;
+  __shared__ long long s_tot[32];
+  const int nops = min(ctl->nops_active[0], ops_cap);
+  const int nact = ctl->nops_active[1];
   int pow2 = 1;
   while (pow2 < nops) pow2 <<= 1;
   for (int i = nops + threadIdx.x; i < pow2; i += blockDim.x) ops[i] = ~0ull;
@@ -780,11 +1004,10 @@ __global__ void __launch_bounds__(1024) bonds_k(PlateletConst k, const double* X
     }
   }
   __syncthreads();
-  // phase C: bond counts, sites, forces on the triangle's vertices
   long long tot = 0;
-  for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+  for (int a = threadIdx.x; a < nact; a += blockDim.x) {
+    const int r = active[a];
     const RecTmp t = tmp[r];
-    if (!t.active) continue;
     int bond = t.bond0, si = t.bond0 ? t.si : -1, sj = t.bond0 ? t.sj : -1;
     for (int o = 0; o < 2; ++o) {
       if (!t.kind[o] || !t.ok[o]) continue;
@@ -797,14 +1020,15 @@ __global__ void __launch_bounds__(1024) bonds_k(PlateletConst k, const double* X
       const int p = r / k.nrec;
       const int eo = p * k.E;
       const int* nd = tri + 6 * rec_tri[r];
+      const double dx = k.dxd;
       const double d1 = t.rx - si * dx, d2 = t.ry - sj * dx, d3 = t.rz;
       const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
       const double fcb = 10.0 * (0.078 - dr) * bond / dr;
       const double fX = fcb * d1, fY = fcb * d2, fZ = fcb * d3;
       double drv[3];
       for (int m = 0; m < 3; ++m) {
-        const double a = t.rx - X[eo + nd[m]], b = t.ry - Y[eo + nd[m]], c = t.rz - Z[eo + nd[m]];
-        drv[m] = sqrt(a * a + b * b + c * c);
+        const double a1 = t.rx - X[eo + nd[m]], b1 = t.ry - Y[eo + nd[m]], c1 = t.rz - Z[eo + nd[m]];
+        drv[m] = sqrt(a1 * a1 + b1 * b1 + c1 * c1);
       }
       const double sum = 1.0 / drv[0] + 1.0 / drv[1] + 1.0 / drv[2];
       for (int m = 0; m < 3; ++m) {
@@ -823,27 +1047,29 @@ __global__ void __launch_bounds__(1024) bonds_k(PlateletConst k, const double* X
   if ((threadIdx.x & 31) == 0) s_tot[threadIdx.x >> 5] = tot;
   __syncthreads();
   if (threadIdx.x == 0) {
-    long long s = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += s_tot[w];
-    ctl->total_bond = (int)s;
+    long long sm = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sm += s_tot[w];
+    ctl->total_bond = (int)sm;
     ctl->nops = nops;
+    ctl->nops_active[0] = 0;
+    ctl->nops_active[1] = 0;
   }
 }
 
 }  // namespace
 
-int membrane_threads() { return 256; }
+int membrane_threads() { return 512; }
 
 cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st) {
   const PlateletConst& k = Pl.k;
   if (k.P == 0) return cudaSuccess;
   if (precision == PF_PREC_FP64)
-    membrane_k<double><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
+    membrane_k<double><<<k.P, 512, 0, st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
                                             Pl.vert_local, Pl.ring, Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0,
                                             Pl.S0_all, Pl.V0, (double*)Pl.nN, (double*)Pl.nelem, (double*)Pl.S,
                                             (double*)Pl.km, Pl.SV, (double*)Pl.Fmem, ctl);
   else
-    membrane_k<float><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
+    membrane_k<float><<<k.P, 512, (size_t)k.E * 4 * sizeof(float), st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
                                            Pl.vert_local, Pl.ring, Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0,
                                            Pl.S0_all, Pl.V0, (float*)Pl.nN, (float*)Pl.nelem, (float*)Pl.S,
                                            (float*)Pl.km, Pl.SV, (float*)Pl.Fmem, ctl);
@@ -854,19 +1080,35 @@ cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_
   const PlateletConst& k = Pl.k;
   const int PE = k.P * k.E;
   if (!k.morse || PE == 0) return cudaSuccess;
-  const unsigned grid = (PE + 127) / 128;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
+  const unsigned grid = (unsigned)std::min(ncells, sms * 16);
+  sort_bins_k<<<(unsigned)std::min(ncells, sms * 8), 256, 0, st>>>(ncells, Pl.bin_count, (float4*)Pl.bin, ctl);
+  bool fast = precision != PF_PREC_FP64;
+  for (int a = 0; a < 3; ++a)
+    if (k.wrap[a] && k.ncell[a] < 3) fast = false;
   if (precision == PF_PREC_FP64)
-    morse_k<double><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, Pl.bin, Pl.Fmorse, ctl);
+    morse_k<double, false><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, (const float4*)Pl.bin,
+                                                 Pl.Fmorse, ctl);
+  else if (fast)
+    morse_k<float, true><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, (const float4*)Pl.bin, Pl.Fmorse,
+                                               ctl);
   else
-    morse_k<float><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, Pl.bin, Pl.Fmorse, ctl);
+    morse_k<float, false><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, (const float4*)Pl.bin,
+                                                Pl.Fmorse, ctl);
   return cudaGetLastError();
 }
 
 cudaError_t fibrin_forces(Fibrin& Fb, int precision, Control* ctl, cudaStream_t st) {
-  (void)precision;
   if (Fb.M == 0) return cudaSuccess;
-  fibrin_k<<<(Fb.M + 255) / 256, 256, 0, st>>>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr, Fb.nbr,
-                                                Fb.L0, Fb.F, ctl);
+  if (precision == PF_PREC_FP64)
+    fibrin_k<double><<<(Fb.M + 127) / 128, 128, 0, st>>>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr,
+                                                         Fb.nbr, Fb.L0, Fb.F, ctl);
+  else
+    fibrin_k<float><<<(Fb.M + 127) / 128, 128, 0, st>>>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr,
+                                                        Fb.nbr, Fb.L0, Fb.F, ctl);
   return cudaGetLastError();
 }
 
@@ -875,21 +1117,33 @@ cudaError_t bond_pass(Platelets& Pl, int precision, Control* ctl, cudaStream_t s
   const int NR = k.P * k.nrec;
   if (NR == 0) return cudaSuccess;
   RecTmp* tmp = (RecTmp*)Pl.rec_tmp;
-  unsigned long long* ops = (unsigned long long*)(tmp + NR);
+  int* active = (int*)(tmp + NR);
+  size_t ops_n = 1;
+  while (ops_n < (size_t)2 * NR) ops_n <<= 1;
+  unsigned long long* ops = (unsigned long long*)(((uintptr_t)(active + NR) + 15) & ~(uintptr_t)15);
   const int cap = 2 * NR;
+  const int PE = k.P * k.E;
+  const int fb = precision == PF_PREC_FP64 ? 8 : 4;
+  const int threads = 256;
+  int blocks = (NR + threads - 1) / threads;
+  bonds_prepare_k<<<blocks, threads, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.r1, Pl.r2, Pl.rec_state,
+                                              tmp, active, ops, cap, Pl.Fbond, fb, ctl);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  (void)PE;
   if (precision == PF_PREC_FP64)
-    bonds_k<double><<<1, 1024, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.r1, Pl.r2, Pl.rec_state,
-                                        Pl.vwf, tmp, ops, cap, (double*)Pl.Fbond, ctl);
+    bonds_resolve_k<double><<<1, 1024, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.rec_state, Pl.vwf, tmp,
+                                                active, ops, cap, (double*)Pl.Fbond, ctl);
   else
-    bonds_k<float><<<1, 1024, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.r1, Pl.r2, Pl.rec_state,
-                                       Pl.vwf, tmp, ops, cap, (float*)Pl.Fbond, ctl);
+    bonds_resolve_k<float><<<1, 1024, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.rec_state, Pl.vwf, tmp,
+                                               active, ops, cap, (float*)Pl.Fbond, ctl);
   return cudaGetLastError();
 }
 
 size_t bond_scratch_bytes(int NR) {
   size_t ops = 1;
   while (ops < (size_t)2 * NR) ops <<= 1;
-  return (size_t)NR * sizeof(RecTmp) + ops * sizeof(unsigned long long) + 64;
+  return (size_t)NR * sizeof(RecTmp) + (size_t)NR * sizeof(int) + 16 + ops * sizeof(unsigned long long) + 64;
 }
 
 cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st) {
@@ -923,7 +1177,7 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
   PlateletConst pk{};
   if (Pl) pk = Pl->k;
   int* bc = (Pl && Pl->k.morse) ? Pl->bin_count : nullptr;
-  int* bn = (Pl && Pl->k.morse) ? Pl->bin : nullptr;
+  float4* bn = (Pl && Pl->k.morse) ? (float4*)Pl->bin : nullptr;
   if (L.precision == PF_PREC_FP64)
     interp_advance_k<double><<<grid, 128, 0, st>>>(
         L.k, pk, (const D4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
@@ -943,7 +1197,8 @@ cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st) {
   const int PE = Pl.k.P * Pl.k.E;
   if (!Pl.k.morse || PE == 0) return cudaSuccess;
   cudaMemsetAsync(Pl.bin_count, 0, sizeof(int) * (size_t)Pl.ncells, st);
-  bin_elements_k<<<(PE + 127) / 128, 128, 0, st>>>(Pl.k, PE, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, Pl.bin, ctl);
+  cudaMemsetAsync(&ctl->occupied, 0, sizeof(int), st);
+  bin_elements_k<<<(PE + 127) / 128, 128, 0, st>>>(Pl.k, PE, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, (float4*)Pl.bin, ctl);
   return cudaGetLastError();
 }
 
