@@ -99,7 +99,9 @@ typedef struct pf_scene {
   int bond_model;               /* PF_BOND_* */
   double p_on, p_off;           /* per-draw probabilities for PF_BOND_CONSTANT */
 
-  /* Morse pair forces between elements (within and between platelets) */
+  /* Morse pair forces between elements (within and between platelets),
+   * force-shifted at the cutoff: f = (F(r) - F(cutoff)) r_hat with
+   * F(r) = 2 rho U0 [e^{2 rho (r_eq - r)} - e^{rho (r_eq - r)}] */
   int morse;                    /* 0 = off */
   double morse_intra[4];        /* U0, rho, r_eq, cutoff (same platelet) */
   double morse_inter[4];        /* U0, rho, r_eq, cutoff (different platelets) */

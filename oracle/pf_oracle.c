@@ -674,8 +674,16 @@ static void build_cells(pfo_sim *s) {
   free(fill);
 }
 
-/* F = 2 rho U0 [e^{2rho(req-r)} - e^{rho(req-r)}] (xi - xj)/r for r < cutoff,
- * the derivative of V(r) = U0[e^{2rho(req-r)} - 2 e^{rho(req-r)}]. */
+/* Force-shifted Morse pair force for 0 < r < cutoff:
+ *   F(r) = 2 rho U0 [e^{2rho(req-r)} - e^{rho(req-r)}]   (-dV/dr of
+ *   V(r) = U0[e^{2rho(req-r)} - 2 e^{rho(req-r)}]),
+ *   f_i += (F(r) - F(cutoff)) (xi - xj)/r,
+ * so the force is continuous at the cutoff (a plain truncation jumps there,
+ * and pairs sitting at the cutoff then decide the result by rounding). */
+static double morse_F(const double *mp, double r) {
+  double ex = exp(mp[1] * (mp[2] - r));
+  return 2.0 * mp[1] * mp[0] * (ex * ex - ex);
+}
 static void morse_forces(pfo_sim *s) {
   build_cells(s);
   const int E = s->E;
@@ -715,8 +723,7 @@ static void morse_forces(pfo_sim *s) {
             double r = nrm3(d[0], d[1], d[2]);
             const double *mp = (h / E == pg) ? s->sc.morse_intra : s->sc.morse_inter;
             if (!(r < mp[3]) || r <= 0) continue;
-            double ex = exp(mp[1] * (mp[2] - r));
-            double f = 2.0 * mp[1] * mp[0] * (ex * ex - ex) / r;
+            double f = (morse_F(mp, r) - morse_F(mp, mp[3])) / r;
             fx += f * d[0]; fy += f * d[1]; fz += f * d[2];
           }
         }

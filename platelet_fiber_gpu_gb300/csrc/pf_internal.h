@@ -79,6 +79,7 @@ struct PlateletConst {
   uint64_t seed;
   int morse;
   double morse_intra[4], morse_inter[4];
+  double morse_fc[2];  // F(cutoff) of the intra / inter parameter sets (force shift)
   int ncell[3];
   double cs[3];
   double L[3];
@@ -110,6 +111,7 @@ struct Platelets {
   int* bin_count = nullptr;
   void* bin = nullptr;  // float4 [ncells][kBinCap]: cell-relative position, element id
   int ncells = 0;
+  double* bounds = nullptr;  // [P][4] origin and bounding radius (Morse culling)
   size_t bytes = 0;
 };
 
@@ -144,6 +146,8 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
 cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st);
 cudaError_t lattice_step_binned(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st);
 size_t bond_scratch_bytes(int NR);
+bool morse_uses_cells(const PlateletConst& k);
+cudaError_t sort_cell_bins(Platelets& Pl, Control* ctl, cudaStream_t st);
 
 int membrane_threads();
 

@@ -281,6 +281,12 @@ static int build_platelets(pfgpu_job* j, const pf_scene* s) {
   k.bond_model = s->bond_model; k.p_on = s->p_on; k.p_off = s->p_off; k.seed = s->seed;
   k.morse = s->morse;
   for (int a = 0; a < 4; ++a) { k.morse_intra[a] = s->morse_intra[a]; k.morse_inter[a] = s->morse_inter[a]; }
+  auto Fcut = [](const double* mp) {
+    const double ex = std::exp(mp[1] * (mp[2] - mp[3]));
+    return 2.0 * mp[1] * mp[0] * (ex * ex - ex);
+  };
+  k.morse_fc[0] = Fcut(s->morse_intra);
+  k.morse_fc[1] = Fcut(s->morse_inter);
   k.nx = s->nx; k.ny = s->ny; k.nz = s->nz;
   const int n3[3] = {s->nx, s->ny, s->nz};
   const double rc = s->morse_intra[3] > s->morse_inter[3] ? s->morse_intra[3] : s->morse_inter[3];
@@ -349,6 +355,7 @@ static int build_platelets(pfgpu_job* j, const pf_scene* s) {
   if (s->vwf) vw.assign(s->vwf, s->vwf + vw.size());
   CK(dupload(j, &P.vwf, vw.data(), vw.size()));
   if (NR) CK(dalloc(j, (char**)&P.rec_tmp, bond_scratch_bytes((int)NR)));
+  CK(dalloc(j, &P.bounds, (size_t)k.P * 4));
   if (k.morse) {
     P.ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
     CK(dalloc(j, &P.bin_count, (size_t)P.ncells));
@@ -390,7 +397,7 @@ static int enqueue_step(pfgpu_job* j) {
     launches++;
     if (Pl->k.morse && Pl->k.P * Pl->k.E) {
       CK(morse_forces(*Pl, j->precision, j->ctl, j->s2));
-      launches += 2;
+      launches += 2;  // bounds + pairs, or bin sort + pairs
     }
     if (Pl->k.nrec) {
       CK(bond_pass(*Pl, j->precision, j->ctl, j->s0));
@@ -411,7 +418,8 @@ static int enqueue_step(pfgpu_job* j) {
     CK(spread_markers(j->L, Pl, Fb, j->ctl, j->s0));
     launches++;
   }
-  CK(lattice_step_binned(j->L, j->ctl, Pl && Pl->k.morse ? Pl->bin_count : nullptr, Pl ? Pl->ncells : 0, j->s0));
+  const bool cells = Pl && Pl->k.morse && morse_uses_cells(Pl->k);
+  CK(lattice_step_binned(j->L, j->ctl, cells ? Pl->bin_count : nullptr, cells ? Pl->ncells : 0, j->s0));
   launches++;
   if (Pl || Fb) {
     CK(lattice_moments_active(j->L, j->ctl, j->s0));

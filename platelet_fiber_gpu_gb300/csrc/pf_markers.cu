@@ -745,6 +745,7 @@ __global__ void __launch_bounds__(128) morse_k(PlateletConst k, const double* X,
   const R U0a = (R)k.morse_intra[0], rhoa = (R)k.morse_intra[1], reqa = (R)k.morse_intra[2], rca = (R)k.morse_intra[3];
   const R U0b = (R)k.morse_inter[0], rhob = (R)k.morse_inter[1], reqb = (R)k.morse_inter[2], rcb = (R)k.morse_inter[3];
   const R rc2a = rca * rca, rc2b = rcb * rcb;
+  const R Fca = (R)k.morse_fc[0], Fcb = (R)k.morse_fc[1];
   const float cs0 = (float)k.cs[0], cs1 = (float)k.cs[1], cs2 = (float)k.cs[2];
   for (int oc = blockIdx.x; oc < nocc; oc += gridDim.x) {
     const int c = occ[oc];
@@ -800,17 +801,18 @@ __global__ void __launch_bounds__(128) morse_k(PlateletConst k, const double* X,
             const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
             if (!(r2 < (intra ? rc2a : rc2b)) || !(r2 > (R)0)) continue;
             const R U0 = intra ? U0a : U0b, rho = intra ? rhoa : rhob, req = intra ? reqa : reqb;
+            const R Fc = intra ? Fca : Fcb;
             R fr;
             if (sizeof(R) == 4) {
               const float rinv = rsqrtf((float)r2);
               const float r = (float)r2 * rinv;
               const float ex = __expf((float)rho * ((float)req - r));
-              fr = (R)(2.0f * (float)rho * (float)U0 * (ex * ex - ex) * rinv);
+              fr = (R)((2.0f * (float)rho * (float)U0 * (ex * ex - ex) - (float)Fc) * rinv);
             } else {
               const R r = sqrt(r2);
               if (!(r < (intra ? rca : rcb))) continue;
               const R ex = exp(rho * (req - r));
-              fr = (R)2.0 * rho * U0 * (ex * ex - ex) / r;
+              fr = ((R)2.0 * rho * U0 * (ex * ex - ex) - Fc) / r;
             }
             ax += fr * d0; ay += fr * d1; az += fr * d2;
           }
@@ -822,6 +824,137 @@ __global__ void __launch_bounds__(128) morse_k(PlateletConst k, const double* X,
         Fm[PE + g] = (double)ay * sc;
         Fm[2 * PE + g] = (double)az * sc;
       }
+    }
+  }
+}
+
+// Per-platelet all-pairs Morse (platelets of at most kMorseTileE elements):
+// the platelet's elements, relative to its first element with the minimum
+// image, are staged in shared memory; several CTAs share a platelet, each
+// owning a slice of its elements; other platelets whose bounding spheres come
+// within the inter-platelet cutoff are staged and scanned the same way.  Same
+// pair set and formula as the cell-list kernel, summed in element order.
+constexpr int kMorseTileE = 2048;
+
+__global__ void platelet_bounds_k(PlateletConst k, const double* X, const double* Y, const double* Z,
+                                  double* bounds /*[P][4]: origin xyz, radius*/, const Control* ctl) {
+  if (ctl->done) return;
+  const int p = blockIdx.x;
+  const int base = p * k.E;
+  const double ox = X[base], oy = Y[base], oz = Z[base];
+  double r2max = 0;
+  for (int e = threadIdx.x; e < k.E; e += blockDim.x) {
+    double d[3] = {X[base + e] - ox, Y[base + e] - oy, Z[base + e] - oz};
+    for (int a = 0; a < 3; ++a)
+      if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
+    r2max = fmax(r2max, d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  }
+  for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+  __shared__ double s_r[32];
+  if ((threadIdx.x & 31) == 0) s_r[threadIdx.x >> 5] = r2max;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, s_r[w]);
+    bounds[4 * p] = ox; bounds[4 * p + 1] = oy; bounds[4 * p + 2] = oz;
+    bounds[4 * p + 3] = sqrt(m);
+  }
+}
+
+template <class R>
+struct Staged;
+template <>
+struct Staged<float> {
+  using T = float4;
+  static __device__ __forceinline__ T make(double x, double y, double z, int id) {
+    return make_float4((float)x, (float)y, (float)z, __int_as_float(id));
+  }
+};
+template <>
+struct Staged<double> {
+  using T = D4;
+  static __device__ __forceinline__ T make(double x, double y, double z, int id) { return D4{x, y, z, (double)id}; }
+};
+
+template <class R>
+__device__ __forceinline__ void stage_platelet(const PlateletConst& k, const double* X, const double* Y,
+                                               const double* Z, int q, double ox, double oy, double oz,
+                                               typename Staged<R>::T* s_t) {
+  const int base = q * k.E;
+  for (int e = threadIdx.x; e < k.E; e += blockDim.x) {
+    double d[3] = {X[base + e] - ox, Y[base + e] - oy, Z[base + e] - oz};
+    for (int a = 0; a < 3; ++a)
+      if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
+    s_t[e] = Staged<R>::make(d[0], d[1], d[2], base + e);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) morse_platelet_k(PlateletConst k, const double* X, const double* Y,
+                                                        const double* Z, const double* bounds, int slices,
+                                                        double* Fm, Control* ctl) {
+  if (ctl->done) return;
+  using T = typename Staged<R>::T;
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  T* s_t = reinterpret_cast<T*>(s_raw);
+  const int PE = k.P * k.E;
+  const int p = blockIdx.x / slices, sl = blockIdx.x % slices;
+  const int per = (k.E + slices - 1) / slices;
+  const int e0 = sl * per, e1 = min(k.E, e0 + per);
+  const double ox = bounds[4 * p], oy = bounds[4 * p + 1], oz = bounds[4 * p + 2], rp = bounds[4 * p + 3];
+  stage_platelet<R>(k, X, Y, Z, p, ox, oy, oz, s_t);
+  __syncthreads();
+  const R U0a = (R)k.morse_intra[0], rhoa = (R)k.morse_intra[1], reqa = (R)k.morse_intra[2];
+  const R rca = (R)k.morse_intra[3], rc2a = rca * rca, Fca = (R)k.morse_fc[0];
+  const R U0b = (R)k.morse_inter[0], rhob = (R)k.morse_inter[1], reqb = (R)k.morse_inter[2];
+  const R rcb = (R)k.morse_inter[3], rc2b = rcb * rcb, Fcb = (R)k.morse_fc[1];
+  for (int e = e0 + threadIdx.x; e - threadIdx.x < e1; e += blockDim.x) {
+    const bool valid = e < e1;
+    T own = valid ? s_t[e] : Staged<R>::make(0, 0, 0, 0);
+    R ax = 0, ay = 0, az = 0;
+    auto pair = [&](const T mb, R U0, R rho, R req, R rc, R rc2, R Fc) {
+      const R d0 = (R)own.x - (R)mb.x, d1 = (R)own.y - (R)mb.y, d2 = (R)own.z - (R)mb.z;
+      const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
+      if (!(r2 < rc2) || !(r2 > (R)0)) return;
+      R fr;
+      if constexpr (sizeof(R) == 4) {
+        const float rinv = rsqrtf(r2);
+        const float r = r2 * rinv;
+        const float ex = __expf(rho * (req - r));
+        fr = (2.0f * rho * U0 * (ex * ex - ex) - Fc) * rinv;
+      } else {
+        const R r = sqrt(r2);
+        if (!(r < rc)) return;
+        const R ex = exp(rho * (req - r));
+        fr = ((R)2.0 * rho * U0 * (ex * ex - ex) - Fc) / r;
+      }
+      ax += fr * d0; ay += fr * d1; az += fr * d2;
+    };
+    if (valid) {
+#pragma unroll 4
+      for (int j = 0; j < k.E; ++j) pair(s_t[j], U0a, rhoa, reqa, rca, rc2a, Fca);
+    }
+    // other platelets whose bounding spheres reach within the cutoff
+    for (int q = 0; q < k.P; ++q) {
+      if (q == p) continue;
+      double d[3] = {bounds[4 * q] - ox, bounds[4 * q + 1] - oy, bounds[4 * q + 2] - oz};
+      for (int a = 0; a < 3; ++a)
+        if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
+      const double reach = rp + bounds[4 * q + 3] + k.morse_inter[3];
+      if (d[0] * d[0] + d[1] * d[1] + d[2] * d[2] >= reach * reach) continue;
+      __syncthreads();
+      T* s_q = s_t + k.E;
+      stage_platelet<R>(k, X, Y, Z, q, ox, oy, oz, s_q);
+      __syncthreads();
+      if (valid)
+        for (int j = 0; j < k.E; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
+    }
+    if (valid) {
+      const int g = p * k.E + e;
+      const double sc = 1.0 / (double)k.f0;
+      Fm[g] = (double)ax * sc;
+      Fm[PE + g] = (double)ay * sc;
+      Fm[2 * PE + g] = (double)az * sc;
     }
   }
 }
@@ -862,7 +995,8 @@ __global__ void fibrin_k(int M, int law, double kk, double mass, const double* X
 
 // ---------------------------------------------------------------- bonds
 struct RecTmp {
-  double rx, ry, rz;
+  double ds[3], dc[3];  // receptor minus anchor for the stored site and the claim site
+  double drv[3];        // receptor to each vertex of its triangle
   int bond0, si, sj, ci, cj;
   int kind[2];  // 0 none, 1 claim, 2 release
   int ok[2];
@@ -907,12 +1041,17 @@ __global__ void bonds_prepare_k(PlateletConst k, const double* X, const double* 
   t.ok[0] = t.ok[1] = 0;
   const double rx = wa * X[eo + nd[0]] + wb * X[eo + nd[1]] + wc * X[eo + nd[2]];
   const double ry = wa * Y[eo + nd[0]] + wb * Y[eo + nd[1]] + wc * Y[eo + nd[2]];
-  t.rx = rx; t.ry = ry; t.rz = rz;
   t.bond0 = bond;
   t.si = st[0]; t.sj = st[1];
   const int si = bond ? st[0] : (int)(rx / dx + 0.5), sj = bond ? st[1] : (int)(ry / dx + 0.5);
   t.ci = (int)(rx / dx + 0.5);
   t.cj = (int)(ry / dx + 0.5);
+  t.ds[0] = rx - t.si * dx; t.ds[1] = ry - t.sj * dx; t.ds[2] = rz;
+  t.dc[0] = rx - t.ci * dx; t.dc[1] = ry - t.cj * dx; t.dc[2] = rz;
+  for (int m = 0; m < 3; ++m) {
+    const double a1 = rx - X[eo + nd[m]], b1 = ry - Y[eo + nd[m]], c1 = rz - Z[eo + nd[m]];
+    t.drv[m] = sqrt(a1 * a1 + b1 * b1 + c1 * c1);
+  }
   const double d1 = rx - si * dx, d2 = ry - sj * dx, d3 = rz;
   const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
   const double w = fabs(0.078 - dr);
@@ -1009,10 +1148,11 @@ __global__ void __launch_bounds__(1024) bonds_resolve_k(PlateletConst k, const d
     const int r = active[a];
     const RecTmp t = tmp[r];
     int bond = t.bond0, si = t.bond0 ? t.si : -1, sj = t.bond0 ? t.sj : -1;
+    bool at_claim = false;
     for (int o = 0; o < 2; ++o) {
       if (!t.kind[o] || !t.ok[o]) continue;
-      if (t.kind[o] == 1) { bond++; si = t.ci; sj = t.cj; }
-      else { bond--; if (bond == 0) { si = -1; sj = -1; } }
+      if (t.kind[o] == 1) { bond++; si = t.ci; sj = t.cj; at_claim = true; }
+      else { bond--; if (bond == 0) { si = -1; sj = -1; at_claim = false; } }
     }
     int* st = rec_state + 3 * r;
     st[0] = si; st[1] = sj;
@@ -1020,16 +1160,12 @@ __global__ void __launch_bounds__(1024) bonds_resolve_k(PlateletConst k, const d
       const int p = r / k.nrec;
       const int eo = p * k.E;
       const int* nd = tri + 6 * rec_tri[r];
-      const double dx = k.dxd;
-      const double d1 = t.rx - si * dx, d2 = t.ry - sj * dx, d3 = t.rz;
+      const double* dv = at_claim ? t.dc : t.ds;
+      const double d1 = dv[0], d2 = dv[1], d3 = dv[2];
       const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
       const double fcb = 10.0 * (0.078 - dr) * bond / dr;
       const double fX = fcb * d1, fY = fcb * d2, fZ = fcb * d3;
-      double drv[3];
-      for (int m = 0; m < 3; ++m) {
-        const double a1 = t.rx - X[eo + nd[m]], b1 = t.ry - Y[eo + nd[m]], c1 = t.rz - Z[eo + nd[m]];
-        drv[m] = sqrt(a1 * a1 + b1 * b1 + c1 * c1);
-      }
+      const double* drv = t.drv;
       const double sum = 1.0 / drv[0] + 1.0 / drv[1] + 1.0 / drv[2];
       for (int m = 0; m < 3; ++m) {
         const int e = eo + nd[m];
@@ -1076,6 +1212,9 @@ cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStre
   return cudaGetLastError();
 }
 
+bool morse_uses_cells(const PlateletConst& k) { return k.E > kMorseTileE; }
+
+
 cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st) {
   const PlateletConst& k = Pl.k;
   const int PE = k.P * k.E;
@@ -1083,6 +1222,22 @@ cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!morse_uses_cells(k)) {
+    platelet_bounds_k<<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, ctl);
+    int slices = (2 * sms + k.P - 1) / k.P;
+    slices = std::max(1, std::min(slices, (k.E + 63) / 64));
+    const size_t smem = 2 * (size_t)k.E * (precision == PF_PREC_FP64 ? sizeof(D4) : sizeof(float4));
+    if (precision == PF_PREC_FP64) {
+      cudaFuncSetAttribute(morse_platelet_k<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      morse_platelet_k<double><<<k.P * slices, 128, smem, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, slices, Pl.Fmorse,
+                                                                ctl);
+    } else {
+      cudaFuncSetAttribute(morse_platelet_k<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      morse_platelet_k<float><<<k.P * slices, 128, smem, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, slices, Pl.Fmorse,
+                                                               ctl);
+    }
+    return cudaGetLastError();
+  }
   const int ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
   const unsigned grid = (unsigned)std::min(ncells, sms * 16);
   sort_bins_k<<<(unsigned)std::min(ncells, sms * 8), 256, 0, st>>>(ncells, Pl.bin_count, (float4*)Pl.bin, ctl);
@@ -1098,6 +1253,14 @@ cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_
   else
     morse_k<float, false><<<grid, 128, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, (const float4*)Pl.bin,
                                                 Pl.Fmorse, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t sort_cell_bins(Platelets& Pl, Control* ctl, cudaStream_t st) {
+  const PlateletConst& k = Pl.k;
+  if (!k.morse) return cudaSuccess;
+  const int ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
+  sort_bins_k<<<(unsigned)std::min(ncells, 1216), 256, 0, st>>>(ncells, Pl.bin_count, (float4*)Pl.bin, ctl);
   return cudaGetLastError();
 }
 
@@ -1176,8 +1339,10 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
   const unsigned grid = (PE + M + 127) / 128 > 0 ? (PE + M + 127) / 128 : 1;
   PlateletConst pk{};
   if (Pl) pk = Pl->k;
-  int* bc = (Pl && Pl->k.morse) ? Pl->bin_count : nullptr;
-  float4* bn = (Pl && Pl->k.morse) ? (float4*)Pl->bin : nullptr;
+  // elements are binned every step only when the Morse pass uses the cell list
+  const bool cells = Pl && Pl->k.morse && morse_uses_cells(Pl->k);
+  int* bc = cells ? Pl->bin_count : nullptr;
+  float4* bn = cells ? (float4*)Pl->bin : nullptr;
   if (L.precision == PF_PREC_FP64)
     interp_advance_k<double><<<grid, 128, 0, st>>>(
         L.k, pk, (const D4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
