@@ -1,0 +1,338 @@
+"""Benchmark of the coupled platelet / fibrin / lattice-Boltzmann step.
+
+Workload (one step = one coupled step of the whole scene): D3Q19 BGK FP32
+channel 256x128x128, shear 1000 1/s through the reference's unit chain,
+50 platelets x 600 SEM elements (Poisson-disk placed), 20k-node / 40k-link
+fibrin mesh on the bottom wall, 200 receptors per platelet with constant
+per-step bond probabilities 1e-2 / 1e-3, Morse pairs.  Seeded synthetic
+inputs; the working set (2 x 318 MB of populations) is larger than L2.
+
+Prints one JSON line (rank 0):
+  value   MLUPS with the state resident in HBM (CUDA events around K graph
+          replays of the step),
+  e2e     the same K-step job through the C ABI from host buffers: scene
+          upload (pfgpu_job_create), K steps, download of the lattice and
+          element state (pfgpu_job_get_*), all inside the timed region,
+  roofline  the fused collide-stream kernel: 152 B/node algorithmic bytes
+          over its CUDA-event-measured duration (serialised pass),
+  cpu_baseline  the CPU oracle (FP64, all host threads) on a bounded sample.
+`--impl reference` times the CPU restatement of the reference's kernels
+(the oracle) instead and prints the same line with impl "reference".
+Multi-GPU: one independent replica per rank (no collective); value is the
+sum of the ranks' node updates over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BYTES_PER_NODE = {0: 304, 1: 152, 2: 76}  # algorithmic bytes per node-step (19 loads + 19 stores)
+PREC_NAME = {0: "f64", 1: "f32", 2: "f16-shifted"}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except (ValueError, KeyError):
+            pass
+    return 6800.0, "fallback"
+
+
+def lbm_traffic_per_node():
+    """DRAM bytes per node-step of the LBM kernel from the committed ncu
+    capture summary (profiles/lbm_step_traffic.json), or None."""
+    p = ROOT / "profiles" / "lbm_step_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text())
+    except ValueError:
+        return None
+
+
+def build_scene(args):
+    from platelet_fiber_gpu_gb300 import workloads as W
+    return W.single_large(seed=args.seed, nx=args.nx, ny=args.ny, nz=args.nz, n_platelets=args.platelets,
+                          n_fib=args.fibrin, n_links=2 * args.fibrin)
+
+
+def cpu_oracle_rate(scene, budget_s: float, max_steps: int, threads: int):
+    """Oracle steps on the host until the budget is spent; returns
+    (MLUPS, steps, seconds, threads)."""
+    from oracle import binding as ob
+    ob.set_threads(threads)
+    o = ob.Oracle(scene)
+    o.step(1)  # warm-up
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps:
+        o.step(1)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return scene.n_nodes * n / dt / 1e6, n, dt
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    scene = build_scene(args)
+    threads = os.cpu_count() or 1
+    total_budget = float(os.environ.get("PF_REF_BUDGET_S", "120"))
+    mlups, n, dt = cpu_oracle_rate(scene, total_budget, args.steps, threads)
+    line = {
+        "impl": "reference", "metric": "MLUPS (coupled LBM+IBM+SEM+fibrin step)", "value": round(mlups, 3),
+        "unit": "MLUPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / n * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(args), "timed_steps": n},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": f"{n} coupled steps of the full scene after 1 warm-up step (budget "
+                                   f"{total_budget:.0f} s); CPU restatement of the reference kernels, FP64, "
+                                   f"OpenMP {threads} threads"},
+        "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_name(args):
+    return (f"single_large: D3Q19 {args.nx}x{args.ny}x{args.nz} shear 1000/s Zou/He walls, {args.platelets} platelets"
+            f" x 600 SEM elements (400 membrane + 200 cytoplasm, Morse U0=1 rho=2 r_eq=0.3 cut 1.0 um), "
+            f"{args.fibrin}-node/{2 * args.fibrin}-link Hookean fibrin on the bottom wall, 200 receptors/platelet, "
+            f"bond p_on/p_off 1e-2/1e-3 per step")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", type=int, default=1, help="0 fp64, 1 fp32, 2 fp16-shifted")
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--nx", type=int, default=256)
+    ap.add_argument("--ny", type=int, default=128)
+    ap.add_argument("--nz", type=int, default=128)
+    ap.add_argument("--platelets", type=int, default=50)
+    ap.add_argument("--fibrin", type=int, default=20000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--profile-steps", type=int, default=200)
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    from platelet_fiber_gpu_gb300 import gpu
+    from platelet_fiber_gpu_gb300.build import build
+    if rank == 0:
+        build()
+    if pg:
+        pg.barrier()
+
+    scene = build_scene(args)
+    prec = args.precision
+    fp16_scale = 4e-3 if prec == 2 else 0.0
+    N = scene.n_nodes
+    PE = scene.n_platelets * scene.n_elem
+
+    def barrier_sync():
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if not pg:
+            return x
+        t = torch.tensor([x], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident throughput: K graph replays of the step
+    job = gpu.Job(scene, prec, fp16_scale)
+    job.step(args.warmup, graph=True)
+    launches = job.launches_per_step
+    barrier_sync()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        stream = torch.cuda.current_stream()
+        start.record(stream)
+        t0 = time.perf_counter()
+        job.step(args.steps, graph=True)  # synchronises the job's stream before returning
+        stop.record(stream)
+        barrier_sync()
+        wall = time.perf_counter() - t0
+    # the job runs on its own stream and step() returns after it finished, so
+    # the host wall time and the event pair bracket the same work
+    dev_ms = start.elapsed_time(stop)
+    t_step = max_over_ranks(max(dev_ms / 1e3, wall) / args.steps)
+    value = world * N / t_step / 1e6
+    clk = clocks.summary()
+
+    # ---- live per-phase CUDA-event timing (serialised pass, same job)
+    phases = job.profile(args.profile_steps)
+    lbm_ms = phases["lbm"] / args.profile_steps
+    job.close()
+
+    # ---- end to end through the C ABI from host buffers
+    import ctypes
+    h2d_bytes = (19 * N + 3 * N + N) * 8 + 4 * PE * 8 + 3 * scene.n_fib * 8
+    d2h_bytes = (19 * N + 4 * N) * 8 + 4 * PE * 8 + 3 * PE * 8
+    barrier_sync()
+    scene.f_init = None
+    t0 = time.perf_counter()
+    j2 = gpu.Job(scene, prec, fp16_scale)
+    j2.step(args.steps, graph=True)
+    L = j2.lattice(fIN=True)
+    E = j2.elements()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    j2.close()
+    e2e_s = max_over_ranks(e2e_s)
+    e2e_value = world * N * args.steps / e2e_s / 1e6
+
+    peak, peak_kind = measured_peak()
+    bpn = BYTES_PER_NODE[prec]
+    achieved = N * bpn / (lbm_ms / 1e3) / 1e9
+    traffic = lbm_traffic_per_node()
+    traffic_per_launch = None
+    if traffic and traffic.get("precision") == prec:
+        traffic_per_launch = traffic["dram_bytes_per_node"] * N
+
+    line = {
+        "metric": "MLUPS (coupled LBM+IBM+SEM+fibrin step)",
+        "value": round(value, 1),
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t_step * 1e3, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": PREC_NAME[prec],
+        "data": "synthetic",
+        "config": {"workload": workload_name(args), "lattice": [args.nx, args.ny, args.nz], "nodes": N,
+                   "elements": PE, "fibrin_nodes": scene.n_fib, "receptors": scene.n_platelets * scene.n_rec,
+                   "parallelism": f"replicas x{world}", "l2": "working set > L2 (2 x 19 x N x 4 B populations)",
+                   "precision": PREC_NAME[prec]},
+        "sem_elem_steps_per_s": round(world * PE / t_step, 1),
+        "e2e": {"value": round(e2e_value, 1), "unit": "MLUPS",
+                "h2d_bytes_per_step": int(h2d_bytes / args.steps), "d2h_bytes_per_step": int(d2h_bytes / args.steps),
+                "seconds": round(e2e_s, 4),
+                "what": "pfgpu_job_create from host arrays + K graph steps + pfgpu_job_get_lattice/elements"},
+        "roofline": {"bound": "hbm", "kernel": "lbm_step_k", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "bytes_per_node": bpn, "launch_ms": round(lbm_ms, 5),
+                     "traffic": traffic_per_launch},
+        "phases_ms_per_step": {k: round(v / args.profile_steps, 5) for k, v in phases.items()},
+        "clocks": clk,
+        "gpu_launches": launches * args.steps,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        small = build_scene(args)
+        mlups, n, dt = cpu_oracle_rate(small, args.cpu_budget, 1000, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count() or 1,
+                                "kind": "port",
+                                "sample": f"{n} coupled steps of the same scene after 1 warm-up step "
+                                          f"({dt:.1f} s), FP64 CPU restatement of the reference kernels"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -111,7 +111,8 @@ struct Platelets {
   int* bin_count = nullptr;
   void* bin = nullptr;  // float4 [ncells][kBinCap]: cell-relative position, element id
   int ncells = 0;
-  double* bounds = nullptr;  // [P][4] origin and bounding radius (Morse culling)
+  double* bounds = nullptr;  // [P][4] centroid and bounding radius (Morse culling)
+  void* relpos = nullptr;    // Real4 [P*E] element positions relative to their centroid
   size_t bytes = 0;
 };
 

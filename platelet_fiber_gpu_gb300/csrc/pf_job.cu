@@ -356,6 +356,7 @@ static int build_platelets(pfgpu_job* j, const pf_scene* s) {
   CK(dupload(j, &P.vwf, vw.data(), vw.size()));
   if (NR) CK(dalloc(j, (char**)&P.rec_tmp, bond_scratch_bytes((int)NR)));
   CK(dalloc(j, &P.bounds, (size_t)k.P * 4));
+  CK(dalloc(j, (char**)&P.relpos, PE * 4 * rb));
   if (k.morse) {
     P.ncells = k.ncell[0] * k.ncell[1] * k.ncell[2];
     CK(dalloc(j, &P.bin_count, (size_t)P.ncells));
@@ -428,6 +429,43 @@ static int enqueue_step(pfgpu_job* j) {
   CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
   launches++;
   j->launches_per_step = launches;
+  return PFGPU_OK;
+}
+
+// Same launches as enqueue_step, on one stream, with an event pair around
+// each phase; the per-phase device times are summed over the steps.
+static const char* kPhaseNames[] = {"membrane", "morse", "fibrin", "bonds", "spread", "lbm", "moments", "interp"};
+static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
+  Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
+  Fibrin* Fb = j->has_fb ? &j->Fb : nullptr;
+  const int NPH = 8;
+  std::vector<cudaEvent_t> ev((size_t)2 * NPH * nsteps, nullptr);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  cudaStream_t s = j->s0;
+  auto rec = [&](int step, int ph, int end) { return cudaEventRecord(ev[((size_t)step * NPH + ph) * 2 + end], s); };
+  const bool cells = Pl && Pl->k.morse && morse_uses_cells(Pl->k);
+  for (int t = 0; t < nsteps; ++t) {
+    CK(rec(t, 0, 0)); if (Pl) CK(membrane_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 0, 1));
+    CK(rec(t, 1, 0)); if (Pl && Pl->k.morse) CK(morse_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 1, 1));
+    CK(rec(t, 2, 0)); if (Fb) CK(fibrin_forces(*Fb, j->precision, j->ctl, s)); CK(rec(t, 2, 1));
+    CK(rec(t, 3, 0)); if (Pl && Pl->k.nrec) CK(bond_pass(*Pl, j->precision, j->ctl, s)); CK(rec(t, 3, 1));
+    CK(rec(t, 4, 0)); if (Pl || Fb) CK(spread_markers(j->L, Pl, Fb, j->ctl, s)); CK(rec(t, 4, 1));
+    CK(rec(t, 5, 0));
+    CK(lattice_step_binned(j->L, j->ctl, cells ? Pl->bin_count : nullptr, cells ? Pl->ncells : 0, s));
+    CK(rec(t, 5, 1));
+    CK(rec(t, 6, 0)); if (Pl || Fb) CK(lattice_moments_active(j->L, j->ctl, s)); CK(rec(t, 6, 1));
+    CK(rec(t, 7, 0)); CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, s));
+    CK(rec(t, 7, 1));
+  }
+  CK(cudaStreamSynchronize(s));
+  for (int ph = 0; ph < NPH; ++ph) ms[ph] = 0;
+  for (int t = 0; t < nsteps; ++t)
+    for (int ph = 0; ph < NPH; ++ph) {
+      float f = 0;
+      CK(cudaEventElapsedTime(&f, ev[((size_t)t * NPH + ph) * 2], ev[((size_t)t * NPH + ph) * 2 + 1]));
+      ms[ph] += f;
+    }
+  for (auto& e : ev) cudaEventDestroy(e);
   return PFGPU_OK;
 }
 
@@ -597,6 +635,14 @@ int pfgpu_job_enqueue(pfgpu_job* j, int nsteps, cudaStream_t) {
   for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(j->graph, j->s0));
   return PFGPU_OK;
 }
+
+int pfgpu_job_profile(pfgpu_job* j, int nsteps, double ms_out[8]) {
+  if (!j || nsteps < 1 || !ms_out) return set_error(PFGPU_ERR_INVALID, "bad arguments");
+  int rc = profile_steps(j, nsteps, ms_out);
+  if (rc) return rc;
+  return check_control(j);
+}
+const char* pfgpu_profile_phase_name(int i) { return (i >= 0 && i < 8) ? kPhaseNames[i] : ""; }
 
 int pfgpu_job_sync(pfgpu_job* j) {
   if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");

@@ -836,31 +836,10 @@ __global__ void __launch_bounds__(128) morse_k(PlateletConst k, const double* X,
 // pair set and formula as the cell-list kernel, summed in element order.
 constexpr int kMorseTileE = 2048;
 
-__global__ void platelet_bounds_k(PlateletConst k, const double* X, const double* Y, const double* Z,
-                                  double* bounds /*[P][4]: origin xyz, radius*/, const Control* ctl) {
-  if (ctl->done) return;
-  const int p = blockIdx.x;
-  const int base = p * k.E;
-  const double ox = X[base], oy = Y[base], oz = Z[base];
-  double r2max = 0;
-  for (int e = threadIdx.x; e < k.E; e += blockDim.x) {
-    double d[3] = {X[base + e] - ox, Y[base + e] - oy, Z[base + e] - oz};
-    for (int a = 0; a < 3; ++a)
-      if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
-    r2max = fmax(r2max, d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-  }
-  for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
-  __shared__ double s_r[32];
-  if ((threadIdx.x & 31) == 0) s_r[threadIdx.x >> 5] = r2max;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double m = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, s_r[w]);
-    bounds[4 * p] = ox; bounds[4 * p + 1] = oy; bounds[4 * p + 2] = oz;
-    bounds[4 * p + 3] = sqrt(m);
-  }
-}
-
+// Per platelet: centroid (minimum image about the first element), bounding
+// radius about the centroid, and every element's position relative to the
+// centroid -- float in the FP32 build, double in the FP64 build -- written
+// once per step so the pair kernel stages plain loads.
 template <class R>
 struct Staged;
 template <>
@@ -869,40 +848,88 @@ struct Staged<float> {
   static __device__ __forceinline__ T make(double x, double y, double z, int id) {
     return make_float4((float)x, (float)y, (float)z, __int_as_float(id));
   }
+  static __device__ __forceinline__ T shift(T a, double ox, double oy, double oz) {
+    return make_float4(a.x + (float)ox, a.y + (float)oy, a.z + (float)oz, a.w);
+  }
 };
 template <>
 struct Staged<double> {
   using T = D4;
   static __device__ __forceinline__ T make(double x, double y, double z, int id) { return D4{x, y, z, (double)id}; }
+  static __device__ __forceinline__ T shift(T a, double ox, double oy, double oz) {
+    return D4{a.x + ox, a.y + oy, a.z + oz, a.w};
+  }
 };
 
+__device__ __forceinline__ double min_image(double d, double L, int wrap) {
+  if (!wrap) return d;
+  if (d > 0.5 * L) d -= L;
+  else if (d < -0.5 * L) d += L;
+  return d;
+}
+
 template <class R>
-__device__ __forceinline__ void stage_platelet(const PlateletConst& k, const double* X, const double* Y,
-                                               const double* Z, int q, double ox, double oy, double oz,
-                                               typename Staged<R>::T* s_t) {
-  const int base = q * k.E;
+__global__ void __launch_bounds__(256) platelet_bounds_k(PlateletConst k, const double* X, const double* Y,
+                                                         const double* Z, double* bounds,
+                                                         typename Staged<R>::T* rel, const Control* ctl) {
+  if (ctl->done) return;
+  const int p = blockIdx.x;
+  const int base = p * k.E;
+  const double ox = X[base], oy = Y[base], oz = Z[base];
+  __shared__ double s_a[256], s_b[256], s_c[256];
+  double sx = 0, sy = 0, sz = 0;
   for (int e = threadIdx.x; e < k.E; e += blockDim.x) {
-    double d[3] = {X[base + e] - ox, Y[base + e] - oy, Z[base + e] - oz};
-    for (int a = 0; a < 3; ++a)
-      if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
-    s_t[e] = Staged<R>::make(d[0], d[1], d[2], base + e);
+    sx += min_image(X[base + e] - ox, k.L[0], k.wrap[0]);
+    sy += min_image(Y[base + e] - oy, k.L[1], k.wrap[1]);
+    sz += min_image(Z[base + e] - oz, k.L[2], k.wrap[2]);
+  }
+  s_a[threadIdx.x] = sx; s_b[threadIdx.x] = sy; s_c[threadIdx.x] = sz;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      s_a[threadIdx.x] += s_a[threadIdx.x + st];
+      s_b[threadIdx.x] += s_b[threadIdx.x + st];
+      s_c[threadIdx.x] += s_c[threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  const double cx_ = ox + s_a[0] / k.E, cy_ = oy + s_b[0] / k.E, cz_ = oz + s_c[0] / k.E;
+  __syncthreads();
+  double r2max = 0;
+  for (int e = threadIdx.x; e < k.E; e += blockDim.x) {
+    const double d0 = min_image(X[base + e] - cx_, k.L[0], k.wrap[0]);
+    const double d1 = min_image(Y[base + e] - cy_, k.L[1], k.wrap[1]);
+    const double d2 = min_image(Z[base + e] - cz_, k.L[2], k.wrap[2]);
+    rel[base + e] = Staged<R>::make(d0, d1, d2, base + e);
+    r2max = fmax(r2max, d0 * d0 + d1 * d1 + d2 * d2);
+  }
+  s_a[threadIdx.x] = r2max;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) s_a[threadIdx.x] = fmax(s_a[threadIdx.x], s_a[threadIdx.x + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    bounds[4 * p] = cx_; bounds[4 * p + 1] = cy_; bounds[4 * p + 2] = cz_;
+    bounds[4 * p + 3] = sqrt(s_a[0]);
   }
 }
 
 template <class R>
-__global__ void __launch_bounds__(128) morse_platelet_k(PlateletConst k, const double* X, const double* Y,
-                                                        const double* Z, const double* bounds, int slices,
-                                                        double* Fm, Control* ctl) {
+__global__ void __launch_bounds__(128) morse_platelet_k(PlateletConst k, const double* bounds,
+                                                        const typename Staged<R>::T* rel, int slices, double* Fm,
+                                                        Control* ctl) {
   if (ctl->done) return;
   using T = typename Staged<R>::T;
   extern __shared__ __align__(16) unsigned char s_raw[];
   T* s_t = reinterpret_cast<T*>(s_raw);
+  T* s_q = s_t + k.E;
   const int PE = k.P * k.E;
   const int p = blockIdx.x / slices, sl = blockIdx.x % slices;
   const int per = (k.E + slices - 1) / slices;
   const int e0 = sl * per, e1 = min(k.E, e0 + per);
-  const double ox = bounds[4 * p], oy = bounds[4 * p + 1], oz = bounds[4 * p + 2], rp = bounds[4 * p + 3];
-  stage_platelet<R>(k, X, Y, Z, p, ox, oy, oz, s_t);
+  const double cxp = bounds[4 * p], cyp = bounds[4 * p + 1], czp = bounds[4 * p + 2], rp = bounds[4 * p + 3];
+  for (int e = threadIdx.x; e < k.E; e += blockDim.x) s_t[e] = rel[p * k.E + e];
   __syncthreads();
   const R U0a = (R)k.morse_intra[0], rhoa = (R)k.morse_intra[1], reqa = (R)k.morse_intra[2];
   const R rca = (R)k.morse_intra[3], rc2a = rca * rca, Fca = (R)k.morse_fc[0];
@@ -910,7 +937,7 @@ __global__ void __launch_bounds__(128) morse_platelet_k(PlateletConst k, const d
   const R rcb = (R)k.morse_inter[3], rc2b = rcb * rcb, Fcb = (R)k.morse_fc[1];
   for (int e = e0 + threadIdx.x; e - threadIdx.x < e1; e += blockDim.x) {
     const bool valid = e < e1;
-    T own = valid ? s_t[e] : Staged<R>::make(0, 0, 0, 0);
+    const T own = valid ? s_t[e] : Staged<R>::make(0, 0, 0, 0);
     R ax = 0, ay = 0, az = 0;
     auto pair = [&](const T mb, R U0, R rho, R req, R rc, R rc2, R Fc) {
       const R d0 = (R)own.x - (R)mb.x, d1 = (R)own.y - (R)mb.y, d2 = (R)own.z - (R)mb.z;
@@ -934,17 +961,17 @@ __global__ void __launch_bounds__(128) morse_platelet_k(PlateletConst k, const d
 #pragma unroll 4
       for (int j = 0; j < k.E; ++j) pair(s_t[j], U0a, rhoa, reqa, rca, rc2a, Fca);
     }
-    // other platelets whose bounding spheres reach within the cutoff
+    // other platelets whose bounding spheres come within the inter cutoff,
+    // shifted into this platelet's centroid frame (minimum image)
     for (int q = 0; q < k.P; ++q) {
       if (q == p) continue;
-      double d[3] = {bounds[4 * q] - ox, bounds[4 * q + 1] - oy, bounds[4 * q + 2] - oz};
-      for (int a = 0; a < 3; ++a)
-        if (k.wrap[a]) d[a] -= k.L[a] * floor(d[a] / k.L[a] + 0.5);
+      const double o0 = min_image(bounds[4 * q] - cxp, k.L[0], k.wrap[0]);
+      const double o1 = min_image(bounds[4 * q + 1] - cyp, k.L[1], k.wrap[1]);
+      const double o2 = min_image(bounds[4 * q + 2] - czp, k.L[2], k.wrap[2]);
       const double reach = rp + bounds[4 * q + 3] + k.morse_inter[3];
-      if (d[0] * d[0] + d[1] * d[1] + d[2] * d[2] >= reach * reach) continue;
+      if (o0 * o0 + o1 * o1 + o2 * o2 >= reach * reach) continue;
       __syncthreads();
-      T* s_q = s_t + k.E;
-      stage_platelet<R>(k, X, Y, Z, q, ox, oy, oz, s_q);
+      for (int j = threadIdx.x; j < k.E; j += blockDim.x) s_q[j] = Staged<R>::shift(rel[q * k.E + j], o0, o1, o2);
       __syncthreads();
       if (valid)
         for (int j = 0; j < k.E; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
@@ -1223,18 +1250,20 @@ cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (!morse_uses_cells(k)) {
-    platelet_bounds_k<<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, ctl);
     int slices = (2 * sms + k.P - 1) / k.P;
     slices = std::max(1, std::min(slices, (k.E + 63) / 64));
-    const size_t smem = 2 * (size_t)k.E * (precision == PF_PREC_FP64 ? sizeof(D4) : sizeof(float4));
     if (precision == PF_PREC_FP64) {
+      platelet_bounds_k<double><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (D4*)Pl.relpos, ctl);
+      const size_t smem = 2 * (size_t)k.E * sizeof(D4);
       cudaFuncSetAttribute(morse_platelet_k<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      morse_platelet_k<double><<<k.P * slices, 128, smem, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, slices, Pl.Fmorse,
-                                                                ctl);
+      morse_platelet_k<double><<<k.P * slices, 128, smem, st>>>(k, Pl.bounds, (const D4*)Pl.relpos, slices,
+                                                                Pl.Fmorse, ctl);
     } else {
+      platelet_bounds_k<float><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (float4*)Pl.relpos, ctl);
+      const size_t smem = 2 * (size_t)k.E * sizeof(float4);
       cudaFuncSetAttribute(morse_platelet_k<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      morse_platelet_k<float><<<k.P * slices, 128, smem, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, slices, Pl.Fmorse,
-                                                               ctl);
+      morse_platelet_k<float><<<k.P * slices, 128, smem, st>>>(k, Pl.bounds, (const float4*)Pl.relpos, slices,
+                                                               Pl.Fmorse, ctl);
     }
     return cudaGetLastError();
   }

@@ -49,6 +49,9 @@ def lib():
         L.pfgpu_job_device_bytes.argtypes = [vp]
         L.pfgpu_job_launches_per_step.argtypes = [vp]
         L.pfgpu_job_destroy.argtypes = [vp]
+        L.pfgpu_job_profile.argtypes = [vp, C.c_int, dp]
+        L.pfgpu_profile_phase_name.restype = C.c_char_p
+        L.pfgpu_profile_phase_name.argtypes = [C.c_int]
         L.pfgpu_scene_device_bytes.restype = C.c_size_t
         L.pfgpu_scene_device_bytes.argtypes = [vp, C.c_int]
         L.pfgpu_last_error.restype = C.c_char_p
@@ -99,6 +102,12 @@ class Job:
     def step(self, n: int = 1, graph: bool = True) -> int:
         f = lib().pfgpu_job_step_graph if graph else lib().pfgpu_job_step
         return check(f(self.h, int(n)), allow_done=True)
+
+    def profile(self, n: int) -> dict:
+        """Per-phase device time (ms, summed over n serialised steps)."""
+        out = np.zeros(8)
+        check(lib().pfgpu_job_profile(self.h, int(n), _p(out)), allow_done=True)
+        return {lib().pfgpu_profile_phase_name(i).decode(): float(out[i]) for i in range(8)}
 
     @property
     def steps(self) -> int:
