@@ -220,7 +220,7 @@ def main():
 
     scene = build_scene(args)
     prec = args.precision
-    fp16_scale = 4e-3 if prec == 2 else 0.0
+    fp16_scale = 0.0
     N = scene.n_nodes
     PE = scene.n_platelets * scene.n_elem
 

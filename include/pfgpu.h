@@ -126,8 +126,9 @@ typedef struct pf_scene {
 typedef struct pfgpu_job pfgpu_job;
 
 /* Creates a device-resident simulation on the current CUDA device.
- * precision: PF_PREC_*; fp16_scale: population scale for PF_PREC_FP16
- * (ignored otherwise). */
+ * precision: PF_PREC_*; fp16_scale: sigma of the FP16 store
+ * q = (f - w)/(w sigma) (<= 0: eight times the shear wall speed in lattice
+ * units, or 0.05), ignored for FP32/FP64. */
 int pfgpu_job_create(const pf_scene *scene, int precision, double fp16_scale, pfgpu_job **out);
 /* Runs nsteps coupled steps (SEM+Morse+fibrin forces, bonds, IBM spreading,
  * fused collide-stream, moments, IBM interpolation, position update).
@@ -153,6 +154,10 @@ int pfgpu_job_get_fibrin(pfgpu_job *job, double *X, double *Y, double *Z, double
 /* Per-platelet FP64 reductions of the last force pass: [P][2] (S_all, V) and
  * the membrane vertex mean curvature km [P][n_membrane]. */
 int pfgpu_job_get_membrane(pfgpu_job *job, double *S_V, double *km);
+/* Morse cell lists rebuilt from the current positions: cell of every element
+ * [P*E], element count of every cell [ncells], members of each cell in
+ * ascending element id packed in cell order, grid dimensions [3]. */
+int pfgpu_job_get_cells(pfgpu_job *job, int *cell_of, int *counts, int *members, int *ncells3);
 /* FP64 conservation sums over the lattice: mass and x/y/z momentum. */
 int pfgpu_job_conservation(pfgpu_job *job, double out[4]);
 int64_t pfgpu_job_step_count(const pfgpu_job *job);

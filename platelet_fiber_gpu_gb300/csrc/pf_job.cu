@@ -124,7 +124,11 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
   uw = uw * s->dx;
   uw = uw / mp[PF_P_UMAX];
   k.uw = (double)uw / k.C;
-  k.fp16_scale = precision == PF_PREC_FP16 ? fp16_scale : 1.0;
+  // FP16 stores q = (f - w) / (w * sigma); sigma defaults to eight times the
+  // wall speed of a shear channel (or 0.05 lattice units otherwise)
+  double sigma = fp16_scale;
+  if (!(sigma > 0)) sigma = (s->bc[2] == PF_BC_ZOUHE_SHEAR && k.uw > 0) ? 8.0 * k.uw : 0.05;
+  k.fp16_scale = precision == PF_PREC_FP16 ? sigma : 1.0;
   k.dtT = s->dt / mp[PF_P_T0];
   return k;
 }
@@ -513,7 +517,6 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   *out = nullptr;
   int rc = validate(s, precision);
   if (rc) return rc;
-  if (precision == PF_PREC_FP16 && !(fp16_scale > 0)) return set_error(PFGPU_ERR_INVALID, "fp16_scale must be > 0");
   pfgpu_job* j = new pfgpu_job();
   j->precision = precision;
   j->detach_rate = s->detach_rate;
@@ -783,3 +786,36 @@ int pfgpu_job_control_(pfgpu_job* j, Control* out) {
 }  // extern "C"
 
 int pfgpu_set_error_(int code, const char* msg) { return set_error(code, msg); }
+
+extern "C" int pfgpu_job_get_cells(pfgpu_job* j, int* cell_of, int* counts, int* members, int* ncells3) {
+  // Rebuilds the Morse cell lists from the current positions (binning +
+  // per-cell sort by element id) and copies them out: the cell of every
+  // element, the element count of every cell and each cell's members in
+  // ascending element id ([ncells][count], packed in cell order).
+  if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
+  CK(cudaStreamSynchronize(j->s0));
+  if (!j->has_pl || !j->Pl.k.morse) return set_error(PFGPU_ERR_UNSUPPORTED, "job has no Morse cell lists");
+  Platelets& P = j->Pl;
+  CK(bin_elements(P, j->ctl, j->s0));
+  CK(sort_cell_bins(P, j->ctl, j->s0));
+  CK(cudaStreamSynchronize(j->s0));
+  const int nc = P.ncells, PE = P.k.P * P.k.E;
+  std::vector<int> cnt(nc);
+  std::vector<float4> bins((size_t)nc * kBinCap);
+  CK(cudaMemcpy(cnt.data(), P.bin_count, nc * sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(bins.data(), P.bin, bins.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+  size_t off = 0;
+  for (int c = 0; c < nc; ++c) {
+    const int n = cnt[c] < kBinCap ? cnt[c] : kBinCap;
+    if (counts) counts[c] = cnt[c];
+    for (int q = 0; q < n; ++q) {
+      int g;
+      std::memcpy(&g, &bins[(size_t)c * kBinCap + q].w, sizeof g);
+      if (members) members[off] = g;
+      if (cell_of && g >= 0 && g < PE) cell_of[g] = c;
+      off++;
+    }
+  }
+  if (ncells3) { ncells3[0] = P.k.ncell[0]; ncells3[1] = P.k.ncell[1]; ncells3[2] = P.k.ncell[2]; }
+  return check_control(j);
+}

@@ -268,6 +268,9 @@ __global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, Platele
       const long long s = ctl->step + 1;
       ctl->step = s;
       ctl->first = 0;
+      // a platelet without receptors has no bonds (the reference's bond
+      // kernel then runs with no threads and totalBond stays at zero)
+      if (!pk.nrec || !pk.P) ctl->total_bond = 0;
       if (detach_rate > 0 && ctl->total_bond == 0 && detach_uniform(seed, s) < detach_rate) ctl->done = 1;
       *done_blocks = 0u;
     }
@@ -915,74 +918,93 @@ __global__ void __launch_bounds__(256) platelet_bounds_k(PlateletConst k, const 
   }
 }
 
+// 32 elements per CTA, each element's partner list split over kMorseSplit
+// warps; the partial sums are added in warp order (deterministic).
+constexpr int kMorseSplit = 4;
+
 template <class R>
-__global__ void __launch_bounds__(128) morse_platelet_k(PlateletConst k, const double* bounds,
-                                                        const typename Staged<R>::T* rel, int slices, double* Fm,
-                                                        Control* ctl) {
+__global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletConst k, const double* bounds,
+                                                                     const typename Staged<R>::T* rel,
+                                                                     int tiles, double* Fm, Control* ctl) {
   if (ctl->done) return;
   using T = typename Staged<R>::T;
   extern __shared__ __align__(16) unsigned char s_raw[];
   T* s_t = reinterpret_cast<T*>(s_raw);
   T* s_q = s_t + k.E;
+  __shared__ R s_part[kMorseSplit][3][32];
   const int PE = k.P * k.E;
-  const int p = blockIdx.x / slices, sl = blockIdx.x % slices;
-  const int per = (k.E + slices - 1) / slices;
-  const int e0 = sl * per, e1 = min(k.E, e0 + per);
+  const int p = blockIdx.x / tiles, tile = blockIdx.x % tiles;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int e = tile * 32 + lane;
+  const bool valid = e < k.E;
   const double cxp = bounds[4 * p], cyp = bounds[4 * p + 1], czp = bounds[4 * p + 2], rp = bounds[4 * p + 3];
-  for (int e = threadIdx.x; e < k.E; e += blockDim.x) s_t[e] = rel[p * k.E + e];
+  for (int j = threadIdx.x; j < k.E; j += blockDim.x) s_t[j] = rel[p * k.E + j];
   __syncthreads();
   const R U0a = (R)k.morse_intra[0], rhoa = (R)k.morse_intra[1], reqa = (R)k.morse_intra[2];
   const R rca = (R)k.morse_intra[3], rc2a = rca * rca, Fca = (R)k.morse_fc[0];
   const R U0b = (R)k.morse_inter[0], rhob = (R)k.morse_inter[1], reqb = (R)k.morse_inter[2];
   const R rcb = (R)k.morse_inter[3], rc2b = rcb * rcb, Fcb = (R)k.morse_fc[1];
-  for (int e = e0 + threadIdx.x; e - threadIdx.x < e1; e += blockDim.x) {
-    const bool valid = e < e1;
-    const T own = valid ? s_t[e] : Staged<R>::make(0, 0, 0, 0);
-    R ax = 0, ay = 0, az = 0;
-    auto pair = [&](const T mb, R U0, R rho, R req, R rc, R rc2, R Fc) {
-      const R d0 = (R)own.x - (R)mb.x, d1 = (R)own.y - (R)mb.y, d2 = (R)own.z - (R)mb.z;
-      const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
-      if (!(r2 < rc2) || !(r2 > (R)0)) return;
-      R fr;
-      if constexpr (sizeof(R) == 4) {
-        const float rinv = rsqrtf(r2);
-        const float r = r2 * rinv;
-        const float ex = __expf(rho * (req - r));
-        fr = (2.0f * rho * U0 * (ex * ex - ex) - Fc) * rinv;
-      } else {
-        const R r = sqrt(r2);
-        if (!(r < rc)) return;
-        const R ex = exp(rho * (req - r));
-        fr = ((R)2.0 * rho * U0 * (ex * ex - ex) - Fc) / r;
-      }
-      ax += fr * d0; ay += fr * d1; az += fr * d2;
-    };
-    if (valid) {
+  const T own = valid ? s_t[e] : Staged<R>::make(0, 0, 0, 0);
+  R ax = 0, ay = 0, az = 0;
+  auto pair = [&](const T mb, R U0, R rho, R req, R rc, R rc2, R Fc) {
+    const R d0 = (R)own.x - (R)mb.x, d1 = (R)own.y - (R)mb.y, d2 = (R)own.z - (R)mb.z;
+    const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
+    if (!(r2 < rc2) || !(r2 > (R)0)) return;
+    R fr;
+    if constexpr (sizeof(R) == 4) {
+      const float rinv = rsqrtf(r2);
+      const float r = r2 * rinv;
+      const float ex = __expf(rho * (req - r));
+      fr = (2.0f * rho * U0 * (ex * ex - ex) - Fc) * rinv;
+    } else {
+      const R r = sqrt(r2);
+      if (!(r < rc)) return;
+      const R ex = exp(rho * (req - r));
+      fr = ((R)2.0 * rho * U0 * (ex * ex - ex) - Fc) / r;
+    }
+    ax += fr * d0; ay += fr * d1; az += fr * d2;
+  };
+  const int chunk = (k.E + kMorseSplit - 1) / kMorseSplit;
+  const int j0 = w * chunk, j1 = min(k.E, j0 + chunk);
+  if (valid) {
 #pragma unroll 4
-      for (int j = 0; j < k.E; ++j) pair(s_t[j], U0a, rhoa, reqa, rca, rc2a, Fca);
-    }
-    // other platelets whose bounding spheres come within the inter cutoff,
-    // shifted into this platelet's centroid frame (minimum image)
-    for (int q = 0; q < k.P; ++q) {
-      if (q == p) continue;
-      const double o0 = min_image(bounds[4 * q] - cxp, k.L[0], k.wrap[0]);
-      const double o1 = min_image(bounds[4 * q + 1] - cyp, k.L[1], k.wrap[1]);
-      const double o2 = min_image(bounds[4 * q + 2] - czp, k.L[2], k.wrap[2]);
-      const double reach = rp + bounds[4 * q + 3] + k.morse_inter[3];
-      if (o0 * o0 + o1 * o1 + o2 * o2 >= reach * reach) continue;
-      __syncthreads();
-      for (int j = threadIdx.x; j < k.E; j += blockDim.x) s_q[j] = Staged<R>::shift(rel[q * k.E + j], o0, o1, o2);
-      __syncthreads();
-      if (valid)
-        for (int j = 0; j < k.E; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
-    }
-    if (valid) {
-      const int g = p * k.E + e;
-      const double sc = 1.0 / (double)k.f0;
-      Fm[g] = (double)ax * sc;
-      Fm[PE + g] = (double)ay * sc;
-      Fm[2 * PE + g] = (double)az * sc;
-    }
+    for (int j = j0; j < j1; ++j) pair(s_t[j], U0a, rhoa, reqa, rca, rc2a, Fca);
+  }
+  // other platelets whose bounding spheres come within the inter cutoff,
+  // shifted into this platelet's centroid frame (minimum image)
+  const R own_r = valid ? (R)sqrt((double)own.x * own.x + (double)own.y * own.y + (double)own.z * own.z) : (R)0;
+  for (int q = 0; q < k.P; ++q) {
+    if (q == p) continue;
+    const double o0 = min_image(bounds[4 * q] - cxp, k.L[0], k.wrap[0]);
+    const double o1 = min_image(bounds[4 * q + 1] - cyp, k.L[1], k.wrap[1]);
+    const double o2 = min_image(bounds[4 * q + 2] - czp, k.L[2], k.wrap[2]);
+    const double rq = bounds[4 * q + 3];
+    const double reach = rp + rq + k.morse_inter[3];
+    const double oq2 = o0 * o0 + o1 * o1 + o2 * o2;
+    if (oq2 >= reach * reach) continue;
+    __syncthreads();
+    for (int j = threadIdx.x; j < k.E; j += blockDim.x) s_q[j] = Staged<R>::shift(rel[q * k.E + j], o0, o1, o2);
+    __syncthreads();
+    if (!valid) continue;
+    // this element is out of reach of platelet q: skip its members
+    const R dq0 = (R)own.x - (R)o0, dq1 = (R)own.y - (R)o1, dq2 = (R)own.z - (R)o2;
+    const R lim = (R)(rq + k.morse_inter[3]) * (R)1.0001 + (R)1e-6;
+    if (dq0 * dq0 + dq1 * dq1 + dq2 * dq2 >= lim * lim) continue;
+    for (int j = j0; j < j1; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
+  }
+  (void)own_r;
+  s_part[w][0][lane] = ax;
+  s_part[w][1][lane] = ay;
+  s_part[w][2][lane] = az;
+  __syncthreads();
+  if (w == 0 && valid) {
+    R sx = 0, sy = 0, sz = 0;
+    for (int t = 0; t < kMorseSplit; ++t) { sx += s_part[t][0][lane]; sy += s_part[t][1][lane]; sz += s_part[t][2][lane]; }
+    const int g = p * k.E + e;
+    const double sc = 1.0 / (double)k.f0;
+    Fm[g] = (double)sx * sc;
+    Fm[PE + g] = (double)sy * sc;
+    Fm[2 * PE + g] = (double)sz * sc;
   }
 }
 
@@ -1250,19 +1272,18 @@ cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (!morse_uses_cells(k)) {
-    int slices = (2 * sms + k.P - 1) / k.P;
-    slices = std::max(1, std::min(slices, (k.E + 63) / 64));
+    const int slices = (k.E + 31) / 32;
     if (precision == PF_PREC_FP64) {
       platelet_bounds_k<double><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (D4*)Pl.relpos, ctl);
       const size_t smem = 2 * (size_t)k.E * sizeof(D4);
       cudaFuncSetAttribute(morse_platelet_k<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      morse_platelet_k<double><<<k.P * slices, 128, smem, st>>>(k, Pl.bounds, (const D4*)Pl.relpos, slices,
+      morse_platelet_k<double><<<k.P * slices, 32 * kMorseSplit, smem, st>>>(k, Pl.bounds, (const D4*)Pl.relpos, slices,
                                                                 Pl.Fmorse, ctl);
     } else {
       platelet_bounds_k<float><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (float4*)Pl.relpos, ctl);
       const size_t smem = 2 * (size_t)k.E * sizeof(float4);
       cudaFuncSetAttribute(morse_platelet_k<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      morse_platelet_k<float><<<k.P * slices, 128, smem, st>>>(k, Pl.bounds, (const float4*)Pl.relpos, slices,
+      morse_platelet_k<float><<<k.P * slices, 32 * kMorseSplit, smem, st>>>(k, Pl.bounds, (const float4*)Pl.relpos, slices,
                                                                Pl.Fmorse, ctl);
     }
     return cudaGetLastError();

@@ -50,6 +50,7 @@ def lib():
         L.pfgpu_job_launches_per_step.argtypes = [vp]
         L.pfgpu_job_destroy.argtypes = [vp]
         L.pfgpu_job_profile.argtypes = [vp, C.c_int, dp]
+        L.pfgpu_job_get_cells.argtypes = [vp, ip, ip, ip, ip]
         L.pfgpu_profile_phase_name.restype = C.c_char_p
         L.pfgpu_profile_phase_name.argtypes = [C.c_int]
         L.pfgpu_scene_device_bytes.restype = C.c_size_t
@@ -157,6 +158,20 @@ class Job:
         km = np.zeros((sc.n_platelets, sc.n_membrane))
         check(lib().pfgpu_job_get_membrane(self.h, _p(SV), _p(km)))
         return dict(S_V=SV, km=km)
+
+    def cells(self):
+        """(cell of each element, count per cell, members per cell in id order, grid dims)"""
+        sc = self.scene
+        PE = sc.n_platelets * sc.n_elem
+        nc = np.zeros(3, dtype=np.int32)
+        cell_of = np.zeros(PE, dtype=np.int32)
+        members = np.zeros(PE, dtype=np.int32)
+        rc = max(sc.morse_intra[3], sc.morse_inter[3])
+        dims = [max(1, int(np.floor(n * np.float64(np.float32(sc.dx)) / rc))) for n in (sc.nx, sc.ny, sc.nz)]
+        counts = np.zeros(int(np.prod(dims)), dtype=np.int32)
+        check(lib().pfgpu_job_get_cells(self.h, _p(cell_of, C.c_int), _p(counts, C.c_int), _p(members, C.c_int),
+                                        _p(nc, C.c_int)))
+        return cell_of, counts, members, nc
 
     def conservation(self):
         out = np.zeros(4)
