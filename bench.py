@@ -241,6 +241,7 @@ def main():
     job = gpu.Job(scene, prec, fp16_scale)
     job.step(args.warmup, graph=True)
     launches = job.launches_per_step
+    lbm_kernel = "lbm_rows_k" if job.lbm_kernel == "rows" else "lbm_step_k"
     barrier_sync()
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
@@ -286,7 +287,7 @@ def main():
     achieved = N * bpn / (lbm_ms / 1e3) / 1e9
     traffic = lbm_traffic_per_node()
     traffic_per_launch = None
-    if traffic and traffic.get("precision") == prec:
+    if traffic and traffic.get("precision") == prec and traffic.get("kernel", lbm_kernel) == lbm_kernel:
         traffic_per_launch = traffic["dram_bytes_per_node"] * N
 
     line = {
@@ -311,7 +312,7 @@ def main():
                 "h2d_bytes_per_step": int(h2d_bytes / args.steps), "d2h_bytes_per_step": int(d2h_bytes / args.steps),
                 "seconds": round(e2e_s, 4),
                 "what": "pfgpu_job_create from host arrays + K graph steps + pfgpu_job_get_lattice/elements"},
-        "roofline": {"bound": "hbm", "kernel": "lbm_step_k", "achieved": round(achieved, 1), "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": lbm_kernel, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "bytes_per_node": bpn, "launch_ms": round(lbm_ms, 5),
                      "traffic": traffic_per_launch},

@@ -164,6 +164,10 @@ int64_t pfgpu_job_step_count(const pfgpu_job *job);
 size_t pfgpu_job_device_bytes(const pfgpu_job *job);
 /* Kernel launches one coupled step issues (graph nodes). */
 int pfgpu_job_launches_per_step(const pfgpu_job *job);
+/* Which collide-stream kernel the job runs: "rows" (rows staged through
+ * shared memory by bulk asynchronous copies; needs nx * sizeof(population)
+ * to be a multiple of 16 bytes) or "direct" (per-node gathers). */
+const char *pfgpu_job_lbm_kernel(const pfgpu_job *job);
 void pfgpu_job_destroy(pfgpu_job *job);
 
 /* Device bytes a job with this scene and precision would allocate. */

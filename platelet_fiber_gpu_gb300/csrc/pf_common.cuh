@@ -44,6 +44,7 @@ enum : uint32_t {
   ERR_BOND_OVERFLOW = 2u,
   ERR_NONFINITE = 4u,
   ERR_MEMBRANE_SIZE = 8u,
+  ERR_WAIT_TIMEOUT = 16u,  // a bounded wait on an mbarrier gave up
 };
 
 // Per-job device-resident control block: written by kernels, read by the host

@@ -65,6 +65,10 @@ struct Lattice {
   unsigned* flags[2] = {nullptr, nullptr};
   int* list[2] = {nullptr, nullptr};
   size_t bytes = 0;
+  // row-staged step: rows per tile, tiles in flight per CTA, persistent grid
+  // (rows_stages == 0: the direct-gather kernel is used)
+  int rows_rpt = 0, rows_stages = -1, rows_grid = 0;
+  size_t rows_smem = 0;
 };
 
 // ------------------------------------------------------------------ markers
@@ -130,6 +134,9 @@ struct Fibrin {
 // All launchers enqueue on `st` and return the launch error.
 cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_dev, const double* ru_dev,
                            Control* ctl, cudaStream_t st);
+// picks the row-staged or the direct-gather step kernel (host only; call
+// before the first step and outside stream capture)
+cudaError_t lattice_configure(Lattice& L);
 cudaError_t lattice_step(Lattice& L, Control* ctl, cudaStream_t st);
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
 // fIN [19][N], fOUT [19][N], rho [N], u [3][N], F [3][N] (double, device)

@@ -570,6 +570,7 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
       if (e == cudaSuccess) e = cudaMemcpy(dF, s->F_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = lattice_upload(L, df, dF, dru, j->ctl, j->s0);
+    if (e == cudaSuccess) e = lattice_configure(L);
     if (e == cudaSuccess) e = cudaStreamSynchronize(j->s0);
     cudaFree(df);
     cudaFree(dF);
@@ -759,6 +760,10 @@ int pfgpu_job_conservation(pfgpu_job* j, double out[4]) {
 
 size_t pfgpu_job_device_bytes(const pfgpu_job* j) { return j ? j->bytes : 0; }
 int pfgpu_job_launches_per_step(const pfgpu_job* j) { return j ? j->launches_per_step : 0; }
+const char* pfgpu_job_lbm_kernel(const pfgpu_job* j) {
+  if (!j) return "";
+  return j->L.rows_stages > 0 ? "rows" : "direct";
+}
 void pfgpu_job_destroy(pfgpu_job* j) {
   if (j && j->s0) cudaStreamSynchronize(j->s0);
   destroy(j);

@@ -12,6 +12,9 @@
 //   geq_d = w_d (drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u.u))
 //   S_d   = w_d (1 - omega/2) (3 c.F + 9 (c.u)(c.F) - 3 u.F)
 // which is the reference's Guo forcing with u -> u/C and F -> F*K*dt/C.
+#include <algorithm>
+#include <cstdlib>
+
 #include "pf_internal.h"
 
 namespace pf {
@@ -245,6 +248,213 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0) ctl->active_count[par ^ 1] = 0;
 }
 
+// ------------------------------------------------------------ row-staged step
+// The same fused step with its loads staged through shared memory: a CTA of
+// kRowThreads threads owns tiles of `rpt` consecutive x-rows.  For a tile and
+// a direction d the source row (y - cy, z - cz) of plane d -- or, through a
+// bounce-back face in y or z, the tile's own row of plane opp(d) -- is one
+// contiguous run of nx populations, copied by a bulk asynchronous copy that
+// completes on the stage's mbarrier.  The x shift of the pull is an index
+// into the staged row (periodic x wraps inside it; a bounce-back x face reads
+// the node's own opp(d) population from global memory).  `stages` tiles are
+// in flight per CTA; the persistent grid walks the tiles in order.
+constexpr int kRowThreads = 256;
+constexpr int kMaxStages = 4;
+constexpr unsigned kWaitLimit = 1u << 22;  // try_wait polls before a stage is given up
+
+__constant__ int c_cy[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1};
+__constant__ int c_cz[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1};
+__constant__ int c_opp[Q] = {0, 2, 1, 4, 3, 6, 5, 12, 11, 14, 13, 8, 7, 10, 9, 18, 17, 16, 15};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait for phase `parity` of a stage barrier; false if it gave up
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
+  for (unsigned it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+
+template <class S, class R>
+__device__ __forceinline__ R from_store(S v, int d, R sigma);
+template <>
+__device__ __forceinline__ double from_store<double, double>(double v, int, double) { return v; }
+template <>
+__device__ __forceinline__ float from_store<float, float>(float v, int, float) { return v; }
+template <>
+__device__ __forceinline__ float from_store<__half, float>(__half v, int d, float sigma) {
+  return __half2float(v) * ((float)wgt(d) * sigma);
+}
+
+template <class S, class R>
+__global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                                          R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                                          int ncells, int rpt, int stages, Control* ctl) {
+  if (ctl->done) return;
+  extern __shared__ __align__(128) unsigned char s_raw[];
+  __shared__ __align__(8) uint64_t s_bar[kMaxStages];
+  const long long step = ctl->step;
+  const int par = (int)(step & 1);
+  const S* __restrict__ gin = par ? gB : gA;
+  S* __restrict__ gout = par ? gA : gB;
+  R4<R>* Fc = par ? FB : FA;
+  R4<R>* Fp = par ? FA : FB;
+  unsigned* flp = par ? flA : flB;
+  const unsigned* flc = par ? flB : flA;
+  const int first = ctl->first;
+  const int nx = k.nx, ny = k.ny, nz = k.nz;
+  const int rows = ny * nz;
+  const int tile_nodes = rpt * nx;
+  const int ntiles = (rows + rpt - 1) / rpt;
+  const size_t N = (size_t)k.N;
+  const unsigned row_bytes = (unsigned)(nx * sizeof(S));
+  S* sbuf = reinterpret_cast<S*>(s_raw);
+  const int lane = threadIdx.x & 31;
+  const bool bbx = k.bc[0] == PF_BC_BOUNCEBACK, bby = k.bc[1] == PF_BC_BOUNCEBACK,
+             bbz = k.bc[2] == PF_BC_BOUNCEBACK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) mbar_init(&s_bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  // warp 0 stages local tile i (the CTA's i-th tile) into stage i % stages
+  auto issue = [&](int i) {
+    const int tile = blockIdx.x + i * gridDim.x;
+    const int s = i % stages;
+    const int r0 = tile * rpt;
+    const int nr = min(rpt, rows - r0);
+    if (lane == 0) mbar_arrive_expect(&s_bar[s], (unsigned)(Q * nr) * row_bytes);
+    __syncwarp();
+    S* dst0 = sbuf + (size_t)s * Q * tile_nodes;
+    for (int c = lane; c < Q * nr; c += 32) {
+      const int d = c / nr, rr = c - d * nr;
+      const int r = r0 + rr;
+      const int y = r % ny, z = r / ny;
+      int sy = y - c_cy[d], sz = z - c_cz[d];
+      bool out = false;
+      if (sy < 0 || sy >= ny) { if (bby) out = true; else sy = sy < 0 ? sy + ny : sy - ny; }
+      if (sz < 0 || sz >= nz) { if (bbz) out = true; else sz = sz < 0 ? sz + nz : sz - nz; }
+      const S* src = out ? gin + (size_t)c_opp[d] * N + (size_t)r * nx
+                         : gin + (size_t)d * N + ((size_t)sy + (size_t)ny * sz) * nx;
+      bulk_load(dst0 + (size_t)d * tile_nodes + (size_t)rr * nx, src, row_bytes, &s_bar[s]);
+    }
+  };
+
+  const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  if (threadIdx.x < 32)
+    for (int i = 0; i < stages && i < my_tiles; ++i) issue(i);
+
+  const R sigma = (R)k.fp16_scale;
+  const R kc = (R)k.kcoll;
+  const R om = (R)k.omega;
+  const R sf = (R)1 - (R)0.5 * om;
+  for (int i = 0; i < my_tiles; ++i) {
+    const int tile = blockIdx.x + i * gridDim.x;
+    const int s = i % stages;
+    const int r0 = tile * rpt;
+    const int nr = min(rpt, rows - r0);
+    const bool ok = mbar_wait(&s_bar[s], (unsigned)((i / stages) & 1));
+    const S* sb = sbuf + (size_t)s * Q * tile_nodes;
+    for (int t = threadIdx.x; t < nr * nx; t += kRowThreads) {
+      const int rr = t / nx, x = t - rr * nx;
+      const int r = r0 + rr;
+      const int y = r % ny, z = r / ny;
+      const size_t n = (size_t)r * nx + x;
+      R g[Q];
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        const bool oyz = (bby && ((cy(d) == 1 && y == 0) || (cy(d) == -1 && y == ny - 1))) ||
+                         (bbz && ((cz(d) == 1 && z == 0) || (cz(d) == -1 && z == nz - 1)));
+        const S* row = sb + d * tile_nodes + rr * nx;
+        if (oyz || cx(d) == 0) {
+          g[d] = from_store<S, R>(row[x], d, sigma);
+        } else {
+          int sx = x - cx(d);
+          if (sx >= 0 && sx < nx) {
+            g[d] = from_store<S, R>(row[sx], d, sigma);
+          } else if (bbx) {
+            g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
+          } else {
+            g[d] = from_store<S, R>(row[sx < 0 ? sx + nx : sx - nx], d, sigma);
+          }
+        }
+      }
+      const int brick = x / kBrickX + k.nbx * r;
+      const unsigned fc = flc[brick], fp = flp[brick];
+      R drho, ux, uy, uz;
+      if (first) {
+        ld_u<R>(ubuf, n, drho, ux, uy, uz);
+      } else {
+        R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
+        if (fp) ld_force<R>(Fp, n, px, py, pz);
+        node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
+      }
+      R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+      if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
+      Fx *= kc; Fy *= kc; Fz *= kc;
+      const R rho = (R)1 + drho;
+      const R usq = ux * ux + uy * uy + uz * uz;
+      const R uF = ux * Fx + uy * Fy + uz * Fz;
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
+        const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
+        const R w = (R)wgt(d);
+        const R geq = w * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq));
+        const R src = w * sf * ((R)3 * cF + (R)9 * cu * cF - (R)3 * uF);
+        const R gn = g[d] - om * (g[d] - geq) + src;
+        StoreTraits<S>::store(gout + (size_t)d * N + n, gn, d,
+                              (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+      }
+      if (fp) zero_force<R>(Fp, n);
+    }
+    // every thread is done with stage s and has read its brick flags
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(&ctl->err, ERR_WAIT_TIMEOUT);
+      // let the copies already issued for later tiles land before exiting
+      for (int j = i + 1; j < my_tiles && j < i + stages; ++j) mbar_wait(&s_bar[j % stages], (unsigned)((j / stages) & 1));
+      return;
+    }
+    for (int b = threadIdx.x; b < nr * k.nbx; b += kRowThreads) {
+      const int brick = r0 * k.nbx + b;
+      if (flp[brick]) flp[brick] = 0;
+    }
+    if (threadIdx.x < 32 && i + stages < my_tiles) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(i + stages);
+    }
+  }
+  if (bin_count) {
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t tot = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = tid; c < (size_t)ncells; c += tot) bin_count[c] = 0;
+    if (tid == 0) ctl->occupied = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->active_count[par ^ 1] = 0;
+}
+
 // (rho, u/C) of the nodes of the active bricks after this step's stream and
 // boundary conditions, with this step's force: input of the IBM interpolation
 // (the reference's velocity_density, LB_kernel.cu:1108-1199).
@@ -378,8 +588,49 @@ __global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
   }
 }
 
+// Row-staged configuration: each staged row is a bulk copy of nx * sizeof(S)
+// bytes, which must be a multiple of 16; tiles hold max(1, 256 / nx) rows;
+// three stages when they fit beside two more CTAs on an SM, else two.
+template <class S, class R>
+void rows_config(Lattice& L) {
+  L.rows_stages = 0;
+  if (getenv("PFGPU_DIRECT_LBM")) return;
+  const int nx = L.k.nx;
+  if ((nx * sizeof(S)) % 16 != 0) return;
+  const int rpt = nx >= kRowThreads ? 1 : kRowThreads / nx;
+  const size_t stage = (size_t)Q * rpt * nx * sizeof(S);
+  int stages = 3;
+  if (3 * stage > 72 * 1024) stages = 2;
+  if ((size_t)stages * stage > 200 * 1024) return;
+  const size_t smem = (size_t)stages * stage;
+  if (cudaFuncSetAttribute(lbm_rows_k<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  int dev = 0, sms = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lbm_rows_k<S, R>, kRowThreads, smem) != cudaSuccess ||
+      occ < 1) {
+    cudaGetLastError();
+    return;
+  }
+  const int ntiles = (L.k.ny * L.k.nz + rpt - 1) / rpt;
+  L.rows_rpt = rpt;
+  L.rows_stages = stages;
+  L.rows_smem = smem;
+  L.rows_grid = std::min(ntiles, sms * occ);
+}
+
 template <class S, class R>
 cudaError_t step_impl(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st) {
+  if (L.rows_stages < 0) rows_config<S, R>(L);
+  if (L.rows_stages > 0) {
+    lbm_rows_k<S, R><<<L.rows_grid, kRowThreads, L.rows_smem, st>>>(
+        L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf, L.flags[0], L.flags[1],
+        bin_count, ncells, L.rows_rpt, L.rows_stages, ctl);
+    return cudaGetLastError();
+  }
   dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);
   lbm_step_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
                                               (R4<R>*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells, ctl);
@@ -464,6 +715,14 @@ cudaError_t lattice_step_binned(Lattice& L, Control* ctl, int* bin_count, int nc
     case PF_PREC_FP64: return step_impl<double, double>(L, ctl, bin_count, ncells, st);
     case PF_PREC_FP32: return step_impl<float, float>(L, ctl, bin_count, ncells, st);
     case PF_PREC_FP16: return step_impl<__half, float>(L, ctl, bin_count, ncells, st);
+  }
+  return cudaErrorInvalidValue;
+}
+cudaError_t lattice_configure(Lattice& L) {
+  switch (L.precision) {
+    case PF_PREC_FP64: rows_config<double, double>(L); return cudaSuccess;
+    case PF_PREC_FP32: rows_config<float, float>(L); return cudaSuccess;
+    case PF_PREC_FP16: rows_config<__half, float>(L); return cudaSuccess;
   }
   return cudaErrorInvalidValue;
 }

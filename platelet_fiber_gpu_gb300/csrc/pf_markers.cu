@@ -970,29 +970,61 @@ __global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletCon
 #pragma unroll 4
     for (int j = j0; j < j1; ++j) pair(s_t[j], U0a, rhoa, reqa, rca, rc2a, Fca);
   }
-  // other platelets whose bounding spheres come within the inter cutoff,
-  // shifted into this platelet's centroid frame (minimum image)
-  const R own_r = valid ? (R)sqrt((double)own.x * own.x + (double)own.y * own.y + (double)own.z * own.z) : (R)0;
-  for (int q = 0; q < k.P; ++q) {
-    if (q == p) continue;
-    const double o0 = min_image(bounds[4 * q] - cxp, k.L[0], k.wrap[0]);
-    const double o1 = min_image(bounds[4 * q + 1] - cyp, k.L[1], k.wrap[1]);
-    const double o2 = min_image(bounds[4 * q + 2] - czp, k.L[2], k.wrap[2]);
-    const double rq = bounds[4 * q + 3];
-    const double reach = rp + rq + k.morse_inter[3];
-    const double oq2 = o0 * o0 + o1 * o1 + o2 * o2;
-    if (oq2 >= reach * reach) continue;
+  // Other platelets whose bounding spheres come within the inter cutoff,
+  // shifted into this platelet's centroid frame (minimum image).  The
+  // candidates are found in chunks of blockDim platelets, one per thread, and
+  // compacted in ascending platelet order into shared memory, so the per-pair
+  // loop below sees only offsets of type R.
+  __shared__ R s_off[32 * kMorseSplit][4];
+  __shared__ int s_qid[32 * kMorseSplit];
+  __shared__ int s_wcount[kMorseSplit];
+  for (int qb = 0; qb < k.P; qb += blockDim.x) {
+    const int q = qb + threadIdx.x;
+    bool near = false;
+    double o0 = 0, o1 = 0, o2 = 0, rq = 0;
+    if (q < k.P && q != p) {
+      o0 = min_image(bounds[4 * q] - cxp, k.L[0], k.wrap[0]);
+      o1 = min_image(bounds[4 * q + 1] - cyp, k.L[1], k.wrap[1]);
+      o2 = min_image(bounds[4 * q + 2] - czp, k.L[2], k.wrap[2]);
+      rq = bounds[4 * q + 3];
+      const double reach = rp + rq + k.morse_inter[3];
+      near = o0 * o0 + o1 * o1 + o2 * o2 < reach * reach;
+    }
+    const unsigned ball = __ballot_sync(0xffffffffu, near);
+    __syncthreads();  // the previous chunk's list is no longer read
+    if (lane == 0) s_wcount[w] = __popc(ball);
     __syncthreads();
-    for (int j = threadIdx.x; j < k.E; j += blockDim.x) s_q[j] = Staged<R>::shift(rel[q * k.E + j], o0, o1, o2);
+    int before = 0, nq = 0;
+    for (int t = 0; t < kMorseSplit; ++t) {
+      if (t < w) before += s_wcount[t];
+      nq += s_wcount[t];
+    }
+    if (near) {
+      const int slot = before + __popc(ball & ((1u << lane) - 1u));
+      s_qid[slot] = q;
+      s_off[slot][0] = (R)o0;
+      s_off[slot][1] = (R)o1;
+      s_off[slot][2] = (R)o2;
+      s_off[slot][3] = (R)(rq + k.morse_inter[3]) * (R)1.0001 + (R)1e-6;
+    }
     __syncthreads();
-    if (!valid) continue;
-    // this element is out of reach of platelet q: skip its members
-    const R dq0 = (R)own.x - (R)o0, dq1 = (R)own.y - (R)o1, dq2 = (R)own.z - (R)o2;
-    const R lim = (R)(rq + k.morse_inter[3]) * (R)1.0001 + (R)1e-6;
-    if (dq0 * dq0 + dq1 * dq1 + dq2 * dq2 >= lim * lim) continue;
-    for (int j = j0; j < j1; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
+    for (int i = 0; i < nq; ++i) {
+      const int qq = s_qid[i];
+      const R f0 = s_off[i][0], f1 = s_off[i][1], f2 = s_off[i][2], lim = s_off[i][3];
+      __syncthreads();  // s_q of the previous platelet is no longer read
+      for (int j = threadIdx.x; j < k.E; j += blockDim.x) {
+        T a = rel[qq * k.E + j];
+        a.x += f0; a.y += f1; a.z += f2;
+        s_q[j] = a;
+      }
+      __syncthreads();
+      if (!valid) continue;
+      // this element is out of reach of platelet qq: skip its members
+      const R dq0 = (R)own.x - f0, dq1 = (R)own.y - f1, dq2 = (R)own.z - f2;
+      if (dq0 * dq0 + dq1 * dq1 + dq2 * dq2 >= lim * lim) continue;
+      for (int j = j0; j < j1; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
+    }
   }
-  (void)own_r;
   s_part[w][0][lane] = ax;
   s_part[w][1][lane] = ay;
   s_part[w][2][lane] = az;
@@ -1001,10 +1033,10 @@ __global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletCon
     R sx = 0, sy = 0, sz = 0;
     for (int t = 0; t < kMorseSplit; ++t) { sx += s_part[t][0][lane]; sy += s_part[t][1][lane]; sz += s_part[t][2][lane]; }
     const int g = p * k.E + e;
-    const double sc = 1.0 / (double)k.f0;
-    Fm[g] = (double)sx * sc;
-    Fm[PE + g] = (double)sy * sc;
-    Fm[2 * PE + g] = (double)sz * sc;
+    const R sc = (R)(1.0 / (double)k.f0);
+    Fm[g] = (double)(sx * sc);
+    Fm[PE + g] = (double)(sy * sc);
+    Fm[2 * PE + g] = (double)(sz * sc);
   }
 }
 

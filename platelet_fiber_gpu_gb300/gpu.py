@@ -49,6 +49,8 @@ def lib():
         L.pfgpu_job_device_bytes.argtypes = [vp]
         L.pfgpu_job_launches_per_step.argtypes = [vp]
         L.pfgpu_job_destroy.argtypes = [vp]
+        L.pfgpu_job_lbm_kernel.restype = C.c_char_p
+        L.pfgpu_job_lbm_kernel.argtypes = [vp]
         L.pfgpu_job_profile.argtypes = [vp, C.c_int, dp]
         L.pfgpu_job_get_cells.argtypes = [vp, ip, ip, ip, ip]
         L.pfgpu_profile_phase_name.restype = C.c_char_p
@@ -121,6 +123,10 @@ class Job:
     @property
     def launches_per_step(self) -> int:
         return int(lib().pfgpu_job_launches_per_step(self.h))
+
+    @property
+    def lbm_kernel(self) -> str:
+        return lib().pfgpu_job_lbm_kernel(self.h).decode()
 
     def lattice(self, fIN=True, fOUT=False):
         N = self.scene.n_nodes
