@@ -173,9 +173,16 @@ __device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z,
   moments(g, drho, jx, jy, jz);
   const R rho = (R)1 + drho;
   const R hk = (R)0.5 * (R)k.kmom;
-  ux = (jx + hk * Fx) / rho;
-  uy = (jy + hk * Fy) / rho;
-  uz = (jz + hk * Fz) / rho;
+  if constexpr (sizeof(R) == 4) {
+    const float ir = __frcp_rn(rho);
+    ux = (jx + hk * Fx) * ir;
+    uy = (jy + hk * Fy) * ir;
+    uz = (jz + hk * Fz) * ir;
+  } else {
+    ux = (jx + hk * Fx) / rho;
+    uy = (jy + hk * Fy) / rho;
+    uz = (jz + hk * Fz) / rho;
+  }
 }
 
 template <class S, class R>
@@ -307,12 +314,14 @@ __device__ __forceinline__ float from_store<__half, float>(__half v, int d, floa
 }
 
 template <class S, class R>
-__global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
-                                                          R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
-                                                          int ncells, int rpt, int stages, Control* ctl) {
+__global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_k(
+    LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB, R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+    int ncells, int rpt, int stages, Control* ctl) {
   if (ctl->done) return;
+  constexpr int kWarps = kRowThreads / 32;
   extern __shared__ __align__(128) unsigned char s_raw[];
-  __shared__ __align__(8) uint64_t s_bar[kMaxStages];
+  __shared__ __align__(8) uint64_t s_full[kMaxStages], s_empty[kMaxStages];
+  __shared__ int4 s_info[kMaxStages][kWarps];  // (y, z, own-row mask) of each staged row
   const long long step = ctl->step;
   const int par = (int)(step & 1);
   const S* __restrict__ gin = par ? gB : gA;
@@ -329,122 +338,155 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
   const size_t N = (size_t)k.N;
   const unsigned row_bytes = (unsigned)(nx * sizeof(S));
   S* sbuf = reinterpret_cast<S*>(s_raw);
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool bbx = k.bc[0] == PF_BC_BOUNCEBACK, bby = k.bc[1] == PF_BC_BOUNCEBACK,
              bbz = k.bc[2] == PF_BC_BOUNCEBACK;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < stages; ++s) mbar_init(&s_bar[s], 1);
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&s_full[s], 1);
+      mbar_init(&s_empty[s], kWarps);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
 
-  // warp 0 stages local tile i (the CTA's i-th tile) into stage i % stages
+  // Warp 0 stages local tile i (the CTA's i-th tile) into stage i % stages:
+  // lanes < nr write the row descriptors, lane 0 arms the full barrier (its
+  // release publishes the descriptors), the lanes then issue one bulk copy
+  // per (direction, row).
   auto issue = [&](int i) {
     const int tile = blockIdx.x + i * gridDim.x;
     const int s = i % stages;
     const int r0 = tile * rpt;
     const int nr = min(rpt, rows - r0);
-    if (lane == 0) mbar_arrive_expect(&s_bar[s], (unsigned)(Q * nr) * row_bytes);
+    if (lane < nr) {
+      const int r = r0 + lane, y = r % ny, z = r / ny;
+      unsigned mask = 0;
+      for (int d = 0; d < Q; ++d) {
+        const bool own = (bby && ((c_cy[d] == 1 && y == 0) || (c_cy[d] == -1 && y == ny - 1))) ||
+                         (bbz && ((c_cz[d] == 1 && z == 0) || (c_cz[d] == -1 && z == nz - 1)));
+        mask |= (unsigned)own << d;
+      }
+      s_info[s][lane] = make_int4(y, z, (int)mask, 0);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive_expect(&s_full[s], (unsigned)(Q * nr) * row_bytes);
     __syncwarp();
     S* dst0 = sbuf + (size_t)s * Q * tile_nodes;
     for (int c = lane; c < Q * nr; c += 32) {
       const int d = c / nr, rr = c - d * nr;
-      const int r = r0 + rr;
-      const int y = r % ny, z = r / ny;
-      int sy = y - c_cy[d], sz = z - c_cz[d];
-      bool out = false;
-      if (sy < 0 || sy >= ny) { if (bby) out = true; else sy = sy < 0 ? sy + ny : sy - ny; }
-      if (sz < 0 || sz >= nz) { if (bbz) out = true; else sz = sz < 0 ? sz + nz : sz - nz; }
-      const S* src = out ? gin + (size_t)c_opp[d] * N + (size_t)r * nx
-                         : gin + (size_t)d * N + ((size_t)sy + (size_t)ny * sz) * nx;
-      bulk_load(dst0 + (size_t)d * tile_nodes + (size_t)rr * nx, src, row_bytes, &s_bar[s]);
+      const int4 inf = s_info[s][rr];
+      const S* src;
+      if ((inf.z >> d) & 1) {
+        src = gin + (size_t)c_opp[d] * N + (size_t)(r0 + rr) * nx;
+      } else {
+        int sy = inf.x - c_cy[d], sz = inf.y - c_cz[d];
+        sy = sy < 0 ? sy + ny : (sy >= ny ? sy - ny : sy);
+        sz = sz < 0 ? sz + nz : (sz >= nz ? sz - nz : sz);
+        src = gin + (size_t)d * N + ((size_t)sy + (size_t)ny * sz) * nx;
+      }
+      bulk_load(dst0 + (size_t)d * tile_nodes + (size_t)rr * nx, src, row_bytes, &s_full[s]);
     }
   };
-
-  const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  if (threadIdx.x < 32)
-    for (int i = 0; i < stages && i < my_tiles; ++i) issue(i);
 
   const R sigma = (R)k.fp16_scale;
   const R kc = (R)k.kcoll;
   const R om = (R)k.omega;
   const R sf = (R)1 - (R)0.5 * om;
-  for (int i = 0; i < my_tiles; ++i) {
-    const int tile = blockIdx.x + i * gridDim.x;
+  // One node: pull from the staged rows (own-row mask for bounce-back faces
+  // in y/z, periodic x inside the row, bounce-back x from global memory),
+  // collide, store.  Called by whole warps; a warp's 32 nodes are one force
+  // brick (nx is a multiple of 32), whose previous-force flag the warp clears.
+  auto node = [&](const S* row, int x, int r, int4 inf) {
+    const int z = inf.y;
+    const unsigned mask = (unsigned)inf.z;
+    const size_t n = (size_t)r * nx + x;
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+    const bool xedge = bbx && (x == 0 || x == nx - 1);
+    R g[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      bool own = false;
+      if (cy(d) != 0 || cz(d) != 0) own = (mask >> d) & 1u;
+      int idx = x;
+      if (cx(d) == 1) idx = own ? x : xm;
+      if (cx(d) == -1) idx = own ? x : xp;
+      g[d] = from_store<S, R>(row[d * tile_nodes + idx], d, sigma);
+      if (cx(d) != 0 && xedge && !own && ((cx(d) == 1 && x == 0) || (cx(d) == -1 && x == nx - 1)))
+        g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
+    }
+    const int brick = (x >> 5) + k.nbx * r;
+    const unsigned fc = flc[brick], fp = flp[brick];
+    R drho, ux, uy, uz;
+    if (first) {
+      ld_u<R>(ubuf, n, drho, ux, uy, uz);
+    } else {
+      R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
+      if (fp) ld_force<R>(Fp, n, px, py, pz);
+      node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
+    }
+    R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+    if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
+    Fx *= kc; Fy *= kc; Fz *= kc;
+    const R rho = (R)1 + drho;
+    const R usq = ux * ux + uy * uy + uz * uz;
+    const R uF = ux * Fx + uy * Fy + uz * Fz;
+    S* o = gout + n;
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
+      const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
+      const R w = (R)wgt(d);
+      const R geq = w * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq));
+      const R src = w * sf * ((R)3 * cF + (R)9 * cu * cF - (R)3 * uF);
+      const R gn = g[d] - om * (g[d] - geq) + src;
+      StoreTraits<S>::store(o + (size_t)d * N, gn, d,
+                            (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+    }
+    if (fp) zero_force<R>(Fp, n);
+    __syncwarp();
+    if (lane == 0 && fp) flp[brick] = 0;
+  };
+
+  const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  int issued = 0;
+  if (warp == 0)
+    for (; issued < stages && issued < my_tiles; ++issued) issue(issued);
+  // tile-invariant part of this thread's node (several rows per tile: one
+  // node per thread; one row per tile: x strides over the row)
+  const int rr0 = rpt == 1 ? 0 : (int)threadIdx.x / nx;
+  const int x0 = rpt == 1 ? (int)threadIdx.x : (int)threadIdx.x - rr0 * nx;
+  bool failed = false;
+  int i = 0;
+  for (; i < my_tiles; ++i) {
     const int s = i % stages;
-    const int r0 = tile * rpt;
+    const int r0 = (blockIdx.x + i * gridDim.x) * rpt;
     const int nr = min(rpt, rows - r0);
-    const bool ok = mbar_wait(&s_bar[s], (unsigned)((i / stages) & 1));
+    if (!mbar_wait(&s_full[s], (unsigned)((i / stages) & 1))) { failed = true; break; }
     const S* sb = sbuf + (size_t)s * Q * tile_nodes;
-    for (int t = threadIdx.x; t < nr * nx; t += kRowThreads) {
-      const int rr = t / nx, x = t - rr * nx;
-      const int r = r0 + rr;
-      const int y = r % ny, z = r / ny;
-      const size_t n = (size_t)r * nx + x;
-      R g[Q];
-#pragma unroll
-      for (int d = 0; d < Q; ++d) {
-        const bool oyz = (bby && ((cy(d) == 1 && y == 0) || (cy(d) == -1 && y == ny - 1))) ||
-                         (bbz && ((cz(d) == 1 && z == 0) || (cz(d) == -1 && z == nz - 1)));
-        const S* row = sb + d * tile_nodes + rr * nx;
-        if (oyz || cx(d) == 0) {
-          g[d] = from_store<S, R>(row[x], d, sigma);
-        } else {
-          int sx = x - cx(d);
-          if (sx >= 0 && sx < nx) {
-            g[d] = from_store<S, R>(row[sx], d, sigma);
-          } else if (bbx) {
-            g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
-          } else {
-            g[d] = from_store<S, R>(row[sx < 0 ? sx + nx : sx - nx], d, sigma);
-          }
-        }
-      }
-      const int brick = x / kBrickX + k.nbx * r;
-      const unsigned fc = flc[brick], fp = flp[brick];
-      R drho, ux, uy, uz;
-      if (first) {
-        ld_u<R>(ubuf, n, drho, ux, uy, uz);
-      } else {
-        R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
-        if (fp) ld_force<R>(Fp, n, px, py, pz);
-        node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
-      }
-      R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
-      if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
-      Fx *= kc; Fy *= kc; Fz *= kc;
-      const R rho = (R)1 + drho;
-      const R usq = ux * ux + uy * uy + uz * uz;
-      const R uF = ux * Fx + uy * Fy + uz * Fz;
-#pragma unroll
-      for (int d = 0; d < Q; ++d) {
-        const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
-        const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
-        const R w = (R)wgt(d);
-        const R geq = w * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq));
-        const R src = w * sf * ((R)3 * cF + (R)9 * cu * cF - (R)3 * uF);
-        const R gn = g[d] - om * (g[d] - geq) + src;
-        StoreTraits<S>::store(gout + (size_t)d * N + n, gn, d,
-                              (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
-      }
-      if (fp) zero_force<R>(Fp, n);
+    if (rpt == 1) {
+      const int4 inf = s_info[s][0];
+      for (int x = x0; x < nx; x += kRowThreads) node(sb, x, r0, inf);
+    } else if (rr0 < nr) {
+      node(sb + rr0 * nx, x0, r0 + rr0, s_info[s][rr0]);
     }
-    // every thread is done with stage s and has read its brick flags
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicOr(&ctl->err, ERR_WAIT_TIMEOUT);
-      // let the copies already issued for later tiles land before exiting
-      for (int j = i + 1; j < my_tiles && j < i + stages; ++j) mbar_wait(&s_bar[j % stages], (unsigned)((j / stages) & 1));
-      return;
-    }
-    for (int b = threadIdx.x; b < nr * k.nbx; b += kRowThreads) {
-      const int brick = r0 * k.nbx + b;
-      if (flp[brick]) flp[brick] = 0;
-    }
-    if (threadIdx.x < 32 && i + stages < my_tiles) {
+    __syncwarp();
+    if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&s_empty[s])) : "memory");
+    if (warp == 0 && issued < my_tiles) {
+      // stage s is free once every warp has arrived on its empty barrier
+      if (!mbar_wait(&s_empty[s], (unsigned)((i / stages) & 1))) { failed = true; break; }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(i + stages);
+      issue(issued++);
     }
+  }
+  if (failed) {
+    if (lane == 0) atomicOr(&ctl->err, ERR_WAIT_TIMEOUT);
+    // let the copies this CTA issued land before it exits
+    // (tiles i .. issued-1 are the latest users of their stages)
+    if (warp == 0)
+      for (int j = i; j < issued; ++j) mbar_wait(&s_full[j % stages], (unsigned)((j / stages) & 1));
+    return;
   }
   if (bin_count) {
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -588,15 +630,16 @@ __global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
   }
 }
 
-// Row-staged configuration: each staged row is a bulk copy of nx * sizeof(S)
-// bytes, which must be a multiple of 16; tiles hold max(1, 256 / nx) rows;
-// three stages when they fit beside two more CTAs on an SM, else two.
+// Row-staged configuration: nx a multiple of 32 (so each staged row, a bulk
+// copy of nx * sizeof(S) bytes, is a multiple of 16 bytes and every warp owns
+// one force brick); tiles hold max(1, 256 / nx) rows; three stages when they
+// fit beside two more CTAs on an SM, else two.
 template <class S, class R>
 void rows_config(Lattice& L) {
   L.rows_stages = 0;
   if (getenv("PFGPU_DIRECT_LBM")) return;
   const int nx = L.k.nx;
-  if ((nx * sizeof(S)) % 16 != 0) return;
+  if (nx % 32 != 0) return;  // a warp's 32 nodes are one force brick
   const int rpt = nx >= kRowThreads ? 1 : kRowThreads / nx;
   const size_t stage = (size_t)Q * rpt * nx * sizeof(S);
   int stages = 3;

@@ -156,13 +156,26 @@ def test_graph_and_direct_stepping_agree(gpu):
     assert a.steps == b.steps == 7
 
 
-@pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "fp32", "fp16"])
-def test_row_staged_and_direct_lbm_kernels_agree(gpu, prec, monkeypatch):
-    """The row-staged step kernel (bulk copies into shared memory) and the
-    direct-gather kernel do the same arithmetic on the same operands: the
-    populations must agree bit for bit."""
+def _lbm_scene(name):
     from platelet_fiber_gpu_gb300 import workloads as W
-    sc = W.mixed_small()
+    if name == "shear":
+        return W.mixed_small(nx=64)
+    sc = W.plain_small(n_fib=0, n_links=0)
+    sc.bc = (1, 1, 1)
+    sc.ibm_wrap = (0, 0, 0)
+    return sc
+
+
+@pytest.mark.parametrize("scene", ["shear", "walls"])
+@pytest.mark.parametrize("prec,tol", [(0, 1e-14), (1, 1e-6), (2, 1e-4)], ids=["fp64", "fp32", "fp16"])
+def test_row_staged_and_direct_lbm_kernels_agree(gpu, scene, prec, tol, monkeypatch):
+    """The row-staged step kernel (bulk copies into shared memory) and the
+    direct-gather kernel do the same arithmetic on the same operands; the
+    compiler may contract a different set of multiply-adds in each, so they
+    agree to a few units in the last place (FP16: one step of the store).
+    Scenes: Zou/He shear walls with periodic x/y, and a box with bounce-back
+    on every axis (the x faces are read from global memory)."""
+    sc = _lbm_scene(scene)
     a = gpu.Job(sc, prec)
     monkeypatch.setenv("PFGPU_DIRECT_LBM", "1")
     b = gpu.Job(sc, prec)
@@ -170,10 +183,21 @@ def test_row_staged_and_direct_lbm_kernels_agree(gpu, prec, monkeypatch):
     assert a.lbm_kernel == "rows" and b.lbm_kernel == "direct"
     a.step(12)
     b.step(12)
-    np.testing.assert_array_equal(a.lattice()["fIN"], b.lattice()["fIN"])
-    np.testing.assert_array_equal(a.elements()["X"], b.elements()["X"])
+    assert rel_max(a.lattice()["fIN"], b.lattice()["fIN"]) < tol
+    assert rel_max(a.elements()["X"], b.elements()["X"]) < tol
+    np.testing.assert_array_equal(a.bonds()["rec_state"], b.bonds()["rec_state"])
     a.close()
     b.close()
+
+
+def test_row_staged_fp64_vs_oracle(gpu):
+    """FP64 row-staged kernel against the oracle on the bounce-back box."""
+    sc = _lbm_scene("walls")
+    r = _run_both(gpu, sc, 15, 0)
+    assert rel_max(r["Lg"]["fIN"], r["Lo"]["fIN"]) < 1e-12
+    assert rel_l2(r["Lg"]["u"], r["Lo"]["u"]) < 1e-10
+    for k in ("X", "Y", "Z"):
+        assert np.abs(r["Eg"][k] - r["Eo"][k]).max() < 1e-12
 
 
 def test_cell_lists_bit_exact(gpu):
