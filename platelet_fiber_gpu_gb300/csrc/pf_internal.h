@@ -67,7 +67,7 @@ struct Lattice {
   size_t bytes = 0;
   // row-staged step: rows per tile, tiles in flight per CTA, persistent grid
   // (rows_stages == 0: the direct-gather kernel is used)
-  int rows_rpt = 0, rows_stages = -1, rows_grid = 0;
+  int rows_rpt = 0, rows_stages = -1, rows_grid = 0, rows_ds = 0;
   size_t rows_smem = 0;
 };
 

@@ -14,6 +14,7 @@
 // which is the reference's Guo forcing with u -> u/C and F -> F*K*dt/C.
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "pf_internal.h"
 
@@ -173,15 +174,51 @@ __device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z,
   moments(g, drho, jx, jy, jz);
   const R rho = (R)1 + drho;
   const R hk = (R)0.5 * (R)k.kmom;
-  if constexpr (sizeof(R) == 4) {
-    const float ir = __frcp_rn(rho);
-    ux = (jx + hk * Fx) * ir;
-    uy = (jy + hk * Fy) * ir;
-    uz = (jz + hk * Fz) * ir;
+  ux = (jx + hk * Fx) / rho;
+  uy = (jy + hk * Fy) / rho;
+  uz = (jz + hk * Fz) / rho;
+}
+
+// BGK collision with Guo forcing of one node, in place on the shifted
+// populations (F already scaled to lattice units, om = 1/tau, sf = 1 - om/2):
+//   g_d <- g_d - om (g_d - geq_d) + S_d.
+// FP64: term by term as written.  FP32: the same polynomial regrouped as
+//   g_d <- (1 - om) g_d + w_d (A + B cu + C cu^2 + D cF + E cu cF)
+// with per-node coefficients, evaluated once per opposite pair (d, opp d),
+// whose cu and cF differ only in sign.
+template <class R>
+__device__ __forceinline__ void collide(R g[Q], R drho, R ux, R uy, R uz, R Fx, R Fy, R Fz, R om, R sf) {
+  const R rho = (R)1 + drho;
+  const R usq = ux * ux + uy * uy + uz * uz;
+  const R uF = ux * Fx + uy * Fy + uz * Fz;
+  if constexpr (sizeof(R) == 8) {
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
+      const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
+      const R w = (R)wgt(d);
+      const R geq = w * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq));
+      const R src = w * sf * ((R)3 * cF + (R)9 * cu * cF - (R)3 * uF);
+      g[d] = g[d] - om * (g[d] - geq) + src;
+    }
   } else {
-    ux = (jx + hk * Fx) / rho;
-    uy = (jy + hk * Fy) / rho;
-    uz = (jz + hk * Fz) / rho;
+    const R omr = om * rho;
+    const R A = om * drho - (R)1.5 * omr * usq - (R)3 * sf * uF;
+    const R B = (R)3 * omr, C = (R)4.5 * omr, D = (R)3 * sf, E = (R)9 * sf;
+    const R omc = (R)1 - om;
+    g[0] = omc * g[0] + (R)wgt(0) * A;
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+      if (opp(d) < d) continue;  // handled with its partner
+      const int o = opp(d);
+      const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
+      const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
+      const R even = A + cu * (C * cu + E * cF);
+      const R odd = B * cu + D * cF;
+      const R w = (R)wgt(d);
+      g[d] = omc * g[d] + w * (even + odd);
+      g[o] = omc * g[o] + w * (even - odd);
+    }
   }
 }
 
@@ -223,24 +260,13 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
     R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
     if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
     const R kc = (R)k.kcoll;
-    Fx *= kc; Fy *= kc; Fz *= kc;
     const R om = (R)k.omega;
-    const R rho = (R)1 + drho;
-    const R usq = ux * ux + uy * uy + uz * uz;
-    const R uF = ux * Fx + uy * Fy + uz * Fz;
-    const R sf = (R)1 - (R)0.5 * om;
+    collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
     const R sigma = (R)k.fp16_scale;
 #pragma unroll
-    for (int d = 0; d < Q; ++d) {
-      const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
-      const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
-      const R w = (R)wgt(d);
-      const R geq = w * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq));
-      const R src = w * sf * ((R)3 * cF + (R)9 * cu * cF - (R)3 * uF);
-      const R gn = g[d] - om * (g[d] - geq) + src;
-      StoreTraits<S>::store(gout + (size_t)d * N + n, gn, d,
+    for (int d = 0; d < Q; ++d)
+      StoreTraits<S>::store(gout + (size_t)d * N + n, g[d], d,
                             (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
-    }
     if (fp) zero_force<R>(Fp, n);
   }
   __syncwarp();
@@ -257,18 +283,25 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
 
 // ------------------------------------------------------------ row-staged step
 // The same fused step with its loads staged through shared memory: a CTA of
-// kRowThreads threads owns tiles of `rpt` consecutive x-rows.  For a tile and
-// a direction d the source row (y - cy, z - cz) of plane d -- or, through a
-// bounce-back face in y or z, the tile's own row of plane opp(d) -- is one
-// contiguous run of nx populations, copied by a bulk asynchronous copy that
-// completes on the stage's mbarrier.  The x shift of the pull is an index
-// into the staged row (periodic x wraps inside it; a bounce-back x face reads
-// the node's own opp(d) population from global memory).  `stages` tiles are
-// in flight per CTA; the persistent grid walks the tiles in order.
+// kRowThreads threads owns tiles of `rpt` consecutive x-rows (rpt * nx <= 256).
+// For a tile and a direction d the source row (y - cy, z - cz) of plane d --
+// or, through a bounce-back face in y or z, the tile's own row of plane
+// opp(d) -- is one contiguous run of nx populations, copied by a bulk
+// asynchronous copy that completes on the stage's "full" mbarrier.  Rows of
+// directions with cx != 0 also get 16-byte halos (the periodic neighbours of
+// the row's ends), so the pull's x shift is a constant offset into shared
+// memory.  Row layout of a stage: [Q][DS] populations, row rr of direction d
+// at d * DS + rr * (nx + 2H), H = 16 / sizeof(S) halo elements per side.
+// Every warp owns one 32-node force brick of one row.  `stages` tiles are in
+// flight per CTA: a warp arrives on the stage's "empty" barrier when done
+// with it, warp 0 refills the stage once all warps have arrived.  The
+// persistent grid walks the tiles in order.
 constexpr int kRowThreads = 256;
 constexpr int kMaxStages = 4;
-constexpr unsigned kWaitLimit = 1u << 22;  // try_wait polls before a stage is given up
+constexpr unsigned kWaitSliceNs = 20000;                 // suspend hint of one try_wait
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // a stage is given up after 1 s
 
+__constant__ int c_cx[Q] = {0, 1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0};
 __constant__ int c_cy[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1};
 __constant__ int c_cz[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1};
 __constant__ int c_opp[Q] = {0, 2, 1, 4, 3, 6, 5, 12, 11, 14, 13, 8, 7, 10, 9, 18, 17, 16, 15};
@@ -289,17 +322,44 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait for phase `parity` of a stage barrier; false if it gave up
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* b, unsigned parity, unsigned hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for phase `parity` of a stage barrier: the waiting thread is
+// suspended in the barrier (up to kWaitSliceNs per try) instead of spinning;
+// false if the phase has not completed after kWaitLimitNs.
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(b, parity)) return true;
-  return false;
+  if (mbar_try_wait(b, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait_hint(b, parity, kWaitSliceNs)) return true;
+    if (global_ns() - t0 > kWaitLimitNs) return false;
+  }
 }
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* b) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                    smem_u32(dst)),
                "l"(src), "r"(bytes), "r"(smem_u32(b))
                : "memory");
+}
+
+// directions with cy == wy (wy != 0) or cz == wz (wz != 0), as a bit mask
+__host__ __device__ constexpr unsigned dir_mask(int wy, int wz) {
+  unsigned m = 0;
+  for (int d = 0; d < Q; ++d)
+    if ((wy != 0 && cy(d) == wy) || (wz != 0 && cz(d) == wz)) m |= 1u << d;
+  return m;
 }
 
 template <class S, class R>
@@ -313,12 +373,13 @@ __device__ __forceinline__ float from_store<__half, float>(__half v, int d, floa
   return __half2float(v) * ((float)wgt(d) * sigma);
 }
 
-template <class S, class R>
+template <class S, class R, int DS>
 __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_k(
     LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB, R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
     int ncells, int rpt, int stages, Control* ctl) {
   if (ctl->done) return;
   constexpr int kWarps = kRowThreads / 32;
+  constexpr int H = 16 / (int)sizeof(S);  // halo elements per side
   extern __shared__ __align__(128) unsigned char s_raw[];
   __shared__ __align__(8) uint64_t s_full[kMaxStages], s_empty[kMaxStages];
   __shared__ int4 s_info[kMaxStages][kWarps];  // (y, z, own-row mask) of each staged row
@@ -332,8 +393,8 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
   const unsigned* flc = par ? flB : flA;
   const int first = ctl->first;
   const int nx = k.nx, ny = k.ny, nz = k.nz;
+  const int RS = nx + 2 * H;  // staged row length
   const int rows = ny * nz;
-  const int tile_nodes = rpt * nx;
   const int ntiles = (rows + rpt - 1) / rpt;
   const size_t N = (size_t)k.N;
   const unsigned row_bytes = (unsigned)(nx * sizeof(S));
@@ -353,8 +414,8 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
 
   // Warp 0 stages local tile i (the CTA's i-th tile) into stage i % stages:
   // lanes < nr write the row descriptors, lane 0 arms the full barrier (its
-  // release publishes the descriptors), the lanes then issue one bulk copy
-  // per (direction, row).
+  // release publishes the descriptors), the lanes then issue the copies, one
+  // (direction, row) per lane: the row, and for cx != 0 its two halos.
   auto issue = [&](int i) {
     const int tile = blockIdx.x + i * gridDim.x;
     const int s = i % stages;
@@ -363,17 +424,17 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     if (lane < nr) {
       const int r = r0 + lane, y = r % ny, z = r / ny;
       unsigned mask = 0;
-      for (int d = 0; d < Q; ++d) {
-        const bool own = (bby && ((c_cy[d] == 1 && y == 0) || (c_cy[d] == -1 && y == ny - 1))) ||
-                         (bbz && ((c_cz[d] == 1 && z == 0) || (c_cz[d] == -1 && z == nz - 1)));
-        mask |= (unsigned)own << d;
-      }
+      if (bby && y == 0) mask |= dir_mask(1, 0);
+      if (bby && y == ny - 1) mask |= dir_mask(-1, 0);
+      if (bbz && z == 0) mask |= dir_mask(0, 1);
+      if (bbz && z == nz - 1) mask |= dir_mask(0, -1);
       s_info[s][lane] = make_int4(y, z, (int)mask, 0);
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive_expect(&s_full[s], (unsigned)(Q * nr) * row_bytes);
+    // 10 of the 19 directions have cx != 0: two 16-byte halos per row each
+    if (lane == 0) mbar_arrive_expect(&s_full[s], (unsigned)nr * ((unsigned)Q * row_bytes + 10u * 32u));
     __syncwarp();
-    S* dst0 = sbuf + (size_t)s * Q * tile_nodes;
+    S* st0 = sbuf + (size_t)s * Q * DS;
     for (int c = lane; c < Q * nr; c += 32) {
       const int d = c / nr, rr = c - d * nr;
       const int4 inf = s_info[s][rr];
@@ -386,7 +447,12 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
         sz = sz < 0 ? sz + nz : (sz >= nz ? sz - nz : sz);
         src = gin + (size_t)d * N + ((size_t)sy + (size_t)ny * sz) * nx;
       }
-      bulk_load(dst0 + (size_t)d * tile_nodes + (size_t)rr * nx, src, row_bytes, &s_full[s]);
+      S* dst = st0 + (size_t)d * DS + (size_t)rr * RS;
+      bulk_load(dst + H, src, row_bytes, &s_full[s]);
+      if (c_cx[d] != 0) {
+        bulk_load(dst, src + (nx - H), 16u, &s_full[s]);
+        bulk_load(dst + H + nx, src, 16u, &s_full[s]);
+      }
     }
   };
 
@@ -394,30 +460,37 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
   const R kc = (R)k.kcoll;
   const R om = (R)k.omega;
   const R sf = (R)1 - (R)0.5 * om;
-  // One node: pull from the staged rows (own-row mask for bounce-back faces
-  // in y/z, periodic x inside the row, bounce-back x from global memory),
-  // collide, store.  Called by whole warps; a warp's 32 nodes are one force
-  // brick (nx is a multiple of 32), whose previous-force flag the warp clears.
-  auto node = [&](const S* row, int x, int r, int4 inf) {
+  // One node; p points at the node's column in direction 0 of its staged row.
+  // Called by whole warps (a warp's 32 nodes are one force brick, whose
+  // previous-force flag the warp clears).
+  auto node = [&](const S* p, int x, int r, int4 inf, unsigned fc, unsigned fp) {
     const int z = inf.y;
     const unsigned mask = (unsigned)inf.z;
     const size_t n = (size_t)r * nx + x;
-    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
-    const bool xedge = bbx && (x == 0 || x == nx - 1);
     R g[Q];
+    if (mask == 0) {
+      // interior row: every direction pulls from x - cx (halos cover the ends)
 #pragma unroll
-    for (int d = 0; d < Q; ++d) {
-      bool own = false;
-      if (cy(d) != 0 || cz(d) != 0) own = (mask >> d) & 1u;
-      int idx = x;
-      if (cx(d) == 1) idx = own ? x : xm;
-      if (cx(d) == -1) idx = own ? x : xp;
-      g[d] = from_store<S, R>(row[d * tile_nodes + idx], d, sigma);
-      if (cx(d) != 0 && xedge && !own && ((cx(d) == 1 && x == 0) || (cx(d) == -1 && x == nx - 1)))
-        g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
+      for (int d = 0; d < Q; ++d) g[d] = from_store<S, R>(p[d * DS - cx(d)], d, sigma);
+    } else {
+      // row on a bounce-back face in y or z: own-row directions are unshifted
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        const bool own = (cy(d) != 0 || cz(d) != 0) && ((mask >> d) & 1u);
+        g[d] = from_store<S, R>(own ? p[d * DS] : p[d * DS - cx(d)], d, sigma);
+      }
+    }
+    if (bbx && (x == 0 || x == nx - 1)) {
+      // bounce-back x face: the node's own opp(d) population
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        if (cx(d) == 0) continue;
+        const bool own = (cy(d) != 0 || cz(d) != 0) && ((mask >> d) & 1u);
+        if (!own && ((cx(d) == 1 && x == 0) || (cx(d) == -1 && x == nx - 1)))
+          g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
+      }
     }
     const int brick = (x >> 5) + k.nbx * r;
-    const unsigned fc = flc[brick], fp = flp[brick];
     R drho, ux, uy, uz;
     if (first) {
       ld_u<R>(ubuf, n, drho, ux, uy, uz);
@@ -428,22 +501,12 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     }
     R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
     if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
-    Fx *= kc; Fy *= kc; Fz *= kc;
-    const R rho = (R)1 + drho;
-    const R usq = ux * ux + uy * uy + uz * uz;
-    const R uF = ux * Fx + uy * Fy + uz * Fz;
+    collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, sf);
     S* o = gout + n;
 #pragma unroll
-    for (int d = 0; d < Q; ++d) {
-      const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
-      const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
-      const R w = (R)wgt(d);
-      const R geq = w * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq));
-      const R src = w * sf * ((R)3 * cF + (R)9 * cu * cF - (R)3 * uF);
-      const R gn = g[d] - om * (g[d] - geq) + src;
-      StoreTraits<S>::store(o + (size_t)d * N, gn, d,
+    for (int d = 0; d < Q; ++d)
+      StoreTraits<S>::store(o + (size_t)d * N, g[d], d,
                             (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
-    }
     if (fp) zero_force<R>(Fp, n);
     __syncwarp();
     if (lane == 0 && fp) flp[brick] = 0;
@@ -453,24 +516,34 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
   int issued = 0;
   if (warp == 0)
     for (; issued < stages && issued < my_tiles; ++issued) issue(issued);
-  // tile-invariant part of this thread's node (several rows per tile: one
-  // node per thread; one row per tile: x strides over the row)
-  const int rr0 = rpt == 1 ? 0 : (int)threadIdx.x / nx;
-  const int x0 = rpt == 1 ? (int)threadIdx.x : (int)threadIdx.x - rr0 * nx;
+  // This thread's node of every tile (rpt * nx <= kRowThreads: at most one):
+  // row rr0 of the tile, column x0.  Its brick flags are loaded one tile
+  // ahead, so their latency hides behind the previous tile's work.
+  const int rr0 = (int)threadIdx.x / nx;
+  const int x0 = (int)threadIdx.x - rr0 * nx;
+  const bool has_node = rr0 < rpt;
+  auto flags_of = [&](int i, unsigned& fc, unsigned& fp) {
+    fc = fp = 0;
+    if (!has_node || i >= my_tiles) return;
+    const int r = (blockIdx.x + i * gridDim.x) * rpt + rr0;
+    if (r >= rows) return;
+    const int brick = (x0 >> 5) + k.nbx * r;
+    fc = flc[brick];
+    fp = flp[brick];
+  };
+  unsigned fc_next, fp_next;
+  flags_of(0, fc_next, fp_next);
   bool failed = false;
   int i = 0;
   for (; i < my_tiles; ++i) {
     const int s = i % stages;
     const int r0 = (blockIdx.x + i * gridDim.x) * rpt;
     const int nr = min(rpt, rows - r0);
+    const unsigned fc = fc_next, fp = fp_next;
+    flags_of(i + 1, fc_next, fp_next);
     if (!mbar_wait(&s_full[s], (unsigned)((i / stages) & 1))) { failed = true; break; }
-    const S* sb = sbuf + (size_t)s * Q * tile_nodes;
-    if (rpt == 1) {
-      const int4 inf = s_info[s][0];
-      for (int x = x0; x < nx; x += kRowThreads) node(sb, x, r0, inf);
-    } else if (rr0 < nr) {
-      node(sb + rr0 * nx, x0, r0 + rr0, s_info[s][rr0]);
-    }
+    if (has_node && rr0 < nr)
+      node(sbuf + (size_t)s * Q * DS + H + rr0 * RS + x0, x0, r0 + rr0, s_info[s][rr0], fc, fp);
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&s_empty[s])) : "memory");
     if (warp == 0 && issued < my_tiles) {
@@ -630,48 +703,62 @@ __global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
   }
 }
 
-// Row-staged configuration: nx a multiple of 32 (so each staged row, a bulk
-// copy of nx * sizeof(S) bytes, is a multiple of 16 bytes and every warp owns
-// one force brick); tiles hold max(1, 256 / nx) rows; three stages when they
-// fit beside two more CTAs on an SM, else two.
-template <class S, class R>
-void rows_config(Lattice& L) {
-  L.rows_stages = 0;
-  if (getenv("PFGPU_DIRECT_LBM")) return;
-  const int nx = L.k.nx;
-  if (nx % 32 != 0) return;  // a warp's 32 nodes are one force brick
-  const int rpt = nx >= kRowThreads ? 1 : kRowThreads / nx;
-  const size_t stage = (size_t)Q * rpt * nx * sizeof(S);
+// Row-staged configuration: nx a multiple of 32 and at most 256 (each staged
+// row is a multiple of 16 bytes, every warp owns one force brick, a tile of
+// max(1, 256 / nx) rows with halos fits the direction stride DS of 272 or
+// 384 populations); three stages when they fit beside two more CTAs on an
+// SM, else two.
+template <class S, class R, int DS>
+bool rows_try(Lattice& L, int rpt) {
+  const size_t stage = (size_t)Q * DS * sizeof(S);
   int stages = 3;
   if (3 * stage > 72 * 1024) stages = 2;
-  if ((size_t)stages * stage > 200 * 1024) return;
   const size_t smem = (size_t)stages * stage;
-  if (cudaFuncSetAttribute(lbm_rows_k<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (cudaFuncSetAttribute(lbm_rows_k<S, R, DS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess) {
     cudaGetLastError();
-    return;
+    return false;
   }
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lbm_rows_k<S, R>, kRowThreads, smem) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lbm_rows_k<S, R, DS>, kRowThreads, smem) != cudaSuccess ||
       occ < 1) {
     cudaGetLastError();
-    return;
+    return false;
   }
   const int ntiles = (L.k.ny * L.k.nz + rpt - 1) / rpt;
   L.rows_rpt = rpt;
   L.rows_stages = stages;
   L.rows_smem = smem;
+  L.rows_ds = DS;
   L.rows_grid = std::min(ntiles, sms * occ);
+  return true;
+}
+
+// The direct-gather kernel is the default (it measured faster on the FP32
+// 256x128x128 channel); PFGPU_LBM_KERNEL=rows selects the row-staged one.
+template <class S, class R>
+void rows_config(Lattice& L) {
+  L.rows_stages = 0;
+  const char* sel = getenv("PFGPU_LBM_KERNEL");
+  if (!sel || strcmp(sel, "rows") != 0) return;
+  const int nx = L.k.nx;
+  if (nx % 32 != 0 || nx > kRowThreads) return;
+  const int rpt = kRowThreads / nx;
+  const int need = rpt * (nx + 2 * (16 / (int)sizeof(S)));
+  if (need <= 272) rows_try<S, R, 272>(L, rpt);
+  else if (need <= 384) rows_try<S, R, 384>(L, rpt);
 }
 
 template <class S, class R>
 cudaError_t step_impl(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st) {
   if (L.rows_stages < 0) rows_config<S, R>(L);
   if (L.rows_stages > 0) {
-    lbm_rows_k<S, R><<<L.rows_grid, kRowThreads, L.rows_smem, st>>>(
-        L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf, L.flags[0], L.flags[1],
-        bin_count, ncells, L.rows_rpt, L.rows_stages, ctl);
+    auto kern = L.rows_ds == 272 ? lbm_rows_k<S, R, 272> : lbm_rows_k<S, R, 384>;
+    kern<<<L.rows_grid, kRowThreads, L.rows_smem, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0],
+                                                       (R4<R>*)L.F[1], (R4<R>*)L.ubuf, L.flags[0], L.flags[1],
+                                                       bin_count, ncells, L.rows_rpt, L.rows_stages, ctl);
     return cudaGetLastError();
   }
   dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);

@@ -176,10 +176,10 @@ def test_row_staged_and_direct_lbm_kernels_agree(gpu, scene, prec, tol, monkeypa
     Scenes: Zou/He shear walls with periodic x/y, and a box with bounce-back
     on every axis (the x faces are read from global memory)."""
     sc = _lbm_scene(scene)
+    monkeypatch.setenv("PFGPU_LBM_KERNEL", "rows")
     a = gpu.Job(sc, prec)
-    monkeypatch.setenv("PFGPU_DIRECT_LBM", "1")
+    monkeypatch.delenv("PFGPU_LBM_KERNEL")
     b = gpu.Job(sc, prec)
-    monkeypatch.delenv("PFGPU_DIRECT_LBM")
     assert a.lbm_kernel == "rows" and b.lbm_kernel == "direct"
     a.step(12)
     b.step(12)
@@ -190,9 +190,10 @@ def test_row_staged_and_direct_lbm_kernels_agree(gpu, scene, prec, tol, monkeypa
     b.close()
 
 
-def test_row_staged_fp64_vs_oracle(gpu):
+def test_row_staged_fp64_vs_oracle(gpu, monkeypatch):
     """FP64 row-staged kernel against the oracle on the bounce-back box."""
     sc = _lbm_scene("walls")
+    monkeypatch.setenv("PFGPU_LBM_KERNEL", "rows")
     r = _run_both(gpu, sc, 15, 0)
     assert rel_max(r["Lg"]["fIN"], r["Lo"]["fIN"]) < 1e-12
     assert rel_l2(r["Lg"]["u"], r["Lo"]["u"]) < 1e-10
