@@ -138,9 +138,11 @@ int pfgpu_job_step(pfgpu_job *job, int nsteps);
 int pfgpu_job_step_graph(pfgpu_job *job, int nsteps);
 int pfgpu_job_sync(pfgpu_job *job);
 /* Runs nsteps steps serialised on one stream with CUDA events around each
- * phase and returns the summed device time per phase in ms: membrane, morse,
- * fibrin, bonds, spread, lbm, moments, interp (pfgpu_profile_phase_name). */
-int pfgpu_job_profile(pfgpu_job *job, int nsteps, double ms_out[8]);
+ * phase and returns the summed device time per phase in ms (ms_out holds
+ * pfgpu_profile_phase_count() entries): flag, membrane, morse, fibrin, bonds,
+ * spread, lbm (both lattice passes), moments, interp. */
+int pfgpu_job_profile(pfgpu_job *job, int nsteps, double *ms_out);
+int pfgpu_profile_phase_count(void);
 const char *pfgpu_profile_phase_name(int i);
 /* Copies state back in scene layouts; any pointer may be NULL. */
 int pfgpu_job_get_lattice(pfgpu_job *job, double *fIN, double *fOUT, double *rho, double *u /*[3][N]*/,

@@ -6,7 +6,8 @@
 //   lattice force 2 x Real4[N]          reference force units, only bricks
 //                                       flagged active are read or non-zero
 //   brick flags   2 x uint32[nbricks]   + active-brick lists (one brick =
-//                                       128 x-nodes of one (y,z) row)
+//                                       32 x-nodes of one (y,z) row), and
+//                                       2 x uint32[nbricks] occupancy bits
 //   u buffer      Real4[N]              (rho-1, u/C) at active bricks; before
 //                                       the first step: the initial rho-1, u/C
 //   elements      double X,Y,RY,Z,V,F   positions stay FP64
@@ -64,6 +65,13 @@ struct Lattice {
   void* ubuf = nullptr;
   unsigned* flags[2] = {nullptr, nullptr};
   int* list[2] = {nullptr, nullptr};
+  // marker occupancy, one bit per node (one 32-bit word per brick), and its
+  // dilation in x and y: scratch of the brick flagging
+  unsigned* mark = nullptr;
+  unsigned* dil = nullptr;
+  // reduced precision: spread/interpolate platelet elements through shared
+  // per-platelet node boxes (1) or per marker with global atomics (0)
+  int ibm_box = 0;
   size_t bytes = 0;
   // row-staged step: rows per tile, tiles in flight per CTA, persistent grid
   // (rows_stages == 0: the direct-gather kernel is used)
@@ -137,7 +145,10 @@ cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_de
 // picks the row-staged or the direct-gather step kernel (host only; call
 // before the first step and outside stream capture)
 cudaError_t lattice_configure(Lattice& L);
-cudaError_t lattice_step(Lattice& L, Control* ctl, cudaStream_t st);
+// part 0: the whole lattice; 1: bricks not flagged for this step's force
+// (may run while the forces are computed); 2: the flagged bricks (after the
+// spreading).  bin_count: Morse cell counters to clear (parts 0 and 2 only).
+cudaError_t lattice_step_part(Lattice& L, Control* ctl, int part, int* bin_count, int ncells, cudaStream_t st);
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
 // fIN [19][N], fOUT [19][N], rho [N], u [3][N], F [3][N] (double, device)
 cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* fIN, double* fOUT, double* rho,
@@ -148,11 +159,16 @@ cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStre
 cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
 cudaError_t fibrin_forces(Fibrin& Fb, int precision, Control* ctl, cudaStream_t st);
 cudaError_t bond_pass(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
+// occupancy bits of the current marker positions (once, after an upload;
+// the position update sets them for the following step)
+cudaError_t mark_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, cudaStream_t st);
+// flags (and lists) the force bricks every marker's stencil can reach this
+// step, before any force exists; spread_markers then only adds forces
+cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st);
 cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st);
 cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, double detach_rate,
                            uint64_t seed, unsigned* done_blocks, cudaStream_t st);
 cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st);
-cudaError_t lattice_step_binned(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st);
 size_t bond_scratch_bytes(int NR);
 bool morse_uses_cells(const PlateletConst& k);
 cudaError_t sort_cell_bins(Platelets& Pl, Control* ctl, cudaStream_t st);

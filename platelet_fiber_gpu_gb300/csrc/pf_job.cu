@@ -50,8 +50,11 @@ struct pfgpu_job {
   Control* ctl = nullptr;
   unsigned* done_blocks = nullptr;
   double* scratch4 = nullptr;
-  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  // s0: critical path (flags, bonds, spreading, flagged bricks, moments,
+  // interpolation); s1-s3: membrane, Morse, fibrin; s4 (lowest priority):
+  // the lattice pass over the bricks without force, beside the force kernels
+  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr, s4 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev4 = nullptr;
   cudaGraphExec_t graph = nullptr;
   double detach_rate = 0;
   uint64_t seed = 0;
@@ -83,10 +86,10 @@ static void destroy(pfgpu_job* j) {
   if (!j) return;
   if (j->graph) cudaGraphExecDestroy(j->graph);
   for (void* p : j->allocs) cudaFree(p);
-  cudaStream_t ss[4] = {j->s0, j->s1, j->s2, j->s3};
+  cudaStream_t ss[5] = {j->s0, j->s1, j->s2, j->s3, j->s4};
   for (cudaStream_t s : ss)
     if (s) cudaStreamDestroy(s);
-  cudaEvent_t ee[4] = {j->ev_fork, j->ev1, j->ev2, j->ev3};
+  cudaEvent_t ee[5] = {j->ev_fork, j->ev1, j->ev2, j->ev3, j->ev4};
   for (cudaEvent_t e : ee)
     if (e) cudaEventDestroy(e);
   delete j;
@@ -389,14 +392,35 @@ static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
   return PFGPU_OK;
 }
 
+// One coupled step.  With markers:
+//   s0: flag the force bricks of this step (from the marker positions)
+//   fork -> s1 membrane | s2 Morse | s3 fibrin | s0 bonds | s4 lattice pass
+//           over the bricks without force
+//   join forces -> s0: spread, lattice pass over the flagged bricks
+//   join s4 -> s0: moments at the flagged bricks, interpolation + advance.
+// Without markers: the lattice pass over everything, then the step close.
 static int enqueue_step(pfgpu_job* j) {
   Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
   Fibrin* Fb = j->has_fb ? &j->Fb : nullptr;
+  const bool cells = Pl && Pl->k.morse && morse_uses_cells(Pl->k);
+  int* bins = cells ? Pl->bin_count : nullptr;
+  const int ncells = cells ? Pl->ncells : 0;
   int launches = 0;
+  if (!Pl && !Fb) {
+    CK(lattice_step_part(j->L, j->ctl, 0, nullptr, 0, j->s0));
+    CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
+    j->launches_per_step = 2;
+    return PFGPU_OK;
+  }
+  CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0));
+  launches++;
   CK(cudaEventRecord(j->ev_fork, j->s0));
   CK(cudaStreamWaitEvent(j->s1, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s2, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s3, j->ev_fork, 0));
+  CK(cudaStreamWaitEvent(j->s4, j->ev_fork, 0));
+  CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, j->s4));
+  launches++;
   if (Pl) {
     CK(membrane_forces(*Pl, j->precision, j->ctl, j->s1));
     launches++;
@@ -419,47 +443,51 @@ static int enqueue_step(pfgpu_job* j) {
   CK(cudaStreamWaitEvent(j->s0, j->ev1, 0));
   CK(cudaStreamWaitEvent(j->s0, j->ev2, 0));
   CK(cudaStreamWaitEvent(j->s0, j->ev3, 0));
-  if (Pl || Fb) {
-    CK(spread_markers(j->L, Pl, Fb, j->ctl, j->s0));
-    launches++;
-  }
-  const bool cells = Pl && Pl->k.morse && morse_uses_cells(Pl->k);
-  CK(lattice_step_binned(j->L, j->ctl, cells ? Pl->bin_count : nullptr, cells ? Pl->ncells : 0, j->s0));
-  launches++;
-  if (Pl || Fb) {
-    CK(lattice_moments_active(j->L, j->ctl, j->s0));
-    launches++;
-  }
+  CK(spread_markers(j->L, Pl, Fb, j->ctl, j->s0));
+  CK(lattice_step_part(j->L, j->ctl, 2, bins, ncells, j->s0));
+  CK(cudaEventRecord(j->ev4, j->s4));
+  CK(cudaStreamWaitEvent(j->s0, j->ev4, 0));
+  CK(lattice_moments_active(j->L, j->ctl, j->s0));
   CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
-  launches++;
+  launches += 4;
   j->launches_per_step = launches;
   return PFGPU_OK;
 }
 
 // Same launches as enqueue_step, on one stream, with an event pair around
-// each phase; the per-phase device times are summed over the steps.
-static const char* kPhaseNames[] = {"membrane", "morse", "fibrin", "bonds", "spread", "lbm", "moments", "interp"};
+// each phase; the per-phase device times are summed over the steps.  "lbm"
+// is both lattice passes (the flagged bricks' pass runs after the spreading).
+static const char* kPhaseNames[] = {"flag",   "membrane", "morse", "fibrin", "bonds",
+                                    "spread", "lbm",      "moments", "interp"};
+constexpr int kNumPhases = 9;
 static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
   Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
   Fibrin* Fb = j->has_fb ? &j->Fb : nullptr;
-  const int NPH = 8;
+  const int NPH = kNumPhases;
   std::vector<cudaEvent_t> ev((size_t)2 * NPH * nsteps, nullptr);
   for (auto& e : ev) CK(cudaEventCreate(&e));
   cudaStream_t s = j->s0;
   auto rec = [&](int step, int ph, int end) { return cudaEventRecord(ev[((size_t)step * NPH + ph) * 2 + end], s); };
   const bool cells = Pl && Pl->k.morse && morse_uses_cells(Pl->k);
+  const bool markers = Pl || Fb;
   for (int t = 0; t < nsteps; ++t) {
-    CK(rec(t, 0, 0)); if (Pl) CK(membrane_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 0, 1));
-    CK(rec(t, 1, 0)); if (Pl && Pl->k.morse) CK(morse_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 1, 1));
-    CK(rec(t, 2, 0)); if (Fb) CK(fibrin_forces(*Fb, j->precision, j->ctl, s)); CK(rec(t, 2, 1));
-    CK(rec(t, 3, 0)); if (Pl && Pl->k.nrec) CK(bond_pass(*Pl, j->precision, j->ctl, s)); CK(rec(t, 3, 1));
-    CK(rec(t, 4, 0)); if (Pl || Fb) CK(spread_markers(j->L, Pl, Fb, j->ctl, s)); CK(rec(t, 4, 1));
-    CK(rec(t, 5, 0));
-    CK(lattice_step_binned(j->L, j->ctl, cells ? Pl->bin_count : nullptr, cells ? Pl->ncells : 0, s));
-    CK(rec(t, 5, 1));
-    CK(rec(t, 6, 0)); if (Pl || Fb) CK(lattice_moments_active(j->L, j->ctl, s)); CK(rec(t, 6, 1));
-    CK(rec(t, 7, 0)); CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, s));
-    CK(rec(t, 7, 1));
+    CK(rec(t, 0, 0)); if (markers) CK(flag_markers(j->L, Pl, Fb, j->ctl, s)); CK(rec(t, 0, 1));
+    CK(rec(t, 1, 0)); if (Pl) CK(membrane_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 1, 1));
+    CK(rec(t, 2, 0)); if (Pl && Pl->k.morse) CK(morse_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 2, 1));
+    CK(rec(t, 3, 0)); if (Fb) CK(fibrin_forces(*Fb, j->precision, j->ctl, s)); CK(rec(t, 3, 1));
+    CK(rec(t, 4, 0)); if (Pl && Pl->k.nrec) CK(bond_pass(*Pl, j->precision, j->ctl, s)); CK(rec(t, 4, 1));
+    CK(rec(t, 5, 0)); if (markers) CK(spread_markers(j->L, Pl, Fb, j->ctl, s)); CK(rec(t, 5, 1));
+    CK(rec(t, 6, 0));
+    if (markers) {
+      CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, s));
+      CK(lattice_step_part(j->L, j->ctl, 2, cells ? Pl->bin_count : nullptr, cells ? Pl->ncells : 0, s));
+    } else {
+      CK(lattice_step_part(j->L, j->ctl, 0, nullptr, 0, s));
+    }
+    CK(rec(t, 6, 1));
+    CK(rec(t, 7, 0)); if (markers) CK(lattice_moments_active(j->L, j->ctl, s)); CK(rec(t, 7, 1));
+    CK(rec(t, 8, 0)); CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, s));
+    CK(rec(t, 8, 1));
   }
   CK(cudaStreamSynchronize(s));
   for (int ph = 0; ph < NPH; ++ph) ms[ph] = 0;
@@ -491,7 +519,7 @@ size_t pfgpu_scene_device_bytes(const pf_scene* s, int precision) {
   const size_t N = (size_t)s->nx * s->ny * s->nz;
   const size_t sb = store_bytes(precision), rb = real_bytes(precision);
   const size_t nbricks = (size_t)((s->nx + kBrickX - 1) / kBrickX) * s->ny * s->nz;
-  size_t b = 2 * 19 * N * sb + 3 * N * 4 * rb + 4 * nbricks * 4;
+  size_t b = 2 * 19 * N * sb + 3 * N * 4 * rb + 6 * nbricks * 4;
   const size_t PE = (size_t)s->n_platelets * s->n_elem;
   b += PE * (4 * 8 + 6 * 8 + 3 * 8 + 6 * rb);
   b += (size_t)s->n_platelets * ((size_t)s->n_node * 3 + (size_t)s->n_tri * 4 + s->n_membrane) * rb;
@@ -531,18 +559,29 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
       return fail(e_ == cudaErrorMemoryAllocation ? PFGPU_ERR_NOMEM : PFGPU_ERR_CUDA);          \
     }                                                                                           \
   } while (0)
-  CKJ(cudaStreamCreateWithFlags(&j->s0, cudaStreamNonBlocking));
-  CKJ(cudaStreamCreateWithFlags(&j->s1, cudaStreamNonBlocking));
-  CKJ(cudaStreamCreateWithFlags(&j->s2, cudaStreamNonBlocking));
-  CKJ(cudaStreamCreateWithFlags(&j->s3, cudaStreamNonBlocking));
+  int prio_low = 0, prio_high = 0;
+  CKJ(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+  CKJ(cudaStreamCreateWithPriority(&j->s0, cudaStreamNonBlocking, prio_high));
+  CKJ(cudaStreamCreateWithPriority(&j->s1, cudaStreamNonBlocking, prio_high));
+  CKJ(cudaStreamCreateWithPriority(&j->s2, cudaStreamNonBlocking, prio_high));
+  CKJ(cudaStreamCreateWithPriority(&j->s3, cudaStreamNonBlocking, prio_high));
+  CKJ(cudaStreamCreateWithPriority(&j->s4, cudaStreamNonBlocking, prio_low));
   CKJ(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev1, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev2, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev3, cudaEventDisableTiming));
+  CKJ(cudaEventCreateWithFlags(&j->ev4, cudaEventDisableTiming));
   // lattice
   Lattice& L = j->L;
   L.precision = precision;
   L.k = lattice_const(s, fp16_scale, precision);
+  {
+    // PFGPU_IBM=boxes: FP32/FP16 platelet elements spread and interpolated
+    // through per-platelet shared-memory node boxes (default: per marker,
+    // which measured faster on the 50-platelet channel)
+    const char* ibm = getenv("PFGPU_IBM");
+    L.ibm_box = ibm && strcmp(ibm, "boxes") == 0;
+  }
   const size_t N = (size_t)L.k.N;
   const size_t sb = store_bytes(precision), rb = real_bytes(precision);
   CKJ(dalloc(j, (char**)&L.g[0], 19 * N * sb));
@@ -554,6 +593,8 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(dalloc(j, &L.flags[1], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.list[0], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.list[1], (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.mark, (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.dil, (size_t)L.k.nbricks));
   CKJ(dalloc(j, &j->ctl, 1));
   CKJ(dalloc(j, &j->done_blocks, 1));
   CKJ(dalloc(j, &j->scratch4, 4));
@@ -594,6 +635,7 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
     rc = build_fibrin(j, s);
     if (rc) return fail(rc);
   }
+  CKJ(mark_markers(j->L, j->has_pl ? &j->Pl : nullptr, j->has_fb ? &j->Fb : nullptr, j->s0));
   CKJ(cudaStreamSynchronize(j->s0));
   *out = j;
   return PFGPU_OK;
@@ -640,13 +682,14 @@ int pfgpu_job_enqueue(pfgpu_job* j, int nsteps, cudaStream_t) {
   return PFGPU_OK;
 }
 
-int pfgpu_job_profile(pfgpu_job* j, int nsteps, double ms_out[8]) {
+int pfgpu_job_profile(pfgpu_job* j, int nsteps, double* ms_out) {
   if (!j || nsteps < 1 || !ms_out) return set_error(PFGPU_ERR_INVALID, "bad arguments");
   int rc = profile_steps(j, nsteps, ms_out);
   if (rc) return rc;
   return check_control(j);
 }
-const char* pfgpu_profile_phase_name(int i) { return (i >= 0 && i < 8) ? kPhaseNames[i] : ""; }
+const char* pfgpu_profile_phase_name(int i) { return (i >= 0 && i < kNumPhases) ? kPhaseNames[i] : ""; }
+int pfgpu_profile_phase_count(void) { return kNumPhases; }
 
 int pfgpu_job_sync(pfgpu_job* j) {
   if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");

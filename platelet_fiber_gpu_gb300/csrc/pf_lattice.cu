@@ -222,63 +222,108 @@ __device__ __forceinline__ void collide(R g[Q], R drho, R ux, R uy, R uz, R Fx, 
   }
 }
 
+// One node of the direct-gather step: pull, moments with the previous
+// force, collision with the current force, store; clears the previous force.
+template <class S, class R>
+__device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restrict__ gin, S* __restrict__ gout,
+                                         const R4<R>* Fc, R4<R>* Fp, const R4<R>* ubuf, int x, int y, int z,
+                                         unsigned fc, unsigned fp, int first) {
+  const size_t N = (size_t)k.N;
+  const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
+  R g[Q];
+  gather<S, R>(k, gin, x, y, z, g);
+  R drho, ux, uy, uz;
+  if (first) {
+    // the first collision after an upload uses the uploaded density and
+    // velocity, and its populations are the uploaded fIN (no boundary pass)
+    ld_u<R>(ubuf, n, drho, ux, uy, uz);
+  } else {
+    R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
+    if (fp) ld_force<R>(Fp, n, px, py, pz);
+    node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
+  }
+  R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+  if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
+  const R kc = (R)k.kcoll;
+  const R om = (R)k.omega;
+  collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
+  const R sigma = (R)k.fp16_scale;
+#pragma unroll
+  for (int d = 0; d < Q; ++d)
+    StoreTraits<S>::store(gout + (size_t)d * N + n, g[d], d,
+                          (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+  if (fp) zero_force<R>(Fp, n);
+}
+
+// Zeroes the Morse cell counters (after this step's Morse pass, before the
+// position update bins the elements again).
+__device__ __forceinline__ void zero_bins(int* bin_count, int ncells, Control* ctl, size_t tid, size_t tot) {
+  for (size_t c = tid; c < (size_t)ncells; c += tot) bin_count[c] = 0;
+  if (tid == 0) ctl->occupied = 0;
+}
+
+// Direct-gather step over the lattice, one x-row segment of kLbmBlock nodes
+// per CTA, one force brick per warp.  skip_flagged: bricks flagged for this
+// step's force are left to lbm_list_k (they run after the spreading).
 template <class S, class R>
 __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
                                                         R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
-                                                        int ncells, Control* ctl) {
+                                                        int ncells, int skip_flagged, Control* ctl) {
   if (ctl->done) return;
-  const long long step = ctl->step;
-  const int par = (int)(step & 1);
+  const int par = (int)(ctl->step & 1);
   const S* __restrict__ gin = par ? gB : gA;
   S* __restrict__ gout = par ? gA : gB;
-  R4<R>* Fc = par ? FB : FA;
+  const R4<R>* Fc = par ? FB : FA;
   R4<R>* Fp = par ? FA : FB;
   unsigned* flp = par ? flA : flB;
   const unsigned* flc = par ? flB : flA;
-  const int first = ctl->first;
   const int x = blockIdx.x * kLbmBlock + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-  // one force brick per warp
   const int bxw = x / kBrickX;
   const bool row_ok = bxw < k.nbx;
   const int brick = bxw + k.nbx * (y + k.ny * z);
-  const unsigned fc = row_ok ? flc[brick] : 0u, fp = row_ok ? flp[brick] : 0u;
-  if (x < k.nx) {
-    const size_t N = (size_t)k.N;
-    const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
-    R g[Q];
-    gather<S, R>(k, gin, x, y, z, g);
-    R drho, ux, uy, uz;
-    if (first) {
-      // the first collision after an upload uses the uploaded density and
-      // velocity, and its populations are the uploaded fIN (no boundary pass)
-      ld_u<R>(ubuf, n, drho, ux, uy, uz);
-    } else {
-      R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
-      if (fp) ld_force<R>(Fp, n, px, py, pz);
-      node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
-    }
-    R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
-    if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
-    const R kc = (R)k.kcoll;
-    const R om = (R)k.omega;
-    collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
-    const R sigma = (R)k.fp16_scale;
-#pragma unroll
-    for (int d = 0; d < Q; ++d)
-      StoreTraits<S>::store(gout + (size_t)d * N + n, g[d], d,
-                            (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
-    if (fp) zero_force<R>(Fp, n);
-  }
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0 && fp) flp[brick] = 0;
+  const unsigned fc = row_ok ? flc[brick] : 0u;
   if (bin_count) {
     const size_t tid = (((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * blockDim.x +
                        threadIdx.x;
-    const size_t tot = (size_t)gridDim.x * gridDim.y * gridDim.z * blockDim.x;
-    for (size_t c = tid; c < (size_t)ncells; c += tot) bin_count[c] = 0;
-    if (tid == 0) ctl->occupied = 0;
+    zero_bins(bin_count, ncells, ctl, tid, (size_t)gridDim.x * gridDim.y * gridDim.z * blockDim.x);
   }
-  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0) ctl->active_count[par ^ 1] = 0;
+  if (skip_flagged && fc) return;  // whole warp: one brick
+  const unsigned fp = row_ok ? flp[brick] : 0u;
+  if (x < k.nx) lbm_node<S, R>(k, gin, gout, Fc, Fp, ubuf, x, y, z, fc, fp, ctl->first);
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0 && fp) flp[brick] = 0;
+}
+
+// The flagged bricks of this step (list[par]), one warp per brick.
+template <class S, class R>
+__global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                                        R4<R>* ubuf, unsigned* flA, unsigned* flB, const int* lA,
+                                                        const int* lB, int* bin_count, int ncells, Control* ctl) {
+  if (ctl->done) return;
+  const int par = (int)(ctl->step & 1);
+  const S* __restrict__ gin = par ? gB : gA;
+  S* __restrict__ gout = par ? gA : gB;
+  const R4<R>* Fc = par ? FB : FA;
+  R4<R>* Fp = par ? FA : FB;
+  unsigned* flp = par ? flA : flB;
+  const int* list = par ? lB : lA;
+  const int cnt = ctl->active_count[par];
+  const int first = ctl->first;
+  if (bin_count)
+    zero_bins(bin_count, ncells, ctl, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+  const int warps = kLbmBlock / 32;
+  const int lane = threadIdx.x & 31;
+  for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < cnt; b += gridDim.x * warps) {
+    const int brick = list[b];
+    const int bx = brick % k.nbx;
+    const int y = (brick / k.nbx) % k.ny;
+    const int z = brick / (k.nbx * k.ny);
+    const int x = bx * kBrickX + lane;
+    const unsigned fp = flp[brick];
+    if (x < k.nx) lbm_node<S, R>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 1u, fp, first);
+    __syncwarp();
+    if (lane == 0 && fp) flp[brick] = 0;
+  }
 }
 
 // ------------------------------------------------------------ row-staged step
@@ -561,13 +606,8 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
       for (int j = i; j < issued; ++j) mbar_wait(&s_full[j % stages], (unsigned)((j / stages) & 1));
     return;
   }
-  if (bin_count) {
-    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t tot = (size_t)gridDim.x * blockDim.x;
-    for (size_t c = tid; c < (size_t)ncells; c += tot) bin_count[c] = 0;
-    if (tid == 0) ctl->occupied = 0;
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->active_count[par ^ 1] = 0;
+  if (bin_count) zero_bins(bin_count, ncells, ctl, (size_t)blockIdx.x * blockDim.x + threadIdx.x,
+                          (size_t)gridDim.x * blockDim.x);
 }
 
 // (rho, u/C) of the nodes of the active bricks after this step's stream and
@@ -751,19 +791,34 @@ void rows_config(Lattice& L) {
   else if (need <= 384) rows_try<S, R, 384>(L, rpt);
 }
 
+// part: 0 the whole lattice, 1 the bricks not flagged for this step's force,
+// 2 the flagged bricks (after the spreading).
 template <class S, class R>
-cudaError_t step_impl(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st) {
+cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int ncells, cudaStream_t st) {
   if (L.rows_stages < 0) rows_config<S, R>(L);
-  if (L.rows_stages > 0) {
+  if (part == 0 && L.rows_stages > 0) {
     auto kern = L.rows_ds == 272 ? lbm_rows_k<S, R, 272> : lbm_rows_k<S, R, 384>;
     kern<<<L.rows_grid, kRowThreads, L.rows_smem, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0],
                                                        (R4<R>*)L.F[1], (R4<R>*)L.ubuf, L.flags[0], L.flags[1],
                                                        bin_count, ncells, L.rows_rpt, L.rows_stages, ctl);
     return cudaGetLastError();
   }
+  if (part == 2) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = sms * 8;
+    const int need = (L.k.nbricks + kLbmBlock / 32 - 1) / (kLbmBlock / 32);
+    if (grid > need) grid = need;
+    lbm_list_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
+                                                (R4<R>*)L.ubuf, L.flags[0], L.flags[1], L.list[0], L.list[1],
+                                                bin_count, ncells, ctl);
+    return cudaGetLastError();
+  }
   dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);
   lbm_step_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
-                                              (R4<R>*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells, ctl);
+                                              (R4<R>*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells,
+                                              part == 1 ? 1 : 0, ctl);
   return cudaGetLastError();
 }
 template <class S, class R>
@@ -840,11 +895,11 @@ cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_de
   return cudaErrorInvalidValue;
 }
 
-cudaError_t lattice_step_binned(Lattice& L, Control* ctl, int* bin_count, int ncells, cudaStream_t st) {
+cudaError_t lattice_step_part(Lattice& L, Control* ctl, int part, int* bin_count, int ncells, cudaStream_t st) {
   switch (L.precision) {
-    case PF_PREC_FP64: return step_impl<double, double>(L, ctl, bin_count, ncells, st);
-    case PF_PREC_FP32: return step_impl<float, float>(L, ctl, bin_count, ncells, st);
-    case PF_PREC_FP16: return step_impl<__half, float>(L, ctl, bin_count, ncells, st);
+    case PF_PREC_FP64: return step_impl<double, double>(L, ctl, part, bin_count, ncells, st);
+    case PF_PREC_FP32: return step_impl<float, float>(L, ctl, part, bin_count, ncells, st);
+    case PF_PREC_FP16: return step_impl<__half, float>(L, ctl, part, bin_count, ncells, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -855,9 +910,6 @@ cudaError_t lattice_configure(Lattice& L) {
     case PF_PREC_FP16: rows_config<__half, float>(L); return cudaSuccess;
   }
   return cudaErrorInvalidValue;
-}
-cudaError_t lattice_step(Lattice& L, Control* ctl, cudaStream_t st) {
-  return lattice_step_binned(L, ctl, nullptr, 0, st);
 }
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st) {
   switch (L.precision) {

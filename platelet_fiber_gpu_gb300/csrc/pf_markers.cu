@@ -87,20 +87,54 @@ __device__ __forceinline__ int axis_stencil(double x, float dxf, int n, int wrap
   return Stencil<R>::axis(x, dxf, 1.0 / (double)dxf, n, wrap, spread, node, w);
 }
 
-// ---------------------------------------------------------------- spreading
+// One marker's force onto its stencil nodes (global atomics).
 template <class R>
-__global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R>* FB, unsigned* flA,
-                                                unsigned* flB, int* lA, int* lB, int PE, const double* X,
+__device__ __forceinline__ void spread_one(const LatticeConst& lk, R4<R>* Fc, double x, double y, double z, R Fx,
+                                           R Fy, R Fz) {
+  int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
+  R wx[5], wy[5], wz[5];
+  const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 1, nxa, rx, wx);
+  const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 1, nya, ry, wy);
+  const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 1, nza, rz, wz);
+  for (int c = 0; c < czn; ++c)
+    for (int b = 0; b < cyn; ++b)
+      for (int a = 0; a < cxn; ++a) {
+        const R delta = wx[a] * wy[b] * wz[c];
+        const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
+        atomic_add3(Fc, n, Fx * delta, Fy * delta, Fz * delta);
+      }
+}
+// Lattice velocity (u/C) interpolated at one marker from the moments buffer.
+template <class R>
+__device__ __forceinline__ void interp_one(const LatticeConst& lk, const R4<R>* ubuf, double x, double y, double z,
+                                           R& ax, R& ay, R& az) {
+  int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
+  R wx[5], wy[5], wz[5];
+  const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 0, nxa, rx, wx);
+  const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 0, nya, ry, wy);
+  const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 0, nza, rz, wz);
+  ax = 0; ay = 0; az = 0;
+  for (int c = 0; c < czn; ++c)
+    for (int b = 0; b < cyn; ++b)
+      for (int a = 0; a < cxn; ++a) {
+        const R delta = wx[a] * wy[b] * wz[c];
+        const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
+        const R4<R> u = ubuf[n];
+        ax += u.y * delta; ay += u.z * delta; az += u.w * delta;
+      }
+}
+
+// ---------------------------------------------------------------- spreading
+// One thread per marker: total element force (membrane + Morse + bonds, kept
+// for the element output) or fibrin force, onto the current force buffer.
+template <class R>
+__global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R>* FB, int PE, const double* X,
                                                 const double* Y, const double* Z, const R* Fmem,
                                                 const double* Fmorse, const R* Fbond, double* Ftot, int M,
                                                 const double* fX, const double* fY, const double* fZ,
                                                 const double* fF, double F0, Control* ctl) {
   if (ctl->done) return;
-  const int par = (int)(ctl->step & 1);
-  R4<R>* Fc = par ? FB : FA;
-  unsigned* fl = par ? flB : flA;
-  int* list = par ? lB : lA;
-  int* counter = &ctl->active_count[par];
+  R4<R>* Fc = (ctl->step & 1) ? FB : FA;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   double x, y, z, fx, fy, fz;
   if (idx < PE) {
@@ -116,58 +150,124 @@ __global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R
   } else {
     return;
   }
-  int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
-  R wx[5], wy[5], wz[5];
-  const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 1, nxa, rx, wx);
-  const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 1, nya, ry, wy);
-  const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 1, nza, rz, wz);
-  const R Fx = (R)fx, Fy = (R)fy, Fz = (R)fz;
-  const bool ref_nodes = sizeof(R) == 8;
-  if (ref_nodes) {
-    // the FP64 build's spreading and interpolation stencils can differ at the
-    // support edge (int*float vs int*double node coordinates): flag the bricks
-    // of every candidate node so the interpolation always finds fresh moments
-    const double inv = 1.0 / (double)lk.dxf;
-    const int bx = (int)floor(x * inv), by = (int)floor(y * inv), bz = (int)floor(z * inv);
-    for (int iz = bz - 2; iz <= bz + 2; ++iz) {
-      if (iz < 0 || iz >= lk.nz) continue;
-      for (int iy0 = by - 2; iy0 <= by + 2; ++iy0) {
-        int iy = iy0;
-        if (iy < 0 || iy >= lk.ny) {
-          if (!lk.ibm_wrap[1]) continue;
-          iy = wrapi(iy, lk.ny);
-        }
-        int last = -1;
-        for (int ix0 = bx - 2; ix0 <= bx + 2; ++ix0) {
-          int ix = ix0;
-          if (ix < 0 || ix >= lk.nx) {
-            if (!lk.ibm_wrap[0]) continue;
-            ix = wrapi(ix, lk.nx);
-          }
-          const int brick = ix / kBrickX + lk.nbx * (iy + lk.ny * iz);
-          if (brick == last) continue;
-          last = brick;
-          if (fl[brick] == 0u && atomicExch(fl + brick, 1u) == 0u) list[atomicAdd(counter, 1)] = brick;
-        }
-      }
-    }
+  spread_one<R>(lk, Fc, x, y, z, (R)fx, (R)fy, (R)fz);
+}
+
+// Force bricks of this step: every brick holding a lattice node within two
+// nodes (per axis) of a marker's base node -- floor(x/dx) as the FP64
+// stencils form it, floor(x * (1/dx)) as the FP32 stencil does -- which
+// contains every node the spreading and interpolation stencils of the
+// marker touch (base + {-2..2} in FP64, base + {-1..2} in FP32).  Set before
+// any force of the step exists, so the lattice pass over the other bricks
+// can run while the forces are computed.  One bit per node (a brick is one
+// 32-bit word): the position update sets each marker's bit for the next
+// step, the bits are dilated by kFlagR in x and y, then in z; a non-zero
+// word flags and lists its brick.
+constexpr int kFlagR = 2;
+
+// Sets the occupancy bit of a marker's base node; nodes outside the lattice
+// are wrapped on IBM-periodic axes, else clamped to the face (its kFlagR
+// neighbourhood still covers every in-range node the stencil can reach).
+__device__ __forceinline__ void mark_node(const LatticeConst& lk, unsigned* mark, double x, double y, double z,
+                                          bool fp64) {
+  const double dxd = (double)lk.dxf, inv = 1.0 / dxd;
+  auto node = [&](double v, int n, int wrap) {
+    const double f = floor(fp64 ? v / dxd : v * inv);
+    const int i = f < -1e9 ? -1000000000 : (f > 1e9 ? 1000000000 : (int)f);
+    if (wrap) return wrapi(i, n);
+    return i < 0 ? 0 : (i >= n ? n - 1 : i);
+  };
+  const int ix = node(x, lk.nx, lk.ibm_wrap[0]);
+  const int iy = node(y, lk.ny, lk.ibm_wrap[1]);
+  const int iz = node(z, lk.nz, 0);
+  atomicOr(mark + (ix >> 5) + lk.nbx * (iy + lk.ny * iz), 1u << (ix & 31));
+}
+
+// occupancy of the initial positions (afterwards the position update marks
+// the positions of the next step)
+__global__ void __launch_bounds__(128) mark_markers_k(LatticeConst lk, unsigned* mark, int PE, const double* X,
+                                                      const double* Y, const double* Z, int M, const double* fX,
+                                                      const double* fY, const double* fZ, bool fp64) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < PE) mark_node(lk, mark, X[idx], Y[idx], Z[idx], fp64);
+  else if (idx < PE + M) mark_node(lk, mark, fX[idx - PE], fY[idx - PE], fZ[idx - PE], fp64);
+}
+
+// word bx of a row dilated by kFlagR bits in x (periodic rows: the
+// neighbour words across the row's ends; when nx is not a multiple of 32, a
+// word next to occupied bits across the wrap is taken as all set, a superset)
+__device__ __forceinline__ unsigned dilate_x(const unsigned* row, int bx, int nbx, bool wrap, bool partial) {
+  const unsigned C = row[bx];
+  unsigned Lw = 0, Rw = 0;
+  if (bx > 0) Lw = row[bx - 1];
+  else if (wrap) Lw = row[nbx - 1];
+  if (bx < nbx - 1) Rw = row[bx + 1];
+  else if (wrap) Rw = row[0];
+  // a partial last word is not bit-adjacent to word 0 across the wrap
+  if (partial && wrap && ((bx == 0 && Lw) || (bx == nbx - 1 && Rw))) return 0xffffffffu;
+  if (!(C | Lw | Rw)) return 0u;
+  const unsigned long long lo = ((unsigned long long)C << 32) | Lw;  // C above its left neighbour
+  const unsigned long long hi = ((unsigned long long)Rw << 32) | C;  // C below its right neighbour
+  unsigned long long dl = lo, dh = hi;
+#pragma unroll
+  for (int r = 1; r <= kFlagR; ++r) {
+    dl |= lo << r;
+    dh |= hi >> r;
   }
-  for (int c = 0; c < czn; ++c)
-    for (int b = 0; b < cyn; ++b) {
-      int last_brick = -1;
-      for (int a = 0; a < cxn; ++a) {
-        if (!ref_nodes) {
-          const int brick = nxa[a] / kBrickX + lk.nbx * (nya[b] + lk.ny * nza[c]);
-          if (brick != last_brick) {
-            last_brick = brick;
-            if (fl[brick] == 0u && atomicExch(fl + brick, 1u) == 0u) list[atomicAdd(counter, 1)] = brick;
-          }
-        }
-        const R delta = wx[a] * wy[b] * wz[c];
-        const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
-        atomic_add3(Fc, n, Fx * delta, Fy * delta, Fz * delta);
-      }
+  return (unsigned)(dl >> 32) | (unsigned)dh;
+}
+
+__global__ void __launch_bounds__(256) dilate_xy_k(LatticeConst lk, const unsigned* mark, unsigned* dil,
+                                                   const Control* ctl) {
+  if (ctl->done) return;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= lk.nbricks) return;
+  const int bx = w % lk.nbx, y = (w / lk.nbx) % lk.ny, z = w / (lk.nbx * lk.ny);
+  const bool wrap = lk.ibm_wrap[0] != 0, partial = (lk.nx & 31) != 0;
+  unsigned acc = 0;
+  for (int dy = -kFlagR; dy <= kFlagR; ++dy) {
+    int yy = y + dy;
+    if (yy < 0 || yy >= lk.ny) {
+      if (!lk.ibm_wrap[1]) continue;
+      yy = wrapi(yy, lk.ny);
     }
+    acc |= dilate_x(mark + (size_t)lk.nbx * (yy + lk.ny * z), bx, lk.nbx, wrap, partial);
+  }
+  dil[w] = acc;
+}
+
+// dilates in z, flags and lists the bricks (list[par], active_count[par]),
+// and clears the occupancy bits for the next step
+__global__ void __launch_bounds__(256) flag_bricks_k(LatticeConst lk, const unsigned* dil, unsigned* mark,
+                                                     unsigned* flA, unsigned* flB, int* lA, int* lB, Control* ctl) {
+  if (ctl->done) return;
+  const int par = (int)(ctl->step & 1);
+  unsigned* fl = par ? flB : flA;
+  int* list = par ? lB : lA;
+  const int lane = threadIdx.x & 31;
+  const int plane = lk.nbx * lk.ny;
+  for (int w0 = blockIdx.x * blockDim.x; w0 < lk.nbricks; w0 += gridDim.x * blockDim.x) {
+    const int w = w0 + threadIdx.x;
+    bool f = false;
+    if (w < lk.nbricks) {
+      const int z = w / plane;
+      unsigned acc = 0;
+      for (int dz = -kFlagR; dz <= kFlagR; ++dz) {
+        const int zz = z + dz;
+        if (zz < 0 || zz >= lk.nz) continue;
+        acc |= dil[w + dz * plane];
+      }
+      f = acc != 0u;
+      if (f) fl[w] = 1u;
+      mark[w] = 0u;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    if (!bal) continue;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctl->active_count[par], __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (f) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
+  }
 }
 
 // ------------------------------------------------------- interp + advance
@@ -205,66 +305,57 @@ __device__ __forceinline__ void bin_put(const PlateletConst& k, double x, double
   else atomicOr(&ctl->err, ERR_BIN_OVERFLOW);
 }
 
-template <class R>
-__global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, PlateletConst pk, const R4<R>* ubuf,
-                                                        int PE, double* X, double* Y, double* RY, double* Z,
-                                                        double* V, int M, double* fX, double* fY, double* fZ,
-                                                        double* fV, const int* ffix, int* bin_count, float4* bin,
-                                                        Control* ctl, unsigned* done_blocks, double detach_rate,
-                                                        uint64_t seed) {
-  if (ctl->done) return;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx < PE + M) {
-    const bool el = idx < PE;
+// Position update of marker idx (element idx < PE, else fibrin node idx-PE)
+// with its interpolated lattice velocity (lattice units): velocity store,
+// move (fixed fibrin nodes stay), periodic wrap, Morse binning, occupancy
+// bit of the next step.
+__device__ __forceinline__ void advance_marker(const LatticeConst& lk, const PlateletConst& pk, int idx, int PE,
+                                               double x, double y, double z, double ax, double ay, double az,
+                                               double* X, double* Y, double* RY, double* Z, double* V, int M,
+                                               double* fX, double* fY, double* fZ, double* fV, const int* ffix,
+                                               int* bin_count, float4* bin, unsigned* mark, Control* ctl,
+                                               bool fp64) {
+  const double vx = ax * lk.C, vy = ay * lk.C, vz = az * lk.C;
+  const float dtT = lk.dtT;
+  const double Lx = (double)lk.nx * (double)lk.dxf, Ly = (double)lk.ny * (double)lk.dxf;
+  if (idx < PE) {
+    V[idx] = vx; V[PE + idx] = vy; V[2 * PE + idx] = vz;
+    x += vx * dtT;
+    if (lk.ibm_wrap[0]) { if (x > Lx) x -= Lx; else if (x < 0) x += Lx; }
+    y += vy * dtT;
+    if (lk.ibm_wrap[1]) { if (y > Ly) y -= Ly; else if (y < 0) y += Ly; }
+    RY[idx] += vy * dtT;
+    z += vz * dtT;
+    X[idx] = x; Y[idx] = y; Z[idx] = z;
+    if (bin) bin_put(pk, x, y, z, idx, bin_count, bin, ctl);
+  } else {
     const int m = idx - PE;
-    double x = el ? X[idx] : fX[m], y = el ? Y[idx] : fY[m], z = el ? Z[idx] : fZ[m];
-    int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
-    R wx[5], wy[5], wz[5];
-    const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 0, nxa, rx, wx);
-    const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 0, nya, ry, wy);
-    const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 0, nza, rz, wz);
-    R ax = 0, ay = 0, az = 0;
-    for (int c = 0; c < czn; ++c)
-      for (int b = 0; b < cyn; ++b)
-        for (int a = 0; a < cxn; ++a) {
-          const R delta = wx[a] * wy[b] * wz[c];
-          const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
-          const R4<R> u = ubuf[n];
-          ax += u.y * delta; ay += u.z * delta; az += u.w * delta;
-        }
-    const double vx = (double)ax * lk.C, vy = (double)ay * lk.C, vz = (double)az * lk.C;
-    const float dtT = lk.dtT;
-    const double Lx = (double)lk.nx * (double)lk.dxf, Ly = (double)lk.ny * (double)lk.dxf;
-    if (el) {
-      V[idx] = vx; V[PE + idx] = vy; V[2 * PE + idx] = vz;
+    fV[m] = vx; fV[M + m] = vy; fV[2 * M + m] = vz;
+    if (!ffix[m]) {
       x += vx * dtT;
       if (lk.ibm_wrap[0]) { if (x > Lx) x -= Lx; else if (x < 0) x += Lx; }
       y += vy * dtT;
       if (lk.ibm_wrap[1]) { if (y > Ly) y -= Ly; else if (y < 0) y += Ly; }
-      RY[idx] += vy * dtT;
       z += vz * dtT;
-      X[idx] = x; Y[idx] = y; Z[idx] = z;
-      if (bin) bin_put(pk, x, y, z, idx, bin_count, bin, ctl);
-    } else {
-      fV[m] = vx; fV[M + m] = vy; fV[2 * M + m] = vz;
-      if (!ffix[m]) {
-        x += vx * dtT;
-        if (lk.ibm_wrap[0]) { if (x > Lx) x -= Lx; else if (x < 0) x += Lx; }
-        y += vy * dtT;
-        if (lk.ibm_wrap[1]) { if (y > Ly) y -= Ly; else if (y < 0) y += Ly; }
-        z += vz * dtT;
-        fX[m] = x; fY[m] = y; fZ[m] = z;
-      }
+      fX[m] = x; fY[m] = y; fZ[m] = z;
     }
   }
-  // the last block to finish closes the step: counter, first flag, and the
-  // detach test of the next step (semLB.cu:451-455)
+  mark_node(lk, mark, x, y, z, fp64);
+}
+
+// The last block to finish closes the step: counter, first flag, the other
+// force buffer's list, and the detach test of the next step
+// (semLB.cu:451-455).
+__device__ __forceinline__ void close_step(const PlateletConst& pk, Control* ctl, unsigned* done_blocks,
+                                           double detach_rate, uint64_t seed) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned prev = atomicAdd(done_blocks, 1u);
     if (prev == gridDim.x - 1) {
       __threadfence();
+      // the next step flags into the other force buffer: empty its list
+      ctl->active_count[(int)(ctl->step & 1) ^ 1] = 0;
       const long long s = ctl->step + 1;
       ctl->step = s;
       ctl->first = 0;
@@ -275,6 +366,352 @@ __global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, Platele
       *done_blocks = 0u;
     }
   }
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, PlateletConst pk, const R4<R>* ubuf,
+                                                        int PE, double* X, double* Y, double* RY, double* Z,
+                                                        double* V, int M, double* fX, double* fY, double* fZ,
+                                                        double* fV, const int* ffix, int* bin_count, float4* bin,
+                                                        unsigned* mark, Control* ctl, unsigned* done_blocks,
+                                                        double detach_rate, uint64_t seed) {
+  if (ctl->done) return;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < PE + M) {
+    const bool el = idx < PE;
+    const int m = idx - PE;
+    const double x = el ? X[idx] : fX[m], y = el ? Y[idx] : fY[m], z = el ? Z[idx] : fZ[m];
+    R ax, ay, az;
+    interp_one<R>(lk, ubuf, x, y, z, ax, ay, az);
+    advance_marker(lk, pk, idx, PE, x, y, z, (double)ax, (double)ay, (double)az, X, Y, RY, Z, V, M, fX, fY, fZ,
+                   fV, ffix, bin_count, bin, mark, ctl, sizeof(R) == 8);
+  }
+  close_step(pk, ctl, done_blocks, detach_rate, seed);
+}
+
+// ------------------------------------------------------ platelet boxes (FP32)
+// FP32 spreading and interpolation of platelet elements through a per-platelet
+// box of lattice nodes in shared memory: one CTA per platelet; the box spans
+// the FP32 stencils (base node + {-1..2} per axis) of all its elements, node
+// indices taken relative to the first element's base node (minimum image on
+// periodic axes).  Weights and nodes are those of the per-marker kernels;
+// only the order of the float sums differs.  A platelet whose box exceeds
+// kBoxCap nodes, and every fibrin node, takes the per-marker path.
+constexpr int kBoxThreads = 512;
+constexpr int kBoxCap = 8192;    // nodes of a platelet box
+constexpr int kBoxElems = 1024;  // elements of a platelet staged in shared memory
+constexpr int kBoxFibrin = 128;  // fibrin nodes per CTA of the box kernels
+
+struct BoxAxis {
+  int base;  // node floor(x / dx)
+  float fr;  // x / dx - base
+};
+__device__ __forceinline__ BoxAxis box_axis(double x, double inv) {
+  const double r = x * inv;
+  const double fb = floor(r);
+  return BoxAxis{(int)fb, (float)(r - fb)};
+}
+// weight of stencil offset o (the FP32 stencil's rule); false outside the
+// support
+__device__ __forceinline__ bool box_weight(float fr, int o, float& w) {
+  const float dd = fr - (float)o;
+  if (!(fabsf(dd) < 2.f)) return false;
+  w = 0.25f * (1.f + cospif(0.5f * dd));
+  return true;
+}
+
+// Box geometry of a platelet from its elements' base nodes SB[axis][0..E)
+// (stride kBoxElems); returns false (box too large, or non-finite
+// positions) for the per-marker path.  i0: first element's base node;
+// lo/ext: box origin (relative to i0) and extent per axis.
+__device__ bool platelet_box(const LatticeConst& lk, const int* SB, int E, int i0[3], int lo[3], int ext[3]) {
+  __shared__ int s_min[3], s_max[3];
+  const int n3[3] = {lk.nx, lk.ny, lk.nz};
+  const int wrap3[3] = {lk.ibm_wrap[0], lk.ibm_wrap[1], 0};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) i0[a] = SB[a * kBoxElems];
+  if (threadIdx.x < 3) { s_min[threadIdx.x] = 0x7fffffff; s_max[threadIdx.x] = -0x7fffffff; }
+  __syncthreads();
+  int mn[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, mx[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      int d = SB[a * kBoxElems + e] - i0[a];
+      if (wrap3[a]) d = wrapi(d + n3[a] / 2, n3[a]) - n3[a] / 2;
+      mn[a] = min(mn[a], d);
+      mx[a] = max(mx[a], d);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    atomicMin(&s_min[a], mn[a]);
+    atomicMax(&s_max[a], mx[a]);
+  }
+  __syncthreads();
+  long long vol = 1;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const long long e = (long long)s_max[a] - (long long)s_min[a] + 4;
+    if (e <= 0 || e > kBoxCap) return false;  // also non-finite positions
+    lo[a] = s_min[a] - 1;
+    ext[a] = (int)e;
+    vol *= e;
+  }
+  return vol <= kBoxCap;
+}
+
+// Stages element e's base node and fraction per axis (FP64 to lattice
+// units once per element; the warp loops then use only these).
+__device__ __forceinline__ void stage_element(int* SB, float* SF, int e, double x, double y, double z, double inv) {
+  const double p3[3] = {x, y, z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const BoxAxis ba = box_axis(p3[a], inv);
+    SB[a * kBoxElems + e] = ba.base;
+    SF[a * kBoxElems + e] = ba.fr;
+  }
+}
+
+// global node of box offset d (relative to i0) on one axis; -1 if outside a
+// non-periodic lattice
+__device__ __forceinline__ int box_global(int i0, int d, int n, int wrap) {
+  const int g = i0 + d;
+  if (g >= 0 && g < n) return g;
+  return wrap ? wrapi(g, n) : -1;
+}
+
+// Shared-memory layout of the box kernels: the node box [3][kBoxCap] floats,
+// then per element (stride kBoxElems) its position (3 doubles), base node
+// (3 ints), fraction (3 floats) and a float3 (force or velocity).
+constexpr size_t kBoxSmem =
+    3 * kBoxCap * sizeof(float) + (size_t)kBoxElems * (3 * sizeof(double) + 3 * sizeof(int) + 6 * sizeof(float));
+
+__global__ void __launch_bounds__(kBoxThreads) spread_box_k(LatticeConst lk, float4* FA, float4* FB, int P, int E,
+                                                            const double* X, const double* Y, const double* Z,
+                                                            const float* Fmem, const double* Fmorse,
+                                                            const float* Fbond, double* Ftot, int M,
+                                                            const double* fX, const double* fY, const double* fZ,
+                                                            const double* fF, double F0, Control* ctl) {
+  if (ctl->done) return;
+  float4* Fc = (ctl->step & 1) ? FB : FA;
+  const int PE = P * E;
+  if ((int)blockIdx.x >= P) {
+    // fibrin nodes: per-marker atomics, kBoxFibrin per CTA (spread over SMs)
+    const int m = ((int)blockIdx.x - P) * kBoxFibrin + threadIdx.x;
+    if (threadIdx.x < kBoxFibrin && m < M)
+      spread_one<float>(lk, Fc, fX[m], fY[m], fZ[m], (float)(fF[m] / F0), (float)(fF[M + m] / F0),
+                        (float)(fF[2 * M + m] / F0));
+    return;
+  }
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  float* s_box = reinterpret_cast<float*>(s_raw);
+  double* s_pos = reinterpret_cast<double*>(s_box + 3 * kBoxCap);  // [3][kBoxElems]
+  float* s_f = reinterpret_cast<float*>(s_pos + 3 * kBoxElems);     // [3][kBoxElems]
+  int* s_b = reinterpret_cast<int*>(s_f + 3 * kBoxElems);           // [3][kBoxElems] base nodes
+  float* s_fr = reinterpret_cast<float*>(s_b + 3 * kBoxElems);      // [3][kBoxElems] fractions
+  const int p = blockIdx.x, base = p * E;
+  const bool staged = E <= kBoxElems;
+  const double inv = 1.0 / (double)lk.dxf;
+  // element forces (kept for the element output) and positions, thread per
+  // element
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    const int g = base + e;
+    double fx = (double)Fmem[g], fy = (double)Fmem[PE + g], fz = (double)Fmem[2 * PE + g];
+    if (Fmorse) { fx += Fmorse[g]; fy += Fmorse[PE + g]; fz += Fmorse[2 * PE + g]; }
+    if (Fbond) { fx += (double)Fbond[g]; fy += (double)Fbond[PE + g]; fz += (double)Fbond[2 * PE + g]; }
+    Ftot[g] = fx; Ftot[PE + g] = fy; Ftot[2 * PE + g] = fz;
+    if (staged) {
+      const double x = X[g], y = Y[g], z = Z[g];
+      s_pos[e] = x; s_pos[kBoxElems + e] = y; s_pos[2 * kBoxElems + e] = z;
+      stage_element(s_b, s_fr, e, x, y, z, inv);
+      s_f[e] = (float)fx; s_f[kBoxElems + e] = (float)fy; s_f[2 * kBoxElems + e] = (float)fz;
+    } else {
+      spread_one<float>(lk, Fc, X[g], Y[g], Z[g], (float)fx, (float)fy, (float)fz);
+    }
+  }
+  if (!staged) return;
+  __syncthreads();
+  int i0[3], lo[3], ext[3];
+  if (!platelet_box(lk, s_b, E, i0, lo, ext)) {
+    for (int e = threadIdx.x; e < E; e += blockDim.x)
+      spread_one<float>(lk, Fc, s_pos[e], s_pos[kBoxElems + e], s_pos[2 * kBoxElems + e], s_f[e],
+                        s_f[kBoxElems + e], s_f[2 * kBoxElems + e]);
+    return;
+  }
+  const int vol = ext[0] * ext[1] * ext[2];
+  for (int i = threadIdx.x; i < vol; i += blockDim.x) {
+    s_box[i] = 0.f;
+    s_box[kBoxCap + i] = 0.f;
+    s_box[2 * kBoxCap + i] = 0.f;
+  }
+  __syncthreads();
+  const int n3[3] = {lk.nx, lk.ny, lk.nz};
+  const int wrap3[3] = {lk.ibm_wrap[0], lk.ibm_wrap[1], 0};
+  // one warp per element, one lane per pair of its 4x4x4 stencil nodes
+  // (x offset lane&3, y offset (lane>>2)&3, z offsets lane>>4 and +2): the
+  // 64 shared-memory atomics of an element go to distinct nodes
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int oa = (lane & 3) - 1, ob = ((lane >> 2) & 3) - 1, oc = (lane >> 4) - 1;
+  for (int e = warp; e < E; e += nwarps) {
+    int dd[3];
+    float fr[3];
+#pragma unroll
+    for (int ax3 = 0; ax3 < 3; ++ax3) {
+      int d = s_b[ax3 * kBoxElems + e] - i0[ax3];
+      if (wrap3[ax3]) d = wrapi(d + n3[ax3] / 2, n3[ax3]) - n3[ax3] / 2;
+      dd[ax3] = d;
+      fr[ax3] = s_fr[ax3 * kBoxElems + e];
+    }
+    float wx, wy;
+    const bool okx = box_weight(fr[0], oa, wx) && box_global(i0[0], dd[0] + oa, n3[0], wrap3[0]) >= 0;
+    const bool oky = box_weight(fr[1], ob, wy) && box_global(i0[1], dd[1] + ob, n3[1], wrap3[1]) >= 0;
+    if (!(okx && oky)) continue;
+    const float wxy = wx * wy;
+    const float Fx = s_f[e], Fy = s_f[kBoxElems + e], Fz = s_f[2 * kBoxElems + e];
+#pragma unroll
+    for (int k2 = 0; k2 < 2; ++k2) {
+      const int o = oc + 2 * k2;
+      float wz;
+      if (!(box_weight(fr[2], o, wz) && box_global(i0[2], dd[2] + o, n3[2], 0) >= 0)) continue;
+      const float delta = wxy * wz;
+      const int i = (dd[0] + oa - lo[0]) + ext[0] * ((dd[1] + ob - lo[1]) + ext[1] * (dd[2] + o - lo[2]));
+      atomicAdd(&s_box[i], Fx * delta);
+      atomicAdd(&s_box[kBoxCap + i], Fy * delta);
+      atomicAdd(&s_box[2 * kBoxCap + i], Fz * delta);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < vol; i += blockDim.x) {
+    const float vx = s_box[i], vy = s_box[kBoxCap + i], vz = s_box[2 * kBoxCap + i];
+    if (vx == 0.f && vy == 0.f && vz == 0.f) continue;
+    const int ax = i % ext[0], ay = (i / ext[0]) % ext[1], az = i / (ext[0] * ext[1]);
+    const int gx = box_global(i0[0], lo[0] + ax, lk.nx, lk.ibm_wrap[0]);
+    const int gy = box_global(i0[1], lo[1] + ay, lk.ny, lk.ibm_wrap[1]);
+    const int gz = box_global(i0[2], lo[2] + az, lk.nz, 0);
+    if (gx < 0 || gy < 0 || gz < 0) continue;
+    atomicAdd(Fc + (size_t)gx + (size_t)lk.nx * ((size_t)gy + (size_t)lk.ny * gz), make_float4(vx, vy, vz, 0.f));
+  }
+}
+
+__global__ void __launch_bounds__(kBoxThreads) interp_box_k(LatticeConst lk, PlateletConst pk, const float4* ubuf,
+                                                            int P, int E, double* X, double* Y, double* RY,
+                                                            double* Z, double* V, int M, double* fX, double* fY,
+                                                            double* fZ, double* fV, const int* ffix, int* bin_count,
+                                                            float4* bin, unsigned* mark, Control* ctl,
+                                                            unsigned* done_blocks, double detach_rate,
+                                                            uint64_t seed) {
+  if (ctl->done) return;
+  const int PE = P * E;
+  if ((int)blockIdx.x >= P) {
+    const int m = ((int)blockIdx.x - P) * kBoxFibrin + threadIdx.x;
+    if (threadIdx.x < kBoxFibrin && m < M) {
+      const double x = fX[m], y = fY[m], z = fZ[m];
+      float ax, ay, az;
+      interp_one<float>(lk, ubuf, x, y, z, ax, ay, az);
+      advance_marker(lk, pk, PE + m, PE, x, y, z, (double)ax, (double)ay, (double)az, X, Y, RY, Z, V, M, fX, fY,
+                     fZ, fV, ffix, bin_count, bin, mark, ctl, false);
+    }
+    close_step(pk, ctl, done_blocks, detach_rate, seed);
+    return;
+  }
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  float* s_box = reinterpret_cast<float*>(s_raw);                   // lattice velocity of the box nodes
+  double* s_pos = reinterpret_cast<double*>(s_box + 3 * kBoxCap);  // [3][kBoxElems]
+  float* s_v = reinterpret_cast<float*>(s_pos + 3 * kBoxElems);     // [3][kBoxElems] interpolated velocity
+  int* s_b = reinterpret_cast<int*>(s_v + 3 * kBoxElems);           // [3][kBoxElems] base nodes
+  float* s_fr = reinterpret_cast<float*>(s_b + 3 * kBoxElems);      // [3][kBoxElems] fractions
+  const int p = blockIdx.x, base = p * E;
+  const bool staged = E <= kBoxElems;
+  const double inv = 1.0 / (double)lk.dxf;
+  if (!staged) {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const int g = base + e;
+      const double x = X[g], y = Y[g], z = Z[g];
+      float ax, ay, az;
+      interp_one<float>(lk, ubuf, x, y, z, ax, ay, az);
+      advance_marker(lk, pk, g, PE, x, y, z, (double)ax, (double)ay, (double)az, X, Y, RY, Z, V, M, fX, fY, fZ,
+                     fV, ffix, bin_count, bin, mark, ctl, false);
+    }
+    close_step(pk, ctl, done_blocks, detach_rate, seed);
+    return;
+  }
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    const double x = X[base + e], y = Y[base + e], z = Z[base + e];
+    s_pos[e] = x;
+    s_pos[kBoxElems + e] = y;
+    s_pos[2 * kBoxElems + e] = z;
+    stage_element(s_b, s_fr, e, x, y, z, inv);
+  }
+  __syncthreads();
+  int i0[3], lo[3], ext[3];
+  const bool boxed = platelet_box(lk, s_b, E, i0, lo, ext);
+  if (boxed) {
+    const int vol = ext[0] * ext[1] * ext[2];
+    for (int i = threadIdx.x; i < vol; i += blockDim.x) {
+      const int ax = i % ext[0], ay = (i / ext[0]) % ext[1], az = i / (ext[0] * ext[1]);
+      const int gx = box_global(i0[0], lo[0] + ax, lk.nx, lk.ibm_wrap[0]);
+      const int gy = box_global(i0[1], lo[1] + ay, lk.ny, lk.ibm_wrap[1]);
+      const int gz = box_global(i0[2], lo[2] + az, lk.nz, 0);
+      float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx >= 0 && gy >= 0 && gz >= 0) u = ubuf[(size_t)gx + (size_t)lk.nx * ((size_t)gy + (size_t)lk.ny * gz)];
+      s_box[i] = u.y; s_box[kBoxCap + i] = u.z; s_box[2 * kBoxCap + i] = u.w;
+    }
+    __syncthreads();
+    const int n3[3] = {lk.nx, lk.ny, lk.nz};
+    const int wrap3[3] = {lk.ibm_wrap[0], lk.ibm_wrap[1], 0};
+    // one warp per element, one lane per pair of its stencil nodes
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int oa = (lane & 3) - 1, ob = ((lane >> 2) & 3) - 1, oc = (lane >> 4) - 1;
+    for (int e = warp; e < E; e += nwarps) {
+      int dd[3];
+      float fr[3];
+#pragma unroll
+      for (int ax3 = 0; ax3 < 3; ++ax3) {
+        int d = s_b[ax3 * kBoxElems + e] - i0[ax3];
+        if (wrap3[ax3]) d = wrapi(d + n3[ax3] / 2, n3[ax3]) - n3[ax3] / 2;
+        dd[ax3] = d;
+        fr[ax3] = s_fr[ax3 * kBoxElems + e];
+      }
+      float ax = 0.f, ay = 0.f, az = 0.f;
+      float wx, wy;
+      const bool okx = box_weight(fr[0], oa, wx) && box_global(i0[0], dd[0] + oa, n3[0], wrap3[0]) >= 0;
+      const bool oky = box_weight(fr[1], ob, wy) && box_global(i0[1], dd[1] + ob, n3[1], wrap3[1]) >= 0;
+      if (okx && oky) {
+        const float wxy = wx * wy;
+#pragma unroll
+        for (int k2 = 0; k2 < 2; ++k2) {
+          const int o = oc + 2 * k2;
+          float wz;
+          if (!(box_weight(fr[2], o, wz) && box_global(i0[2], dd[2] + o, n3[2], 0) >= 0)) continue;
+          const float delta = wxy * wz;
+          const int i = (dd[0] + oa - lo[0]) + ext[0] * ((dd[1] + ob - lo[1]) + ext[1] * (dd[2] + o - lo[2]));
+          ax += s_box[i] * delta;
+          ay += s_box[kBoxCap + i] * delta;
+          az += s_box[2 * kBoxCap + i] * delta;
+        }
+      }
+#pragma unroll
+      for (int sh = 16; sh > 0; sh >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, sh);
+        ay += __shfl_xor_sync(0xffffffffu, ay, sh);
+        az += __shfl_xor_sync(0xffffffffu, az, sh);
+      }
+      if (lane == 0) { s_v[e] = ax; s_v[kBoxElems + e] = ay; s_v[2 * kBoxElems + e] = az; }
+    }
+  } else {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      float ax, ay, az;
+      interp_one<float>(lk, ubuf, s_pos[e], s_pos[kBoxElems + e], s_pos[2 * kBoxElems + e], ax, ay, az);
+      s_v[e] = ax; s_v[kBoxElems + e] = ay; s_v[2 * kBoxElems + e] = az;
+    }
+  }
+  __syncthreads();
+  // thread per element: move it
+  for (int e = threadIdx.x; e < E; e += blockDim.x)
+    advance_marker(lk, pk, base + e, PE, s_pos[e], s_pos[kBoxElems + e], s_pos[2 * kBoxElems + e], (double)s_v[e],
+                   (double)s_v[kBoxElems + e], (double)s_v[2 * kBoxElems + e], X, Y, RY, Z, V, M, fX, fY, fZ, fV,
+                   ffix, bin_count, bin, mark, ctl, false);
+  close_step(pk, ctl, done_blocks, detach_rate, seed);
 }
 
 __global__ void bin_elements_k(PlateletConst pk, int PE, const double* X, const double* Y, const double* Z,
@@ -1397,20 +1834,56 @@ cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
   if (PE + M == 0) return cudaSuccess;
   const unsigned grid = (PE + M + 127) / 128;
   const double F0 = Pl ? (double)Pl->k.f0 : 1.0;
-  if (L.precision == PF_PREC_FP64)
+  if (L.precision != PF_PREC_FP64 && !L.ibm_box)
+    spread_k<float><<<grid, 128, 0, st>>>(
+        L.k, (float4*)L.F[0], (float4*)L.F[1], PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr,
+        Pl ? Pl->Z : nullptr, Pl ? (float*)Pl->Fmem : nullptr, (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr,
+        (Pl && Pl->k.nrec) ? (float*)Pl->Fbond : nullptr, Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr,
+        Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr, Fb ? Fb->F : nullptr, F0, ctl);
+  else if (L.precision == PF_PREC_FP64)
     spread_k<double><<<grid, 128, 0, st>>>(
-        L.k, (D4*)L.F[0], (D4*)L.F[1], L.flags[0], L.flags[1], L.list[0], L.list[1], PE, Pl ? Pl->X : nullptr,
+        L.k, (D4*)L.F[0], (D4*)L.F[1], PE, Pl ? Pl->X : nullptr,
         Pl ? Pl->Y : nullptr, Pl ? Pl->Z : nullptr, Pl ? (double*)Pl->Fmem : nullptr,
         (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr, (Pl && Pl->k.nrec) ? (double*)Pl->Fbond : nullptr,
         Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr,
         Fb ? Fb->F : nullptr, F0, ctl);
-  else
-    spread_k<float><<<grid, 128, 0, st>>>(
-        L.k, (float4*)L.F[0], (float4*)L.F[1], L.flags[0], L.flags[1], L.list[0], L.list[1], PE,
-        Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->Z : nullptr, Pl ? (float*)Pl->Fmem : nullptr,
-        (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr, (Pl && Pl->k.nrec) ? (float*)Pl->Fbond : nullptr,
-        Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr,
-        Fb ? Fb->F : nullptr, F0, ctl);
+  else {
+    // FP32: one CTA per platelet box, then the fibrin nodes
+    cudaFuncSetAttribute(spread_box_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBoxSmem);
+    const int P = Pl ? Pl->k.P : 0, E = Pl ? Pl->k.E : 0;
+    const unsigned g2 = (unsigned)(P + (M + kBoxFibrin - 1) / kBoxFibrin);
+    spread_box_k<<<g2, kBoxThreads, (int)kBoxSmem, st>>>(
+        L.k, (float4*)L.F[0], (float4*)L.F[1], P, E, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr,
+        Pl ? Pl->Z : nullptr, Pl ? (float*)Pl->Fmem : nullptr, (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr,
+        (Pl && Pl->k.nrec) ? (float*)Pl->Fbond : nullptr, Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr,
+        Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr, Fb ? Fb->F : nullptr, F0, ctl);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t mark_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, cudaStream_t st) {
+  const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
+  const int M = Fb ? Fb->M : 0;
+  if (PE + M == 0) return cudaSuccess;
+  mark_markers_k<<<(PE + M + 127) / 128, 128, 0, st>>>(L.k, L.mark, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr,
+                                                       Pl ? Pl->Z : nullptr, M, Fb ? Fb->X : nullptr,
+                                                       Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr,
+                                                       L.precision == PF_PREC_FP64);
+  return cudaGetLastError();
+}
+
+cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st) {
+  const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
+  const int M = Fb ? Fb->M : 0;
+  if (PE + M == 0) return cudaSuccess;
+  const int nb = L.k.nbricks;
+  dilate_xy_k<<<(nb + 255) / 256, 256, 0, st>>>(L.k, L.mark, L.dil, ctl);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = (nb + 255) / 256;
+  if (grid > 8 * sms) grid = 8 * sms;
+  flag_bricks_k<<<grid, 256, 0, st>>>(L.k, L.dil, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1], ctl);
   return cudaGetLastError();
 }
 
@@ -1429,14 +1902,24 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
     interp_advance_k<double><<<grid, 128, 0, st>>>(
         L.k, pk, (const D4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
-        Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, ctl, done_blocks,
+        Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
         detach_rate, seed);
-  else
+  else if (PE + M == 0 || !L.ibm_box)
     interp_advance_k<float><<<grid, 128, 0, st>>>(
         L.k, pk, (const float4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
-        Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, ctl, done_blocks,
+        Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
         detach_rate, seed);
+  else {
+    cudaFuncSetAttribute(interp_box_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBoxSmem);
+    const int P = Pl ? Pl->k.P : 0, E = Pl ? Pl->k.E : 0;
+    const unsigned g2 = (unsigned)(P + (M + kBoxFibrin - 1) / kBoxFibrin);
+    interp_box_k<<<g2, kBoxThreads, (int)kBoxSmem, st>>>(
+        L.k, pk, (const float4*)L.ubuf, P, E, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
+        Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
+        Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
+        detach_rate, seed);
+  }
   return cudaGetLastError();
 }
 

@@ -53,6 +53,7 @@ def lib():
         L.pfgpu_job_lbm_kernel.argtypes = [vp]
         L.pfgpu_job_profile.argtypes = [vp, C.c_int, dp]
         L.pfgpu_job_get_cells.argtypes = [vp, ip, ip, ip, ip]
+        L.pfgpu_profile_phase_count.restype = C.c_int
         L.pfgpu_profile_phase_name.restype = C.c_char_p
         L.pfgpu_profile_phase_name.argtypes = [C.c_int]
         L.pfgpu_scene_device_bytes.restype = C.c_size_t
@@ -108,9 +109,10 @@ class Job:
 
     def profile(self, n: int) -> dict:
         """Per-phase device time (ms, summed over n serialised steps)."""
-        out = np.zeros(8)
+        k = lib().pfgpu_profile_phase_count()
+        out = np.zeros(k)
         check(lib().pfgpu_job_profile(self.h, int(n), _p(out)), allow_done=True)
-        return {lib().pfgpu_profile_phase_name(i).decode(): float(out[i]) for i in range(8)}
+        return {lib().pfgpu_profile_phase_name(i).decode(): float(out[i]) for i in range(k)}
 
     @property
     def steps(self) -> int:

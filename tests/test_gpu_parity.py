@@ -190,6 +190,34 @@ def test_row_staged_and_direct_lbm_kernels_agree(gpu, scene, prec, tol, monkeypa
     b.close()
 
 
+@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-4)], ids=["fp32", "fp16"])
+def test_platelet_box_ibm_matches_per_marker(gpu, prec, tol, monkeypatch):
+    """Reduced precision spreads and interpolates platelet elements through a
+    shared-memory node box per platelet; the per-marker kernels use the same
+    nodes and weights, so only the order of float sums differs (in FP16 a
+    last-bit difference can move a population by one step of the store)."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small()
+    monkeypatch.setenv("PFGPU_IBM", "boxes")
+    a = gpu.Job(sc, prec)
+    monkeypatch.delenv("PFGPU_IBM")
+    b = gpu.Job(sc, prec)
+    # five steps: the scene's Morse and bond dynamics amplify last-bit
+    # differences over longer runs
+    a.step(5)
+    b.step(5)
+    La, Lb = a.lattice(), b.lattice()
+    assert rel_l2(La["u"], Lb["u"]) < tol
+    assert rel_l2(La["F"], Lb["F"]) < 10 * tol
+    Ea, Eb = a.elements(), b.elements()
+    for k in ("X", "Y", "Z"):
+        assert np.abs(Ea[k] - Eb[k]).max() < 1e-3 * tol
+    assert rel_l2(Ea["V"], Eb["V"]) < 10 * tol
+    np.testing.assert_array_equal(a.bonds()["rec_state"], b.bonds()["rec_state"])
+    a.close()
+    b.close()
+
+
 def test_row_staged_fp64_vs_oracle(gpu, monkeypatch):
     """FP64 row-staged kernel against the oracle on the bounce-back box."""
     sc = _lbm_scene("walls")
