@@ -192,6 +192,54 @@ int pfgpu_batch_num_jobs(const pfgpu_batch *b);
 void pfgpu_batch_destroy(pfgpu_batch *b);
 
 /* ------------------------------------------------------------ misc */
+/* ---- membrane pass without allocation ------------------------------------
+ * No counterpart in the reference (its membrane pass runs inside
+ * sem_invokeGPUKernel_Force on buffers sem_allocGPUKernel allocated).
+ * The membrane forces of n_platelets platelets -- springs on RY, wall
+ * repulsion, area/volume penalty, bending: the pass pfgpu_job_step runs --
+ * computed from caller-owned device arrays into F_out, for callers that may
+ * not allocate device memory while they run (a solver loop with a fixed
+ * memory budget, code between a custom allocator's arena set-up and use).
+ * It calls no cudaMalloc/cudaFree or other allocating routine: its scratch
+ * (node triangle lists, normals, strains, curvatures) is a fixed static
+ * device array of PFGPU_NOALLOC_SCRATCH_BYTES, and a call that needs more
+ * (about P * (12 n_node + 16 n_tri + 4 n_membrane) bytes in FP32, twice that
+ * in FP64, plus 80 n_node) returns PFGPU_ERR_INVALID with the sizes in
+ * pfgpu_last_error().
+ * - The first call on a device looks up the scratch's address
+ *   (cudaGetSymbolAddress with that device current); make it before any
+ *   stream capture.
+ * - The scratch is shared: calls that overlap in time, on any streams or
+ *   host threads, race on it.  Serialise them.
+ * - Nothing needs to start at zero: each call zeroes the scratch's control
+ *   word on `stream` and writes every other scratch word before reading it.
+ * Inputs use the pf_scene layouts (device pointers); F_out is [3][P*n_elem]
+ * in units of F0, double for PF_PREC_FP64 and float otherwise; S_V_out
+ * ([P][2]: area, volume) and km_out ([P][n_membrane]: mean curvature, the
+ * real type of F_out) may be NULL.  Asynchronous on `stream` (a
+ * cudaStream_t, NULL for the default stream). */
+#define PFGPU_NOALLOC_SCRATCH_BYTES (8u << 20)
+typedef struct {
+  int n_platelets, n_elem, n_membrane, n_tri, n_node;
+  int precision;       /* PF_PREC_* */
+  int membrane_forces; /* PF_MEM_* mask */
+  float kspring, ks, kv, kbend, f0; /* reference parameters (float) */
+  const double *X, *Y, *RY, *Z;     /* [P * n_elem] */
+  const int *tri;                   /* [n_tri][6] */
+  const int *node_ntri;             /* [n_node] */
+  const int *ring;                  /* [n_membrane][10] */
+  const int *spring_ptr;            /* [n_elem + 1] */
+  const int *spring_nbr;            /* [spring_ptr[n_elem]] */
+  const double *spring_L0;          /* [spring_ptr[n_elem]] */
+  const double *S0;                 /* [P][n_tri] */
+  const double *S0_all, *V0;        /* [P] */
+  void *F_out;                      /* [3][P * n_elem] */
+  double *S_V_out;                  /* [P][2] or NULL */
+  void *km_out;                     /* [P][n_membrane] or NULL */
+} pf_membrane_args;
+int pfgpu_membrane_forces_noalloc(const pf_membrane_args *args, void *stream);
+size_t pfgpu_membrane_noalloc_scratch_bytes(void);
+
 const char *pfgpu_last_error(void);
 int pfgpu_version(void);
 /* Philox-4x32-10 uniforms of the receptor stream (step, receptor) -> (u1, u2),

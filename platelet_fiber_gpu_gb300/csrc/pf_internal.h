@@ -169,10 +169,18 @@ cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
 cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, double detach_rate,
                            uint64_t seed, unsigned* done_blocks, cudaStream_t st);
 cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st);
+cudaError_t membrane_forces_raw(const PlateletConst& k, int precision, const double* X, const double* Y,
+                                const double* RY, const double* Z, const int* tri, const int* node_ntri,
+                                const int* node_tri, const int* vert_local, const int* ring, const int* sp_ptr,
+                                const int* sp_nbr, const double* sp_L0, const double* S0, const double* S0_all,
+                                const double* V0, void* nN, void* nelem, void* S, void* km, double* SV, void* F,
+                                Control* ctl, cudaStream_t st);
 size_t bond_scratch_bytes(int NR);
 bool morse_uses_cells(const PlateletConst& k);
 cudaError_t sort_cell_bins(Platelets& Pl, Control* ctl, cudaStream_t st);
 
 int membrane_threads();
+// sets the message pfgpu_last_error returns; returns code
+int report_error(int code, const char* msg);
 
 }  // namespace pf

@@ -33,6 +33,10 @@ static int set_error(int code, const std::string& msg) {
   return code;
 }
 
+namespace pf {
+int report_error(int code, const char* msg) { return set_error(code, msg); }
+}  // namespace pf
+
 #define CK(call)                                                                               \
   do {                                                                                         \
     cudaError_t e_ = (call);                                                                   \

@@ -1730,6 +1730,26 @@ cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStre
   return cudaGetLastError();
 }
 
+// The membrane pass on caller-given arrays (the no-allocation entry point):
+// same kernel and launch shape as membrane_forces.
+cudaError_t membrane_forces_raw(const PlateletConst& k, int precision, const double* X, const double* Y,
+                                const double* RY, const double* Z, const int* tri, const int* node_ntri,
+                                const int* node_tri, const int* vert_local, const int* ring, const int* sp_ptr,
+                                const int* sp_nbr, const double* sp_L0, const double* S0, const double* S0_all,
+                                const double* V0, void* nN, void* nelem, void* S, void* km, double* SV, void* F,
+                                Control* ctl, cudaStream_t st) {
+  if (k.P == 0) return cudaSuccess;
+  if (precision == PF_PREC_FP64)
+    membrane_k<double><<<k.P, 512, 0, st>>>(k, X, Y, RY, Z, tri, node_ntri, node_tri, vert_local, ring, sp_ptr,
+                                            sp_nbr, sp_L0, S0, S0_all, V0, (double*)nN, (double*)nelem, (double*)S,
+                                            (double*)km, SV, (double*)F, ctl);
+  else
+    membrane_k<float><<<k.P, 512, (size_t)k.E * 4 * sizeof(float), st>>>(
+        k, X, Y, RY, Z, tri, node_ntri, node_tri, vert_local, ring, sp_ptr, sp_nbr, sp_L0, S0, S0_all, V0,
+        (float*)nN, (float*)nelem, (float*)S, (float*)km, SV, (float*)F, ctl);
+  return cudaGetLastError();
+}
+
 bool morse_uses_cells(const PlateletConst& k) { return k.E > kMorseTileE; }
 
 
