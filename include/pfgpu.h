@@ -137,6 +137,9 @@ int pfgpu_job_step(pfgpu_job *job, int nsteps);
 /* Same, captured once in a CUDA graph and replayed (no host work per step). */
 int pfgpu_job_step_graph(pfgpu_job *job, int nsteps);
 int pfgpu_job_sync(pfgpu_job *job);
+/* Enqueues nsteps replays of the step graph without waiting (pfgpu_job_sync
+ * waits and reports PFGPU_DONE / device errors). */
+int pfgpu_job_enqueue(pfgpu_job *job, int nsteps);
 /* Runs nsteps steps serialised on one stream with CUDA events around each
  * phase and returns the summed device time per phase in ms (ms_out holds
  * pfgpu_profile_phase_count() entries): flag, membrane, morse, fibrin, bonds,
@@ -176,15 +179,20 @@ void pfgpu_job_destroy(pfgpu_job *job);
 size_t pfgpu_scene_device_bytes(const pf_scene *scene, int precision);
 
 /* ------------------------------------------------------------ batch API */
-/* Many independent jobs advanced together by one persistent kernel per phase
- * over an offset table (continuous batching).  Jobs may join and leave
- * between steps. */
+/* Continuous batching of independent jobs on one GPU: each admitted job keeps
+ * its own state and captured step graph; pfgpu_batch_step enqueues every live
+ * job's steps on the job's own streams (so small lattices run side by side)
+ * and waits for all of them.  Jobs join and leave between batch steps;
+ * admission is checked against a device-memory budget. */
 typedef struct pfgpu_batch pfgpu_batch;
 int pfgpu_batch_create(size_t hbm_budget_bytes, pfgpu_batch **out);
 /* Admits a job if it fits the budget; returns PFGPU_ERR_NOMEM otherwise.
  * *slot receives the job's id within the batch. */
 int pfgpu_batch_admit(pfgpu_batch *b, const pf_scene *scene, int precision, double fp16_scale, int *slot);
+/* nsteps steps of every live job; a job whose platelet detached stops and its
+ * status turns PFGPU_DONE (retire it). */
 int pfgpu_batch_step(pfgpu_batch *b, int nsteps);
+int pfgpu_batch_status(pfgpu_batch *b, int slot);
 int pfgpu_batch_retire(pfgpu_batch *b, int slot);
 pfgpu_job *pfgpu_batch_job(pfgpu_batch *b, int slot);
 size_t pfgpu_batch_bytes_in_use(const pfgpu_batch *b);

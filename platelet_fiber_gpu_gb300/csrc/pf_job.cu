@@ -676,7 +676,7 @@ int pfgpu_job_step_graph(pfgpu_job* j, int nsteps) {
   return check_control(j);
 }
 
-int pfgpu_job_enqueue(pfgpu_job* j, int nsteps, cudaStream_t) {
+int pfgpu_job_enqueue(pfgpu_job* j, int nsteps) {
   if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
   if (!j->graph) {
     int rc = pfgpu_job_step_graph(j, 0);

@@ -60,6 +60,17 @@ def lib():
         L.pfgpu_scene_device_bytes.argtypes = [vp, C.c_int]
         L.pfgpu_last_error.restype = C.c_char_p
         L.pfgpu_receptor_uniforms.argtypes = [C.c_uint64, C.c_int64, C.c_int64, dp]
+        L.pfgpu_batch_create.argtypes = [C.c_size_t, C.POINTER(vp)]
+        L.pfgpu_batch_admit.argtypes = [vp, vp, C.c_int, C.c_double, ip]
+        L.pfgpu_batch_step.argtypes = [vp, C.c_int]
+        L.pfgpu_batch_status.argtypes = [vp, C.c_int]
+        L.pfgpu_batch_retire.argtypes = [vp, C.c_int]
+        L.pfgpu_batch_job.restype = vp
+        L.pfgpu_batch_job.argtypes = [vp, C.c_int]
+        L.pfgpu_batch_bytes_in_use.restype = C.c_size_t
+        L.pfgpu_batch_bytes_in_use.argtypes = [vp]
+        L.pfgpu_batch_num_jobs.argtypes = [vp]
+        L.pfgpu_batch_destroy.argtypes = [vp]
         L.pfgpu_detach_uniform.restype = C.c_double
         L.pfgpu_detach_uniform.argtypes = [C.c_uint64, C.c_int64]
         _lib = L
@@ -185,3 +196,71 @@ class Job:
         out = np.zeros(4)
         check(lib().pfgpu_job_conservation(self.h, _p(out)))
         return out
+
+
+class _BatchJob(Job):
+    """A job owned by a Batch (read-only view: the batch destroys it)."""
+
+    def __init__(self, scene: Scene, handle):
+        self.scene = scene
+        self.h = C.c_void_p(handle)
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """Continuous batching of independent jobs (pfgpu_batch): jobs are
+    admitted against a device-memory budget, stepped together, retired."""
+
+    def __init__(self, hbm_budget_bytes: int):
+        h = C.c_void_p()
+        check(lib().pfgpu_batch_create(int(hbm_budget_bytes), C.byref(h)))
+        self.h = h
+        self._scenes = {}
+        self._c = {}
+
+    def admit(self, scene: Scene, precision: int = 1, fp16_scale: float = 0.0):
+        """Slot id, or None if the job does not fit the budget."""
+        c = scene.to_c()
+        slot = C.c_int(-1)
+        rc = lib().pfgpu_batch_admit(self.h, C.byref(c), precision, fp16_scale, C.byref(slot))
+        if rc == 3:
+            return None
+        check(rc)
+        self._scenes[slot.value] = scene
+        self._c[slot.value] = c
+        return slot.value
+
+    def step(self, n: int = 1):
+        check(lib().pfgpu_batch_step(self.h, int(n)))
+
+    def status(self, slot: int) -> int:
+        return check(lib().pfgpu_batch_status(self.h, slot), allow_done=True)
+
+    def job(self, slot: int) -> Job:
+        return _BatchJob(self._scenes[slot], lib().pfgpu_batch_job(self.h, slot))
+
+    def retire(self, slot: int):
+        check(lib().pfgpu_batch_retire(self.h, slot))
+        self._scenes.pop(slot, None)
+        self._c.pop(slot, None)
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(lib().pfgpu_batch_bytes_in_use(self.h))
+
+    @property
+    def num_jobs(self) -> int:
+        return int(lib().pfgpu_batch_num_jobs(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pfgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -271,3 +271,54 @@ def mixed_small(seed: int = 3, nx=40, ny=32, nz=20, n_platelets=3, level=1, n_cy
     sc.seed = seed
     sc.meta.update(workload="mixed_small")
     return sc
+
+
+_BATCH_TEMPLATE = {}
+
+
+def _batch_template(seed: int):
+    if seed not in _BATCH_TEMPLATE:
+        axes = (1.0, 1.0, 0.5)
+        v, t = M.ellipsoid_fibonacci(400, axes, seed)
+        _BATCH_TEMPLATE[seed] = PlateletTemplate(v, t, 200, seed, axes)
+    return _BATCH_TEMPLATE[seed]
+
+
+def batch_job(seed: int, index: int, steps_range=None) -> Scene:
+    """One job of the many-job workload: node count log-uniform in
+    [32^3, 128*64*64] with aspect 2:1:1 rounded to multiples of 8, 1-8
+    platelets (as many as fit) of the single_large template, 1k-5k fibrin
+    nodes on the bottom wall, shear uniform in [100, 2000] 1/s, 200 receptors
+    per platelet with constant per-step probabilities 1e-2 / 1e-3.  The job's
+    own stream of draws is seeded by (seed, index)."""
+    rng = np.random.default_rng([seed, index])
+    nodes = float(np.exp(rng.uniform(np.log(32 ** 3), np.log(128 * 64 * 64))))
+    a = max(16, int(round((nodes / 2) ** (1 / 3) / 8)) * 8)
+    nx, ny, nz = 2 * a, a, a
+    tpl = _batch_template(seed)
+    axes = (1.0, 1.0, 0.5)
+    shear = float(rng.uniform(100.0, 2000.0))
+    params = reference_params(dx=REF_DX, dt=REF_DT, nz=nz, shear=shear, mean_bond=tpl.mean_bond)
+    sc = Scene(nx=nx, ny=ny, nz=nz, dx=REF_DX, dt=REF_DT, params=params,
+               bc=(BC_PERIODIC, BC_PERIODIC, BC_ZOUHE_SHEAR), ibm_wrap=(1, 1, 0))
+    L = np.array([nx, ny, nz]) * REF_DX
+    rmin = 2 * axes[0] + 2 * REF_DX
+    want = int(rng.integers(1, 9))
+    fit = max(1, int(np.prod(L - np.array([2 * axes[0], 2 * axes[1], 2 * axes[2] + 0.65])) / rmin ** 3 // 2))
+    n_pl = min(want, fit)
+    centers = poisson_disk(n_pl, (axes[0], axes[1], axes[2] + 0.05),
+                           (L[0] - axes[0], L[1] - axes[1], L[2] - axes[2] - 0.6), rmin, rng,
+                           fixed_z=axes[2] + 0.05, n_fixed=1)
+    _place(sc, tpl, centers, L[1])
+    _receptors_random(sc, 200, rng)
+    sc.params[P_NUMRECEPTORS] = 200 * len(centers)
+    sc.bond_model = BOND_CONSTANT
+    sc.p_on, sc.p_off = 1e-2, 1e-3
+    sc.morse = 1
+    n_fib = int(rng.integers(1000, 5001))
+    _fibrin(sc, n_fib, 2 * n_fib, 3 * REF_DX, rng, 0.5)
+    sc.seed = (seed << 20) + index
+    sc.meta.update(workload="batch_job", shear=shear, index=index)
+    if steps_range is not None:
+        sc.meta["steps"] = int(rng.integers(steps_range[0], steps_range[1] + 1))
+    return sc

@@ -1,0 +1,63 @@
+"""Batch API (continuous batching of independent jobs): jobs stepped together
+give the results they give alone; admission respects the device-memory
+budget; retiring returns the memory."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from platelet_fiber_gpu_gb300 import build
+    build.build()
+    from platelet_fiber_gpu_gb300 import gpu as g
+    return g
+
+
+def test_batched_jobs_match_standalone(gpu):
+    from platelet_fiber_gpu_gb300 import workloads as W
+    scenes = [W.mixed_small(seed=3), W.mixed_small(seed=5, nx=48)]
+    b = gpu.Batch(8 << 30)
+    slots = [b.admit(sc, 0) for sc in scenes]
+    assert None not in slots and b.num_jobs == 2
+    b.step(4)
+    b.step(6)
+    for sc, s in zip(scenes, slots):
+        ref = gpu.Job(sc, 0)
+        ref.step(10)
+        got = b.job(s)
+        assert got.steps == 10
+        a, r = got.lattice()["fIN"], ref.lattice()["fIN"]
+        assert np.abs(a - r).max() / np.abs(r).max() < 1e-13
+        np.testing.assert_array_equal(got.bonds()["rec_state"], ref.bonds()["rec_state"])
+        ref.close()
+    b.close()
+
+
+def test_batch_budget_and_retire(gpu):
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small()
+    need = gpu.scene_device_bytes(sc, 1)
+    b = gpu.Batch(int(need * 1.5))
+    s0 = b.admit(sc, 1)
+    assert s0 is not None
+    used = b.bytes_in_use
+    assert 0 < used <= need
+    assert b.admit(sc, 1) is None  # a second copy does not fit
+    b.retire(s0)
+    assert b.bytes_in_use == 0 and b.num_jobs == 0
+    s1 = b.admit(sc, 1)
+    assert s1 == s0
+    b.step(2)
+    assert b.status(s1) == 0
+    b.close()
+
+
+def test_served_loop_small(gpu):
+    """A short Poisson-arrival run of the serving loop completes every job and
+    reports latencies."""
+    from platelet_fiber_gpu_gb300 import serve
+    r = serve.run_served(1, rate=8.0, duration=0.5, steps_range=(20, 60), pool=3, chunk=20)
+    assert r["jobs"] >= 1 and r["mlups"] > 0
+    assert 0 < r["latency_p50_s"] <= r["latency_p99_s"]
