@@ -127,6 +127,23 @@ def lbm_traffic_per_node():
         return None
 
 
+def reduce_max(dist, x: float, device: str) -> float:
+    """Maximum of x over the ranks of an initialised process group (the
+    slowest replica's time); x itself without one."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, nodes_per_replica: int, t_step_max: float) -> float:
+    """Whole-job MLUPS of `world` independent replicas: all node updates
+    over the slowest replica's step time."""
+    return world * nodes_per_replica / t_step_max / 1e6
+
+
 def build_scene(args):
     from platelet_fiber_gpu_gb300 import workloads as W
     return W.single_large(seed=args.seed, nx=args.nx, ny=args.ny, nz=args.nz, n_platelets=args.platelets,
@@ -231,11 +248,7 @@ def main():
         torch.cuda.synchronize()
 
     def max_over_ranks(x: float) -> float:
-        if not pg:
-            return x
-        t = torch.tensor([x], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(pg, x, "cuda")
 
     # ---- device-resident throughput: K graph replays of the step
     job = gpu.Job(scene, prec, fp16_scale)
@@ -257,7 +270,7 @@ def main():
     # the host wall time and the event pair bracket the same work
     dev_ms = start.elapsed_time(stop)
     t_step = max_over_ranks(max(dev_ms / 1e3, wall) / args.steps)
-    value = world * N / t_step / 1e6
+    value = replica_value(world, N, t_step)
     clk = clocks.summary()
 
     # ---- live per-phase CUDA-event timing (serialised pass, same job)
@@ -280,7 +293,7 @@ def main():
     e2e_s = time.perf_counter() - t0
     j2.close()
     e2e_s = max_over_ranks(e2e_s)
-    e2e_value = world * N * args.steps / e2e_s / 1e6
+    e2e_value = replica_value(world, N * args.steps, e2e_s)
 
     peak, peak_kind = measured_peak()
     bpn = BYTES_PER_NODE[prec]

@@ -54,6 +54,7 @@ struct LatticeConst {
   double body[3];     // body force, reference units
   double uw;          // top-wall velocity / C
   double fp16_scale;  // sigma of the FP16 store
+  float hs[3], hinv[3];  // w * sigma and 1 / (w * sigma) for w = 1/3, 1/18, 1/36 (FP16 store)
   float dtT;          // dt / T0 (float, sem_kernel.cu:2106): position update factor
 };
 

@@ -136,6 +136,11 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
   double sigma = fp16_scale;
   if (!(sigma > 0)) sigma = (s->bc[2] == PF_BC_ZOUHE_SHEAR && k.uw > 0) ? 8.0 * k.uw : 0.05;
   k.fp16_scale = precision == PF_PREC_FP16 ? sigma : 1.0;
+  const double wc[3] = {1.0 / 3.0, 1.0 / 18.0, 1.0 / 36.0};
+  for (int c = 0; c < 3; ++c) {
+    k.hs[c] = (float)(wc[c] * k.fp16_scale);
+    k.hinv[c] = 1.0f / k.hs[c];
+  }
   k.dtT = s->dt / mp[PF_P_T0];
   return k;
 }

@@ -22,14 +22,17 @@ namespace pf {
 
 namespace {
 
-template <class S, class R>
-struct Lat {
-  static __device__ __forceinline__ R scale(int d, R sigma) { return (R)wgt(d) * sigma; }
-};
+// weight class of a direction (rest, axis, diagonal): index of the FP16
+// store scales w_d * sigma and their inverses in LatticeConst
+__host__ __device__ constexpr int wcls(int d) { return d == 0 ? 0 : (d < 7 ? 1 : 2); }
 
 template <class S, class R>
-__device__ __forceinline__ R ld(const S* p, int d, R sigma) {
-  return (R)StoreTraits<S>::load(p, d, (decltype(StoreTraits<S>::load(p, 0, R(0))))(wgt(d) * sigma));
+__device__ __forceinline__ R ld(const S* p, int d, const LatticeConst& k) {
+  return (R)StoreTraits<S>::load(p, d, (decltype(StoreTraits<S>::load(p, 0, R(0))))k.hs[wcls(d)]);
+}
+template <class S, class R>
+__device__ __forceinline__ void st(S* p, R v, int d, const LatticeConst& k) {
+  StoreTraits<S>::store(p, v, d, (decltype(StoreTraits<S>::load(p, 0, R(0))))k.hinv[wcls(d)]);
 }
 
 template <class R>
@@ -83,7 +86,6 @@ __device__ __forceinline__ void gather(const LatticeConst& k, const S* __restric
                                        R g[Q]) {
   const int nx = k.nx, ny = k.ny, nz = k.nz;
   const size_t N = (size_t)k.N;
-  const R sigma = (R)k.fp16_scale;
   int xm = x - 1, xp = x + 1, ym = y - 1, yp = y + 1, zm = z - 1, zp = z + 1;
   bool oxm = false, oxp = false, oym = false, oyp = false, ozm = false, ozp = false;
   if (xm < 0) { if (k.bc[0] == PF_BC_BOUNCEBACK) oxm = true; else xm = nx - 1; }
@@ -101,9 +103,9 @@ __device__ __forceinline__ void gather(const LatticeConst& k, const S* __restric
     const bool out = (cx(d) == 1 && oxm) || (cx(d) == -1 && oxp) || (cy(d) == 1 && oym) ||
                      (cy(d) == -1 && oyp) || (cz(d) == 1 && ozm) || (cz(d) == -1 && ozp);
     if (out) {
-      g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
+      g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), k);
     } else {
-      g[d] = ld<S, R>(gin + (size_t)d * N + (size_t)sx + (size_t)nx * ((size_t)sy + (size_t)ny * sz), d, sigma);
+      g[d] = ld<S, R>(gin + (size_t)d * N + (size_t)sx + (size_t)nx * ((size_t)sy + (size_t)ny * sz), d, k);
     }
   }
 }
@@ -247,11 +249,9 @@ __device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restr
   const R kc = (R)k.kcoll;
   const R om = (R)k.omega;
   collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
-  const R sigma = (R)k.fp16_scale;
 #pragma unroll
   for (int d = 0; d < Q; ++d)
-    StoreTraits<S>::store(gout + (size_t)d * N + n, g[d], d,
-                          (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+    st<S, R>(gout + (size_t)d * N + n, g[d], d, k);
   if (fp) zero_force<R>(Fp, n);
 }
 
@@ -408,14 +408,14 @@ __host__ __device__ constexpr unsigned dir_mask(int wy, int wz) {
 }
 
 template <class S, class R>
-__device__ __forceinline__ R from_store(S v, int d, R sigma);
+__device__ __forceinline__ R from_store(S v, int d, const LatticeConst& k);
 template <>
-__device__ __forceinline__ double from_store<double, double>(double v, int, double) { return v; }
+__device__ __forceinline__ double from_store<double, double>(double v, int, const LatticeConst&) { return v; }
 template <>
-__device__ __forceinline__ float from_store<float, float>(float v, int, float) { return v; }
+__device__ __forceinline__ float from_store<float, float>(float v, int, const LatticeConst&) { return v; }
 template <>
-__device__ __forceinline__ float from_store<__half, float>(__half v, int d, float sigma) {
-  return __half2float(v) * ((float)wgt(d) * sigma);
+__device__ __forceinline__ float from_store<__half, float>(__half v, int d, const LatticeConst& k) {
+  return __half2float(v) * k.hs[wcls(d)];
 }
 
 template <class S, class R, int DS>
@@ -501,7 +501,6 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     }
   };
 
-  const R sigma = (R)k.fp16_scale;
   const R kc = (R)k.kcoll;
   const R om = (R)k.omega;
   const R sf = (R)1 - (R)0.5 * om;
@@ -516,13 +515,13 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     if (mask == 0) {
       // interior row: every direction pulls from x - cx (halos cover the ends)
 #pragma unroll
-      for (int d = 0; d < Q; ++d) g[d] = from_store<S, R>(p[d * DS - cx(d)], d, sigma);
+      for (int d = 0; d < Q; ++d) g[d] = from_store<S, R>(p[d * DS - cx(d)], d, k);
     } else {
       // row on a bounce-back face in y or z: own-row directions are unshifted
 #pragma unroll
       for (int d = 0; d < Q; ++d) {
         const bool own = (cy(d) != 0 || cz(d) != 0) && ((mask >> d) & 1u);
-        g[d] = from_store<S, R>(own ? p[d * DS] : p[d * DS - cx(d)], d, sigma);
+        g[d] = from_store<S, R>(own ? p[d * DS] : p[d * DS - cx(d)], d, k);
       }
     }
     if (bbx && (x == 0 || x == nx - 1)) {
@@ -532,7 +531,7 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
         if (cx(d) == 0) continue;
         const bool own = (cy(d) != 0 || cz(d) != 0) && ((mask >> d) & 1u);
         if (!own && ((cx(d) == 1 && x == 0) || (cx(d) == -1 && x == nx - 1)))
-          g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), sigma);
+          g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), k);
       }
     }
     const int brick = (x >> 5) + k.nbx * r;
@@ -550,8 +549,7 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     S* o = gout + n;
 #pragma unroll
     for (int d = 0; d < Q; ++d)
-      StoreTraits<S>::store(o + (size_t)d * N, g[d], d,
-                            (decltype(StoreTraits<S>::load(gout, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+      st<S, R>(o + (size_t)d * N, g[d], d, k);
     if (fp) zero_force<R>(Fp, n);
     __syncwarp();
     if (lane == 0 && fp) flp[brick] = 0;
@@ -661,10 +659,9 @@ __global__ void download_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, con
   } else {
     node_state<R>(k, g, z, apply_bc != 0, Fx, Fy, Fz, drho, ux, uy, uz);
   }
-  const R sigma = (R)k.fp16_scale;
   for (int d = 0; d < Q; ++d) {
     if (fIN) fIN[(size_t)d * N + n] = (double)g[d] + wgt(d);
-    if (fOUT) fOUT[(size_t)d * N + n] = (double)ld<S, R>(gsrc + (size_t)d * N + n, d, sigma) + wgt(d);
+    if (fOUT) fOUT[(size_t)d * N + n] = (double)ld<S, R>(gsrc + (size_t)d * N + n, d, k) + wgt(d);
   }
   if (rho_o) rho_o[n] = 1.0 + (double)drho;
   if (u_o) {
@@ -690,7 +687,6 @@ __global__ void upload_k(LatticeConst k, S* g, const double* fIN, R4<R>* Fprev, 
   const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   const int x = (int)(n % k.nx), y = (int)((n / k.nx) % k.ny), z = (int)(n / ((size_t)k.nx * k.ny));
-  const R sigma = (R)k.fp16_scale;
   for (int d = 0; d < Q; ++d) {
     int tx = x + cx(d), ty = y + cy(d), tz = z + cz(d);
     bool out = false;
@@ -699,8 +695,7 @@ __global__ void upload_k(LatticeConst k, S* g, const double* fIN, R4<R>* Fprev, 
     if (tz < 0 || tz >= k.nz) { if (k.bc[2] == PF_BC_BOUNCEBACK) out = true; else tz = (tz + k.nz) % k.nz; }
     double f = out ? fIN[(size_t)opp(d) * N + n]
                    : fIN[(size_t)d * N + (size_t)tx + (size_t)k.nx * ((size_t)ty + (size_t)k.ny * tz)];
-    StoreTraits<S>::store(g + (size_t)d * N + n, (R)(f - wgt(d)), d,
-                          (decltype(StoreTraits<S>::load(g, 0, R(0))))((R)1 / ((R)wgt(d) * sigma)));
+    st<S, R>(g + (size_t)d * N + n, (R)(f - wgt(d)), d, k);
   }
   R fx = 0, fy = 0, fz = 0;
   if (F) { fx = (R)F[n]; fy = (R)F[N + n]; fz = (R)F[2 * N + n]; }

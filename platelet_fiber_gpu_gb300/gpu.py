@@ -6,6 +6,7 @@ present, every call raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
@@ -31,6 +32,10 @@ def lib():
     if _lib is None:
         if not LIB_PATH.exists():
             raise RuntimeError(f"{LIB_PATH} is not built; run platelet_fiber_gpu_gb300.build.build()")
+        # independent jobs run on their own streams; more hardware work queues
+        # than the default 8 keep them from serialising (read when the CUDA
+        # context is created, so it only applies if nothing created it yet)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
         L = C.CDLL(str(LIB_PATH))
         vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
         L.pfgpu_job_create.argtypes = [vp, C.c_int, C.c_double, C.POINTER(vp)]
