@@ -110,6 +110,25 @@ __device__ __forceinline__ void gather(const LatticeConst& k, const S* __restric
   }
 }
 
+// The same pull for lattices without bounce-back faces (every axis periodic
+// or Zou/He, which streams periodically) whose population index 19 N fits
+// 32 bits: no face tests, 32-bit offsets (nine source rows, three columns).
+template <class S, class R>
+__device__ __forceinline__ void gather_fast(const LatticeConst& k, const S* __restrict__ gin, int x, int y, int z,
+                                            R g[Q]) {
+  const unsigned nx = (unsigned)k.nx, ny = (unsigned)k.ny, nz = (unsigned)k.nz;
+  const unsigned N = (unsigned)k.N;
+  const unsigned xs[3] = {x == 0 ? nx - 1 : (unsigned)x - 1, (unsigned)x, (unsigned)x + 1 == nx ? 0u : x + 1u};
+  const unsigned ys[3] = {y == 0 ? ny - 1 : (unsigned)y - 1, (unsigned)y, (unsigned)y + 1 == ny ? 0u : y + 1u};
+  const unsigned zs[3] = {z == 0 ? nz - 1 : (unsigned)z - 1, (unsigned)z, (unsigned)z + 1 == nz ? 0u : z + 1u};
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    // pull from x - c: index 0 of each triple is the -1 neighbour
+    const unsigned off = (unsigned)d * N + xs[1 - cx(d)] + nx * (ys[1 - cy(d)] + ny * zs[1 - cz(d)]);
+    g[d] = ld<S, R>(gin + off, d, k);
+  }
+}
+
 // Zou/He planes: z=0 no-slip (LB_kernel.cu:395-600) and z=nz-1 moving plate
 // (:602-780, where C, Nzx, Nzy are float).  Writes the unknowns, returns the
 // boundary density; velocity is the wall's.
@@ -226,14 +245,16 @@ __device__ __forceinline__ void collide(R g[Q], R drho, R ux, R uy, R uz, R Fx, 
 
 // One node of the direct-gather step: pull, moments with the previous
 // force, collision with the current force, store; clears the previous force.
-template <class S, class R>
+// FAST: no bounce-back face and 32-bit population indices (gather_fast).
+template <class S, class R, bool FAST>
 __device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restrict__ gin, S* __restrict__ gout,
                                          const R4<R>* Fc, R4<R>* Fp, const R4<R>* ubuf, int x, int y, int z,
                                          unsigned fc, unsigned fp, int first) {
   const size_t N = (size_t)k.N;
   const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
   R g[Q];
-  gather<S, R>(k, gin, x, y, z, g);
+  if constexpr (FAST) gather_fast<S, R>(k, gin, x, y, z, g);
+  else gather<S, R>(k, gin, x, y, z, g);
   R drho, ux, uy, uz;
   if (first) {
     // the first collision after an upload uses the uploaded density and
@@ -249,9 +270,14 @@ __device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restr
   const R kc = (R)k.kcoll;
   const R om = (R)k.omega;
   collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
+  if constexpr (FAST) {
+    const unsigned N32 = (unsigned)N, n32 = (unsigned)n;
 #pragma unroll
-  for (int d = 0; d < Q; ++d)
-    st<S, R>(gout + (size_t)d * N + n, g[d], d, k);
+    for (int d = 0; d < Q; ++d) st<S, R>(gout + ((unsigned)d * N32 + n32), g[d], d, k);
+  } else {
+#pragma unroll
+    for (int d = 0; d < Q; ++d) st<S, R>(gout + (size_t)d * N + n, g[d], d, k);
+  }
   if (fp) zero_force<R>(Fp, n);
 }
 
@@ -265,7 +291,7 @@ __device__ __forceinline__ void zero_bins(int* bin_count, int ncells, Control* c
 // Direct-gather step over the lattice, one x-row segment of kLbmBlock nodes
 // per CTA, one force brick per warp.  skip_flagged: bricks flagged for this
 // step's force are left to lbm_list_k (they run after the spreading).
-template <class S, class R>
+template <class S, class R, bool FAST>
 __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
                                                         R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
                                                         int ncells, int skip_flagged, Control* ctl) {
@@ -289,13 +315,13 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
   }
   if (skip_flagged && fc) return;  // whole warp: one brick
   const unsigned fp = row_ok ? flp[brick] : 0u;
-  if (x < k.nx) lbm_node<S, R>(k, gin, gout, Fc, Fp, ubuf, x, y, z, fc, fp, ctl->first);
+  if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, fc, fp, ctl->first);
   __syncwarp();
   if ((threadIdx.x & 31) == 0 && fp) flp[brick] = 0;
 }
 
 // The flagged bricks of this step (list[par]), one warp per brick.
-template <class S, class R>
+template <class S, class R, bool FAST>
 __global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
                                                         R4<R>* ubuf, unsigned* flA, unsigned* flB, const int* lA,
                                                         const int* lB, int* bin_count, int ncells, Control* ctl) {
@@ -320,7 +346,7 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S
     const int z = brick / (k.nbx * k.ny);
     const int x = bx * kBrickX + lane;
     const unsigned fp = flp[brick];
-    if (x < k.nx) lbm_node<S, R>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 1u, fp, first);
+    if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 1u, fp, first);
     __syncwarp();
     if (lane == 0 && fp) flp[brick] = 0;
   }
@@ -786,6 +812,12 @@ void rows_config(Lattice& L) {
   else if (need <= 384) rows_try<S, R, 384>(L, rpt);
 }
 
+// No bounce-back face and 19 N populations addressable with 32 bits.
+inline bool fast_lattice(const Lattice& L) {
+  return L.k.bc[0] != PF_BC_BOUNCEBACK && L.k.bc[1] != PF_BC_BOUNCEBACK && L.k.bc[2] != PF_BC_BOUNCEBACK &&
+         19ull * (unsigned long long)L.k.N < (1ull << 32) && !getenv("PFGPU_GENERIC_GATHER");
+}
+
 // part: 0 the whole lattice, 1 the bricks not flagged for this step's force,
 // 2 the flagged bricks (after the spreading).
 template <class S, class R>
@@ -805,15 +837,15 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
     int grid = sms * 8;
     const int need = (L.k.nbricks + kLbmBlock / 32 - 1) / (kLbmBlock / 32);
     if (grid > need) grid = need;
-    lbm_list_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
-                                                (R4<R>*)L.ubuf, L.flags[0], L.flags[1], L.list[0], L.list[1],
-                                                bin_count, ncells, ctl);
+    auto kern = fast_lattice(L) ? lbm_list_k<S, R, true> : lbm_list_k<S, R, false>;
+    kern<<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
+                                     L.flags[0], L.flags[1], L.list[0], L.list[1], bin_count, ncells, ctl);
     return cudaGetLastError();
   }
   dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);
-  lbm_step_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1],
-                                              (R4<R>*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells,
-                                              part == 1 ? 1 : 0, ctl);
+  auto kern = fast_lattice(L) ? lbm_step_k<S, R, true> : lbm_step_k<S, R, false>;
+  kern<<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
+                                   L.flags[0], L.flags[1], bin_count, ncells, part == 1 ? 1 : 0, ctl);
   return cudaGetLastError();
 }
 template <class S, class R>
