@@ -54,11 +54,10 @@ struct pfgpu_job {
   Control* ctl = nullptr;
   unsigned* done_blocks = nullptr;
   double* scratch4 = nullptr;
-  // s0: critical path (flags, bonds, spreading, flagged bricks, moments,
-  // interpolation); s1-s3: membrane, Morse, fibrin; s4 (lowest priority):
-  // the lattice pass over the bricks without force, beside the force kernels
-  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr, s4 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev4 = nullptr;
+  // s0: critical path (flags, lattice passes, bonds, spreading, moments,
+  // interpolation); s1-s3: membrane, Morse, fibrin
+  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   cudaGraphExec_t graph = nullptr;
   double detach_rate = 0;
   uint64_t seed = 0;
@@ -90,10 +89,10 @@ static void destroy(pfgpu_job* j) {
   if (!j) return;
   if (j->graph) cudaGraphExecDestroy(j->graph);
   for (void* p : j->allocs) cudaFree(p);
-  cudaStream_t ss[5] = {j->s0, j->s1, j->s2, j->s3, j->s4};
+  cudaStream_t ss[4] = {j->s0, j->s1, j->s2, j->s3};
   for (cudaStream_t s : ss)
     if (s) cudaStreamDestroy(s);
-  cudaEvent_t ee[5] = {j->ev_fork, j->ev1, j->ev2, j->ev3, j->ev4};
+  cudaEvent_t ee[4] = {j->ev_fork, j->ev1, j->ev2, j->ev3};
   for (cudaEvent_t e : ee)
     if (e) cudaEventDestroy(e);
   delete j;
@@ -402,11 +401,14 @@ static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
 }
 
 // One coupled step.  With markers:
-//   s0: flag the force bricks of this step (from the marker positions)
-//   fork -> s1 membrane | s2 Morse | s3 fibrin | s0 bonds | s4 lattice pass
-//           over the bricks without force
-//   join forces -> s0: spread, lattice pass over the flagged bricks
-//   join s4 -> s0: moments at the flagged bricks, interpolation + advance.
+//   s0: flag the force bricks of this step (from the marker positions), then
+//       the lattice pass over the bricks without force
+//   fork -> s1 membrane | s2 Morse | s3 fibrin | s0 bonds
+//   join -> s0: spread, lattice pass over the flagged bricks, moments at the
+//       flagged bricks, interpolation + advance.
+// The force kernels are latency-bound and leave most of the GPU idle, but run
+// beside the lattice pass they were starved of SMs (the membrane pass took
+// three times as long), so the lattice pass runs first, alone.
 // Without markers: the lattice pass over everything, then the step close.
 static int enqueue_step(pfgpu_job* j) {
   Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
@@ -422,14 +424,12 @@ static int enqueue_step(pfgpu_job* j) {
     return PFGPU_OK;
   }
   CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0));
-  launches++;
+  CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, j->s0));
+  launches += 2;
   CK(cudaEventRecord(j->ev_fork, j->s0));
   CK(cudaStreamWaitEvent(j->s1, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s2, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s3, j->ev_fork, 0));
-  CK(cudaStreamWaitEvent(j->s4, j->ev_fork, 0));
-  CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, j->s4));
-  launches++;
   if (Pl) {
     CK(membrane_forces(*Pl, j->precision, j->ctl, j->s1));
     launches++;
@@ -454,8 +454,6 @@ static int enqueue_step(pfgpu_job* j) {
   CK(cudaStreamWaitEvent(j->s0, j->ev3, 0));
   CK(spread_markers(j->L, Pl, Fb, j->ctl, j->s0));
   CK(lattice_step_part(j->L, j->ctl, 2, bins, ncells, j->s0));
-  CK(cudaEventRecord(j->ev4, j->s4));
-  CK(cudaStreamWaitEvent(j->s0, j->ev4, 0));
   CK(lattice_moments_active(j->L, j->ctl, j->s0));
   CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
   launches += 4;
@@ -574,12 +572,10 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(cudaStreamCreateWithPriority(&j->s1, cudaStreamNonBlocking, prio_high));
   CKJ(cudaStreamCreateWithPriority(&j->s2, cudaStreamNonBlocking, prio_high));
   CKJ(cudaStreamCreateWithPriority(&j->s3, cudaStreamNonBlocking, prio_high));
-  CKJ(cudaStreamCreateWithPriority(&j->s4, cudaStreamNonBlocking, prio_low));
   CKJ(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev1, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev2, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev3, cudaEventDisableTiming));
-  CKJ(cudaEventCreateWithFlags(&j->ev4, cudaEventDisableTiming));
   // lattice
   Lattice& L = j->L;
   L.precision = precision;
