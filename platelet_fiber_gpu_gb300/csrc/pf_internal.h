@@ -116,6 +116,7 @@ struct Platelets {
   // membrane scratch (Real)
   void *nN = nullptr, *nelem = nullptr, *S = nullptr, *km = nullptr;
   double* SV = nullptr;  // [P][2]
+  bool mem_items = false;  // FP32 membrane through the item-parallel kernel
   // receptors
   int *rec_tri = nullptr, *rec_state = nullptr, *vwf = nullptr;
   float *r1 = nullptr, *r2 = nullptr;
@@ -181,6 +182,9 @@ bool morse_uses_cells(const PlateletConst& k);
 cudaError_t sort_cell_bins(Platelets& Pl, Control* ctl, cudaStream_t st);
 
 int membrane_threads();
+// whether the FP32 membrane pass of these platelets runs item-parallel
+// (shared-memory fit; PFGPU_MEMBRANE_PER_VERTEX=1 turns it off)
+bool membrane_items(const PlateletConst& k);
 // sets the message pfgpu_last_error returns; returns code
 int report_error(int code, const char* msg);
 

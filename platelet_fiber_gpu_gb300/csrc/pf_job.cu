@@ -54,10 +54,11 @@ struct pfgpu_job {
   Control* ctl = nullptr;
   unsigned* done_blocks = nullptr;
   double* scratch4 = nullptr;
-  // s0: critical path (flags, lattice passes, bonds, spreading, moments,
-  // interpolation); s1-s3: membrane, Morse, fibrin
-  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  // s0: flags, bonds, then the critical path after the forces (spreading,
+  // flagged lattice pass, moments, interpolation); s1-s3: membrane, Morse,
+  // fibrin; sL (low priority): the lattice pass over the force-free bricks
+  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr, sL = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev_flag = nullptr, evL = nullptr;
   cudaGraphExec_t graph = nullptr;
   double detach_rate = 0;
   uint64_t seed = 0;
@@ -89,10 +90,10 @@ static void destroy(pfgpu_job* j) {
   if (!j) return;
   if (j->graph) cudaGraphExecDestroy(j->graph);
   for (void* p : j->allocs) cudaFree(p);
-  cudaStream_t ss[4] = {j->s0, j->s1, j->s2, j->s3};
+  cudaStream_t ss[5] = {j->s0, j->s1, j->s2, j->s3, j->sL};
   for (cudaStream_t s : ss)
     if (s) cudaStreamDestroy(s);
-  cudaEvent_t ee[4] = {j->ev_fork, j->ev1, j->ev2, j->ev3};
+  cudaEvent_t ee[6] = {j->ev_fork, j->ev1, j->ev2, j->ev3, j->ev_flag, j->evL};
   for (cudaEvent_t e : ee)
     if (e) cudaEventDestroy(e);
   delete j;
@@ -401,14 +402,17 @@ static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
 }
 
 // One coupled step.  With markers:
-//   s0: flag the force bricks of this step (from the marker positions), then
-//       the lattice pass over the bricks without force
-//   fork -> s1 membrane | s2 Morse | s3 fibrin | s0 bonds
+//   fork -> s1 membrane | s2 Morse | s3 fibrin
+//           s0 flag the force bricks of this step (from the marker
+//              positions), then bonds
+//           sL (after the flags) the lattice pass over the bricks without
+//              force
 //   join -> s0: spread, lattice pass over the flagged bricks, moments at the
 //       flagged bricks, interpolation + advance.
-// The force kernels are latency-bound and leave most of the GPU idle, but run
-// beside the lattice pass they were starved of SMs (the membrane pass took
-// three times as long), so the lattice pass runs first, alone.
+// The force kernels are latency-bound and occupy few SMs; the memory-bound
+// lattice pass fills the rest.  It runs at low stream priority, so the force
+// kernels' blocks, enqueued first, are dispatched before its blocks take the
+// SMs.
 // Without markers: the lattice pass over everything, then the step close.
 static int enqueue_step(pfgpu_job* j) {
   Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
@@ -423,13 +427,14 @@ static int enqueue_step(pfgpu_job* j) {
     j->launches_per_step = 2;
     return PFGPU_OK;
   }
-  CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0));
-  CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, j->s0));
-  launches += 2;
   CK(cudaEventRecord(j->ev_fork, j->s0));
   CK(cudaStreamWaitEvent(j->s1, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s2, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s3, j->ev_fork, 0));
+  CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0));
+  CK(cudaEventRecord(j->ev_flag, j->s0));
+  CK(cudaStreamWaitEvent(j->sL, j->ev_flag, 0));
+  launches += 2;
   if (Pl) {
     CK(membrane_forces(*Pl, j->precision, j->ctl, j->s1));
     launches++;
@@ -446,9 +451,13 @@ static int enqueue_step(pfgpu_job* j) {
     CK(fibrin_forces(*Fb, j->precision, j->ctl, j->s3));
     launches++;
   }
+  CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, j->sL));
+  launches++;
+  CK(cudaEventRecord(j->evL, j->sL));
   CK(cudaEventRecord(j->ev1, j->s1));
   CK(cudaEventRecord(j->ev2, j->s2));
   CK(cudaEventRecord(j->ev3, j->s3));
+  CK(cudaStreamWaitEvent(j->s0, j->evL, 0));
   CK(cudaStreamWaitEvent(j->s0, j->ev1, 0));
   CK(cudaStreamWaitEvent(j->s0, j->ev2, 0));
   CK(cudaStreamWaitEvent(j->s0, j->ev3, 0));
@@ -572,6 +581,9 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(cudaStreamCreateWithPriority(&j->s1, cudaStreamNonBlocking, prio_high));
   CKJ(cudaStreamCreateWithPriority(&j->s2, cudaStreamNonBlocking, prio_high));
   CKJ(cudaStreamCreateWithPriority(&j->s3, cudaStreamNonBlocking, prio_high));
+  CKJ(cudaStreamCreateWithPriority(&j->sL, cudaStreamNonBlocking, prio_low));
+  CKJ(cudaEventCreateWithFlags(&j->ev_flag, cudaEventDisableTiming));
+  CKJ(cudaEventCreateWithFlags(&j->evL, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev1, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev2, cudaEventDisableTiming));
@@ -633,6 +645,7 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
     j->has_pl = true;
     rc = build_platelets(j, s);
     if (rc) return fail(rc);
+    j->Pl.mem_items = membrane_items(j->Pl.k);
     CKJ(bin_elements(j->Pl, j->ctl, j->s0));
   }
   if (s->n_fib > 0) {

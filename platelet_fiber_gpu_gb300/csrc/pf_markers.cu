@@ -124,6 +124,78 @@ __device__ __forceinline__ void interp_one(const LatticeConst& lk, const R4<R>* 
       }
 }
 
+// FP32 stencil as four fixed slots per axis (base + {-1..2}): a slot the
+// variable-length stencil leaves out has weight zero and a clamped in-range
+// node, so the fully unrolled 4x4x4 gather issues all 64 loads at once and
+// adds the same non-zero terms in the same order (a zero term leaves a float
+// sum unchanged).
+__device__ __forceinline__ void axis4(double x, double inv_dx, int n, int wrap, int node[4], float w[4]) {
+  const double r = x * inv_dx;
+  const double fb = floor(r);
+  const int base = (int)fb;
+  const float fr = (float)(r - fb);
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const float dd = fr - (float)(s - 1);
+    float ws = fabsf(dd) < 2.f ? 0.25f * (1.f + cospif(0.5f * dd)) : 0.f;
+    int nd = base + s - 1;
+    if (nd < 0 || nd >= n) {
+      if (wrap) {
+        nd = wrapi(nd, n);
+      } else {
+        nd = nd < 0 ? 0 : n - 1;
+        ws = 0.f;
+      }
+    }
+    node[s] = nd;
+    w[s] = ws;
+  }
+}
+template <>
+__device__ __forceinline__ void spread_one<float>(const LatticeConst& lk, R4<float>* Fc, double x, double y,
+                                                  double z, float Fx, float Fy, float Fz) {
+  int nxa[4], nya[4], nza[4];
+  float wx[4], wy[4], wz[4];
+  const double inv = 1.0 / (double)lk.dxf;
+  axis4(x, inv, lk.nx, lk.ibm_wrap[0], nxa, wx);
+  axis4(y, inv, lk.ny, lk.ibm_wrap[1], nya, wy);
+  axis4(z, inv, lk.nz, 0, nza, wz);
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const size_t row = (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const float delta = wx[a] * wy[b] * wz[c];
+        if (delta != 0.f) atomic_add3(Fc, row + nxa[a], Fx * delta, Fy * delta, Fz * delta);
+      }
+    }
+}
+template <>
+__device__ __forceinline__ void interp_one<float>(const LatticeConst& lk, const R4<float>* ubuf, double x, double y,
+                                                  double z, float& ax, float& ay, float& az) {
+  int nxa[4], nya[4], nza[4];
+  float wx[4], wy[4], wz[4];
+  const double inv = 1.0 / (double)lk.dxf;
+  axis4(x, inv, lk.nx, lk.ibm_wrap[0], nxa, wx);
+  axis4(y, inv, lk.ny, lk.ibm_wrap[1], nya, wy);
+  axis4(z, inv, lk.nz, 0, nza, wz);
+  ax = 0.f; ay = 0.f; az = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const size_t row = (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const float delta = wx[a] * wy[b] * wz[c];
+        const R4<float> u = ubuf[row + nxa[a]];
+        ax += u.y * delta; ay += u.z * delta; az += u.w * delta;
+      }
+    }
+}
+
 // ---------------------------------------------------------------- spreading
 // One thread per marker: total element force (membrane + Morse + bonds, kept
 // for the element output) or fibrin force, onto the current force buffer.
@@ -1129,6 +1201,405 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
   }
 }
 
+// FP32 membrane pass with the per-vertex loops split into items: one CTA of
+// kMem32Threads per platelet, every intermediate in shared memory.
+//   items: (vertex v, j-th triangle of v) for the curvature trace and the
+//   area/volume gradient, (vertex v, j-th ring neighbour) for the bending
+//   geometry; each item writes its own slot and the per-vertex sums run over
+//   the slots in j order, so the result does not depend on scheduling.
+// Arithmetic differs from membrane_k<float> in the rounding only:
+//   - tangents a1 = dx/ds, a3 = dx/dt of the 6-node element whose mid-side
+//     nodes sit at the side midpoints are exactly c1 - c0 and c2 - c0;
+//   - the curvature tensor is used through its trace, tr(A) with
+//     A^T = M^-1 [a2 a4 0]^T, M = rows (a1, a3, n), by the adjugate:
+//     tr = (a2 . (a3 x n) + a4 . (n x a1)) / det M;
+//   - the circumcentre of (xi, xj, x2) is solved relative to xi, where the
+//     right-hand side is -|r|^2/2 for the two edges and 0 for the normal.
+constexpr int kMem32Threads = 512;
+constexpr int kMem32Slots = 10;  // triangles / ring neighbours per vertex
+
+struct Mem32Layout {
+  int cap;  // item slots: 3 T (one per triangle corner)
+  size_t pos, fs, nel, sst, nN, km, res, off, cnt, tri, item, itri, bytes;
+  __host__ __device__ Mem32Layout(const PlateletConst& k) {
+    cap = 3 * k.T;
+    size_t o = 0;
+    auto take = [&](size_t n, size_t sz) {
+      const size_t at = o;
+      o += (n * sz + 15) & ~(size_t)15;
+      return at;
+    };
+    pos = take((size_t)k.E, sizeof(float4));
+    fs = take((size_t)3 * k.E, sizeof(float));
+    nel = take((size_t)3 * k.T, sizeof(float));
+    sst = take((size_t)k.T, sizeof(float));
+    nN = take((size_t)3 * k.NN, sizeof(float));
+    km = take((size_t)k.Em, sizeof(float));
+    res = take((size_t)6 * cap, sizeof(float));
+    off = take((size_t)k.Em + 1, sizeof(int));
+    cnt = take((size_t)k.NN, sizeof(int));
+    tri = take((size_t)6 * k.T, sizeof(int));
+    item = take((size_t)cap, sizeof(int));
+    itri = take((size_t)cap, sizeof(int));
+    bytes = o;
+  }
+};
+
+__device__ __forceinline__ void cross3(const float a[3], const float b[3], float c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ float dot3(const float a[3], const float b[3]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+__device__ __forceinline__ float len3(const float a[3]) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ void ld3(const float4* p, int e, float c[3]) {
+  const float4 v = p[e];
+  c[0] = v.x; c[1] = v.y; c[2] = v.z;
+}
+// Heron's formula; the product is clamped at zero (a right triangle whose
+// hypotenuse equals a leg in floating point has a zero factor).
+__device__ __forceinline__ float heron(float l1, float l2, float l3) {
+  const float pe = 0.5f * (l1 + l2 + l3);
+  return sqrtf(fmaxf(0.f, pe * (pe - l1) * (pe - l2) * (pe - l3)));
+}
+
+__global__ void __launch_bounds__(kMem32Threads, 2)
+    membrane32_k(PlateletConst k, const double* X, const double* Y, const double* RY, const double* Z,
+                 const int* tri, const int* node_ntri, const int* node_tri, const int* vert_local, const int* ring,
+                 const int* sp_ptr, const int* sp_nbr, const double* sp_L0, const double* S0,
+                 const double* S0_all, const double* V0, float* kmv, double* SV, float* Fmem, Control* ctl) {
+  if (ctl->done) return;
+  constexpr int NT = kMem32Threads, NW = NT / 32;
+  const int p = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int E = k.E, Em = k.Em, T = k.T, NN = k.NN, PE = k.P * k.E;
+  const int base = p * E;
+  const float invF0 = 1.f / k.f0;
+  const Mem32Layout lay(k);
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* s_pos = reinterpret_cast<float4*>(smem + lay.pos);
+  float* s_fs = reinterpret_cast<float*>(smem + lay.fs);
+  float* s_nel = reinterpret_cast<float*>(smem + lay.nel);
+  float* s_sst = reinterpret_cast<float*>(smem + lay.sst);
+  float* s_nN = reinterpret_cast<float*>(smem + lay.nN);
+  float* s_km = reinterpret_cast<float*>(smem + lay.km);
+  float* s_res = reinterpret_cast<float*>(smem + lay.res);
+  int* s_off = reinterpret_cast<int*>(smem + lay.off);
+  int* s_cnt = reinterpret_cast<int*>(smem + lay.cnt);
+  int* s_tri = reinterpret_cast<int*>(smem + lay.tri);
+  int* s_item = reinterpret_cast<int*>(smem + lay.item);
+  int* s_itri = reinterpret_cast<int*>(smem + lay.itri);
+  const int cap = lay.cap;
+  float* r_tr = s_res;              // curvature trace of item
+  float* r_av = s_res + cap;        // area/volume force of item, 3 components
+  float* r_area = s_res + 4 * cap;  // bending: mixed area of the item's sector
+  float* r_w = s_res + 5 * cap;     // bending: 0.5 (cot alpha + cot beta)
+  __shared__ double s_da[NW], s_db[NW];
+  __shared__ int s_di[NW], s_ws[NW];
+  __shared__ int s_wall_idx, s_total;
+  __shared__ float s_wall_f;
+  __shared__ double s_Sall, s_V;
+
+  // phase 0: positions relative to element 0, the lowest element, node
+  // triangle counts and triangles staged, per-thread sums of the vertex
+  // triangle counts (a contiguous chunk of vertices per thread)
+  const double ox = X[base], oy = Y[base], oz = Z[base], ory = RY[base];
+  double zmin = 1e300;
+  int imin = 0x7fffffff;
+  for (int e = tid; e < E; e += NT) {
+    const double zz = Z[base + e];
+    s_pos[e] = make_float4((float)(X[base + e] - ox), (float)(Y[base + e] - oy), (float)(zz - oz),
+                           (float)(RY[base + e] - ory));
+    if (zz < zmin) { zmin = zz; imin = e; }  // e ascending: first index of the minimum
+  }
+  for (int q = tid; q < NN; q += NT) s_cnt[q] = node_ntri[q];
+  for (int i = tid; i < 6 * T; i += NT) s_tri[i] = tri[i];
+  const int chunk = (Em + NT - 1) / NT;
+  const int v0 = min(Em, tid * chunk), v1 = min(Em, v0 + chunk);
+  int mine = 0;
+  for (int v = v0; v < v1; ++v) mine += node_ntri[v];
+  int incl = mine;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double z2 = __shfl_xor_sync(0xffffffffu, zmin, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, imin, o);
+    if (z2 < zmin || (z2 == zmin && i2 < imin)) { zmin = z2; imin = i2; }
+  }
+  if (lane == 0) { s_da[wid] = zmin; s_di[wid] = imin; }
+  if (lane == 31) s_ws[wid] = incl;
+  __syncthreads();
+  if (tid == 0) {
+    double zm = s_da[0];
+    int im = s_di[0];
+    for (int w = 1; w < NW; ++w)
+      if (s_da[w] < zm || (s_da[w] == zm && s_di[w] < im)) { zm = s_da[w]; im = s_di[w]; }
+    s_wall_idx = -1;
+    s_wall_f = 0.f;
+    if ((k.mask & PF_MEM_WALL) && E > 0 && zm <= 0.02) {
+      s_wall_idx = im;
+      s_wall_f = (float)(5e-4 * 2000 * exp(-2000 * zm) / (1 - exp(-2000 * zm)) / (double)k.f0);
+    }
+  }
+  // exclusive offsets of this thread's vertices: earlier warps' totals plus
+  // the inclusive scan within the warp, less this thread's own sum
+  {
+    int before = 0, total = 0;
+    for (int w = 0; w < NW; ++w) {
+      const int s = s_ws[w];
+      before += w < wid ? s : 0;
+      total += s;
+    }
+    int run = before + incl - mine;
+    for (int v = v0; v < v1; ++v) {
+      s_off[v] = run;
+      run += s_cnt[v];
+    }
+    if (tid == 0) { s_off[Em] = total; s_total = total; }
+  }
+  const bool surface = (k.mask & (PF_MEM_AREAVOL | PF_MEM_BEND)) != 0;
+  __syncthreads();
+  if (surface && s_total > cap) {  // a vertex listed in more triangles than it has corners
+    if (tid == 0) atomicOr(&ctl->err, ERR_MEMBRANE_SIZE);
+    return;
+  }
+
+  // phase 1: springs on RY plus the wall force (sem_kernel.cu:355-389);
+  // triangle normals, strains, FP64 area and volume sums; the item table
+  const int wall = s_wall_idx;
+  for (int e = tid; e < E; e += NT) {
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    if (e == wall && e != 0) fz = s_wall_f;
+    if (k.mask & PF_MEM_SPRING) {
+      const float4 pe = s_pos[e];
+      for (int q = sp_ptr[e]; q < sp_ptr[e + 1]; ++q) {
+        const float4 pn = s_pos[sp_nbr[q]];
+        const float d1 = pn.x - pe.x, d2 = pn.w - pe.w, d3 = pn.z - pe.z;
+        const float r = sqrtf(d1 * d1 + d2 * d2 + d3 * d3);
+        const float fc = k.kspring * (r - (float)sp_L0[q]) / r * invF0;
+        fx += fc * d1;
+        fy += fc * d2;
+        fz += fc * d3;
+      }
+    }
+    if (e == wall && e == 0) fz += s_wall_f;
+    s_fs[3 * e] = fx;
+    s_fs[3 * e + 1] = fy;
+    s_fs[3 * e + 2] = fz;
+  }
+  if (!surface) {
+    __syncthreads();
+    for (int e = tid; e < E; e += NT) {
+      Fmem[base + e] = s_fs[3 * e];
+      Fmem[PE + base + e] = s_fs[3 * e + 1];
+      Fmem[2 * PE + base + e] = s_fs[3 * e + 2];
+    }
+    if (tid == 0) { SV[2 * p] = 0; SV[2 * p + 1] = 0; }
+    return;
+  }
+  double pa = 0, pv = 0;
+  for (int t = tid; t < T; t += NT) {
+    const int* nd = s_tri + 6 * t;
+    float c0[3], c1[3], c2[3], e12[3], e13[3], n[3];
+    ld3(s_pos, nd[0], c0); ld3(s_pos, nd[1], c1); ld3(s_pos, nd[2], c2);
+    for (int i = 0; i < 3; ++i) { e12[i] = c1[i] - c0[i]; e13[i] = c2[i] - c0[i]; }
+    cross3(e12, e13, n);
+    const float nn = len3(n);
+    const float ninv = -1.f / nn;
+    for (int i = 0; i < 3; ++i) n[i] *= ninv;
+    const float St = 0.5f * nn;
+    const float S0e = (float)S0[(size_t)p * T + t];
+    s_sst[t] = (St - S0e) / S0e;
+    s_nel[3 * t] = n[0]; s_nel[3 * t + 1] = n[1]; s_nel[3 * t + 2] = n[2];
+    float cc[3];
+    for (int i = 0; i < 3; ++i) cc[i] = (1.f / 3.f) * (c0[i] + c1[i] + c2[i]);
+    pa += (double)St;
+    pv += (double)((1.f / 3.f) * dot3(cc, n) * St);
+  }
+  for (int v = tid; v < Em; v += NT) {
+    const int o = s_off[v], c = s_cnt[v];
+    for (int j = 0; j < c; ++j) {
+      s_item[o + j] = (v << 4) | j;
+      s_itri[o + j] = (node_tri[kMem32Slots * v + j] << 2) | vert_local[kMem32Slots * v + j];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    pa += __shfl_xor_sync(0xffffffffu, pa, o);
+    pv += __shfl_xor_sync(0xffffffffu, pv, o);
+  }
+  if (lane == 0) { s_da[wid] = pa; s_db[wid] = pv; }
+  __syncthreads();
+
+  // phase 2: nodal normals (mean of the element normals, normalised); the
+  // global area and volume
+  if (tid == 0) {
+    double a = 0, b = 0;
+    for (int w = 0; w < NW; ++w) { a += s_da[w]; b += s_db[w]; }
+    s_Sall = a;
+    s_V = b;
+    SV[2 * p] = a;
+    SV[2 * p + 1] = b;
+  }
+  for (int q = tid; q < NN; q += NT) {
+    const int cnt = s_cnt[q];
+    float a[3] = {0.f, 0.f, 0.f};
+    for (int j = 0; j < cnt; ++j) {
+      const int t = node_tri[kMem32Slots * q + j];
+      a[0] += s_nel[3 * t]; a[1] += s_nel[3 * t + 1]; a[2] += s_nel[3 * t + 2];
+    }
+    if (cnt > 0) {
+      // mean then normalise: the 1/cnt factor cancels in the direction
+      const float inv = rsqrtf(dot3(a, a));
+      for (int i = 0; i < 3; ++i) a[i] *= inv;
+    }
+    s_nN[3 * q] = a[0]; s_nN[3 * q + 1] = a[1]; s_nN[3 * q + 2] = a[2];
+  }
+  __syncthreads();
+
+  // phase 3: items -- curvature trace, area/volume gradient
+  // (sem_kernel.cu:1640-1749), bending geometry (:1499-1638)
+  const int total = s_total;
+  const float sglob = (float)((s_Sall - S0_all[p]) / S0_all[p]);
+  const float vglob = (float)((s_V - V0[p]) / V0[p]);
+  for (int it = tid; it < 3 * total; it += NT) {
+    const int kind = it >= total ? (it >= 2 * total ? 2 : 1) : 0;
+    const int i = it - kind * total;
+    if (kind == 0) {
+      const int t = s_itri[i] >> 2, li = s_itri[i] & 3;
+      const int* nd = s_tri + 6 * t;
+      float c0[3], c1[3], c2[3], a1[3], a3[3], a2[3] = {0.f, 0.f, 0.f}, a4[3] = {0.f, 0.f, 0.f};
+      ld3(s_pos, nd[0], c0); ld3(s_pos, nd[1], c1); ld3(s_pos, nd[2], c2);
+      for (int d = 0; d < 3; ++d) { a1[d] = c1[d] - c0[d]; a3[d] = c2[d] - c0[d]; }
+      const float s_ = li == 1 ? 1.f : 0.f, t_ = li == 2 ? 1.f : 0.f;
+      const float gs[6] = {4 * s_ + 4 * t_ - 3, 4 * s_ - 1, 0, -8 * s_ - 4 * t_ + 4, -4 * t_, 4 * t_};
+      const float gt[6] = {4 * t_ + 4 * s_ - 3, 0, 4 * t_ - 1, -4 * s_, -8 * t_ - 4 * s_ + 4, 4 * s_};
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const int nq = nd[q];
+        for (int d = 0; d < 3; ++d) {
+          const float nv = s_nN[3 * nq + d];
+          a2[d] += nv * gs[q];
+          a4[d] += nv * gt[q];
+        }
+      }
+      const int nl_ = li == 0 ? nd[0] : li == 1 ? nd[1] : nd[2];
+      const float nl[3] = {s_nN[3 * nl_], s_nN[3 * nl_ + 1], s_nN[3 * nl_ + 2]};
+      float q0[3], q1[3];
+      cross3(a3, nl, q0);
+      cross3(nl, a1, q1);
+      r_tr[i] = (dot3(a2, q0) + dot3(a4, q1)) / dot3(a1, q0);
+    } else if (kind == 1) {
+      const int t = s_itri[i] >> 2, li = s_itri[i] & 3;
+      const int* nd = s_tri + 6 * t;
+      float c0[3], c1[3], c2[3], L0[3], L1[3], Li[3], cc[3], n[3];
+      ld3(s_pos, nd[0], c0); ld3(s_pos, nd[1], c1); ld3(s_pos, nd[2], c2);
+      for (int d = 0; d < 3; ++d) {
+        L0[d] = c1[d] - c2[d];
+        L1[d] = c2[d] - c0[d];
+        Li[d] = li == 0 ? L0[d] : li == 1 ? L1[d] : c0[d] - c1[d];
+        cc[d] = (1.f / 3.f) * (c0[d] + c1[d] + c2[d]);
+        n[d] = s_nel[3 * t + d];
+      }
+      float f[3] = {0.f, 0.f, 0.f};
+      if (k.mask & PF_MEM_AREAVOL) {
+        float dS[3], lc[3], t01[3];
+        cross3(Li, n, dS);
+        cross3(L0, L1, t01);
+        cross3(Li, cc, lc);
+        const float fa = -0.5f * -k.ks * (s_sst[t] + sglob) * invF0;
+        const float fv = -k.kv * vglob * (1.f / 6.f) * invF0;
+        for (int d = 0; d < 3; ++d) f[d] = fa * dS[d] + fv * (t01[d] * (1.f / 3.f) + lc[d]);
+      }
+      r_av[i] = f[0]; r_av[cap + i] = f[1]; r_av[2 * cap + i] = f[2];
+    } else {
+      const int v = s_item[i] >> 4, j = s_item[i] & 15;
+      const int cnt = s_cnt[v];
+      const int* rg = ring + kMem32Slots * v;
+      const int jn = rg[j], jp = rg[j == 0 ? cnt - 1 : j - 1], jx = rg[j == cnt - 1 ? 0 : j + 1];
+      float xi[3], xj[3], x1[3], x2[3];
+      ld3(s_pos, v, xi); ld3(s_pos, jn, xj); ld3(s_pos, jp, x1); ld3(s_pos, jx, x2);
+      float rij[3], ri2[3], r2j[3], ri1[3], r1j[3];
+      for (int d = 0; d < 3; ++d) {
+        rij[d] = xi[d] - xj[d]; ri2[d] = xi[d] - x2[d]; r2j[d] = x2[d] - xj[d];
+        ri1[d] = xi[d] - x1[d]; r1j[d] = x1[d] - xj[d];
+      }
+      const float ai = dot3(rij, ri2), a2 = -dot3(ri2, r2j), aj = dot3(rij, r2j), a1 = -dot3(r1j, ri1);
+      // circumcentre ce = xi + w; h = xi - (xi+xj)/2, h2 = xi - (xi+x2)/2
+      float w[3], h[3], h2[3];
+      for (int d = 0; d < 3; ++d) { h[d] = 0.5f * rij[d]; h2[d] = 0.5f * ri2[d]; }
+      if (ai < 0) {
+        for (int d = 0; d < 3; ++d) w[d] = -0.5f * (rij[d] + ri2[d]);
+      } else if (a2 < 0) {
+        for (int d = 0; d < 3; ++d) w[d] = -h[d];
+      } else if (aj < 0) {
+        for (int d = 0; d < 3; ++d) w[d] = -h2[d];
+      } else {
+        float nrm[3], u0[3], u1[3];
+        cross3(rij, ri2, nrm);
+        cross3(ri2, nrm, u0);
+        cross3(nrm, rij, u1);
+        const float dinv = 1.f / dot3(rij, u0);
+        const float d0 = -0.5f * dot3(rij, rij) * dinv, d1 = -0.5f * dot3(ri2, ri2) * dinv;
+        for (int d = 0; d < 3; ++d) w[d] = d0 * u0[d] + d1 * u1[d];
+      }
+      float wh[3], wh2[3];
+      for (int d = 0; d < 3; ++d) { wh[d] = w[d] + h[d]; wh2[d] = w[d] + h2[d]; }
+      const float L3 = len3(w);
+      r_area[i] = heron(len3(h), len3(wh), L3) + heron(len3(h2), len3(wh2), L3);
+      // cot(acos(c)) = c / sqrt(1 - c^2), c the cosine of the angle at x1 / x2
+      const float ca = a1 * rsqrtf(dot3(ri1, ri1) * dot3(r1j, r1j));
+      const float cb = a2 * rsqrtf(dot3(ri2, ri2) * dot3(r2j, r2j));
+      r_w[i] = 0.5f * (ca * rsqrtf(1.f - ca * ca) + cb * rsqrtf(1.f - cb * cb));
+    }
+  }
+  __syncthreads();
+
+  // phase 4: mean curvature km = tr / 2 of the node average
+  for (int v = tid; v < Em; v += NT) {
+    const int o = s_off[v], cnt = s_cnt[v];
+    float tr = 0.f;
+    for (int j = 0; j < cnt; ++j) tr += r_tr[o + j];
+    const float km = cnt > 0 ? 0.5f * (tr / (float)cnt) : 0.f;
+    s_km[v] = km;
+    kmv[(size_t)p * Em + v] = km;
+  }
+  __syncthreads();
+
+  // phase 5: element force = springs + area/volume + bending
+  const float Kb = k.kbend * invF0;
+  for (int e = tid; e < E; e += NT) {
+    float fx = s_fs[3 * e], fy = s_fs[3 * e + 1], fz = s_fs[3 * e + 2];
+    if (e < Em) {
+      const int o = s_off[e], cnt = s_cnt[e];
+      if (k.mask & PF_MEM_AREAVOL)
+        for (int j = 0; j < cnt; ++j) {
+          fx += r_av[o + j];
+          fy += r_av[cap + o + j];
+          fz += r_av[2 * cap + o + j];
+        }
+      if (k.mask & PF_MEM_BEND) {
+        const int* rg = ring + kMem32Slots * e;
+        const float kmi = s_km[e];
+        float Ai = 0.f, sum = 0.f;
+        for (int j = 0; j < cnt; ++j) {
+          Ai += r_area[o + j];
+          sum += r_w[o + j] * (s_km[rg[j]] - kmi);
+        }
+        const float g = Kb * sum / Ai;
+        fx += g * s_nN[3 * e];
+        fy += g * s_nN[3 * e + 1];
+        fz += g * s_nN[3 * e + 2];
+      }
+    }
+    Fmem[base + e] = fx;
+    Fmem[PE + base + e] = fy;
+    Fmem[2 * PE + base + e] = fz;
+  }
+}
+
 // ---------------------------------------------------------------- Morse
 // Cell bins are sorted by element id after binning, so a cell list is the
 // same set in the same order as the oracle's counting sort, and the pair sums
@@ -1714,9 +2185,40 @@ __global__ void __launch_bounds__(1024) bonds_resolve_k(PlateletConst k, const d
 
 int membrane_threads() { return 512; }
 
+// The item-parallel FP32 kernel takes a platelet whose intermediates fit in
+// shared memory (about 150 KB for 600 elements, 796 six-node triangles);
+// PFGPU_MEMBRANE_PER_VERTEX=1 selects the per-vertex kernel instead.
+constexpr size_t kMem32MaxSmem = 200u << 10;
+bool membrane_items(const PlateletConst& k) {
+  if (getenv("PFGPU_MEMBRANE_PER_VERTEX")) return false;
+  return Mem32Layout(k).bytes <= kMem32MaxSmem && k.E < (1 << 26);
+}
+
+static cudaError_t launch_mem32(const PlateletConst& k, const double* X, const double* Y, const double* RY,
+                                const double* Z, const int* tri, const int* node_ntri, const int* node_tri,
+                                const int* vert_local, const int* ring, const int* sp_ptr, const int* sp_nbr,
+                                const double* sp_L0, const double* S0, const double* S0_all, const double* V0,
+                                float* km, double* SV, float* F, Control* ctl, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(membrane32_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMem32MaxSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  membrane32_k<<<k.P, kMem32Threads, Mem32Layout(k).bytes, st>>>(k, X, Y, RY, Z, tri, node_ntri, node_tri,
+                                                                 vert_local, ring, sp_ptr, sp_nbr, sp_L0, S0,
+                                                                 S0_all, V0, km, SV, F, ctl);
+  return cudaGetLastError();
+}
+
 cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st) {
   const PlateletConst& k = Pl.k;
   if (k.P == 0) return cudaSuccess;
+  if (precision != PF_PREC_FP64 && Pl.mem_items)
+    return launch_mem32(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri, Pl.vert_local, Pl.ring,
+                        Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0, Pl.S0_all, Pl.V0, (float*)Pl.km, Pl.SV,
+                        (float*)Pl.Fmem, ctl, st);
   if (precision == PF_PREC_FP64)
     membrane_k<double><<<k.P, 512, 0, st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
                                             Pl.vert_local, Pl.ring, Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0,
@@ -1739,6 +2241,9 @@ cudaError_t membrane_forces_raw(const PlateletConst& k, int precision, const dou
                                 const double* V0, void* nN, void* nelem, void* S, void* km, double* SV, void* F,
                                 Control* ctl, cudaStream_t st) {
   if (k.P == 0) return cudaSuccess;
+  if (precision != PF_PREC_FP64 && membrane_items(k))
+    return launch_mem32(k, X, Y, RY, Z, tri, node_ntri, node_tri, vert_local, ring, sp_ptr, sp_nbr, sp_L0, S0,
+                        S0_all, V0, (float*)km, SV, (float*)F, ctl, st);
   if (precision == PF_PREC_FP64)
     membrane_k<double><<<k.P, 512, 0, st>>>(k, X, Y, RY, Z, tri, node_ntri, node_tri, vert_local, ring, sp_ptr,
                                             sp_nbr, sp_L0, S0, S0_all, V0, (double*)nN, (double*)nelem, (double*)S,

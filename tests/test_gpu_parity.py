@@ -247,6 +247,49 @@ def test_row_staged_fp64_vs_oracle(gpu, monkeypatch):
         assert np.abs(r["Eg"][k] - r["Eo"][k]).max() < 1e-12
 
 
+def _stretched_membrane_scene():
+    """Platelets stretched about their centroids (3, 4, 5 % along x, y, z) so
+    that springs, area, volume and bending all carry force; Morse pairs,
+    bonds and fibrin off, so the element force after one step is the membrane
+    force at the initial positions."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small(n_fib=0, n_links=0, n_rec=0)
+    sc.morse = 0
+    for name, s in (("X", 1.03), ("RY", 1.04), ("Z", 1.05)):
+        a = np.asarray(getattr(sc, name), float).reshape(sc.n_platelets, sc.n_elem)
+        c = a.mean(axis=1, keepdims=True)
+        setattr(sc, name, (c + (a - c) * s).ravel())
+    sc.Y = sc.RY.copy()
+    return sc
+
+
+def test_fp32_membrane_kernels_vs_oracle(gpu, monkeypatch):
+    """FP32 membrane pass: the item-parallel kernel (default) and the
+    per-vertex kernel (PFGPU_MEMBRANE_PER_VERTEX=1) against the FP64 oracle
+    on stretched platelets; FP32 element forces and mean curvature within
+    1e-4 relative L2, FP64-summed area and volume within 1e-6."""
+    from oracle import binding as ob
+    sc = _stretched_membrane_scene()
+    o = ob.Oracle(sc)
+    o.step(1)
+    Fo, Mo = o.elements()["F"], o.membrane()
+    o.close()
+    assert np.linalg.norm(Fo) > 0
+    got = {}
+    for kern in ("items", "per_vertex"):
+        if kern == "per_vertex":
+            monkeypatch.setenv("PFGPU_MEMBRANE_PER_VERTEX", "1")
+        j = gpu.Job(sc, 1)
+        j.step(1, graph=False)
+        got[kern] = (j.elements()["F"], j.membrane())
+        j.close()
+    monkeypatch.delenv("PFGPU_MEMBRANE_PER_VERTEX")
+    for kern, (F, M) in got.items():
+        assert rel_l2(F, Fo) < 1e-4, kern
+        np.testing.assert_allclose(M["S_V"], Mo["S_V"], rtol=1e-6, err_msg=kern)
+        assert rel_l2(M["km"], Mo["km"]) < 1e-4, kern
+
+
 def test_cell_lists_bit_exact(gpu):
     from oracle import binding as ob
     from platelet_fiber_gpu_gb300 import workloads as W
