@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
 // (rho, u/C) of the nodes of the active bricks after this step's stream and
 // boundary conditions, with this step's force: input of the IBM interpolation
 // (the reference's velocity_density, LB_kernel.cu:1108-1199).
-template <class S, class R>
+template <class S, class R, bool FAST>
 __global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, const S* gA, const S* gB,
                                                               const R4<R>* FA, const R4<R>* FB, R4<R>* ubuf,
                                                               const int* lA, const int* lB, const Control* ctl) {
@@ -658,7 +658,8 @@ __global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, co
     if (x >= k.nx) continue;
     const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
     R g[Q];
-    gather<S, R>(k, gnew, x, y, z, g);
+    if constexpr (FAST) gather_fast<S, R>(k, gnew, x, y, z, g);
+    else gather<S, R>(k, gnew, x, y, z, g);
     R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
     ld_force<R>(Fc, n, Fx, Fy, Fz);
     R drho, ux, uy, uz;
@@ -856,7 +857,8 @@ cudaError_t moments_impl(Lattice& L, Control* ctl, cudaStream_t st) {
   int grid = sms * 8;
   const int need = (L.k.nbricks + kLbmBlock / 32 - 1) / (kLbmBlock / 32);
   if (grid > need) grid = need;
-  moments_active_k<S, R><<<grid, kLbmBlock, 0, st>>>(L.k, (const S*)L.g[0], (const S*)L.g[1],
+  auto kern = fast_lattice(L) ? moments_active_k<S, R, true> : moments_active_k<S, R, false>;
+  kern<<<grid, kLbmBlock, 0, st>>>(L.k, (const S*)L.g[0], (const S*)L.g[1],
                                                     (const R4<R>*)L.F[0], (const R4<R>*)L.F[1], (R4<R>*)L.ubuf,
                                                     L.list[0], L.list[1], ctl);
   return cudaGetLastError();
