@@ -45,6 +45,7 @@ enum : uint32_t {
   ERR_NONFINITE = 4u,
   ERR_MEMBRANE_SIZE = 8u,
   ERR_WAIT_TIMEOUT = 16u,  // a bounded wait on an mbarrier gave up
+  ERR_FAR_FLAGGED = 32u,   // a force brick lay in the far region (a marker moved over a node)
 };
 
 // Per-job device-resident control block: written by kernels, read by the host
@@ -60,6 +61,10 @@ struct Control {
   int pad;
   int nops_active[2];     // bond pass counters: operations, active receptors
   int occupied;           // Morse cells holding at least one element
+  // pipelined far-region lattice pass: the step it computes next, and
+  // whether that step is the first after an upload
+  int far_first;
+  long long far_step;
 };
 
 // ------------------------------------------------------------- Philox

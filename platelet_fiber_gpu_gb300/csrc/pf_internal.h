@@ -70,6 +70,10 @@ struct Lattice {
   // dilation in x and y: scratch of the brick flagging
   unsigned* mark = nullptr;
   unsigned* dil = nullptr;
+  // near region per step parity: bricks within one brick (x) and two rows
+  // (y, z) of a force brick of the previous step; the rest (far) is updated
+  // by the pipelined far pass while the previous step's tail runs
+  unsigned char* near[2] = {nullptr, nullptr};
   // reduced precision: spread/interpolate platelet elements through shared
   // per-platelet node boxes (1) or per marker with global atomics (0)
   int ibm_box = 0;
@@ -149,8 +153,15 @@ cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_de
 cudaError_t lattice_configure(Lattice& L);
 // part 0: the whole lattice; 1: bricks not flagged for this step's force
 // (may run while the forces are computed); 2: the flagged bricks (after the
-// spreading).  bin_count: Morse cell counters to clear (parts 0 and 2 only).
+// spreading); 3: the far region of step far_step (near[] clear); 4: the
+// unflagged bricks of the near region.  bin_count: Morse cell counters to
+// clear (parts 0 and 2 only).
 cudaError_t lattice_step_part(Lattice& L, Control* ctl, int part, int* bin_count, int ncells, cudaStream_t st);
+// near region: from this step's flags into near[next parity] (from_mark 0),
+// or from the occupancy bits into near[this parity] (from_mark 1)
+cudaError_t lattice_near(Lattice& L, Control* ctl, int from_mark, cudaStream_t st);
+// far pass counter: sync (far_step = step) or advance after a far pass
+cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st);
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
 // fIN [19][N], fOUT [19][N], rho [N], u [3][N], F [3][N] (double, device)
 cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* fIN, double* fOUT, double* rho,
@@ -166,8 +177,17 @@ cudaError_t bond_pass(Platelets& Pl, int precision, Control* ctl, cudaStream_t s
 cudaError_t mark_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, cudaStream_t st);
 // flags (and lists) the force bricks every marker's stencil can reach this
 // step, before any force exists; spread_markers then only adds forces
-cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st);
+// check_near: every flagged brick must lie in near[step parity] (pipelined
+// schedule), else ERR_FAR_FLAGGED
+cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st,
+                         bool check_near = false);
 cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st);
+// Reduced precision with per-marker spreading: each force part is spread
+// as soon as it exists (part 0: element membrane + Morse forces, 1: bond
+// forces, 2: fibrin forces) instead of spread_markers after all forces; the
+// position update then writes the element force totals.
+bool spread_split(const Lattice& L);
+cudaError_t spread_part(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, int part, cudaStream_t st);
 cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, double detach_rate,
                            uint64_t seed, unsigned* done_blocks, cudaStream_t st);
 cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st);

@@ -57,8 +57,13 @@ struct pfgpu_job {
   // s0: flags, bonds, then the critical path after the forces (spreading,
   // flagged lattice pass, moments, interpolation); s1-s3: membrane, Morse,
   // fibrin; sL (low priority): the lattice pass over the force-free bricks
-  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr, sL = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev_flag = nullptr, evL = nullptr;
+  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr, sL = nullptr, sF = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev_flag = nullptr, evL = nullptr,
+              ev_far = nullptr;
+  // pipelined schedule (PFGPU_PIPELINE=1): the far region of the next step
+  // is updated during this step (far_ready: the far pass of the current step
+  // is done)
+  bool pipeline = false, far_ready = false;
   cudaGraphExec_t graph = nullptr;
   double detach_rate = 0;
   uint64_t seed = 0;
@@ -90,10 +95,10 @@ static void destroy(pfgpu_job* j) {
   if (!j) return;
   if (j->graph) cudaGraphExecDestroy(j->graph);
   for (void* p : j->allocs) cudaFree(p);
-  cudaStream_t ss[5] = {j->s0, j->s1, j->s2, j->s3, j->sL};
+  cudaStream_t ss[6] = {j->s0, j->s1, j->s2, j->s3, j->sL, j->sF};
   for (cudaStream_t s : ss)
     if (s) cudaStreamDestroy(s);
-  cudaEvent_t ee[6] = {j->ev_fork, j->ev1, j->ev2, j->ev3, j->ev_flag, j->evL};
+  cudaEvent_t ee[7] = {j->ev_fork, j->ev1, j->ev2, j->ev3, j->ev_flag, j->evL, j->ev_far};
   for (cudaEvent_t e : ee)
     if (e) cudaEventDestroy(e);
   delete j;
@@ -405,15 +410,46 @@ static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
 //   fork -> s1 membrane | s2 Morse | s3 fibrin
 //           s0 flag the force bricks of this step (from the marker
 //              positions), then bonds
-//           sL (after the flags) the lattice pass over the bricks without
-//              force
+//           sL (after the flags) the lattice pass over the unflagged bricks
 //   join -> s0: spread, lattice pass over the flagged bricks, moments at the
 //       flagged bricks, interpolation + advance.
 // The force kernels are latency-bound and occupy few SMs; the memory-bound
 // lattice pass fills the rest.  It runs at low stream priority, so the force
 // kernels' blocks, enqueued first, are dispatched before its blocks take the
 // SMs.
+//
+// Pipelined (PFGPU_PIPELINE=1): the lattice splits into the near region of a
+// step -- bricks within one brick in x and two rows in y and z of a brick
+// flagged in the previous step -- and the far region.  No far brick is
+// flagged in this step or the previous one as long as no marker's base node
+// moves more than one node per step (the flagging checks it), and no far
+// node pulls from a flagged node of the previous step.  So the far region
+// of step t+1 depends only on the unflagged passes of step t, and its pass
+// runs beside step t's spreading, flagged-brick pass, moments and
+// interpolation:
+//   sL: lattice pass over the near, unflagged bricks of step t
+//   sF: near region of step t+1 (from the flags of step t), then, after
+//       the sL pass, the far pass of step t+1
+// Before the first pipelined step (after creation or a profile run) the far
+// pass of the current step runs alone (prologue), with its near region
+// taken from the occupancy bits.  On the 256x128x128 channel the far pass,
+// memory-bound, slows the latency-bound tail kernels it runs beside more
+// than it saves, so the serial schedule is the default.
+// Reduced precision spreads each force part as soon as it exists (membrane
+// and Morse forces on s1, bond forces on s0, fibrin forces on s3), so after
+// the join only the flagged-brick pass, the moments and the interpolation
+// remain.
 // Without markers: the lattice pass over everything, then the step close.
+static int far_prologue(pfgpu_job* j) {
+  if (!j->pipeline || j->far_ready || !(j->has_pl || j->has_fb)) return PFGPU_OK;
+  CK(lattice_far_counter(j->ctl, 1, j->s0));
+  CK(lattice_near(j->L, j->ctl, 1, j->s0));
+  CK(lattice_step_part(j->L, j->ctl, 3, nullptr, 0, j->s0));
+  CK(lattice_far_counter(j->ctl, 0, j->s0));
+  j->far_ready = true;
+  return PFGPU_OK;
+}
+
 static int enqueue_step(pfgpu_job* j) {
   Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
   Fibrin* Fb = j->has_fb ? &j->Fb : nullptr;
@@ -427,33 +463,62 @@ static int enqueue_step(pfgpu_job* j) {
     j->launches_per_step = 2;
     return PFGPU_OK;
   }
+  const bool pipe = j->pipeline;
   CK(cudaEventRecord(j->ev_fork, j->s0));
   CK(cudaStreamWaitEvent(j->s1, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s2, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s3, j->ev_fork, 0));
-  CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0));
+  CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0, pipe));
   CK(cudaEventRecord(j->ev_flag, j->s0));
   CK(cudaStreamWaitEvent(j->sL, j->ev_flag, 0));
   launches += 2;
+  if (pipe) {
+    CK(cudaStreamWaitEvent(j->sF, j->ev_flag, 0));
+    CK(lattice_near(j->L, j->ctl, 0, j->sF));
+    launches++;
+  }
+  // split: each force part is spread on its own stream as soon as it exists
+  const bool split = spread_split(j->L);
   if (Pl) {
     CK(membrane_forces(*Pl, j->precision, j->ctl, j->s1));
     launches++;
     if (Pl->k.morse && Pl->k.P * Pl->k.E) {
       CK(morse_forces(*Pl, j->precision, j->ctl, j->s2));
       launches += 2;  // bounds + pairs, or bin sort + pairs
+      CK(cudaEventRecord(j->ev2, j->s2));
+      if (split) CK(cudaStreamWaitEvent(j->s1, j->ev2, 0));
+    }
+    if (split) {
+      CK(spread_part(j->L, Pl, Fb, j->ctl, 0, j->s1));
+      launches++;
     }
     if (Pl->k.nrec) {
       CK(bond_pass(*Pl, j->precision, j->ctl, j->s0));
       launches += 2;
+      if (split) {
+        CK(spread_part(j->L, Pl, Fb, j->ctl, 1, j->s0));
+        launches++;
+      }
     }
   }
   if (Fb) {
     CK(fibrin_forces(*Fb, j->precision, j->ctl, j->s3));
     launches++;
+    if (split) {
+      CK(spread_part(j->L, Pl, Fb, j->ctl, 2, j->s3));
+      launches++;
+    }
   }
-  CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, j->sL));
+  CK(lattice_step_part(j->L, j->ctl, pipe ? 4 : 1, nullptr, 0, j->sL));
   launches++;
   CK(cudaEventRecord(j->evL, j->sL));
+  if (pipe) {
+    CK(cudaStreamWaitEvent(j->sF, j->evL, 0));
+    CK(lattice_step_part(j->L, j->ctl, 3, nullptr, 0, j->sF));
+    CK(lattice_far_counter(j->ctl, 0, j->sF));
+    CK(cudaEventRecord(j->ev_far, j->sF));
+    launches += 2;
+  }
   CK(cudaEventRecord(j->ev1, j->s1));
   CK(cudaEventRecord(j->ev2, j->s2));
   CK(cudaEventRecord(j->ev3, j->s3));
@@ -461,11 +526,15 @@ static int enqueue_step(pfgpu_job* j) {
   CK(cudaStreamWaitEvent(j->s0, j->ev1, 0));
   CK(cudaStreamWaitEvent(j->s0, j->ev2, 0));
   CK(cudaStreamWaitEvent(j->s0, j->ev3, 0));
-  CK(spread_markers(j->L, Pl, Fb, j->ctl, j->s0));
+  if (!split) {
+    CK(spread_markers(j->L, Pl, Fb, j->ctl, j->s0));
+    launches++;
+  }
   CK(lattice_step_part(j->L, j->ctl, 2, bins, ncells, j->s0));
   CK(lattice_moments_active(j->L, j->ctl, j->s0));
   CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
-  launches += 4;
+  launches += 3;
+  if (pipe) CK(cudaStreamWaitEvent(j->s0, j->ev_far, 0));
   j->launches_per_step = launches;
   return PFGPU_OK;
 }
@@ -492,7 +561,13 @@ static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
     CK(rec(t, 2, 0)); if (Pl && Pl->k.morse) CK(morse_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 2, 1));
     CK(rec(t, 3, 0)); if (Fb) CK(fibrin_forces(*Fb, j->precision, j->ctl, s)); CK(rec(t, 3, 1));
     CK(rec(t, 4, 0)); if (Pl && Pl->k.nrec) CK(bond_pass(*Pl, j->precision, j->ctl, s)); CK(rec(t, 4, 1));
-    CK(rec(t, 5, 0)); if (markers) CK(spread_markers(j->L, Pl, Fb, j->ctl, s)); CK(rec(t, 5, 1));
+    CK(rec(t, 5, 0));
+    if (markers && spread_split(j->L)) {
+      for (int part = 0; part < 3; ++part) CK(spread_part(j->L, Pl, Fb, j->ctl, part, s));
+    } else if (markers) {
+      CK(spread_markers(j->L, Pl, Fb, j->ctl, s));
+    }
+    CK(rec(t, 5, 1));
     CK(rec(t, 6, 0));
     if (markers) {
       CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, s));
@@ -506,6 +581,9 @@ static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
     CK(rec(t, 8, 1));
   }
   CK(cudaStreamSynchronize(s));
+  // these steps updated the whole lattice: the next pipelined step starts
+  // with its own far pass
+  j->far_ready = false;
   for (int ph = 0; ph < NPH; ++ph) ms[ph] = 0;
   for (int t = 0; t < nsteps; ++t)
     for (int ph = 0; ph < NPH; ++ph) {
@@ -535,7 +613,7 @@ size_t pfgpu_scene_device_bytes(const pf_scene* s, int precision) {
   const size_t N = (size_t)s->nx * s->ny * s->nz;
   const size_t sb = store_bytes(precision), rb = real_bytes(precision);
   const size_t nbricks = (size_t)((s->nx + kBrickX - 1) / kBrickX) * s->ny * s->nz;
-  size_t b = 2 * 19 * N * sb + 3 * N * 4 * rb + 6 * nbricks * 4;
+  size_t b = 2 * 19 * N * sb + 3 * N * 4 * rb + 6 * nbricks * 4 + 2 * nbricks;
   const size_t PE = (size_t)s->n_platelets * s->n_elem;
   b += PE * (4 * 8 + 6 * 8 + 3 * 8 + 6 * rb);
   b += (size_t)s->n_platelets * ((size_t)s->n_node * 3 + (size_t)s->n_tri * 4 + s->n_membrane) * rb;
@@ -582,6 +660,12 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(cudaStreamCreateWithPriority(&j->s2, cudaStreamNonBlocking, prio_high));
   CKJ(cudaStreamCreateWithPriority(&j->s3, cudaStreamNonBlocking, prio_high));
   CKJ(cudaStreamCreateWithPriority(&j->sL, cudaStreamNonBlocking, prio_low));
+  CKJ(cudaStreamCreateWithPriority(&j->sF, cudaStreamNonBlocking, prio_low));
+  CKJ(cudaEventCreateWithFlags(&j->ev_far, cudaEventDisableTiming));
+  {
+    const char* pl = getenv("PFGPU_PIPELINE");
+    j->pipeline = pl && strcmp(pl, "1") == 0;
+  }
   CKJ(cudaEventCreateWithFlags(&j->ev_flag, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->evL, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
@@ -612,6 +696,8 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(dalloc(j, &L.list[1], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.mark, (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.dil, (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.near[0], (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.near[1], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &j->ctl, 1));
   CKJ(dalloc(j, &j->done_blocks, 1));
   CKJ(dalloc(j, &j->scratch4, 4));
@@ -661,6 +747,10 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
 
 int pfgpu_job_step(pfgpu_job* j, int nsteps) {
   if (!j || nsteps < 0) return set_error(PFGPU_ERR_INVALID, "bad job or step count");
+  if (nsteps > 0) {
+    int rc = far_prologue(j);
+    if (rc) return rc;
+  }
   for (int i = 0; i < nsteps; ++i) {
     int rc = enqueue_step(j);
     if (rc) return rc;
@@ -685,6 +775,10 @@ int pfgpu_job_step_graph(pfgpu_job* j, int nsteps) {
     cudaGraphDestroy(g);
     CK(e);
   }
+  if (nsteps > 0) {
+    int rc = far_prologue(j);
+    if (rc) return rc;
+  }
   for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(j->graph, j->s0));
   CK(cudaStreamSynchronize(j->s0));
   return check_control(j);
@@ -694,6 +788,10 @@ int pfgpu_job_enqueue(pfgpu_job* j, int nsteps) {
   if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
   if (!j->graph) {
     int rc = pfgpu_job_step_graph(j, 0);
+    if (rc) return rc;
+  }
+  if (nsteps > 0) {
+    int rc = far_prologue(j);
     if (rc) return rc;
   }
   for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(j->graph, j->s0));

@@ -289,14 +289,26 @@ __device__ __forceinline__ void zero_bins(int* bin_count, int ncells, Control* c
 }
 
 // Direct-gather step over the lattice, one x-row segment of kLbmBlock nodes
-// per CTA, one force brick per warp.  skip_flagged: bricks flagged for this
-// step's force are left to lbm_list_k (they run after the spreading).
+// per CTA, one force brick per warp.  mode:
+//   kPassAll     every brick;
+//   kPassUnflag  bricks not flagged for this step's force (the flagged ones
+//                are left to lbm_list_k, after the spreading);
+//   kPassNear    unflagged bricks of the near region (near[par] set);
+//   kPassFar     the far region (near[par] clear) of step ctl->far_step,
+//                which may run while the previous step's spreading,
+//                flagged-brick pass and interpolation are still running: it
+//                takes its parity and first-step flag from far_step /
+//                far_first, and has no force (no far brick is flagged in
+//                this step or the previous one).
+enum : int { kPassAll = 0, kPassUnflag = 1, kPassNear = 4, kPassFar = 3 };
 template <class S, class R, bool FAST>
 __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
                                                         R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
-                                                        int ncells, int skip_flagged, Control* ctl) {
+                                                        int ncells, int mode, const unsigned char* nearA,
+                                                        const unsigned char* nearB, Control* ctl) {
   if (ctl->done) return;
-  const int par = (int)(ctl->step & 1);
+  const bool far = mode == kPassFar;
+  const int par = (int)((far ? ctl->far_step : ctl->step) & 1);
   const S* __restrict__ gin = par ? gB : gA;
   S* __restrict__ gout = par ? gA : gB;
   const R4<R>* Fc = par ? FB : FA;
@@ -307,17 +319,67 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
   const int bxw = x / kBrickX;
   const bool row_ok = bxw < k.nbx;
   const int brick = bxw + k.nbx * (y + k.ny * z);
-  const unsigned fc = row_ok ? flc[brick] : 0u;
   if (bin_count) {
     const size_t tid = (((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * blockDim.x +
                        threadIdx.x;
     zero_bins(bin_count, ncells, ctl, tid, (size_t)gridDim.x * gridDim.y * gridDim.z * blockDim.x);
   }
-  if (skip_flagged && fc) return;  // whole warp: one brick
+  // whole warp: one brick
+  if (mode == kPassNear || far) {
+    const unsigned char* nr = par ? nearB : nearA;
+    const bool is_near = row_ok && nr[brick] != 0;
+    if (is_near == far) return;
+  }
+  if (far) {
+    if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 0u, 0u, ctl->far_first);
+    return;
+  }
+  const unsigned fc = row_ok ? flc[brick] : 0u;
+  if (mode != kPassAll && fc) return;
   const unsigned fp = row_ok ? flp[brick] : 0u;
   if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, fc, fp, ctl->first);
   __syncwarp();
   if ((threadIdx.x & 31) == 0 && fp) flp[brick] = 0;
+}
+
+// Near region of a step from a per-brick word array (non-zero: set): every
+// brick within rx bricks in x and ry, rz rows in y, z of a set brick, all
+// axes wrapped (a superset is always safe).  src_mark: from the occupancy
+// bits into near[step parity] (before the first pipelined step, with the
+// flags' own reach added); else from this step's flags into near[next
+// parity].
+__global__ void __launch_bounds__(256) near_bricks_k(LatticeConst k, const unsigned* flA, const unsigned* flB,
+                                                     const unsigned* mark, unsigned char* nearA,
+                                                     unsigned char* nearB, int src_mark, int rx, int ry, int rz,
+                                                     const Control* ctl) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= k.nbricks) return;
+  const int par = (int)(ctl->step & 1);
+  const unsigned* src = src_mark ? mark : (par ? flB : flA);
+  unsigned char* dst = (src_mark ? par : par ^ 1) ? nearB : nearA;
+  const int bx = w % k.nbx, y = (w / k.nbx) % k.ny, z = w / (k.nbx * k.ny);
+  unsigned acc = 0;
+  for (int dz = -rz; dz <= rz && !acc; ++dz) {
+    const int zz = wrapi(z + dz, k.nz);
+    for (int dy = -ry; dy <= ry; ++dy) {
+      const int yy = wrapi(y + dy, k.ny);
+      const unsigned* row = src + (size_t)k.nbx * (yy + (size_t)k.ny * zz);
+      for (int dx = -rx; dx <= rx; ++dx) acc |= row[wrapi(bx + dx, k.nbx)];
+    }
+  }
+  dst[w] = acc != 0u;
+}
+
+// far_sync: the next far pass computes the current step (before the first
+// pipelined step); far_close: after a far pass.
+__global__ void far_counter_k(Control* ctl, int sync) {
+  if (sync) {
+    ctl->far_step = ctl->step;
+    ctl->far_first = ctl->first;
+  } else {
+    ctl->far_step = ctl->far_step + 1;
+    ctl->far_first = 0;
+  }
 }
 
 // The flagged bricks of this step (list[par]), one warp per brick.
@@ -846,7 +908,7 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
   dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);
   auto kern = fast_lattice(L) ? lbm_step_k<S, R, true> : lbm_step_k<S, R, false>;
   kern<<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
-                                   L.flags[0], L.flags[1], bin_count, ncells, part == 1 ? 1 : 0, ctl);
+                                   L.flags[0], L.flags[1], bin_count, ncells, part, L.near[0], L.near[1], ctl);
   return cudaGetLastError();
 }
 template <class S, class R>
@@ -931,6 +993,21 @@ cudaError_t lattice_step_part(Lattice& L, Control* ctl, int part, int* bin_count
     case PF_PREC_FP16: return step_impl<__half, float>(L, ctl, part, bin_count, ncells, st);
   }
   return cudaErrorInvalidValue;
+}
+cudaError_t lattice_near(Lattice& L, Control* ctl, int from_mark, cudaStream_t st) {
+  const int nb = L.k.nbricks;
+  // from this step's flags: one brick in x, two rows in y and z (a marker's
+  // base node moves at most one node per step, and a far node's pull must
+  // not reach a flagged node); from the occupancy bits: plus the flags'
+  // own reach (two nodes: one brick, two rows)
+  const int rx = from_mark ? 2 : 1, ry = from_mark ? 4 : 2, rz = from_mark ? 4 : 2;
+  near_bricks_k<<<(nb + 255) / 256, 256, 0, st>>>(L.k, L.flags[0], L.flags[1], L.mark, L.near[0], L.near[1],
+                                                  from_mark, rx, ry, rz, ctl);
+  return cudaGetLastError();
+}
+cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st) {
+  far_counter_k<<<1, 1, 0, st>>>(ctl, sync);
+  return cudaGetLastError();
 }
 cudaError_t lattice_configure(Lattice& L) {
   switch (L.precision) {

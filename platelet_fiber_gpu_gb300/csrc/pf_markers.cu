@@ -225,6 +225,22 @@ __global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R
   spread_one<R>(lk, Fc, x, y, z, (R)fx, (R)fy, (R)fz);
 }
 
+// FP32 spreading of one force part as soon as it exists: n markers at
+// (X, Y, Z) with force Fa (float, may be null) + Fd / div (double, may be
+// null), components n apart; markers whose part is zero add nothing.
+__global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA, float4* FB, int n,
+                                                     const double* X, const double* Y, const double* Z,
+                                                     const float* Fa, const double* Fd, double div, Control* ctl) {
+  if (ctl->done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double fx = 0, fy = 0, fz = 0;
+  if (Fa) { fx = (double)Fa[i]; fy = (double)Fa[n + i]; fz = (double)Fa[2 * n + i]; }
+  if (Fd) { fx += Fd[i] / div; fy += Fd[n + i] / div; fz += Fd[2 * n + i] / div; }
+  if (fx == 0 && fy == 0 && fz == 0) return;
+  spread_one<float>(lk, (ctl->step & 1) ? FB : FA, X[i], Y[i], Z[i], (float)fx, (float)fy, (float)fz);
+}
+
 // Force bricks of this step: every brick holding a lattice node within two
 // nodes (per axis) of a marker's base node -- floor(x/dx) as the FP64
 // stencils form it, floor(x * (1/dx)) as the FP32 stencil does -- which
@@ -309,13 +325,19 @@ __global__ void __launch_bounds__(256) dilate_xy_k(LatticeConst lk, const unsign
 }
 
 // dilates in z, flags and lists the bricks (list[par], active_count[par]),
-// and clears the occupancy bits for the next step
+// and clears the occupancy bits for the next step.  With the near region of
+// the pipelined schedule (nearA/B): a flagged brick outside it was updated
+// without force by the far pass, an error (a marker moved more than one node
+// in one step).
 __global__ void __launch_bounds__(256) flag_bricks_k(LatticeConst lk, const unsigned* dil, unsigned* mark,
-                                                     unsigned* flA, unsigned* flB, int* lA, int* lB, Control* ctl) {
+                                                     unsigned* flA, unsigned* flB, int* lA, int* lB,
+                                                     const unsigned char* nearA, const unsigned char* nearB,
+                                                     Control* ctl) {
   if (ctl->done) return;
   const int par = (int)(ctl->step & 1);
   unsigned* fl = par ? flB : flA;
   int* list = par ? lB : lA;
+  const unsigned char* nr = par ? nearB : nearA;
   const int lane = threadIdx.x & 31;
   const int plane = lk.nbx * lk.ny;
   for (int w0 = blockIdx.x * blockDim.x; w0 < lk.nbricks; w0 += gridDim.x * blockDim.x) {
@@ -330,7 +352,10 @@ __global__ void __launch_bounds__(256) flag_bricks_k(LatticeConst lk, const unsi
         acc |= dil[w + dz * plane];
       }
       f = acc != 0u;
-      if (f) fl[w] = 1u;
+      if (f) {
+        fl[w] = 1u;
+        if (nr && !nr[w]) atomicOr(&ctl->err, ERR_FAR_FLAGGED);
+      }
       mark[w] = 0u;
     }
     const unsigned bal = __ballot_sync(0xffffffffu, f);
@@ -440,18 +465,27 @@ __device__ __forceinline__ void close_step(const PlateletConst& pk, Control* ctl
   }
 }
 
+// Ftot (optional): the element force total of the step (membrane + Morse +
+// bonds), written here when the parts were spread separately.
 template <class R>
 __global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, PlateletConst pk, const R4<R>* ubuf,
                                                         int PE, double* X, double* Y, double* RY, double* Z,
                                                         double* V, int M, double* fX, double* fY, double* fZ,
                                                         double* fV, const int* ffix, int* bin_count, float4* bin,
                                                         unsigned* mark, Control* ctl, unsigned* done_blocks,
-                                                        double detach_rate, uint64_t seed) {
+                                                        double detach_rate, uint64_t seed, const R* Fmem,
+                                                        const double* Fmorse, const R* Fbond, double* Ftot) {
   if (ctl->done) return;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx < PE + M) {
     const bool el = idx < PE;
     const int m = idx - PE;
+    if (el && Ftot) {
+      double fx = (double)Fmem[idx], fy = (double)Fmem[PE + idx], fz = (double)Fmem[2 * PE + idx];
+      if (Fmorse) { fx += Fmorse[idx]; fy += Fmorse[PE + idx]; fz += Fmorse[2 * PE + idx]; }
+      if (Fbond) { fx += (double)Fbond[idx]; fy += (double)Fbond[PE + idx]; fz += (double)Fbond[2 * PE + idx]; }
+      Ftot[idx] = fx; Ftot[PE + idx] = fy; Ftot[2 * PE + idx] = fz;
+    }
     const double x = el ? X[idx] : fX[m], y = el ? Y[idx] : fY[m], z = el ? Z[idx] : fZ[m];
     R ax, ay, az;
     interp_one<R>(lk, ubuf, x, y, z, ax, ay, az);
@@ -2386,6 +2420,25 @@ cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
   return cudaGetLastError();
 }
 
+bool spread_split(const Lattice& L) { return L.precision != PF_PREC_FP64 && !L.ibm_box; }
+
+cudaError_t spread_part(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, int part, cudaStream_t st) {
+  if (part == 2) {
+    if (!Fb || Fb->M == 0) return cudaSuccess;
+    const double F0 = Pl ? (double)Pl->k.f0 : 1.0;
+    spread_part_k<<<(Fb->M + 127) / 128, 128, 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], Fb->M, Fb->X, Fb->Y,
+                                                       Fb->Z, nullptr, Fb->F, F0, ctl);
+    return cudaGetLastError();
+  }
+  const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
+  if (PE == 0 || (part == 1 && !Pl->k.nrec)) return cudaSuccess;
+  const float* Fa = (const float*)(part == 0 ? Pl->Fmem : Pl->Fbond);
+  const double* Fd = part == 0 && Pl->k.morse ? Pl->Fmorse : nullptr;
+  spread_part_k<<<(PE + 127) / 128, 128, 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], PE, Pl->X, Pl->Y, Pl->Z,
+                                                  Fa, Fd, 1.0, ctl);
+  return cudaGetLastError();
+}
+
 cudaError_t mark_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, cudaStream_t st) {
   const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
   const int M = Fb ? Fb->M : 0;
@@ -2397,7 +2450,7 @@ cudaError_t mark_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, cudaStream_t st)
   return cudaGetLastError();
 }
 
-cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st) {
+cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st, bool check_near) {
   const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
   const int M = Fb ? Fb->M : 0;
   if (PE + M == 0) return cudaSuccess;
@@ -2408,7 +2461,8 @@ cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cu
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int grid = (nb + 255) / 256;
   if (grid > 8 * sms) grid = 8 * sms;
-  flag_bricks_k<<<grid, 256, 0, st>>>(L.k, L.dil, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1], ctl);
+  flag_bricks_k<<<grid, 256, 0, st>>>(L.k, L.dil, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1],
+                                      check_near ? L.near[0] : nullptr, check_near ? L.near[1] : nullptr, ctl);
   return cudaGetLastError();
 }
 
@@ -2428,13 +2482,14 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
         L.k, pk, (const D4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
         Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
-        detach_rate, seed);
+        detach_rate, seed, nullptr, nullptr, nullptr, nullptr);
   else if (PE + M == 0 || !L.ibm_box)
     interp_advance_k<float><<<grid, 128, 0, st>>>(
         L.k, pk, (const float4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
         Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
-        detach_rate, seed);
+        detach_rate, seed, Pl ? (const float*)Pl->Fmem : nullptr, (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr,
+        (Pl && Pl->k.nrec) ? (const float*)Pl->Fbond : nullptr, Pl ? Pl->Ftot : nullptr);
   else {
     cudaFuncSetAttribute(interp_box_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBoxSmem);
     const int P = Pl ? Pl->k.P : 0, E = Pl ? Pl->k.E : 0;

@@ -156,6 +156,36 @@ def test_graph_and_direct_stepping_agree(gpu):
     assert a.steps == b.steps == 7
 
 
+@pytest.mark.parametrize("prec,tol", [(0, 1e-14), (1, 1e-6)], ids=["fp64", "fp32"])
+def test_pipelined_and_serial_schedules_agree(gpu, prec, tol, monkeypatch):
+    """The pipelined schedule updates the far region of step t+1 (bricks
+    more than one brick / two rows from step t's force bricks) while step t
+    spreads, passes its force bricks and interpolates; every node update is
+    the one the serial schedule makes.  Graph and direct stepping, and a
+    profile run in between (which restarts the pipeline), on a channel
+    whose markers cover a small part of the lattice."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small(nx=256, ny=64, nz=32, n_platelets=2, n_fib=40, n_links=60)
+    monkeypatch.setenv("PFGPU_PIPELINE", "0")
+    a = gpu.Job(sc, prec)
+    monkeypatch.setenv("PFGPU_PIPELINE", "1")
+    b = gpu.Job(sc, prec)
+    monkeypatch.delenv("PFGPU_PIPELINE")
+    for j in (a, b):
+        j.step(5)
+        j.step(3, graph=False)
+        j.profile(2)
+        j.step(4)
+        assert j.steps == 14
+    assert rel_max(a.lattice()["fIN"], b.lattice()["fIN"]) < tol
+    for k in ("X", "Y", "Z"):
+        assert rel_max(a.elements()[k], b.elements()[k]) < tol
+    assert rel_max(a.fibrin()["X"], b.fibrin()["X"]) < tol
+    np.testing.assert_array_equal(a.bonds()["rec_state"], b.bonds()["rec_state"])
+    a.close()
+    b.close()
+
+
 def _lbm_scene(name):
     from platelet_fiber_gpu_gb300 import workloads as W
     if name == "shear":
