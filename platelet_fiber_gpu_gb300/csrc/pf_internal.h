@@ -66,10 +66,10 @@ struct Lattice {
   void* ubuf = nullptr;
   unsigned* flags[2] = {nullptr, nullptr};
   int* list[2] = {nullptr, nullptr};
-  // marker occupancy, one bit per node (one 32-bit word per brick), and its
-  // dilation in x and y: scratch of the brick flagging
+  // marker occupancy, one bit per node (one 32-bit word per brick), two
+  // buffers by step parity: the position update marks the next step's
+  // buffer, the flagging reads this step's, the flagged-brick pass clears it
   unsigned* mark = nullptr;
-  unsigned* dil = nullptr;
   // near region per step parity: bricks within one brick (x) and two rows
   // (y, z) of a force brick of the previous step; the rest (far) is updated
   // by the pipelined far pass while the previous step's tail runs

@@ -694,8 +694,7 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(dalloc(j, &L.flags[1], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.list[0], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.list[1], (size_t)L.k.nbricks));
-  CKJ(dalloc(j, &L.mark, (size_t)L.k.nbricks));
-  CKJ(dalloc(j, &L.dil, (size_t)L.k.nbricks));
+  CKJ(dalloc(j, &L.mark, 2 * (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.near[0], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &L.near[1], (size_t)L.k.nbricks));
   CKJ(dalloc(j, &j->ctl, 1));

@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(256) near_bricks_k(LatticeConst k, const unsig
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= k.nbricks) return;
   const int par = (int)(ctl->step & 1);
-  const unsigned* src = src_mark ? mark : (par ? flB : flA);
+  const unsigned* src = src_mark ? mark + (size_t)par * k.nbricks : (par ? flB : flA);
   unsigned char* dst = (src_mark ? par : par ^ 1) ? nearB : nearA;
   const int bx = w % k.nbx, y = (w / k.nbx) % k.ny, z = w / (k.nbx * k.ny);
   unsigned acc = 0;
@@ -386,7 +386,8 @@ __global__ void far_counter_k(Control* ctl, int sync) {
 template <class S, class R, bool FAST>
 __global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
                                                         R4<R>* ubuf, unsigned* flA, unsigned* flB, const int* lA,
-                                                        const int* lB, int* bin_count, int ncells, Control* ctl) {
+                                                        const int* lB, int* bin_count, int ncells, unsigned* mark,
+                                                        Control* ctl) {
   if (ctl->done) return;
   const int par = (int)(ctl->step & 1);
   const S* __restrict__ gin = par ? gB : gA;
@@ -395,6 +396,9 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S
   R4<R>* Fp = par ? FA : FB;
   unsigned* flp = par ? flA : flB;
   const int* list = par ? lB : lA;
+  // this step's occupancy bits, all inside flagged bricks: cleared here, the
+  // last reader, for the position update two steps on
+  unsigned* mk = mark + (size_t)par * k.nbricks;
   const int cnt = ctl->active_count[par];
   const int first = ctl->first;
   if (bin_count)
@@ -410,7 +414,10 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S
     const unsigned fp = flp[brick];
     if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 1u, fp, first);
     __syncwarp();
-    if (lane == 0 && fp) flp[brick] = 0;
+    if (lane == 0) {
+      if (fp) flp[brick] = 0;
+      mk[brick] = 0u;
+    }
   }
 }
 
@@ -902,7 +909,8 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
     if (grid > need) grid = need;
     auto kern = fast_lattice(L) ? lbm_list_k<S, R, true> : lbm_list_k<S, R, false>;
     kern<<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
-                                     L.flags[0], L.flags[1], L.list[0], L.list[1], bin_count, ncells, ctl);
+                                     L.flags[0], L.flags[1], L.list[0], L.list[1], bin_count, ncells, L.mark,
+                                     ctl);
     return cudaGetLastError();
   }
   dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);

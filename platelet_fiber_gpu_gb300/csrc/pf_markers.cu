@@ -249,8 +249,8 @@ __global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA
 // any force of the step exists, so the lattice pass over the other bricks
 // can run while the forces are computed.  One bit per node (a brick is one
 // 32-bit word): the position update sets each marker's bit for the next
-// step, the bits are dilated by kFlagR in x and y, then in z; a non-zero
-// word flags and lists its brick.
+// step, the bits are dilated by kFlagR in x, y and z; a non-zero word flags
+// and lists its brick.
 constexpr int kFlagR = 2;
 
 // Sets the occupancy bit of a marker's base node; nodes outside the lattice
@@ -281,16 +281,12 @@ __global__ void __launch_bounds__(128) mark_markers_k(LatticeConst lk, unsigned*
   else if (idx < PE + M) mark_node(lk, mark, fX[idx - PE], fY[idx - PE], fZ[idx - PE], fp64);
 }
 
-// word bx of a row dilated by kFlagR bits in x (periodic rows: the
-// neighbour words across the row's ends; when nx is not a multiple of 32, a
-// word next to occupied bits across the wrap is taken as all set, a superset)
-__device__ __forceinline__ unsigned dilate_x(const unsigned* row, int bx, int nbx, bool wrap, bool partial) {
-  const unsigned C = row[bx];
-  unsigned Lw = 0, Rw = 0;
-  if (bx > 0) Lw = row[bx - 1];
-  else if (wrap) Lw = row[nbx - 1];
-  if (bx < nbx - 1) Rw = row[bx + 1];
-  else if (wrap) Rw = row[0];
+// word bx (C) of a row dilated by kFlagR bits in x, from its left and right
+// neighbour words (periodic rows: across the row's ends; when nx is not a
+// multiple of 32, a word next to occupied bits across the wrap is taken as
+// all set, a superset)
+__device__ __forceinline__ unsigned dilate_words(unsigned C, unsigned Lw, unsigned Rw, int bx, int nbx, bool wrap,
+                                                 bool partial) {
   // a partial last word is not bit-adjacent to word 0 across the wrap
   if (partial && wrap && ((bx == 0 && Lw) || (bx == nbx - 1 && Rw))) return 0xffffffffu;
   if (!(C | Lw | Rw)) return 0u;
@@ -305,66 +301,73 @@ __device__ __forceinline__ unsigned dilate_x(const unsigned* row, int bx, int nb
   return (unsigned)(dl >> 32) | (unsigned)dh;
 }
 
-__global__ void __launch_bounds__(256) dilate_xy_k(LatticeConst lk, const unsigned* mark, unsigned* dil,
-                                                   const Control* ctl) {
-  if (ctl->done) return;
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= lk.nbricks) return;
-  const int bx = w % lk.nbx, y = (w / lk.nbx) % lk.ny, z = w / (lk.nbx * lk.ny);
-  const bool wrap = lk.ibm_wrap[0] != 0, partial = (lk.nx & 31) != 0;
-  unsigned acc = 0;
-  for (int dy = -kFlagR; dy <= kFlagR; ++dy) {
-    int yy = y + dy;
-    if (yy < 0 || yy >= lk.ny) {
-      if (!lk.ibm_wrap[1]) continue;
-      yy = wrapi(yy, lk.ny);
-    }
-    acc |= dilate_x(mark + (size_t)lk.nbx * (yy + lk.ny * z), bx, lk.nbx, wrap, partial);
-  }
-  dil[w] = acc;
-}
-
-// dilates in z, flags and lists the bricks (list[par], active_count[par]),
-// and clears the occupancy bits for the next step.  With the near region of
-// the pipelined schedule (nearA/B): a flagged brick outside it was updated
-// without force by the far pass, an error (a marker moved more than one node
-// in one step).
-__global__ void __launch_bounds__(256) flag_bricks_k(LatticeConst lk, const unsigned* dil, unsigned* mark,
-                                                     unsigned* flA, unsigned* flB, int* lA, int* lB,
-                                                     const unsigned char* nearA, const unsigned char* nearB,
-                                                     Control* ctl) {
+// One kernel per step: each brick word dilated by kFlagR nodes in x (bits),
+// y (rows, wrapped on an IBM-periodic axis) and z (planes); a non-zero word
+// flags and lists its brick (list[par], active_count[par]).  The occupancy
+// bits of the step (buffer par) are left for the flagged-brick lattice pass
+// to clear.  With the near region of the pipelined schedule (nearA/B): a
+// flagged brick outside it was updated without force by the far pass, an
+// error (a marker moved more than one node in one step).
+__global__ void __launch_bounds__(256) flag_k(LatticeConst lk, const unsigned* mark, unsigned* flA, unsigned* flB,
+                                              int* lA, int* lB, const unsigned char* nearA,
+                                              const unsigned char* nearB, Control* ctl) {
   if (ctl->done) return;
   const int par = (int)(ctl->step & 1);
+  const unsigned* mk = mark + (size_t)par * lk.nbricks;
   unsigned* fl = par ? flB : flA;
   int* list = par ? lB : lA;
   const unsigned char* nr = par ? nearB : nearA;
   const int lane = threadIdx.x & 31;
-  const int plane = lk.nbx * lk.ny;
-  for (int w0 = blockIdx.x * blockDim.x; w0 < lk.nbricks; w0 += gridDim.x * blockDim.x) {
-    const int w = w0 + threadIdx.x;
-    bool f = false;
-    if (w < lk.nbricks) {
-      const int z = w / plane;
-      unsigned acc = 0;
-      for (int dz = -kFlagR; dz <= kFlagR; ++dz) {
-        const int zz = z + dz;
-        if (zz < 0 || zz >= lk.nz) continue;
-        acc |= dil[w + dz * plane];
+  const bool wrap = lk.ibm_wrap[0] != 0, partial = (lk.nx & 31) != 0;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  bool f = false;
+  if (w < lk.nbricks) {
+    const int bx = w % lk.nbx, y = (w / lk.nbx) % lk.ny, z = w / (lk.nbx * lk.ny);
+    // rows of the 5x5 (y, z) neighbourhood; the loops are unrolled so that
+    // all 75 word loads are in flight together
+    int rows[2 * kFlagR + 1];
+    bool rok[2 * kFlagR + 1];
+#pragma unroll
+    for (int d = -kFlagR; d <= kFlagR; ++d) {
+      int yy = y + d;
+      rok[d + kFlagR] = true;
+      if (yy < 0 || yy >= lk.ny) {
+        rok[d + kFlagR] = lk.ibm_wrap[1] != 0;
+        yy = wrapi(yy, lk.ny);
       }
-      f = acc != 0u;
-      if (f) {
-        fl[w] = 1u;
-        if (nr && !nr[w]) atomicOr(&ctl->err, ERR_FAR_FLAGGED);
-      }
-      mark[w] = 0u;
+      rows[d + kFlagR] = yy;
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, f);
-    if (!bal) continue;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&ctl->active_count[par], __popc(bal));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (f) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
+    // the dilation distributes over OR: dilate the OR of the 25 rows' words
+    constexpr int D = 2 * kFlagR + 1;
+    unsigned C = 0, Lw = 0, Rw = 0;
+    const int lx = bx > 0 ? bx - 1 : (wrap ? lk.nbx - 1 : -1);
+    const int rx = bx < lk.nbx - 1 ? bx + 1 : (wrap ? 0 : -1);
+#pragma unroll
+    for (int dz = 0; dz < D; ++dz) {
+      const int zz = z + dz - kFlagR;
+      if (zz < 0 || zz >= lk.nz) continue;
+#pragma unroll
+      for (int dy = 0; dy < D; ++dy) {
+        if (!rok[dy]) continue;
+        const unsigned* row = mk + (size_t)lk.nbx * (rows[dy] + (size_t)lk.ny * zz);
+        C |= row[bx];
+        if (lx >= 0) Lw |= row[lx];
+        if (rx >= 0) Rw |= row[rx];
+      }
+    }
+    const unsigned acc = dilate_words(C, Lw, Rw, bx, lk.nbx, wrap, partial);
+    f = acc != 0u;
+    if (f) {
+      fl[w] = 1u;
+      if (nr && !nr[w]) atomicOr(&ctl->err, ERR_FAR_FLAGGED);
+    }
   }
+  const unsigned bal = __ballot_sync(0xffffffffu, f);
+  if (!bal) return;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(&ctl->active_count[par], __popc(bal));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (f) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
 }
 
 // ------------------------------------------------------- interp + advance
@@ -437,7 +440,8 @@ __device__ __forceinline__ void advance_marker(const LatticeConst& lk, const Pla
       fX[m] = x; fY[m] = y; fZ[m] = z;
     }
   }
-  mark_node(lk, mark, x, y, z, fp64);
+  // the occupancy bits of the next step (buffer of the other parity)
+  mark_node(lk, mark + (size_t)((int)(ctl->step & 1) ^ 1) * lk.nbricks, x, y, z, fp64);
 }
 
 // The last block to finish closes the step: counter, first flag, the other
@@ -1635,6 +1639,33 @@ __global__ void __launch_bounds__(kMem32Threads, 2)
 }
 
 // ---------------------------------------------------------------- Morse
+// FP32 Morse force over distance, F(r)/r, force-shifted to zero at the
+// cutoff: (2 rho U0 (e^2 - e) - F(rc)) / r with e = exp(rho (req - r)),
+// evaluated without a branch (e = 2^(K1 - K2 r), K2 = rho log2(e),
+// K1 = K2 req); zero outside 0 < r^2 < rc^2.
+struct MorseF32 {
+  float rc2, K1, K2, A, Fc;
+  __host__ __device__ MorseF32(const double prm[4], double fc) {
+    const float rho = (float)prm[1], rc = (float)prm[3];
+    rc2 = rc * rc;
+    K2 = rho * 1.44269504088896341f;
+    K1 = K2 * (float)prm[2];
+    A = 2.0f * rho * (float)prm[0];
+    Fc = (float)fc;
+  }
+};
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float morse_fr(const MorseF32& m, float r2) {
+  const bool in = r2 < m.rc2 && r2 > 0.f;
+  const float rinv = rsqrtf(in ? r2 : 1.f);
+  const float ex = ex2_approx(fmaf(-m.K2, r2 * rinv, m.K1));
+  const float fr = fmaf(m.A, ex * (ex - 1.f), -m.Fc) * rinv;
+  return in ? fr : 0.f;
+}
 // Cell bins are sorted by element id after binning, so a cell list is the
 // same set in the same order as the oracle's counting sort, and the pair sums
 // below run in a fixed order.
@@ -1813,50 +1844,59 @@ __device__ __forceinline__ double min_image(double d, double L, int wrap) {
   return d;
 }
 
+constexpr int kBoundsThreads = 512;
 template <class R>
-__global__ void __launch_bounds__(256) platelet_bounds_k(PlateletConst k, const double* X, const double* Y,
-                                                         const double* Z, double* bounds,
-                                                         typename Staged<R>::T* rel, const Control* ctl) {
+__global__ void __launch_bounds__(kBoundsThreads) platelet_bounds_k(PlateletConst k, const double* X,
+                                                                    const double* Y, const double* Z,
+                                                                    double* bounds, typename Staged<R>::T* rel,
+                                                                    const Control* ctl) {
   if (ctl->done) return;
-  const int p = blockIdx.x;
+  constexpr int NW = kBoundsThreads / 32;
+  const int p = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int base = p * k.E;
   const double ox = X[base], oy = Y[base], oz = Z[base];
-  __shared__ double s_a[256], s_b[256], s_c[256];
+  __shared__ double s_w[3][NW];
+  __shared__ double s_c[3];
+  __shared__ double s_r[NW];
+  // centroid: minimum-image offsets from the first element, summed per
+  // thread, per warp, then over the warps in order
   double sx = 0, sy = 0, sz = 0;
-  for (int e = threadIdx.x; e < k.E; e += blockDim.x) {
+  for (int e = threadIdx.x; e < k.E; e += kBoundsThreads) {
     sx += min_image(X[base + e] - ox, k.L[0], k.wrap[0]);
     sy += min_image(Y[base + e] - oy, k.L[1], k.wrap[1]);
     sz += min_image(Z[base + e] - oz, k.L[2], k.wrap[2]);
   }
-  s_a[threadIdx.x] = sx; s_b[threadIdx.x] = sy; s_c[threadIdx.x] = sz;
-  __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-    if (threadIdx.x < st) {
-      s_a[threadIdx.x] += s_a[threadIdx.x + st];
-      s_b[threadIdx.x] += s_b[threadIdx.x + st];
-      s_c[threadIdx.x] += s_c[threadIdx.x + st];
-    }
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    sz += __shfl_xor_sync(0xffffffffu, sz, o);
   }
-  const double cx_ = ox + s_a[0] / k.E, cy_ = oy + s_b[0] / k.E, cz_ = oz + s_c[0] / k.E;
+  if (lane == 0) { s_w[0][wid] = sx; s_w[1][wid] = sy; s_w[2][wid] = sz; }
   __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0;
+    for (int w = 0; w < NW; ++w) t += s_w[threadIdx.x][w];
+    s_c[threadIdx.x] = (threadIdx.x == 0 ? ox : threadIdx.x == 1 ? oy : oz) + t / k.E;
+  }
+  __syncthreads();
+  const double cx_ = s_c[0], cy_ = s_c[1], cz_ = s_c[2];
+  // positions relative to the centroid, and the bounding radius
   double r2max = 0;
-  for (int e = threadIdx.x; e < k.E; e += blockDim.x) {
+  for (int e = threadIdx.x; e < k.E; e += kBoundsThreads) {
     const double d0 = min_image(X[base + e] - cx_, k.L[0], k.wrap[0]);
     const double d1 = min_image(Y[base + e] - cy_, k.L[1], k.wrap[1]);
     const double d2 = min_image(Z[base + e] - cz_, k.L[2], k.wrap[2]);
     rel[base + e] = Staged<R>::make(d0, d1, d2, base + e);
     r2max = fmax(r2max, d0 * d0 + d1 * d1 + d2 * d2);
   }
-  s_a[threadIdx.x] = r2max;
+  for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+  if (lane == 0) s_r[wid] = r2max;
   __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-    if (threadIdx.x < st) s_a[threadIdx.x] = fmax(s_a[threadIdx.x], s_a[threadIdx.x + st]);
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {
+    double m = 0;
+    for (int w = 0; w < NW; ++w) m = fmax(m, s_r[w]);
     bounds[4 * p] = cx_; bounds[4 * p + 1] = cy_; bounds[4 * p + 2] = cz_;
-    bounds[4 * p + 3] = sqrt(s_a[0]);
+    bounds[4 * p + 3] = sqrt(m);
   }
 }
 
@@ -1888,6 +1928,13 @@ __global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletCon
   const R rcb = (R)k.morse_inter[3], rc2b = rcb * rcb, Fcb = (R)k.morse_fc[1];
   const T own = valid ? s_t[e] : Staged<R>::make(0, 0, 0, 0);
   R ax = 0, ay = 0, az = 0;
+  const MorseF32 fa(k.morse_intra, k.morse_fc[0]), fb(k.morse_inter, k.morse_fc[1]);
+  // FP32: branchless (every lane evaluates, out-of-range pairs add zero)
+  auto pair32 = [&](const T mb, const MorseF32& m) {
+    const float d0 = (float)own.x - (float)mb.x, d1 = (float)own.y - (float)mb.y, d2 = (float)own.z - (float)mb.z;
+    const float fr = morse_fr(m, d0 * d0 + d1 * d1 + d2 * d2);
+    ax += fr * d0; ay += fr * d1; az += fr * d2;
+  };
   auto pair = [&](const T mb, R U0, R rho, R req, R rc, R rc2, R Fc) {
     const R d0 = (R)own.x - (R)mb.x, d1 = (R)own.y - (R)mb.y, d2 = (R)own.z - (R)mb.z;
     const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
@@ -1909,8 +1956,12 @@ __global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletCon
   const int chunk = (k.E + kMorseSplit - 1) / kMorseSplit;
   const int j0 = w * chunk, j1 = min(k.E, j0 + chunk);
   if (valid) {
+    if constexpr (sizeof(R) == 4) {
 #pragma unroll 4
-    for (int j = j0; j < j1; ++j) pair(s_t[j], U0a, rhoa, reqa, rca, rc2a, Fca);
+      for (int j = j0; j < j1; ++j) pair32(s_t[j], fa);
+    } else {
+      for (int j = j0; j < j1; ++j) pair(s_t[j], U0a, rhoa, reqa, rca, rc2a, Fca);
+    }
   }
   // Other platelets whose bounding spheres come within the inter cutoff,
   // shifted into this platelet's centroid frame (minimum image).  The
@@ -1964,7 +2015,11 @@ __global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletCon
       // this element is out of reach of platelet qq: skip its members
       const R dq0 = (R)own.x - f0, dq1 = (R)own.y - f1, dq2 = (R)own.z - f2;
       if (dq0 * dq0 + dq1 * dq1 + dq2 * dq2 >= lim * lim) continue;
-      for (int j = j0; j < j1; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
+      if constexpr (sizeof(R) == 4) {
+        for (int j = j0; j < j1; ++j) pair32(s_q[j], fb);
+      } else {
+        for (int j = j0; j < j1; ++j) pair(s_q[j], U0b, rhob, reqb, rcb, rc2b, Fcb);
+      }
     }
   }
   s_part[w][0][lane] = ax;
@@ -2302,13 +2357,13 @@ cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_
   if (!morse_uses_cells(k)) {
     const int slices = (k.E + 31) / 32;
     if (precision == PF_PREC_FP64) {
-      platelet_bounds_k<double><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (D4*)Pl.relpos, ctl);
+      platelet_bounds_k<double><<<k.P, kBoundsThreads, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (D4*)Pl.relpos, ctl);
       const size_t smem = 2 * (size_t)k.E * sizeof(D4);
       cudaFuncSetAttribute(morse_platelet_k<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       morse_platelet_k<double><<<k.P * slices, 32 * kMorseSplit, smem, st>>>(k, Pl.bounds, (const D4*)Pl.relpos, slices,
                                                                 Pl.Fmorse, ctl);
     } else {
-      platelet_bounds_k<float><<<k.P, 256, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (float4*)Pl.relpos, ctl);
+      platelet_bounds_k<float><<<k.P, kBoundsThreads, 0, st>>>(k, Pl.X, Pl.Y, Pl.Z, Pl.bounds, (float4*)Pl.relpos, ctl);
       const size_t smem = 2 * (size_t)k.E * sizeof(float4);
       cudaFuncSetAttribute(morse_platelet_k<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       morse_platelet_k<float><<<k.P * slices, 32 * kMorseSplit, smem, st>>>(k, Pl.bounds, (const float4*)Pl.relpos, slices,
@@ -2455,14 +2510,8 @@ cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cu
   const int M = Fb ? Fb->M : 0;
   if (PE + M == 0) return cudaSuccess;
   const int nb = L.k.nbricks;
-  dilate_xy_k<<<(nb + 255) / 256, 256, 0, st>>>(L.k, L.mark, L.dil, ctl);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int grid = (nb + 255) / 256;
-  if (grid > 8 * sms) grid = 8 * sms;
-  flag_bricks_k<<<grid, 256, 0, st>>>(L.k, L.dil, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1],
-                                      check_near ? L.near[0] : nullptr, check_near ? L.near[1] : nullptr, ctl);
+  flag_k<<<(nb + 255) / 256, 256, 0, st>>>(L.k, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1],
+                                           check_near ? L.near[0] : nullptr, check_near ? L.near[1] : nullptr, ctl);
   return cudaGetLastError();
 }
 
