@@ -303,15 +303,29 @@ __device__ __forceinline__ unsigned dilate_words(unsigned C, unsigned Lw, unsign
 
 // One kernel per step: each brick word dilated by kFlagR nodes in x (bits),
 // y (rows, wrapped on an IBM-periodic axis) and z (planes); a non-zero word
-// flags and lists its brick (list[par], active_count[par]).  The occupancy
-// bits of the step (buffer par) are left for the flagged-brick lattice pass
-// to clear.  With the near region of the pipelined schedule (nearA/B): a
-// flagged brick outside it was updated without force by the far pass, an
-// error (a marker moved more than one node in one step).
-__global__ void __launch_bounds__(256) flag_k(LatticeConst lk, const unsigned* mark, unsigned* flA, unsigned* flB,
-                                              int* lA, int* lB, const unsigned char* nearA,
-                                              const unsigned char* nearB, Control* ctl) {
+// flags and lists its brick (list[par], active_count[par]).  The dilation
+// distributes over OR, so it is done separably: a CTA takes kFlagRows whole
+// rows of one z-plane, ORs each row word (and its y halo) over the five
+// planes into shared memory, then over the five rows, then dilates in x.
+// The occupancy bits of the step (buffer par) are left for the
+// flagged-brick lattice pass to clear.  With the near region of the
+// pipelined schedule (nearA/B): a flagged brick outside it was updated
+// without force by the far pass, an error (a marker moved more than one
+// node in one step).
+constexpr int kFlagThreads = 256;
+constexpr int kFlagWords = 4096;  // shared words per stage (rows + halo) x nbx
+__host__ __device__ inline int flag_rows(int nbx) {
+  int r = kFlagThreads / nbx;
+  if (r < 1) r = 1;
+  while (r > 1 && (r + 2 * kFlagR) * nbx > kFlagWords) --r;
+  return r;
+}
+__global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const unsigned* mark, unsigned* flA,
+                                                       unsigned* flB, int* lA, int* lB, const unsigned char* nearA,
+                                                       const unsigned char* nearB, Control* ctl) {
   if (ctl->done) return;
+  __shared__ unsigned s_z[kFlagWords];  // OR over the planes, rows y0-2 .. y0+R+1
+  __shared__ unsigned s_yz[kFlagWords];  // OR over the rows too, rows y0 .. y0+R-1
   const int par = (int)(ctl->step & 1);
   const unsigned* mk = mark + (size_t)par * lk.nbricks;
   unsigned* fl = par ? flB : flA;
@@ -319,55 +333,62 @@ __global__ void __launch_bounds__(256) flag_k(LatticeConst lk, const unsigned* m
   const unsigned char* nr = par ? nearB : nearA;
   const int lane = threadIdx.x & 31;
   const bool wrap = lk.ibm_wrap[0] != 0, partial = (lk.nx & 31) != 0;
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  bool f = false;
-  if (w < lk.nbricks) {
-    const int bx = w % lk.nbx, y = (w / lk.nbx) % lk.ny, z = w / (lk.nbx * lk.ny);
-    // rows of the 5x5 (y, z) neighbourhood; the loops are unrolled so that
-    // all 75 word loads are in flight together
-    int rows[2 * kFlagR + 1];
-    bool rok[2 * kFlagR + 1];
-#pragma unroll
-    for (int d = -kFlagR; d <= kFlagR; ++d) {
-      int yy = y + d;
-      rok[d + kFlagR] = true;
-      if (yy < 0 || yy >= lk.ny) {
-        rok[d + kFlagR] = lk.ibm_wrap[1] != 0;
-        yy = wrapi(yy, lk.ny);
-      }
-      rows[d + kFlagR] = yy;
+  const int nbx = lk.nbx, R = flag_rows(nbx);
+  const int ytiles = (lk.ny + R - 1) / R;
+  const int z = blockIdx.x / ytiles, y0 = (blockIdx.x % ytiles) * R;
+  const int halo = (R + 2 * kFlagR) * nbx;
+  for (int i = threadIdx.x; i < halo; i += kFlagThreads) {
+    const int bx = i % nbx;
+    int yy = y0 - kFlagR + i / nbx;
+    unsigned acc = 0;
+    bool ok = true;
+    if (yy < 0 || yy >= lk.ny) {
+      ok = lk.ibm_wrap[1] != 0;
+      yy = wrapi(yy, lk.ny);
     }
-    // the dilation distributes over OR: dilate the OR of the 25 rows' words
-    constexpr int D = 2 * kFlagR + 1;
-    unsigned C = 0, Lw = 0, Rw = 0;
-    const int lx = bx > 0 ? bx - 1 : (wrap ? lk.nbx - 1 : -1);
-    const int rx = bx < lk.nbx - 1 ? bx + 1 : (wrap ? 0 : -1);
+    if (ok)
 #pragma unroll
-    for (int dz = 0; dz < D; ++dz) {
-      const int zz = z + dz - kFlagR;
-      if (zz < 0 || zz >= lk.nz) continue;
+      for (int dz = -kFlagR; dz <= kFlagR; ++dz) {
+        const int zz = z + dz;
+        if (zz >= 0 && zz < lk.nz) acc |= mk[bx + (size_t)nbx * (yy + (size_t)lk.ny * zz)];
+      }
+    s_z[i] = acc;
+  }
+  __syncthreads();
+  const int outs = R * nbx;
+  for (int i = threadIdx.x; i < outs; i += kFlagThreads) {
+    unsigned acc = 0;
 #pragma unroll
-      for (int dy = 0; dy < D; ++dy) {
-        if (!rok[dy]) continue;
-        const unsigned* row = mk + (size_t)lk.nbx * (rows[dy] + (size_t)lk.ny * zz);
-        C |= row[bx];
-        if (lx >= 0) Lw |= row[lx];
-        if (rx >= 0) Rw |= row[rx];
+    for (int dy = 0; dy <= 2 * kFlagR; ++dy) acc |= s_z[i + dy * nbx];
+    s_yz[i] = acc;
+  }
+  __syncthreads();
+  // rounds of kFlagThreads so that every lane of a warp reaches the ballot
+  for (int i0 = 0; i0 < outs; i0 += kFlagThreads) {
+    const int i = i0 + threadIdx.x;
+    const int bx = i % nbx, y = y0 + i / nbx;
+    bool f = false;
+    int w = 0;
+    if (i < outs && y < lk.ny) {
+      const int rowbase = i - bx;
+      const unsigned C = s_yz[i];
+      const unsigned Lw = bx > 0 ? s_yz[i - 1] : (wrap ? s_yz[rowbase + nbx - 1] : 0u);
+      const unsigned Rw = bx < nbx - 1 ? s_yz[i + 1] : (wrap ? s_yz[rowbase] : 0u);
+      w = bx + nbx * (y + lk.ny * z);
+      f = dilate_words(C, Lw, Rw, bx, nbx, wrap, partial) != 0u;
+      if (f) {
+        fl[w] = 1u;
+        if (nr && !nr[w]) atomicOr(&ctl->err, ERR_FAR_FLAGGED);
       }
     }
-    const unsigned acc = dilate_words(C, Lw, Rw, bx, lk.nbx, wrap, partial);
-    f = acc != 0u;
-    if (f) {
-      fl[w] = 1u;
-      if (nr && !nr[w]) atomicOr(&ctl->err, ERR_FAR_FLAGGED);
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    if (bal) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&ctl->active_count[par], __popc(bal));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (f) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
     }
   }
-  const unsigned bal = __ballot_sync(0xffffffffu, f);
-  if (!bal) return;
-  int base = 0;
-  if (lane == 0) base = atomicAdd(&ctl->active_count[par], __popc(bal));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (f) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
 }
 
 // ------------------------------------------------------- interp + advance
@@ -2509,8 +2530,9 @@ cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cu
   const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
   const int M = Fb ? Fb->M : 0;
   if (PE + M == 0) return cudaSuccess;
-  const int nb = L.k.nbricks;
-  flag_k<<<(nb + 255) / 256, 256, 0, st>>>(L.k, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1],
+  const int R = flag_rows(L.k.nbx);
+  if ((R + 2 * kFlagR) * L.k.nbx > kFlagWords) return cudaErrorInvalidValue;  // rows wider than 131072 nodes
+  flag_k<<<L.k.nz * ((L.k.ny + R - 1) / R), kFlagThreads, 0, st>>>(L.k, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1],
                                            check_near ? L.near[0] : nullptr, check_near ? L.near[1] : nullptr, ctl);
   return cudaGetLastError();
 }
