@@ -236,7 +236,12 @@ __global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA
   if (i >= n) return;
   double fx = 0, fy = 0, fz = 0;
   if (Fa) { fx = (double)Fa[i]; fy = (double)Fa[n + i]; fz = (double)Fa[2 * n + i]; }
-  if (Fd) { fx += Fd[i] / div; fy += Fd[n + i] / div; fz += Fd[2 * n + i] / div; }
+  // div: F0 for fibrin forces (a product with its FP64 reciprocal; FP64
+  // division is slow on this GPU)
+  if (Fd) {
+    const double r = 1.0 / div;
+    fx += Fd[i] * r; fy += Fd[n + i] * r; fz += Fd[2 * n + i] * r;
+  }
   if (fx == 0 && fy == 0 && fz == 0) return;
   spread_one<float>(lk, (ctl->step & 1) ? FB : FA, X[i], Y[i], Z[i], (float)fx, (float)fy, (float)fz);
 }
@@ -1858,10 +1863,11 @@ struct Staged<double> {
   }
 };
 
-__device__ __forceinline__ double min_image(double d, double L, int wrap) {
+template <class T = double>
+__device__ __forceinline__ T min_image(T d, T L, int wrap) {
   if (!wrap) return d;
-  if (d > 0.5 * L) d -= L;
-  else if (d < -0.5 * L) d += L;
+  if (d > (T)0.5 * L) d -= L;
+  else if (d < (T)-0.5 * L) d += L;
   return d;
 }
 
@@ -1876,16 +1882,19 @@ __global__ void __launch_bounds__(kBoundsThreads) platelet_bounds_k(PlateletCons
   const int p = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int base = p * k.E;
   const double ox = X[base], oy = Y[base], oz = Z[base];
-  __shared__ double s_w[3][NW];
+  __shared__ R s_w[3][NW];
   __shared__ double s_c[3];
-  __shared__ double s_r[NW];
+  __shared__ R s_r[NW];
   // centroid: minimum-image offsets from the first element, summed per
-  // thread, per warp, then over the warps in order
-  double sx = 0, sy = 0, sz = 0;
+  // thread, per warp, then over the warps in order.  The FP32 build forms
+  // each offset with one FP64 subtraction and sums in FP32 (the centroid
+  // only fixes the frame of the float positions; FP64 is slow on this GPU)
+  R sx = 0, sy = 0, sz = 0;
+  const R Lx = (R)k.L[0], Ly = (R)k.L[1], Lz = (R)k.L[2];
   for (int e = threadIdx.x; e < k.E; e += kBoundsThreads) {
-    sx += min_image(X[base + e] - ox, k.L[0], k.wrap[0]);
-    sy += min_image(Y[base + e] - oy, k.L[1], k.wrap[1]);
-    sz += min_image(Z[base + e] - oz, k.L[2], k.wrap[2]);
+    sx += min_image<R>((R)(X[base + e] - ox), Lx, k.wrap[0]);
+    sy += min_image<R>((R)(Y[base + e] - oy), Ly, k.wrap[1]);
+    sz += min_image<R>((R)(Z[base + e] - oz), Lz, k.wrap[2]);
   }
   for (int o = 16; o > 0; o >>= 1) {
     sx += __shfl_xor_sync(0xffffffffu, sx, o);
@@ -1895,18 +1904,18 @@ __global__ void __launch_bounds__(kBoundsThreads) platelet_bounds_k(PlateletCons
   if (lane == 0) { s_w[0][wid] = sx; s_w[1][wid] = sy; s_w[2][wid] = sz; }
   __syncthreads();
   if (threadIdx.x < 3) {
-    double t = 0;
+    R t = 0;
     for (int w = 0; w < NW; ++w) t += s_w[threadIdx.x][w];
-    s_c[threadIdx.x] = (threadIdx.x == 0 ? ox : threadIdx.x == 1 ? oy : oz) + t / k.E;
+    s_c[threadIdx.x] = (threadIdx.x == 0 ? ox : threadIdx.x == 1 ? oy : oz) + (double)(t / (R)k.E);
   }
   __syncthreads();
   const double cx_ = s_c[0], cy_ = s_c[1], cz_ = s_c[2];
   // positions relative to the centroid, and the bounding radius
-  double r2max = 0;
+  R r2max = 0;
   for (int e = threadIdx.x; e < k.E; e += kBoundsThreads) {
-    const double d0 = min_image(X[base + e] - cx_, k.L[0], k.wrap[0]);
-    const double d1 = min_image(Y[base + e] - cy_, k.L[1], k.wrap[1]);
-    const double d2 = min_image(Z[base + e] - cz_, k.L[2], k.wrap[2]);
+    const R d0 = min_image<R>((R)(X[base + e] - cx_), Lx, k.wrap[0]);
+    const R d1 = min_image<R>((R)(Y[base + e] - cy_), Ly, k.wrap[1]);
+    const R d2 = min_image<R>((R)(Z[base + e] - cz_), Lz, k.wrap[2]);
     rel[base + e] = Staged<R>::make(d0, d1, d2, base + e);
     r2max = fmax(r2max, d0 * d0 + d1 * d1 + d2 * d2);
   }
@@ -1914,10 +1923,10 @@ __global__ void __launch_bounds__(kBoundsThreads) platelet_bounds_k(PlateletCons
   if (lane == 0) s_r[wid] = r2max;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double m = 0;
+    R m = 0;
     for (int w = 0; w < NW; ++w) m = fmax(m, s_r[w]);
     bounds[4 * p] = cx_; bounds[4 * p + 1] = cy_; bounds[4 * p + 2] = cz_;
-    bounds[4 * p + 3] = sqrt(m);
+    bounds[4 * p + 3] = sqrt((double)m);
   }
 }
 
