@@ -147,6 +147,11 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
     k.hinv[c] = 1.0f / k.hs[c];
   }
   k.dtT = s->dt / mp[PF_P_T0];
+  k.omega_f = (float)k.omega;
+  k.kcoll_f = (float)k.kcoll;
+  k.kmom_f = (float)k.kmom;
+  for (int a = 0; a < 3; ++a) k.body_f[a] = (float)k.body[a];
+  k.uw_f = (float)k.uw;
   return k;
 }
 

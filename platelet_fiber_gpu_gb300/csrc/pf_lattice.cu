@@ -26,6 +26,14 @@ namespace {
 // store scales w_d * sigma and their inverses in LatticeConst
 __host__ __device__ constexpr int wcls(int d) { return d == 0 ? 0 : (d < 7 ? 1 : 2); }
 
+// a lattice constant in the arithmetic type: the double, or its float
+// rounding stored beside it
+template <class R>
+__device__ __forceinline__ R kv(double d, float f) {
+  if constexpr (sizeof(R) == 4) return f;
+  else return (R)d;
+}
+
 template <class S, class R>
 __device__ __forceinline__ R ld(const S* p, int d, const LatticeConst& k) {
   return (R)StoreTraits<S>::load(p, d, (decltype(StoreTraits<S>::load(p, 0, R(0))))k.hs[wcls(d)]);
@@ -187,14 +195,14 @@ __device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z,
     return;
   }
   if (apply_bc && k.bc[2] == PF_BC_ZOUHE_SHEAR && z == k.nz - 1) {
-    drho = zouhe_top(g, (R)k.uw);
-    ux = 0; uy = (R)k.uw; uz = 0;
+    drho = zouhe_top(g, kv<R>(k.uw, k.uw_f));
+    ux = 0; uy = kv<R>(k.uw, k.uw_f); uz = 0;
     return;
   }
   R jx, jy, jz;
   moments(g, drho, jx, jy, jz);
   const R rho = (R)1 + drho;
-  const R hk = (R)0.5 * (R)k.kmom;
+  const R hk = (R)0.5 * kv<R>(k.kmom, k.kmom_f);
   ux = (jx + hk * Fx) / rho;
   uy = (jy + hk * Fy) / rho;
   uz = (jz + hk * Fz) / rho;
@@ -261,14 +269,14 @@ __device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restr
     // velocity, and its populations are the uploaded fIN (no boundary pass)
     ld_u<R>(ubuf, n, drho, ux, uy, uz);
   } else {
-    R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
+    R px = kv<R>(k.body[0], k.body_f[0]), py = kv<R>(k.body[1], k.body_f[1]), pz = kv<R>(k.body[2], k.body_f[2]);
     if (fp) ld_force<R>(Fp, n, px, py, pz);
     node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
   }
-  R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+  R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
   if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
-  const R kc = (R)k.kcoll;
-  const R om = (R)k.omega;
+  const R kc = kv<R>(k.kcoll, k.kcoll_f);
+  const R om = kv<R>(k.omega, k.omega_f);
   collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
   // one pointer stepped by N: a 64-bit add per store instead of forming
   // each direction's index (16 % fewer instructions in the FP32 pass)
@@ -596,8 +604,8 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     }
   };
 
-  const R kc = (R)k.kcoll;
-  const R om = (R)k.omega;
+  const R kc = kv<R>(k.kcoll, k.kcoll_f);
+  const R om = kv<R>(k.omega, k.omega_f);
   const R sf = (R)1 - (R)0.5 * om;
   // One node; p points at the node's column in direction 0 of its staged row.
   // Called by whole warps (a warp's 32 nodes are one force brick, whose
@@ -634,11 +642,11 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     if (first) {
       ld_u<R>(ubuf, n, drho, ux, uy, uz);
     } else {
-      R px = (R)k.body[0], py = (R)k.body[1], pz = (R)k.body[2];
+      R px = kv<R>(k.body[0], k.body_f[0]), py = kv<R>(k.body[1], k.body_f[1]), pz = kv<R>(k.body[2], k.body_f[2]);
       if (fp) ld_force<R>(Fp, n, px, py, pz);
       node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
     }
-    R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+    R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
     if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
     collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, sf);
     S* o = gout + n;
@@ -729,7 +737,7 @@ __global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, co
     R g[Q];
     if constexpr (FAST) gather_fast<S, R>(k, gnew, x, y, z, g);
     else gather<S, R>(k, gnew, x, y, z, g);
-    R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+    R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
     ld_force<R>(Fc, n, Fx, Fy, Fz);
     R drho, ux, uy, uz;
     node_state<R>(k, g, z, true, Fx, Fy, Fz, drho, ux, uy, uz);
@@ -747,7 +755,7 @@ __global__ void download_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, con
   const int x = (int)(n % k.nx), y = (int)((n / k.nx) % k.ny), z = (int)(n / ((size_t)k.nx * k.ny));
   R g[Q];
   gather<S, R>(k, gsrc, x, y, z, g);
-  R Fx = (R)k.body[0], Fy = (R)k.body[1], Fz = (R)k.body[2];
+  R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
   ld_force<R>(Fsrc, n, Fx, Fy, Fz);
   R drho, ux, uy, uz;
   if (use_ubuf) {
@@ -816,7 +824,7 @@ __global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
     gather<S, R>(k, gsrc, x, y, z, g);
     if (k.bc[2] == PF_BC_ZOUHE_SHEAR && (z == 0 || z == k.nz - 1)) {
       if (z == 0) zouhe_bottom(g);
-      else zouhe_top(g, (R)k.uw);
+      else zouhe_top(g, kv<R>(k.uw, k.uw_f));
     }
     for (int d = 0; d < Q; ++d) {
       double f = (double)g[d] + wgt(d);
