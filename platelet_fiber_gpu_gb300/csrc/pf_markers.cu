@@ -246,16 +246,16 @@ __global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA
   spread_one<float>(lk, (ctl->step & 1) ? FB : FA, X[i], Y[i], Z[i], (float)fx, (float)fy, (float)fz);
 }
 
-// Force bricks of this step: every brick holding a lattice node within two
-// nodes (per axis) of a marker's base node -- floor(x/dx) as the FP64
-// stencils form it, floor(x * (1/dx)) as the FP32 stencil does -- which
-// contains every node the spreading and interpolation stencils of the
-// marker touch (base + {-2..2} in FP64, base + {-1..2} in FP32).  Set before
-// any force of the step exists, so the lattice pass over the other bricks
-// can run while the forces are computed.  One bit per node (a brick is one
-// 32-bit word): the position update sets each marker's bit for the next
-// step, the bits are dilated by kFlagR in x, y and z; a non-zero word flags
-// and lists its brick.
+// Force bricks of this step: every brick holding a lattice node that the
+// spreading and interpolation stencils of a marker touch: base + {-2..2} per
+// axis in FP64, base + {-1..2} in FP32, the base node being floor(x/dx) as
+// the FP64 stencils form it, floor(x * (1/dx)) as the FP32 stencil does.
+// Set before any force of the step exists, so the lattice pass over the
+// other bricks can run while the forces are computed.  One bit per node (a
+// brick is one 32-bit word): the position update sets each marker's bit for
+// the next step, the bits are dilated in x, y and z by the stencil's reach
+// (a mark at node b flags b-2 .. b+2 in FP64, b-1 .. b+2 in FP32); a
+// non-zero word flags and lists its brick.
 constexpr int kFlagR = 2;
 
 // Sets the occupancy bit of a marker's base node; nodes outside the lattice
@@ -290,28 +290,32 @@ __global__ void __launch_bounds__(128) mark_markers_k(LatticeConst lk, unsigned*
 // neighbour words (periodic rows: across the row's ends; when nx is not a
 // multiple of 32, a word next to occupied bits across the wrap is taken as
 // all set, a superset)
+// hi: reach of a mark towards lower x (nodes n - hi .. n flag from a mark at
+// n, the stencil's upper reach); marks reach kFlagR nodes towards higher x.
 __device__ __forceinline__ unsigned dilate_words(unsigned C, unsigned Lw, unsigned Rw, int bx, int nbx, bool wrap,
-                                                 bool partial) {
+                                                 bool partial, int hi) {
   // a partial last word is not bit-adjacent to word 0 across the wrap
   if (partial && wrap && ((bx == 0 && Lw) || (bx == nbx - 1 && Rw))) return 0xffffffffu;
   if (!(C | Lw | Rw)) return 0u;
   const unsigned long long lo = ((unsigned long long)C << 32) | Lw;  // C above its left neighbour
-  const unsigned long long hi = ((unsigned long long)Rw << 32) | C;  // C below its right neighbour
-  unsigned long long dl = lo, dh = hi;
+  const unsigned long long hi_w = ((unsigned long long)Rw << 32) | C;  // C below its right neighbour
+  unsigned long long dl = lo, dh = hi_w;
 #pragma unroll
   for (int r = 1; r <= kFlagR; ++r) {
     dl |= lo << r;
-    dh |= hi >> r;
+    if (r <= hi) dh |= hi_w >> r;
   }
   return (unsigned)(dl >> 32) | (unsigned)dh;
 }
 
-// One kernel per step: each brick word dilated by kFlagR nodes in x (bits),
-// y (rows, wrapped on an IBM-periodic axis) and z (planes); a non-zero word
-// flags and lists its brick (list[par], active_count[par]).  The dilation
-// distributes over OR, so it is done separably: a CTA takes kFlagRows whole
-// rows of one z-plane, ORs each row word (and its y halo) over the five
-// planes into shared memory, then over the five rows, then dilates in x.
+// One kernel per step: each brick word dilated by the stencil's reach in x
+// (bits), y (rows, wrapped on an IBM-periodic axis) and z (planes): marks up
+// to kFlagR nodes below a node and up to hi above it (2 FP64, 1 FP32) flag
+// it; a non-zero word flags and lists its brick (list[par],
+// active_count[par]).  The dilation distributes over OR, so it is done
+// separably: a CTA takes flag_rows() whole rows of one z-plane, ORs each row
+// word (and its y halo) over the planes into shared memory, then over the
+// rows, then dilates in x.
 // The occupancy bits of the step (buffer par) are left for the
 // flagged-brick lattice pass to clear.  With the near region of the
 // pipelined schedule (nearA/B): a flagged brick outside it was updated
@@ -327,7 +331,7 @@ __host__ __device__ inline int flag_rows(int nbx) {
 }
 __global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const unsigned* mark, unsigned* flA,
                                                        unsigned* flB, int* lA, int* lB, const unsigned char* nearA,
-                                                       const unsigned char* nearB, Control* ctl) {
+                                                       const unsigned char* nearB, int hi, Control* ctl) {
   if (ctl->done) return;
   __shared__ unsigned s_z[kFlagWords];  // OR over the planes, rows y0-2 .. y0+R+1
   __shared__ unsigned s_yz[kFlagWords];  // OR over the rows too, rows y0 .. y0+R-1
@@ -354,6 +358,7 @@ __global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const un
     if (ok)
 #pragma unroll
       for (int dz = -kFlagR; dz <= kFlagR; ++dz) {
+        if (dz > hi) break;
         const int zz = z + dz;
         if (zz >= 0 && zz < lk.nz) acc |= mk[bx + (size_t)nbx * (yy + (size_t)lk.ny * zz)];
       }
@@ -364,7 +369,8 @@ __global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const un
   for (int i = threadIdx.x; i < outs; i += kFlagThreads) {
     unsigned acc = 0;
 #pragma unroll
-    for (int dy = 0; dy <= 2 * kFlagR; ++dy) acc |= s_z[i + dy * nbx];
+    for (int dy = 0; dy <= 2 * kFlagR; ++dy)
+      if (dy <= kFlagR + hi) acc |= s_z[i + dy * nbx];
     s_yz[i] = acc;
   }
   __syncthreads();
@@ -380,7 +386,7 @@ __global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const un
       const unsigned Lw = bx > 0 ? s_yz[i - 1] : (wrap ? s_yz[rowbase + nbx - 1] : 0u);
       const unsigned Rw = bx < nbx - 1 ? s_yz[i + 1] : (wrap ? s_yz[rowbase] : 0u);
       w = bx + nbx * (y + lk.ny * z);
-      f = dilate_words(C, Lw, Rw, bx, nbx, wrap, partial) != 0u;
+      f = dilate_words(C, Lw, Rw, bx, nbx, wrap, partial, hi) != 0u;
       if (f) {
         fl[w] = 1u;
         if (nr && !nr[w]) atomicOr(&ctl->err, ERR_FAR_FLAGGED);
@@ -2542,7 +2548,8 @@ cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cu
   const int R = flag_rows(L.k.nbx);
   if ((R + 2 * kFlagR) * L.k.nbx > kFlagWords) return cudaErrorInvalidValue;  // rows wider than 131072 nodes
   flag_k<<<L.k.nz * ((L.k.ny + R - 1) / R), kFlagThreads, 0, st>>>(L.k, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1],
-                                           check_near ? L.near[0] : nullptr, check_near ? L.near[1] : nullptr, ctl);
+                                           check_near ? L.near[0] : nullptr, check_near ? L.near[1] : nullptr,
+                                           L.precision == PF_PREC_FP64 ? kFlagR : kFlagR - 1, ctl);
   return cudaGetLastError();
 }
 
