@@ -173,6 +173,27 @@ int pfgpu_job_launches_per_step(const pfgpu_job *job);
  * shared memory by bulk asynchronous copies; needs nx * sizeof(population)
  * to be a multiple of 16 bytes) or "direct" (per-node gathers). */
 const char *pfgpu_job_lbm_kernel(const pfgpu_job *job);
+
+/* ---- element output dumps ----------------------------------------------
+ * The reference driver's element files, written from a job's state
+ * (replaces the fopen/fwrite/fprintf blocks of gpuSEM_LB.c:1327-1336,
+ * 1376-1407, 1464-1494 and 1533): in `dir`, cellsPos.data, cellsVel.data,
+ * cellsForce.data (per element x, y, z, z -- RY for the position's y, the
+ * last value repeated "for alignment in the octal dump"), the three
+ * "Timestep ElemID X Y Z" ASCII tables and cellsPauseTime.dat (appended).
+ * PFGPU_OUT_FP64 writes doubles as the reference does; PFGPU_OUT_FP32 writes
+ * floats, the 16-byte records convBtoXYZ.py reads through `od -f`. */
+enum { PFGPU_OUT_FP64 = 0, PFGPU_OUT_FP32 = 1 };
+typedef struct pfgpu_output pfgpu_output;
+/* Opens the files and writes the initial frame (timestep 0 tables; all
+ * three binary files). */
+int pfgpu_output_open(pfgpu_job *job, const char *dir, int mode, pfgpu_output **out);
+/* Appends one frame at the job's current step: positions to cellsPos.data
+ * and a row per element to each table (gpuSEM_LB.c:1464-1494). */
+int pfgpu_output_frame(pfgpu_output *out);
+/* Appends "<step * dt>, <seed>" to cellsPauseTime.dat (gpuSEM_LB.c:1533)
+ * and closes the files. */
+int pfgpu_output_close(pfgpu_output *out, int seed);
 void pfgpu_job_destroy(pfgpu_job *job);
 
 /* Device bytes a job with this scene and precision would allocate. */

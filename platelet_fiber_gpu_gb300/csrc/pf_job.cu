@@ -946,6 +946,11 @@ double pfgpu_detach_uniform(uint64_t seed, int64_t step) { return detach_uniform
 
 // internal accessors for the batch and drop-in layers
 cudaStream_t pfgpu_job_stream_(pfgpu_job* j) { return j->s0; }
+void pfgpu_job_elem_dims_(const pfgpu_job* j, int* P, int* E, double* dt) {
+  *P = j->has_pl ? j->Pl.k.P : 0;
+  *E = j->has_pl ? j->Pl.k.E : 0;
+  *dt = (double)j->L.k.dtf;
+}
 int pfgpu_job_control_(pfgpu_job* j, Control* out) {
   CK(cudaMemcpy(out, j->ctl, sizeof *out, cudaMemcpyDeviceToHost));
   return PFGPU_OK;

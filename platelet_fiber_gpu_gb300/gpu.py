@@ -56,6 +56,9 @@ def lib():
         L.pfgpu_job_destroy.argtypes = [vp]
         L.pfgpu_job_lbm_kernel.restype = C.c_char_p
         L.pfgpu_job_lbm_kernel.argtypes = [vp]
+        L.pfgpu_output_open.argtypes = [vp, C.c_char_p, C.c_int, C.POINTER(vp)]
+        L.pfgpu_output_frame.argtypes = [vp]
+        L.pfgpu_output_close.argtypes = [vp, C.c_int]
         L.pfgpu_job_profile.argtypes = [vp, C.c_int, dp]
         L.pfgpu_job_get_cells.argtypes = [vp, ip, ip, ip, ip]
         L.pfgpu_profile_phase_count.restype = C.c_int
@@ -146,6 +149,11 @@ class Job:
     def lbm_kernel(self) -> str:
         return lib().pfgpu_job_lbm_kernel(self.h).decode()
 
+    def output(self, directory: str, fp32: bool = False) -> "Output":
+        """The reference driver's element dumps in `directory` (initial frame
+        written now); fp32: float records for convBtoXYZ.py."""
+        return Output(self, directory, fp32)
+
     def lattice(self, fIN=True, fOUT=False):
         N = self.scene.n_nodes
         a = np.zeros((19, N)) if fIN else None
@@ -201,6 +209,24 @@ class Job:
         out = np.zeros(4)
         check(lib().pfgpu_job_conservation(self.h, _p(out)))
         return out
+
+
+class Output:
+    """cellsPos/Vel/Force.data, the ASCII tables and cellsPauseTime.dat of a
+    job (pfgpu_output_*)."""
+
+    def __init__(self, job: Job, directory: str, fp32: bool = False):
+        self.job = job
+        self.h = C.c_void_p()
+        check(lib().pfgpu_output_open(job.h, str(directory).encode(), 1 if fp32 else 0, C.byref(self.h)))
+
+    def frame(self):
+        check(lib().pfgpu_output_frame(self.h))
+
+    def close(self, seed: int = 0):
+        if self.h:
+            check(lib().pfgpu_output_close(self.h, int(seed)))
+            self.h = C.c_void_p()
 
 
 class _BatchJob(Job):
