@@ -241,6 +241,15 @@ def single_large(seed: int = 2, nx=256, ny=128, nz=128, n_platelets=50, n_membra
     return sc
 
 
+def mixed_large(seed: int = 5) -> Scene:
+    """The mixed-precision large case: single_large's scene scaled to a
+    512x256x256 channel with 500 platelets and a 100k-node / 200k-link fibrin
+    mesh on the bottom wall."""
+    sc = single_large(seed=seed, nx=512, ny=256, nz=256, n_platelets=500, n_fib=100000, n_links=200000)
+    sc.meta.update(workload="mixed_large")
+    return sc
+
+
 def mixed_small(seed: int = 3, nx=40, ny=32, nz=20, n_platelets=3, level=1, n_cyto=12, n_fib=300,
                 n_links=600, n_rec=40, bell=False) -> Scene:
     """Every feature of single_large on a lattice the oracle steps in seconds."""
