@@ -146,6 +146,8 @@ def replica_value(world: int, nodes_per_replica: int, t_step_max: float) -> floa
 
 def build_scene(args):
     from platelet_fiber_gpu_gb300 import workloads as W
+    if getattr(args, "workload", "single_large") == "plain_small":
+        return W.plain_small()
     return W.single_large(seed=args.seed, nx=args.nx, ny=args.ny, nz=args.nz, n_platelets=args.platelets,
                           n_fib=args.fibrin, n_links=2 * args.fibrin)
 
@@ -193,6 +195,9 @@ def run_reference(args, rank):
 
 
 def workload_name(args):
+    if getattr(args, "workload", "single_large") == "plain_small":
+        return ("plain_small: D3Q19 64x32x32 body-force channel, bounce-back walls on y and z, periodic x, "
+                "1 platelet x 600 SEM elements, 200-node/400-link Hookean fibrin mesh")
     return (f"single_large: D3Q19 {args.nx}x{args.ny}x{args.nz} shear 1000/s Zou/He walls, {args.platelets} platelets"
             f" x 600 SEM elements (400 membrane + 200 cytoplasm, Morse U0=1 rho=2 r_eq=0.3 cut 1.0 um), "
             f"{args.fibrin}-node/{2 * args.fibrin}-link Hookean fibrin on the bottom wall, 200 receptors/platelet, "
@@ -215,6 +220,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--profile-steps", type=int, default=200)
+    ap.add_argument("--workload", default="single_large", choices=["single_large", "plain_small"],
+                    help="single_large (the 256x128x128 channel) or plain_small (the 64x32x32 body-force channel)")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -316,7 +323,7 @@ def main():
         "vs_baseline": None,
         "dtype": PREC_NAME[prec],
         "data": "synthetic",
-        "config": {"workload": workload_name(args), "lattice": [args.nx, args.ny, args.nz], "nodes": N,
+        "config": {"workload": workload_name(args), "lattice": [scene.nx, scene.ny, scene.nz], "nodes": N,
                    "elements": PE, "fibrin_nodes": scene.n_fib, "receptors": scene.n_platelets * scene.n_rec,
                    "parallelism": f"replicas x{world}", "l2": "working set > L2 (2 x 19 x N x 4 B populations)",
                    "precision": PREC_NAME[prec]},
