@@ -122,6 +122,27 @@ struct StoreTraits<__half> {
   __device__ static void store(__half* p, float v, int, float inv_s) { *p = __float2half_rn(v * inv_s); }
 };
 
+// The job owning CTA b of a fused batch launch: the last j with
+// start[j] <= b (jobs with no CTAs have start[j] == start[j + 1]).
+__device__ __forceinline__ int batch_job_of(const int* start, int nj, int b) {
+  int lo = 0, hi = nj;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (start[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// word-parallel copy of a trivially copyable struct by the threads of a CTA
+// (a fused batch kernel's per-job constants into shared memory)
+template <class T>
+__device__ __forceinline__ void cta_copy(T& dst, const T& src) {
+  static_assert(sizeof(T) % 4 == 0, "word copy");
+  for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(&dst)[i] = reinterpret_cast<const int*>(&src)[i];
+}
+
 __device__ inline int wrapi(int a, int n) {
   int r = a % n;
   return r < 0 ? r + n : r;

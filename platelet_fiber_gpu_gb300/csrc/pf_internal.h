@@ -148,6 +148,43 @@ struct Fibrin {
   size_t bytes = 0;
 };
 
+// ------------------------------------------------------------------ batches
+// One job of a fused batch step: copies of the job's lattice, platelet and
+// fibrin handles (device pointers and constants), read by the batch kernels.
+struct BatchDesc {
+  Lattice L;
+  Platelets Pl;
+  Fibrin Fb;
+  int has_pl, has_fb;
+  Control* ctl;
+  unsigned* done_blocks;
+  double detach_rate;
+  uint64_t seed;
+};
+// Kernels of a fused batch step; each runs over all jobs of the batch, a job
+// owning the CTAs [start[j], start[j+1]) of the launch.
+enum BatchKernel : int {
+  BK_FLAG = 0, BK_LBM_UNFLAGGED, BK_MEMBRANE, BK_BOUNDS, BK_MORSE, BK_BOND_PREP, BK_BOND_RESOLVE, BK_FIBRIN,
+  BK_SPREAD_ELEM, BK_SPREAD_BOND, BK_SPREAD_FIB, BK_LBM_FLAGGED, BK_MOMENTS, BK_INTERP, BK_COUNT
+};
+// row segments of kLbmBlock nodes per CTA of the fused unflagged lattice pass
+constexpr int kBatchRows = 8;
+// CTAs job `d` needs for kernel `kind` (0: the kernel has no work for it)
+int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs);
+// whether the batch kernels can take this job (row width of the flagging)
+bool batch_supported(const BatchDesc& d);
+// Block size and dynamic shared memory of a batch kernel
+int batch_threads(int kind);
+size_t batch_smem(const BatchDesc& d, int kind);
+// Launches one batch kernel over `total` CTAs; precision and fast gather are
+// the batch's (all jobs share them).
+cudaError_t batch_launch(int kind, const BatchDesc* descs, const int* start, int njobs, int total, size_t smem,
+                         int precision, bool fast, cudaStream_t st);
+// the lattice part of batch_launch (pf_lattice.cu)
+cudaError_t batch_launch_lattice(int kind, const BatchDesc* descs, const int* start, int njobs, int total,
+                                 int precision, bool fast, cudaStream_t st);
+bool fast_gather(const Lattice& L);
+
 // ------------------------------------------------------------------ launchers
 // All launchers enqueue on `st` and return the launch error.
 cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_dev, const double* ru_dev,

@@ -946,6 +946,25 @@ double pfgpu_detach_uniform(uint64_t seed, int64_t step) { return detach_uniform
 
 // internal accessors for the batch and drop-in layers
 cudaStream_t pfgpu_job_stream_(pfgpu_job* j) { return j->s0; }
+// The job's handles for a fused batch step; returns 0 when the job cannot
+// take part (FP64, platelet boxes, the pipelined schedule, cell-list Morse,
+// or a platelet too large for the item-parallel membrane kernel).
+int pfgpu_job_batch_desc_(pfgpu_job* j, BatchDesc* d, int* precision, int* fast) {
+  if (j->precision == PF_PREC_FP64 || j->L.ibm_box || j->pipeline) return 0;
+  if (j->has_pl && (!j->Pl.mem_items || (j->Pl.k.morse && morse_uses_cells(j->Pl.k)))) return 0;
+  d->L = j->L;
+  d->Pl = j->has_pl ? j->Pl : Platelets();
+  d->Fb = j->has_fb ? j->Fb : Fibrin();
+  d->has_pl = j->has_pl;
+  d->has_fb = j->has_fb;
+  d->ctl = j->ctl;
+  d->done_blocks = j->done_blocks;
+  d->detach_rate = j->detach_rate;
+  d->seed = j->seed;
+  *precision = j->precision;
+  *fast = fast_gather(j->L) ? 1 : 0;
+  return 1;
+}
 void pfgpu_job_elem_dims_(const pfgpu_job* j, int* P, int* E, double* dt) {
   *P = j->has_pl ? j->Pl.k.P : 0;
   *E = j->has_pl ? j->Pl.k.E : 0;

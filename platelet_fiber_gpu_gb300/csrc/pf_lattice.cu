@@ -309,11 +309,13 @@ __device__ __forceinline__ void zero_bins(int* bin_count, int ncells, Control* c
 //                far_first, and has no force (no far brick is flagged in
 //                this step or the previous one).
 enum : int { kPassAll = 0, kPassUnflag = 1, kPassNear = 4, kPassFar = 3 };
+// bid / nblk: the CTA's index and the number of CTAs of this lattice's pass
+// (the launch is one-dimensional: x-row segments, then rows, then planes)
 template <class S, class R, bool FAST>
-__global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
-                                                        R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
-                                                        int ncells, int mode, const unsigned char* nearA,
-                                                        const unsigned char* nearB, Control* ctl) {
+__device__ __forceinline__ void lbm_step_body(const LatticeConst& k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                              R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                              int ncells, int mode, const unsigned char* nearA,
+                                              const unsigned char* nearB, Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   const bool far = mode == kPassFar;
   const int par = (int)((far ? ctl->far_step : ctl->step) & 1);
@@ -323,15 +325,14 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
   R4<R>* Fp = par ? FA : FB;
   unsigned* flp = par ? flA : flB;
   const unsigned* flc = par ? flB : flA;
-  const int x = blockIdx.x * kLbmBlock + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  const int gx = (k.nx + kLbmBlock - 1) / kLbmBlock;
+  const int yz = bid / gx;
+  const int x = (bid - yz * gx) * kLbmBlock + threadIdx.x, y = yz % k.ny, z = yz / k.ny;
   const int bxw = x / kBrickX;
   const bool row_ok = bxw < k.nbx;
   const int brick = bxw + k.nbx * (y + k.ny * z);
-  if (bin_count) {
-    const size_t tid = (((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * blockDim.x +
-                       threadIdx.x;
-    zero_bins(bin_count, ncells, ctl, tid, (size_t)gridDim.x * gridDim.y * gridDim.z * blockDim.x);
-  }
+  if (bin_count)
+    zero_bins(bin_count, ncells, ctl, (size_t)bid * blockDim.x + threadIdx.x, (size_t)nblk * blockDim.x);
   // whole warp: one brick
   if (mode == kPassNear || far) {
     const unsigned char* nr = par ? nearB : nearA;
@@ -348,6 +349,14 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
   if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, fc, fp, ctl->first);
   __syncwarp();
   if ((threadIdx.x & 31) == 0 && fp) flp[brick] = 0;
+}
+template <class S, class R, bool FAST>
+__global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                                        R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                                        int ncells, int mode, const unsigned char* nearA,
+                                                        const unsigned char* nearB, Control* ctl) {
+  lbm_step_body<S, R, FAST>(k, gA, gB, FA, FB, ubuf, flA, flB, bin_count, ncells, mode, nearA, nearB, ctl,
+                            blockIdx.x, gridDim.x);
 }
 
 // Near region of a step from a per-brick word array (non-zero: set): every
@@ -392,10 +401,10 @@ __global__ void far_counter_k(Control* ctl, int sync) {
 
 // The flagged bricks of this step (list[par]), one warp per brick.
 template <class S, class R, bool FAST>
-__global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
-                                                        R4<R>* ubuf, unsigned* flA, unsigned* flB, const int* lA,
-                                                        const int* lB, int* bin_count, int ncells, unsigned* mark,
-                                                        Control* ctl) {
+__device__ __forceinline__ void lbm_list_body(const LatticeConst& k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                              R4<R>* ubuf, unsigned* flA, unsigned* flB, const int* lA,
+                                              const int* lB, int* bin_count, int ncells, unsigned* mark,
+                                              Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   const int par = (int)(ctl->step & 1);
   const S* __restrict__ gin = par ? gB : gA;
@@ -410,10 +419,10 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S
   const int cnt = ctl->active_count[par];
   const int first = ctl->first;
   if (bin_count)
-    zero_bins(bin_count, ncells, ctl, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+    zero_bins(bin_count, ncells, ctl, (size_t)bid * blockDim.x + threadIdx.x, (size_t)nblk * blockDim.x);
   const int warps = kLbmBlock / 32;
   const int lane = threadIdx.x & 31;
-  for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < cnt; b += gridDim.x * warps) {
+  for (int b = bid * warps + (threadIdx.x >> 5); b < cnt; b += nblk * warps) {
     const int brick = list[b];
     const int bx = brick % k.nbx;
     const int y = (brick / k.nbx) % k.ny;
@@ -427,6 +436,14 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S
       mk[brick] = 0u;
     }
   }
+}
+template <class S, class R, bool FAST>
+__global__ void __launch_bounds__(kLbmBlock) lbm_list_k(LatticeConst k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
+                                                        R4<R>* ubuf, unsigned* flA, unsigned* flB, const int* lA,
+                                                        const int* lB, int* bin_count, int ncells, unsigned* mark,
+                                                        Control* ctl) {
+  lbm_list_body<S, R, FAST>(k, gA, gB, FA, FB, ubuf, flA, flB, lA, lB, bin_count, ncells, mark, ctl, blockIdx.x,
+                            gridDim.x);
 }
 
 // ------------------------------------------------------------ row-staged step
@@ -715,9 +732,9 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
 // boundary conditions, with this step's force: input of the IBM interpolation
 // (the reference's velocity_density, LB_kernel.cu:1108-1199).
 template <class S, class R, bool FAST>
-__global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, const S* gA, const S* gB,
-                                                              const R4<R>* FA, const R4<R>* FB, R4<R>* ubuf,
-                                                              const int* lA, const int* lB, const Control* ctl) {
+__device__ __forceinline__ void moments_body(const LatticeConst& k, const S* gA, const S* gB, const R4<R>* FA,
+                                             const R4<R>* FB, R4<R>* ubuf, const int* lA, const int* lB,
+                                             const Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   const int par = (int)(ctl->step & 1);
   const S* gnew = par ? gA : gB;
@@ -726,7 +743,7 @@ __global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, co
   const int cnt = ctl->active_count[par];
   const int warps = kLbmBlock / 32;
   const int lane = threadIdx.x & 31;
-  for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < cnt; b += gridDim.x * warps) {
+  for (int b = bid * warps + (threadIdx.x >> 5); b < cnt; b += nblk * warps) {
     const int brick = list[b];
     const int bx = brick % k.nbx;
     const int y = (brick / k.nbx) % k.ny;
@@ -743,6 +760,54 @@ __global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, co
     node_state<R>(k, g, z, true, Fx, Fy, Fz, drho, ux, uy, uz);
     st_u<R>(ubuf, n, drho, ux, uy, uz);
   }
+}
+template <class S, class R, bool FAST>
+__global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, const S* gA, const S* gB,
+                                                              const R4<R>* FA, const R4<R>* FB, R4<R>* ubuf,
+                                                              const int* lA, const int* lB, const Control* ctl) {
+  moments_body<S, R, FAST>(k, gA, gB, FA, FB, ubuf, lA, lB, ctl, blockIdx.x, gridDim.x);
+}
+
+// ------------------------------------------------------------- batch kernels
+// lattice passes of a fused batch: the job's LatticeConst is copied to shared
+// memory (no aliasing with the populations the pass writes)
+template <class S, class R, bool FAST>
+__global__ void __launch_bounds__(kLbmBlock) lbm_step_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  __shared__ LatticeConst s_k;
+  const int j = batch_job_of(start, nj, blockIdx.x);
+  const BatchDesc& d = descs[j];
+  cta_copy(s_k, d.L.k);
+  __syncthreads();
+  const Lattice& L = d.L;
+  // kBatchRows row segments per CTA (amortizes the per-CTA set-up)
+  const int segs = ((s_k.nx + kLbmBlock - 1) / kLbmBlock) * s_k.ny * s_k.nz;
+  for (int r = (blockIdx.x - start[j]) * kBatchRows, e = min(segs, r + kBatchRows); r < e; ++r)
+    lbm_step_body<S, R, FAST>(s_k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
+                              L.flags[0], L.flags[1], nullptr, 0, 1, L.near[0], L.near[1], d.ctl, r, segs);
+}
+template <class S, class R, bool FAST>
+__global__ void __launch_bounds__(kLbmBlock) lbm_list_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  __shared__ LatticeConst s_k;
+  const int j = batch_job_of(start, nj, blockIdx.x);
+  const BatchDesc& d = descs[j];
+  cta_copy(s_k, d.L.k);
+  __syncthreads();
+  const Lattice& L = d.L;
+  lbm_list_body<S, R, FAST>(s_k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
+                            L.flags[0], L.flags[1], L.list[0], L.list[1], nullptr, 0, L.mark, d.ctl,
+                            blockIdx.x - start[j], start[j + 1] - start[j]);
+}
+template <class S, class R, bool FAST>
+__global__ void __launch_bounds__(kLbmBlock) moments_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  __shared__ LatticeConst s_k;
+  const int j = batch_job_of(start, nj, blockIdx.x);
+  const BatchDesc& d = descs[j];
+  cta_copy(s_k, d.L.k);
+  __syncthreads();
+  const Lattice& L = d.L;
+  moments_body<S, R, FAST>(s_k, (const S*)L.g[0], (const S*)L.g[1], (const R4<R>*)L.F[0], (const R4<R>*)L.F[1],
+                           (R4<R>*)L.ubuf, L.list[0], L.list[1], d.ctl, blockIdx.x - start[j],
+                           start[j + 1] - start[j]);
 }
 
 // Full-lattice post-stream state in the reference's host layouts (double).
@@ -921,7 +986,7 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
                                      ctl);
     return cudaGetLastError();
   }
-  dim3 grid((L.k.nx + kLbmBlock - 1) / kLbmBlock, L.k.ny, L.k.nz);
+  const unsigned grid = (unsigned)((L.k.nx + kLbmBlock - 1) / kLbmBlock) * L.k.ny * L.k.nz;
   auto kern = fast_lattice(L) ? lbm_step_k<S, R, true> : lbm_step_k<S, R, false>;
   kern<<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
                                    L.flags[0], L.flags[1], bin_count, ncells, part, L.near[0], L.near[1], ctl);
@@ -1025,6 +1090,31 @@ cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st) {
   far_counter_k<<<1, 1, 0, st>>>(ctl, sync);
   return cudaGetLastError();
 }
+bool fast_gather(const Lattice& L) { return fast_lattice(L); }
+
+template <class S, bool FAST>
+static cudaError_t batch_lattice_impl(int kind, const BatchDesc* d, const int* start, int nj, int total,
+                                      cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  switch (kind) {
+    case BK_LBM_UNFLAGGED: lbm_step_batch_k<S, float, FAST><<<total, kLbmBlock, 0, st>>>(d, start, nj); break;
+    case BK_LBM_FLAGGED: lbm_list_batch_k<S, float, FAST><<<total, kLbmBlock, 0, st>>>(d, start, nj); break;
+    case BK_MOMENTS: moments_batch_k<S, float, FAST><<<total, kLbmBlock, 0, st>>>(d, start, nj); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+cudaError_t batch_launch_lattice(int kind, const BatchDesc* d, const int* start, int nj, int total, int precision,
+                                 bool fast, cudaStream_t st) {
+  if (precision == PF_PREC_FP32)
+    return fast ? batch_lattice_impl<float, true>(kind, d, start, nj, total, st)
+                : batch_lattice_impl<float, false>(kind, d, start, nj, total, st);
+  if (precision == PF_PREC_FP16)
+    return fast ? batch_lattice_impl<__half, true>(kind, d, start, nj, total, st)
+                : batch_lattice_impl<__half, false>(kind, d, start, nj, total, st);
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t lattice_configure(Lattice& L) {
   switch (L.precision) {
     case PF_PREC_FP64: rows_config<double, double>(L); return cudaSuccess;

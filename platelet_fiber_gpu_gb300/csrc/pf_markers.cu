@@ -228,11 +228,11 @@ __global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R
 // FP32 spreading of one force part as soon as it exists: n markers at
 // (X, Y, Z) with force Fa (float, may be null) + Fd / div (double, may be
 // null), components n apart; markers whose part is zero add nothing.
-__global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA, float4* FB, int n,
+__device__ __forceinline__ void spread_part_k_body(const LatticeConst& lk, float4* FA, float4* FB, int n,
                                                      const double* X, const double* Y, const double* Z,
-                                                     const float* Fa, const double* Fd, double div, Control* ctl) {
+                                                     const float* Fa, const double* Fd, double div, Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = bid * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double fx = 0, fy = 0, fz = 0;
   if (Fa) { fx = (double)Fa[i]; fy = (double)Fa[n + i]; fz = (double)Fa[2 * n + i]; }
@@ -244,6 +244,11 @@ __global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA
   }
   if (fx == 0 && fy == 0 && fz == 0) return;
   spread_one<float>(lk, (ctl->step & 1) ? FB : FA, X[i], Y[i], Z[i], (float)fx, (float)fy, (float)fz);
+}
+__global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA, float4* FB, int n,
+                                                     const double* X, const double* Y, const double* Z,
+                                                     const float* Fa, const double* Fd, double div, Control* ctl) {
+  spread_part_k_body(lk, FA, FB, n, X, Y, Z, Fa, Fd, div, ctl, blockIdx.x, gridDim.x);
 }
 
 // Force bricks of this step: every brick holding a lattice node that the
@@ -329,9 +334,9 @@ __host__ __device__ inline int flag_rows(int nbx) {
   while (r > 1 && (r + 2 * kFlagR) * nbx > kFlagWords) --r;
   return r;
 }
-__global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const unsigned* mark, unsigned* flA,
+__device__ __forceinline__ void flag_k_body(const LatticeConst& lk, const unsigned* mark, unsigned* flA,
                                                        unsigned* flB, int* lA, int* lB, const unsigned char* nearA,
-                                                       const unsigned char* nearB, int hi, Control* ctl) {
+                                                       const unsigned char* nearB, int hi, Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   __shared__ unsigned s_z[kFlagWords];  // OR over the planes, rows y0-2 .. y0+R+1
   __shared__ unsigned s_yz[kFlagWords];  // OR over the rows too, rows y0 .. y0+R-1
@@ -344,7 +349,7 @@ __global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const un
   const bool wrap = lk.ibm_wrap[0] != 0, partial = (lk.nx & 31) != 0;
   const int nbx = lk.nbx, R = flag_rows(nbx);
   const int ytiles = (lk.ny + R - 1) / R;
-  const int z = blockIdx.x / ytiles, y0 = (blockIdx.x % ytiles) * R;
+  const int z = bid / ytiles, y0 = (bid % ytiles) * R;
   const int halo = (R + 2 * kFlagR) * nbx;
   for (int i = threadIdx.x; i < halo; i += kFlagThreads) {
     const int bx = i % nbx;
@@ -400,6 +405,11 @@ __global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const un
       if (f) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
     }
   }
+}
+__global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const unsigned* mark, unsigned* flA,
+                                                       unsigned* flB, int* lA, int* lB, const unsigned char* nearA,
+                                                       const unsigned char* nearB, int hi, Control* ctl) {
+  flag_k_body(lk, mark, flA, flB, lA, lB, nearA, nearB, hi, ctl, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------- interp + advance
@@ -480,12 +490,12 @@ __device__ __forceinline__ void advance_marker(const LatticeConst& lk, const Pla
 // force buffer's list, and the detach test of the next step
 // (semLB.cu:451-455).
 __device__ __forceinline__ void close_step(const PlateletConst& pk, Control* ctl, unsigned* done_blocks,
-                                           double detach_rate, uint64_t seed) {
+                                           double detach_rate, uint64_t seed, int nblk) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned prev = atomicAdd(done_blocks, 1u);
-    if (prev == gridDim.x - 1) {
+    if (prev == (unsigned)nblk - 1) {
       __threadfence();
       // the next step flags into the other force buffer: empty its list
       ctl->active_count[(int)(ctl->step & 1) ^ 1] = 0;
@@ -504,15 +514,15 @@ __device__ __forceinline__ void close_step(const PlateletConst& pk, Control* ctl
 // Ftot (optional): the element force total of the step (membrane + Morse +
 // bonds), written here when the parts were spread separately.
 template <class R>
-__global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, PlateletConst pk, const R4<R>* ubuf,
+__device__ __forceinline__ void interp_advance_k_body(const LatticeConst& lk, const PlateletConst& pk, const R4<R>* ubuf,
                                                         int PE, double* X, double* Y, double* RY, double* Z,
                                                         double* V, int M, double* fX, double* fY, double* fZ,
                                                         double* fV, const int* ffix, int* bin_count, float4* bin,
                                                         unsigned* mark, Control* ctl, unsigned* done_blocks,
                                                         double detach_rate, uint64_t seed, const R* Fmem,
-                                                        const double* Fmorse, const R* Fbond, double* Ftot) {
+                                                        const double* Fmorse, const R* Fbond, double* Ftot, int bid, int nblk) {
   if (ctl->done) return;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = bid * blockDim.x + threadIdx.x;
   if (idx < PE + M) {
     const bool el = idx < PE;
     const int m = idx - PE;
@@ -528,7 +538,17 @@ __global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, Platele
     advance_marker(lk, pk, idx, PE, x, y, z, (double)ax, (double)ay, (double)az, X, Y, RY, Z, V, M, fX, fY, fZ,
                    fV, ffix, bin_count, bin, mark, ctl, sizeof(R) == 8);
   }
-  close_step(pk, ctl, done_blocks, detach_rate, seed);
+  close_step(pk, ctl, done_blocks, detach_rate, seed, nblk);
+}
+template <class R>
+__global__ void __launch_bounds__(128) interp_advance_k(LatticeConst lk, PlateletConst pk, const R4<R>* ubuf,
+                                                        int PE, double* X, double* Y, double* RY, double* Z,
+                                                        double* V, int M, double* fX, double* fY, double* fZ,
+                                                        double* fV, const int* ffix, int* bin_count, float4* bin,
+                                                        unsigned* mark, Control* ctl, unsigned* done_blocks,
+                                                        double detach_rate, uint64_t seed, const R* Fmem,
+                                                        const double* Fmorse, const R* Fbond, double* Ftot) {
+  interp_advance_k_body<R>(lk, pk, ubuf, PE, X, Y, RY, Z, V, M, fX, fY, fZ, fV, ffix, bin_count, bin, mark, ctl, done_blocks, detach_rate, seed, Fmem, Fmorse, Fbond, Ftot, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------ platelet boxes (FP32)
@@ -753,7 +773,7 @@ __global__ void __launch_bounds__(kBoxThreads) interp_box_k(LatticeConst lk, Pla
       advance_marker(lk, pk, PE + m, PE, x, y, z, (double)ax, (double)ay, (double)az, X, Y, RY, Z, V, M, fX, fY,
                      fZ, fV, ffix, bin_count, bin, mark, ctl, false);
     }
-    close_step(pk, ctl, done_blocks, detach_rate, seed);
+    close_step(pk, ctl, done_blocks, detach_rate, seed, gridDim.x);
     return;
   }
   extern __shared__ __align__(16) unsigned char s_raw[];
@@ -774,7 +794,7 @@ __global__ void __launch_bounds__(kBoxThreads) interp_box_k(LatticeConst lk, Pla
       advance_marker(lk, pk, g, PE, x, y, z, (double)ax, (double)ay, (double)az, X, Y, RY, Z, V, M, fX, fY, fZ,
                      fV, ffix, bin_count, bin, mark, ctl, false);
     }
-    close_step(pk, ctl, done_blocks, detach_rate, seed);
+    close_step(pk, ctl, done_blocks, detach_rate, seed, gridDim.x);
     return;
   }
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
@@ -853,7 +873,7 @@ __global__ void __launch_bounds__(kBoxThreads) interp_box_k(LatticeConst lk, Pla
     advance_marker(lk, pk, base + e, PE, s_pos[e], s_pos[kBoxElems + e], s_pos[2 * kBoxElems + e], (double)s_v[e],
                    (double)s_v[kBoxElems + e], (double)s_v[2 * kBoxElems + e], X, Y, RY, Z, V, M, fX, fY, fZ, fV,
                    ffix, bin_count, bin, mark, ctl, false);
-  close_step(pk, ctl, done_blocks, detach_rate, seed);
+  close_step(pk, ctl, done_blocks, detach_rate, seed, gridDim.x);
 }
 
 __global__ void bin_elements_k(PlateletConst pk, int PE, const double* X, const double* Y, const double* Z,
@@ -1335,14 +1355,13 @@ __device__ __forceinline__ float heron(float l1, float l2, float l3) {
   return sqrtf(fmaxf(0.f, pe * (pe - l1) * (pe - l2) * (pe - l3)));
 }
 
-__global__ void __launch_bounds__(kMem32Threads, 2)
-    membrane32_k(PlateletConst k, const double* X, const double* Y, const double* RY, const double* Z,
+__device__ __forceinline__ void membrane32_k_body(const PlateletConst& k, const double* X, const double* Y, const double* RY, const double* Z,
                  const int* tri, const int* node_ntri, const int* node_tri, const int* vert_local, const int* ring,
                  const int* sp_ptr, const int* sp_nbr, const double* sp_L0, const double* S0,
-                 const double* S0_all, const double* V0, float* kmv, double* SV, float* Fmem, Control* ctl) {
+                 const double* S0_all, const double* V0, float* kmv, double* SV, float* Fmem, Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   constexpr int NT = kMem32Threads, NW = NT / 32;
-  const int p = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int p = bid, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int E = k.E, Em = k.Em, T = k.T, NN = k.NN, PE = k.P * k.E;
   const int base = p * E;
   const float invF0 = 1.f / k.f0;
@@ -1669,6 +1688,13 @@ __global__ void __launch_bounds__(kMem32Threads, 2)
     Fmem[2 * PE + base + e] = fz;
   }
 }
+__global__ void __launch_bounds__(kMem32Threads, 2)
+    membrane32_k(PlateletConst k, const double* X, const double* Y, const double* RY, const double* Z,
+                 const int* tri, const int* node_ntri, const int* node_tri, const int* vert_local, const int* ring,
+                 const int* sp_ptr, const int* sp_nbr, const double* sp_L0, const double* S0,
+                 const double* S0_all, const double* V0, float* kmv, double* SV, float* Fmem, Control* ctl) {
+  membrane32_k_body(k, X, Y, RY, Z, tri, node_ntri, node_tri, vert_local, ring, sp_ptr, sp_nbr, sp_L0, S0, S0_all, V0, kmv, SV, Fmem, ctl, blockIdx.x, gridDim.x);
+}
 
 // ---------------------------------------------------------------- Morse
 // FP32 Morse force over distance, F(r)/r, force-shifted to zero at the
@@ -1879,13 +1905,13 @@ __device__ __forceinline__ T min_image(T d, T L, int wrap) {
 
 constexpr int kBoundsThreads = 512;
 template <class R>
-__global__ void __launch_bounds__(kBoundsThreads) platelet_bounds_k(PlateletConst k, const double* X,
+__device__ __forceinline__ void platelet_bounds_k_body(const PlateletConst& k, const double* X,
                                                                     const double* Y, const double* Z,
                                                                     double* bounds, typename Staged<R>::T* rel,
-                                                                    const Control* ctl) {
+                                                                    const Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   constexpr int NW = kBoundsThreads / 32;
-  const int p = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int p = bid, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int base = p * k.E;
   const double ox = X[base], oy = Y[base], oz = Z[base];
   __shared__ R s_w[3][NW];
@@ -1935,15 +1961,22 @@ __global__ void __launch_bounds__(kBoundsThreads) platelet_bounds_k(PlateletCons
     bounds[4 * p + 3] = sqrt((double)m);
   }
 }
+template <class R>
+__global__ void __launch_bounds__(kBoundsThreads) platelet_bounds_k(PlateletConst k, const double* X,
+                                                                    const double* Y, const double* Z,
+                                                                    double* bounds, typename Staged<R>::T* rel,
+                                                                    const Control* ctl) {
+  platelet_bounds_k_body<R>(k, X, Y, Z, bounds, rel, ctl, blockIdx.x, gridDim.x);
+}
 
 // 32 elements per CTA, each element's partner list split over kMorseSplit
 // warps; the partial sums are added in warp order (deterministic).
 constexpr int kMorseSplit = 4;
 
 template <class R>
-__global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletConst k, const double* bounds,
+__device__ __forceinline__ void morse_platelet_k_body(const PlateletConst& k, const double* bounds,
                                                                      const typename Staged<R>::T* rel,
-                                                                     int tiles, double* Fm, Control* ctl) {
+                                                                     int tiles, double* Fm, Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   using T = typename Staged<R>::T;
   extern __shared__ __align__(16) unsigned char s_raw[];
@@ -1951,7 +1984,7 @@ __global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletCon
   T* s_q = s_t + k.E;
   __shared__ R s_part[kMorseSplit][3][32];
   const int PE = k.P * k.E;
-  const int p = blockIdx.x / tiles, tile = blockIdx.x % tiles;
+  const int p = bid / tiles, tile = bid % tiles;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int e = tile * 32 + lane;
   const bool valid = e < k.E;
@@ -2072,13 +2105,19 @@ __global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletCon
     Fm[2 * PE + g] = (double)(sz * sc);
   }
 }
+template <class R>
+__global__ void __launch_bounds__(32 * kMorseSplit) morse_platelet_k(PlateletConst k, const double* bounds,
+                                                                     const typename Staged<R>::T* rel,
+                                                                     int tiles, double* Fm, Control* ctl) {
+  morse_platelet_k_body<R>(k, bounds, rel, tiles, Fm, ctl, blockIdx.x, gridDim.x);
+}
 
 // ---------------------------------------------------------------- fibrin
 template <class R>
-__global__ void fibrin_k(int M, int law, double kk, double mass, const double* X, const double* Y, const double* Z,
-                         const int* ptr, const int* nbr, const double* L0, double* F, const Control* ctl) {
+__device__ __forceinline__ void fibrin_k_body(int M, int law, double kk, double mass, const double* X, const double* Y, const double* Z,
+                         const int* ptr, const int* nbr, const double* L0, double* F, const Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
-  const int ni = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ni = bid * blockDim.x + threadIdx.x;
   if (ni >= M) return;
   R fx = 0, fy = 0, fz = 0;
   const double xi = X[ni], yi = Y[ni], zi = Z[ni];
@@ -2106,6 +2145,11 @@ __global__ void fibrin_k(int M, int law, double kk, double mass, const double* X
   F[M + ni] = (double)fy;
   F[2 * M + ni] = (double)fz;
 }
+template <class R>
+__global__ void fibrin_k(int M, int law, double kk, double mass, const double* X, const double* Y, const double* Z,
+                         const int* ptr, const int* nbr, const double* L0, double* F, const Control* ctl) {
+  fibrin_k_body<R>(M, law, kk, mass, X, Y, Z, ptr, nbr, L0, F, ctl, blockIdx.x, gridDim.x);
+}
 
 // ---------------------------------------------------------------- bonds
 struct RecTmp {
@@ -2126,15 +2170,15 @@ __device__ __forceinline__ unsigned long long op_key(int site, int rid, int opi)
 // slot operations they imply.  Receptors on the triangle above the bond
 // range and unbound do nothing (sem_kernel.cu:1812).  Every receptor reads
 // totalBond before any addition: avaiBond = NUMOFRECEPTORS.
-__global__ void bonds_prepare_k(PlateletConst k, const double* X, const double* Y, const double* Z,
+__device__ __forceinline__ void bonds_prepare_k_body(const PlateletConst& k, const double* X, const double* Y, const double* Z,
                                 const int* tri, const int* rec_tri, const float* r1a, const float* r2a,
                                 const int* rec_state, RecTmp* tmp, int* active, unsigned long long* ops, int ops_cap,
-                                void* Fbond, int fbond_bytes, Control* ctl) {
+                                void* Fbond, int fbond_bytes, Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   const int PE = k.P * k.E;
   const int NR = k.P * k.nrec;
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gsz = gridDim.x * blockDim.x;
+  const int gid = bid * blockDim.x + threadIdx.x;
+  const int gsz = nblk * blockDim.x;
   for (int i = gid; i < 3 * PE * fbond_bytes / 4; i += gsz) ((int*)Fbond)[i] = 0;
   const int r = gid;
   if (r >= NR) return;
@@ -2207,17 +2251,23 @@ __global__ void bonds_prepare_k(PlateletConst k, const double* X, const double* 
     else atomicOr(&ctl->err, ERR_BOND_OVERFLOW);
   }
 }
+__global__ void bonds_prepare_k(PlateletConst k, const double* X, const double* Y, const double* Z,
+                                const int* tri, const int* rec_tri, const float* r1a, const float* r2a,
+                                const int* rec_state, RecTmp* tmp, int* active, unsigned long long* ops, int ops_cap,
+                                void* Fbond, int fbond_bytes, Control* ctl) {
+  bonds_prepare_k_body(k, X, Y, Z, tri, rec_tri, r1a, r2a, rec_state, tmp, active, ops, ops_cap, Fbond, fbond_bytes, ctl, blockIdx.x, gridDim.x);
+}
 
 // Bond pass, part 2 (one CTA): slot operations sorted by (site, receptor,
 // operation) and applied site by site in that order -- the outcome of a serial
 // schedule of sem_kernel.cu:1750-2083 -- then bond counts, stored sites and
 // the bond spring force on the triangle's vertices.
 template <class R>
-__global__ void __launch_bounds__(1024) bonds_resolve_k(PlateletConst k, const double* X, const double* Y,
+__device__ __forceinline__ void bonds_resolve_k_body(const PlateletConst& k, const double* X, const double* Y,
                                                         const double* Z, const int* tri, const int* rec_tri,
                                                         int* rec_state, int* vwf, RecTmp* tmp, const int* active,
                                                         unsigned long long* ops, int ops_cap, R* Fbond,
-                                                        Control* ctl) {
+                                                        Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   const int PE = k.P * k.E;
   __shared__ long long s_tot[32];
@@ -2305,6 +2355,146 @@ __global__ void __launch_bounds__(1024) bonds_resolve_k(PlateletConst k, const d
     ctl->nops_active[1] = 0;
   }
 }
+template <class R>
+__global__ void __launch_bounds__(1024) bonds_resolve_k(PlateletConst k, const double* X, const double* Y,
+                                                        const double* Z, const int* tri, const int* rec_tri,
+                                                        int* rec_state, int* vwf, RecTmp* tmp, const int* active,
+                                                        unsigned long long* ops, int ops_cap, R* Fbond,
+                                                        Control* ctl) {
+  bonds_resolve_k_body<R>(k, X, Y, Z, tri, rec_tri, rec_state, vwf, tmp, active, ops, ops_cap, Fbond, ctl, blockIdx.x, gridDim.x);
+}
+
+// ------------------------------------------------------------- batch kernels
+// One launch per kernel over all jobs of a fused batch; CTA b belongs to job
+// batch_job_of(start, nj, b) and runs the job's body with its local CTA
+// index.  The job's constants are copied to shared memory first.
+#define PF_BATCH_PROLOGUE                                 \
+  const int j = batch_job_of(start, nj, blockIdx.x);      \
+  const BatchDesc& d = descs[j];                          \
+  const int bid = blockIdx.x - start[j], nblk = start[j + 1] - start[j];
+
+__global__ void __launch_bounds__(kFlagThreads) flag_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ LatticeConst s_lk;
+  cta_copy(s_lk, d.L.k);
+  __syncthreads();
+  flag_k_body(s_lk, d.L.mark, d.L.flags[0], d.L.flags[1], d.L.list[0], d.L.list[1], nullptr, nullptr,
+              kFlagR - 1, d.ctl, bid, nblk);
+}
+
+__global__ void __launch_bounds__(kMem32Threads, 1) membrane_batch_k(const BatchDesc* descs, const int* start,
+                                                                     int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ PlateletConst s_pk;
+  cta_copy(s_pk, d.Pl.k);
+  __syncthreads();
+  const Platelets& Pl = d.Pl;
+  membrane32_k_body(s_pk, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri, Pl.vert_local, Pl.ring,
+                    Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0, Pl.S0_all, Pl.V0, (float*)Pl.km, Pl.SV,
+                    (float*)Pl.Fmem, d.ctl, bid, nblk);
+}
+
+__global__ void __launch_bounds__(kBoundsThreads) bounds_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ PlateletConst s_pk;
+  cta_copy(s_pk, d.Pl.k);
+  __syncthreads();
+  platelet_bounds_k_body<float>(s_pk, d.Pl.X, d.Pl.Y, d.Pl.Z, d.Pl.bounds, (float4*)d.Pl.relpos, d.ctl, bid,
+                                nblk);
+}
+
+__global__ void __launch_bounds__(32 * kMorseSplit) morse_batch_k(const BatchDesc* descs, const int* start,
+                                                                  int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ PlateletConst s_pk;
+  cta_copy(s_pk, d.Pl.k);
+  __syncthreads();
+  morse_platelet_k_body<float>(s_pk, d.Pl.bounds, (const float4*)d.Pl.relpos, (s_pk.E + 31) / 32, d.Pl.Fmorse,
+                               d.ctl, bid, nblk);
+}
+
+// the bond pass's scratch inside rec_tmp (the layout bond_pass uses)
+struct BondScratch {
+  RecTmp* tmp;
+  int* active;
+  unsigned long long* ops;
+  int cap;
+};
+__device__ __forceinline__ BondScratch bond_scratch(const Platelets& Pl) {
+  const int NR = Pl.k.P * Pl.k.nrec;
+  BondScratch b;
+  b.tmp = (RecTmp*)Pl.rec_tmp;
+  b.active = (int*)(b.tmp + NR);
+  b.ops = (unsigned long long*)(((uintptr_t)(b.active + NR) + 15) & ~(uintptr_t)15);
+  b.cap = 2 * NR;
+  return b;
+}
+__global__ void __launch_bounds__(256) bond_prep_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ PlateletConst s_pk;
+  cta_copy(s_pk, d.Pl.k);
+  __syncthreads();
+  const Platelets& Pl = d.Pl;
+  const BondScratch b = bond_scratch(Pl);
+  bonds_prepare_k_body(s_pk, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.r1, Pl.r2, Pl.rec_state, b.tmp, b.active,
+                       b.ops, b.cap, Pl.Fbond, 4, d.ctl, bid, nblk);
+}
+__global__ void __launch_bounds__(1024) bond_resolve_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ PlateletConst s_pk;
+  cta_copy(s_pk, d.Pl.k);
+  __syncthreads();
+  const Platelets& Pl = d.Pl;
+  const BondScratch b = bond_scratch(Pl);
+  bonds_resolve_k_body<float>(s_pk, Pl.X, Pl.Y, Pl.Z, Pl.tri, Pl.rec_tri, Pl.rec_state, Pl.vwf, b.tmp, b.active,
+                              b.ops, b.cap, (float*)Pl.Fbond, d.ctl, bid, nblk);
+}
+
+__global__ void __launch_bounds__(128) fibrin_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  PF_BATCH_PROLOGUE
+  const Fibrin& Fb = d.Fb;
+  fibrin_k_body<float>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr, Fb.nbr, Fb.L0, Fb.F, d.ctl, bid,
+                       nblk);
+}
+
+// part 0: element membrane + Morse forces, 1: bond forces, 2: fibrin forces
+template <int PART>
+__global__ void __launch_bounds__(128) spread_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ LatticeConst s_lk;
+  cta_copy(s_lk, d.L.k);
+  __syncthreads();
+  float4* FA = (float4*)d.L.F[0];
+  float4* FB = (float4*)d.L.F[1];
+  if constexpr (PART == 2) {
+    const Fibrin& Fb = d.Fb;
+    spread_part_k_body(s_lk, FA, FB, Fb.M, Fb.X, Fb.Y, Fb.Z, nullptr, Fb.F, d.has_pl ? (double)d.Pl.k.f0 : 1.0,
+                       d.ctl, bid, nblk);
+  } else {
+    const Platelets& Pl = d.Pl;
+    const int PE = Pl.k.P * Pl.k.E;
+    spread_part_k_body(s_lk, FA, FB, PE, Pl.X, Pl.Y, Pl.Z, (const float*)(PART == 0 ? Pl.Fmem : Pl.Fbond),
+                       PART == 0 && Pl.k.morse ? Pl.Fmorse : nullptr, 1.0, d.ctl, bid, nblk);
+  }
+}
+
+__global__ void __launch_bounds__(128) interp_batch_k(const BatchDesc* descs, const int* start, int nj) {
+  PF_BATCH_PROLOGUE
+  __shared__ LatticeConst s_lk;
+  __shared__ PlateletConst s_pk;
+  cta_copy(s_lk, d.L.k);
+  cta_copy(s_pk, d.Pl.k);
+  __syncthreads();
+  const Platelets& Pl = d.Pl;
+  const Fibrin& Fb = d.Fb;
+  const bool pl = d.has_pl != 0, fb = d.has_fb != 0;
+  interp_advance_k_body<float>(
+      s_lk, s_pk, (const float4*)d.L.ubuf, pl ? s_pk.P * s_pk.E : 0, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.V, fb ? Fb.M : 0,
+      Fb.X, Fb.Y, Fb.Z, Fb.V, Fb.fixed, nullptr, nullptr, d.L.mark, d.ctl, d.done_blocks, d.detach_rate, d.seed,
+      pl ? (const float*)Pl.Fmem : nullptr, (pl && s_pk.morse) ? Pl.Fmorse : nullptr,
+      (pl && s_pk.nrec) ? (const float*)Pl.Fbond : nullptr, pl ? Pl.Ftot : nullptr, bid, nblk);
+}
+#undef PF_BATCH_PROLOGUE
 
 }  // namespace
 
@@ -2596,6 +2786,102 @@ cudaError_t bin_elements(Platelets& Pl, Control* ctl, cudaStream_t st) {
   cudaMemsetAsync(Pl.bin_count, 0, sizeof(int) * (size_t)Pl.ncells, st);
   cudaMemsetAsync(&ctl->occupied, 0, sizeof(int), st);
   bin_elements_k<<<(PE + 127) / 128, 128, 0, st>>>(Pl.k, PE, Pl.X, Pl.Y, Pl.Z, Pl.bin_count, (float4*)Pl.bin, ctl);
+  return cudaGetLastError();
+}
+
+
+bool batch_supported(const BatchDesc& d) {
+  // the flag kernel stages whole rows (plus halo) of a plane in shared memory
+  return (flag_rows(d.L.k.nbx) + 2 * kFlagR) * d.L.k.nbx <= kFlagWords;
+}
+
+int batch_threads(int kind) {
+  switch (kind) {
+    case BK_FLAG: return kFlagThreads;
+    case BK_MEMBRANE: return kMem32Threads;
+    case BK_BOUNDS: return kBoundsThreads;
+    case BK_MORSE: return 32 * kMorseSplit;
+    case BK_BOND_PREP: return 256;
+    case BK_BOND_RESOLVE: return 1024;
+    case BK_LBM_UNFLAGGED: case BK_LBM_FLAGGED: case BK_MOMENTS: return kLbmBlock;
+    default: return 128;
+  }
+}
+
+size_t batch_smem(const BatchDesc& d, int kind) {
+  if (!d.has_pl) return 0;
+  if (kind == BK_MEMBRANE) return Mem32Layout(d.Pl.k).bytes;
+  if (kind == BK_MORSE) return 2 * (size_t)d.Pl.k.E * sizeof(float4);
+  return 0;
+}
+
+int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs) {
+  const LatticeConst& lk = d.L.k;
+  const PlateletConst& pk = d.Pl.k;
+  const int PE = d.has_pl ? pk.P * pk.E : 0;
+  const int M = d.has_fb ? d.Fb.M : 0;
+  const int NR = d.has_pl ? pk.P * pk.nrec : 0;
+  const bool markers = PE + M > 0;
+  switch (kind) {
+    case BK_FLAG: {
+      if (!markers) return 0;
+      const int R = flag_rows(lk.nbx);
+      return lk.nz * ((lk.ny + R - 1) / R);
+    }
+    case BK_LBM_UNFLAGGED: return (((lk.nx + kLbmBlock - 1) / kLbmBlock) * lk.ny * lk.nz + kBatchRows - 1) / kBatchRows;
+    case BK_MEMBRANE: return PE ? pk.P : 0;
+    case BK_BOUNDS: return PE && pk.morse ? pk.P : 0;
+    case BK_MORSE: return PE && pk.morse ? pk.P * ((pk.E + 31) / 32) : 0;
+    case BK_BOND_PREP: return NR ? (NR + 255) / 256 : 0;
+    case BK_BOND_RESOLVE: return NR ? 1 : 0;
+    case BK_FIBRIN: return M ? (M + 127) / 128 : 0;
+    case BK_SPREAD_ELEM: return PE ? (PE + 127) / 128 : 0;
+    case BK_SPREAD_BOND: return PE && pk.nrec ? (PE + 127) / 128 : 0;
+    case BK_SPREAD_FIB: return M ? (M + 127) / 128 : 0;
+    case BK_LBM_FLAGGED:
+    case BK_MOMENTS: {
+      if (!markers) return 0;
+      const int need = (lk.nbricks + kLbmBlock / 32 - 1) / (kLbmBlock / 32);
+      const int cap = std::max(8, (sms * 8 + njobs - 1) / std::max(1, njobs));
+      return std::min(need, cap);
+    }
+    case BK_INTERP: return std::max(1, (PE + M + 127) / 128);
+  }
+  return 0;
+}
+
+cudaError_t batch_launch(int kind, const BatchDesc* descs, const int* start, int nj, int total, size_t smem,
+                         int precision, bool fast, cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  switch (kind) {
+    case BK_LBM_UNFLAGGED: case BK_LBM_FLAGGED: case BK_MOMENTS:
+      return batch_launch_lattice(kind, descs, start, nj, total, precision, fast, st);
+    case BK_FLAG: flag_batch_k<<<total, kFlagThreads, 0, st>>>(descs, start, nj); break;
+    case BK_MEMBRANE: {
+      static bool attr = false;
+      if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(membrane_batch_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kMem32MaxSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+      }
+      membrane_batch_k<<<total, kMem32Threads, smem, st>>>(descs, start, nj);
+      break;
+    }
+    case BK_BOUNDS: bounds_batch_k<<<total, kBoundsThreads, 0, st>>>(descs, start, nj); break;
+    case BK_MORSE:
+      cudaFuncSetAttribute(morse_batch_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      morse_batch_k<<<total, 32 * kMorseSplit, smem, st>>>(descs, start, nj);
+      break;
+    case BK_BOND_PREP: bond_prep_batch_k<<<total, 256, 0, st>>>(descs, start, nj); break;
+    case BK_BOND_RESOLVE: bond_resolve_batch_k<<<total, 1024, 0, st>>>(descs, start, nj); break;
+    case BK_FIBRIN: fibrin_batch_k<<<total, 128, 0, st>>>(descs, start, nj); break;
+    case BK_SPREAD_ELEM: spread_batch_k<0><<<total, 128, 0, st>>>(descs, start, nj); break;
+    case BK_SPREAD_BOND: spread_batch_k<1><<<total, 128, 0, st>>>(descs, start, nj); break;
+    case BK_SPREAD_FIB: spread_batch_k<2><<<total, 128, 0, st>>>(descs, start, nj); break;
+    case BK_INTERP: interp_batch_k<<<total, 128, 0, st>>>(descs, start, nj); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

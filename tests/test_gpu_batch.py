@@ -61,3 +61,46 @@ def test_served_loop_small(gpu):
     r = serve.run_served(1, rate=8.0, duration=0.5, steps_range=(20, 60), pool=3, chunk=20)
     assert r["jobs"] >= 1 and r["mlups"] > 0
     assert 0 < r["latency_p50_s"] <= r["latency_p99_s"]
+
+
+def _fused_scenes():
+    from platelet_fiber_gpu_gb300 import workloads as W
+    return [W.mixed_small(seed=3), W.mixed_small(seed=5, nx=48, n_fib=0, n_links=0), W.batch_job(3, 0),
+            W.batch_job(3, 5)]
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 1e-5), (2, 1e-3)], ids=["fp32", "fp16"])
+def test_fused_batch_matches_standalone(gpu, prec, tol, monkeypatch):
+    """Reduced-precision batches step through the fused batch kernels (one
+    launch per kernel over every job, per-job CTA offsets); each job's state
+    matches the same job stepped alone and the per-job-graph batch
+    (PFGPU_BATCH_FUSED=0).  Float atomics make the spreading order differ, so
+    the lattice agrees to rounding; bond states exactly."""
+    scenes = _fused_scenes()
+    fused = gpu.Batch(16 << 30)
+    fslots = [fused.admit(sc, prec) for sc in scenes]
+    monkeypatch.setenv("PFGPU_BATCH_FUSED", "0")
+    plain = gpu.Batch(16 << 30)
+    pslots = [plain.admit(sc, prec) for sc in scenes]
+    plain.step(4)
+    plain.step(3)
+    monkeypatch.delenv("PFGPU_BATCH_FUSED")
+    fused.step(4)
+    fused.step(3)
+    for sc, fs, ps in zip(scenes, fslots, pslots):
+        ref = gpu.Job(sc, prec)
+        ref.step(7)
+        for other in (fused.job(fs), plain.job(ps)):
+            assert other.steps == 7
+            a, r = other.lattice()["fIN"], ref.lattice()["fIN"]
+            assert np.abs(a - r).max() / np.abs(r).max() < tol
+            if sc.n_platelets:
+                ea, er = other.elements(), ref.elements()
+                for k in ("X", "Y", "Z"):
+                    assert np.abs(ea[k] - er[k]).max() < 1e-6
+                np.testing.assert_array_equal(other.bonds()["rec_state"], ref.bonds()["rec_state"])
+            if sc.n_fib:
+                assert np.abs(other.fibrin()["X"] - ref.fibrin()["X"]).max() < 1e-6
+        ref.close()
+    fused.close()
+    plain.close()
