@@ -201,10 +201,14 @@ size_t pfgpu_scene_device_bytes(const pf_scene *scene, int precision);
 
 /* ------------------------------------------------------------ batch API */
 /* Continuous batching of independent jobs on one GPU: each admitted job keeps
- * its own state and captured step graph; pfgpu_batch_step enqueues every live
- * job's steps on the job's own streams (so small lattices run side by side)
- * and waits for all of them.  Jobs join and leave between batch steps;
- * admission is checked against a device-memory budget. */
+ * its own device state.  A batch step of FP32 or FP16 jobs is one captured
+ * graph in which each kernel of the coupled step runs once over the CTAs of
+ * every job (a per-job CTA offset table); its block and tile shapes are picked
+ * by an autotuner that measures candidate shapes on the batch's own steps
+ * (PFGPU_BATCH_TUNE=0: fixed defaults; PFGPU_TUNE_CACHE=path: results kept in
+ * a text file).  Other batches replay each job's own step graph on the job's
+ * streams.  Jobs join and leave between batch steps; admission is checked
+ * against a device-memory budget. */
 typedef struct pfgpu_batch pfgpu_batch;
 int pfgpu_batch_create(size_t hbm_budget_bytes, pfgpu_batch **out);
 /* Admits a job if it fits the budget; returns PFGPU_ERR_NOMEM otherwise.
@@ -216,6 +220,13 @@ int pfgpu_batch_step(pfgpu_batch *b, int nsteps);
 int pfgpu_batch_status(pfgpu_batch *b, int slot);
 int pfgpu_batch_retire(pfgpu_batch *b, int slot);
 pfgpu_job *pfgpu_batch_job(pfgpu_batch *b, int slot);
+/* The fused step's shapes: shape[0] row segments per CTA of the unflagged
+ * lattice pass, shape[1] CTAs per SM of the near-region list and moments
+ * passes, shape[2] threads per CTA of the marker passes.  *state: 0 still
+ * tuning, 1 fixed (tuned, forced or tuning off), -1 no fused step. */
+int pfgpu_batch_shape(pfgpu_batch *b, int shape[3], int *state);
+/* Forces the fused step's shapes; lbm_rows = 0 hands them back to the tuner. */
+int pfgpu_batch_set_shape(pfgpu_batch *b, int lbm_rows, int list_per_sm, int marker_threads);
 size_t pfgpu_batch_bytes_in_use(const pfgpu_batch *b);
 int pfgpu_batch_num_jobs(const pfgpu_batch *b);
 void pfgpu_batch_destroy(pfgpu_batch *b);

@@ -167,22 +167,36 @@ enum BatchKernel : int {
   BK_FLAG = 0, BK_LBM_UNFLAGGED, BK_MEMBRANE, BK_BOUNDS, BK_MORSE, BK_BOND_PREP, BK_BOND_RESOLVE, BK_FIBRIN,
   BK_SPREAD_ELEM, BK_SPREAD_BOND, BK_SPREAD_FIB, BK_LBM_FLAGGED, BK_MOMENTS, BK_INTERP, BK_COUNT
 };
-// row segments of kLbmBlock nodes per CTA of the fused unflagged lattice pass
-constexpr int kBatchRows = 8;
+// Block and tile shapes of a fused batch step (picked by the batch autotuner)
+struct BatchTune {
+  int lbm_rows;        // row segments of kLbmBlock nodes per CTA, unflagged lattice pass
+  int list_per_sm;     // CTAs per SM (shared by the batch) of the near-region list and moments passes
+  int marker_threads;  // threads per CTA of the spreading, fibrin and interpolation passes
+};
+constexpr BatchTune kBatchTuneDefault = {8, 8, 128};
+constexpr int kMarkerThreadsMax = 256;
+// Autotuner (pf_tune.cu), per shape class: the key of a batch's class; the
+// best shape so far (true once the search is done); the next shape to
+// measure that is not in `busy` (false: none until results come in, or
+// done); a measurement in device ns per lattice-node update.
+std::string tune_key(int precision, bool fast, long long nodes, int njobs, long long markers);
+bool tune_best(const std::string& key, BatchTune* best);
+bool tune_next(const std::string& key, const std::vector<BatchTune>& busy, BatchTune* out);
+void tune_record(const std::string& key, const BatchTune& t, float ns_per_node);
 // CTAs job `d` needs for kernel `kind` (0: the kernel has no work for it)
-int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs);
+int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs, const BatchTune& t);
 // whether the batch kernels can take this job (row width of the flagging)
 bool batch_supported(const BatchDesc& d);
 // Block size and dynamic shared memory of a batch kernel
-int batch_threads(int kind);
+int batch_threads(int kind, const BatchTune& t);
 size_t batch_smem(const BatchDesc& d, int kind);
 // Launches one batch kernel over `total` CTAs; precision and fast gather are
 // the batch's (all jobs share them).
 cudaError_t batch_launch(int kind, const BatchDesc* descs, const int* start, int njobs, int total, size_t smem,
-                         int precision, bool fast, cudaStream_t st);
+                         int precision, bool fast, const BatchTune& t, cudaStream_t st);
 // the lattice part of batch_launch (pf_lattice.cu)
 cudaError_t batch_launch_lattice(int kind, const BatchDesc* descs, const int* start, int njobs, int total,
-                                 int precision, bool fast, cudaStream_t st);
+                                 int precision, bool fast, int lbm_rows, cudaStream_t st);
 bool fast_gather(const Lattice& L);
 
 // ------------------------------------------------------------------ launchers

@@ -772,16 +772,17 @@ __global__ void __launch_bounds__(kLbmBlock) moments_active_k(LatticeConst k, co
 // lattice passes of a fused batch: the job's LatticeConst is copied to shared
 // memory (no aliasing with the populations the pass writes)
 template <class S, class R, bool FAST>
-__global__ void __launch_bounds__(kLbmBlock) lbm_step_batch_k(const BatchDesc* descs, const int* start, int nj) {
+__global__ void __launch_bounds__(kLbmBlock) lbm_step_batch_k(const BatchDesc* descs, const int* start, int nj,
+                                                              int rows) {
   __shared__ LatticeConst s_k;
   const int j = batch_job_of(start, nj, blockIdx.x);
   const BatchDesc& d = descs[j];
   cta_copy(s_k, d.L.k);
   __syncthreads();
   const Lattice& L = d.L;
-  // kBatchRows row segments per CTA (amortizes the per-CTA set-up)
+  // `rows` row segments per CTA (amortizes the per-CTA set-up)
   const int segs = ((s_k.nx + kLbmBlock - 1) / kLbmBlock) * s_k.ny * s_k.nz;
-  for (int r = (blockIdx.x - start[j]) * kBatchRows, e = min(segs, r + kBatchRows); r < e; ++r)
+  for (int r = (blockIdx.x - start[j]) * rows, e = min(segs, r + rows); r < e; ++r)
     lbm_step_body<S, R, FAST>(s_k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
                               L.flags[0], L.flags[1], nullptr, 0, 1, L.near[0], L.near[1], d.ctl, r, segs);
 }
@@ -1093,11 +1094,13 @@ cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st) {
 bool fast_gather(const Lattice& L) { return fast_lattice(L); }
 
 template <class S, bool FAST>
-static cudaError_t batch_lattice_impl(int kind, const BatchDesc* d, const int* start, int nj, int total,
+static cudaError_t batch_lattice_impl(int kind, const BatchDesc* d, const int* start, int nj, int total, int rows,
                                       cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
   switch (kind) {
-    case BK_LBM_UNFLAGGED: lbm_step_batch_k<S, float, FAST><<<total, kLbmBlock, 0, st>>>(d, start, nj); break;
+    case BK_LBM_UNFLAGGED:
+      lbm_step_batch_k<S, float, FAST><<<total, kLbmBlock, 0, st>>>(d, start, nj, rows);
+      break;
     case BK_LBM_FLAGGED: lbm_list_batch_k<S, float, FAST><<<total, kLbmBlock, 0, st>>>(d, start, nj); break;
     case BK_MOMENTS: moments_batch_k<S, float, FAST><<<total, kLbmBlock, 0, st>>>(d, start, nj); break;
     default: return cudaErrorInvalidValue;
@@ -1105,13 +1108,13 @@ static cudaError_t batch_lattice_impl(int kind, const BatchDesc* d, const int* s
   return cudaGetLastError();
 }
 cudaError_t batch_launch_lattice(int kind, const BatchDesc* d, const int* start, int nj, int total, int precision,
-                                 bool fast, cudaStream_t st) {
+                                 bool fast, int rows, cudaStream_t st) {
   if (precision == PF_PREC_FP32)
-    return fast ? batch_lattice_impl<float, true>(kind, d, start, nj, total, st)
-                : batch_lattice_impl<float, false>(kind, d, start, nj, total, st);
+    return fast ? batch_lattice_impl<float, true>(kind, d, start, nj, total, rows, st)
+                : batch_lattice_impl<float, false>(kind, d, start, nj, total, rows, st);
   if (precision == PF_PREC_FP16)
-    return fast ? batch_lattice_impl<__half, true>(kind, d, start, nj, total, st)
-                : batch_lattice_impl<__half, false>(kind, d, start, nj, total, st);
+    return fast ? batch_lattice_impl<__half, true>(kind, d, start, nj, total, rows, st)
+                : batch_lattice_impl<__half, false>(kind, d, start, nj, total, rows, st);
   return cudaErrorInvalidValue;
 }
 

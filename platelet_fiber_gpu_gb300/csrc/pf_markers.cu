@@ -2450,7 +2450,7 @@ __global__ void __launch_bounds__(1024) bond_resolve_batch_k(const BatchDesc* de
                               b.ops, b.cap, (float*)Pl.Fbond, d.ctl, bid, nblk);
 }
 
-__global__ void __launch_bounds__(128) fibrin_batch_k(const BatchDesc* descs, const int* start, int nj) {
+__global__ void __launch_bounds__(kMarkerThreadsMax) fibrin_batch_k(const BatchDesc* descs, const int* start, int nj) {
   PF_BATCH_PROLOGUE
   const Fibrin& Fb = d.Fb;
   fibrin_k_body<float>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr, Fb.nbr, Fb.L0, Fb.F, d.ctl, bid,
@@ -2459,7 +2459,7 @@ __global__ void __launch_bounds__(128) fibrin_batch_k(const BatchDesc* descs, co
 
 // part 0: element membrane + Morse forces, 1: bond forces, 2: fibrin forces
 template <int PART>
-__global__ void __launch_bounds__(128) spread_batch_k(const BatchDesc* descs, const int* start, int nj) {
+__global__ void __launch_bounds__(kMarkerThreadsMax) spread_batch_k(const BatchDesc* descs, const int* start, int nj) {
   PF_BATCH_PROLOGUE
   __shared__ LatticeConst s_lk;
   cta_copy(s_lk, d.L.k);
@@ -2478,7 +2478,7 @@ __global__ void __launch_bounds__(128) spread_batch_k(const BatchDesc* descs, co
   }
 }
 
-__global__ void __launch_bounds__(128) interp_batch_k(const BatchDesc* descs, const int* start, int nj) {
+__global__ void __launch_bounds__(kMarkerThreadsMax) interp_batch_k(const BatchDesc* descs, const int* start, int nj) {
   PF_BATCH_PROLOGUE
   __shared__ LatticeConst s_lk;
   __shared__ PlateletConst s_pk;
@@ -2795,7 +2795,7 @@ bool batch_supported(const BatchDesc& d) {
   return (flag_rows(d.L.k.nbx) + 2 * kFlagR) * d.L.k.nbx <= kFlagWords;
 }
 
-int batch_threads(int kind) {
+int batch_threads(int kind, const BatchTune& t) {
   switch (kind) {
     case BK_FLAG: return kFlagThreads;
     case BK_MEMBRANE: return kMem32Threads;
@@ -2804,7 +2804,7 @@ int batch_threads(int kind) {
     case BK_BOND_PREP: return 256;
     case BK_BOND_RESOLVE: return 1024;
     case BK_LBM_UNFLAGGED: case BK_LBM_FLAGGED: case BK_MOMENTS: return kLbmBlock;
-    default: return 128;
+    default: return t.marker_threads;
   }
 }
 
@@ -2815,7 +2815,7 @@ size_t batch_smem(const BatchDesc& d, int kind) {
   return 0;
 }
 
-int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs) {
+int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs, const BatchTune& t) {
   const LatticeConst& lk = d.L.k;
   const PlateletConst& pk = d.Pl.k;
   const int PE = d.has_pl ? pk.P * pk.E : 0;
@@ -2828,34 +2828,37 @@ int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs) {
       const int R = flag_rows(lk.nbx);
       return lk.nz * ((lk.ny + R - 1) / R);
     }
-    case BK_LBM_UNFLAGGED: return (((lk.nx + kLbmBlock - 1) / kLbmBlock) * lk.ny * lk.nz + kBatchRows - 1) / kBatchRows;
+    case BK_LBM_UNFLAGGED:
+      return (((lk.nx + kLbmBlock - 1) / kLbmBlock) * lk.ny * lk.nz + t.lbm_rows - 1) / t.lbm_rows;
     case BK_MEMBRANE: return PE ? pk.P : 0;
     case BK_BOUNDS: return PE && pk.morse ? pk.P : 0;
     case BK_MORSE: return PE && pk.morse ? pk.P * ((pk.E + 31) / 32) : 0;
     case BK_BOND_PREP: return NR ? (NR + 255) / 256 : 0;
     case BK_BOND_RESOLVE: return NR ? 1 : 0;
-    case BK_FIBRIN: return M ? (M + 127) / 128 : 0;
-    case BK_SPREAD_ELEM: return PE ? (PE + 127) / 128 : 0;
-    case BK_SPREAD_BOND: return PE && pk.nrec ? (PE + 127) / 128 : 0;
-    case BK_SPREAD_FIB: return M ? (M + 127) / 128 : 0;
+    case BK_FIBRIN: return M ? (M + t.marker_threads - 1) / t.marker_threads : 0;
+    case BK_SPREAD_ELEM: return PE ? (PE + t.marker_threads - 1) / t.marker_threads : 0;
+    case BK_SPREAD_BOND: return PE && pk.nrec ? (PE + t.marker_threads - 1) / t.marker_threads : 0;
+    case BK_SPREAD_FIB: return M ? (M + t.marker_threads - 1) / t.marker_threads : 0;
     case BK_LBM_FLAGGED:
     case BK_MOMENTS: {
       if (!markers) return 0;
       const int need = (lk.nbricks + kLbmBlock / 32 - 1) / (kLbmBlock / 32);
-      const int cap = std::max(8, (sms * 8 + njobs - 1) / std::max(1, njobs));
+      const int cap = std::max(8, (sms * t.list_per_sm + njobs - 1) / std::max(1, njobs));
       return std::min(need, cap);
     }
-    case BK_INTERP: return std::max(1, (PE + M + 127) / 128);
+    case BK_INTERP: return std::max(1, (PE + M + t.marker_threads - 1) / t.marker_threads);
   }
   return 0;
 }
 
 cudaError_t batch_launch(int kind, const BatchDesc* descs, const int* start, int nj, int total, size_t smem,
-                         int precision, bool fast, cudaStream_t st) {
+                         int precision, bool fast, const BatchTune& t, cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
+  const int mt = t.marker_threads;
+  if (mt < 32 || mt > kMarkerThreadsMax || mt % 32) return cudaErrorInvalidValue;
   switch (kind) {
     case BK_LBM_UNFLAGGED: case BK_LBM_FLAGGED: case BK_MOMENTS:
-      return batch_launch_lattice(kind, descs, start, nj, total, precision, fast, st);
+      return batch_launch_lattice(kind, descs, start, nj, total, precision, fast, t.lbm_rows, st);
     case BK_FLAG: flag_batch_k<<<total, kFlagThreads, 0, st>>>(descs, start, nj); break;
     case BK_MEMBRANE: {
       static bool attr = false;
@@ -2875,11 +2878,11 @@ cudaError_t batch_launch(int kind, const BatchDesc* descs, const int* start, int
       break;
     case BK_BOND_PREP: bond_prep_batch_k<<<total, 256, 0, st>>>(descs, start, nj); break;
     case BK_BOND_RESOLVE: bond_resolve_batch_k<<<total, 1024, 0, st>>>(descs, start, nj); break;
-    case BK_FIBRIN: fibrin_batch_k<<<total, 128, 0, st>>>(descs, start, nj); break;
-    case BK_SPREAD_ELEM: spread_batch_k<0><<<total, 128, 0, st>>>(descs, start, nj); break;
-    case BK_SPREAD_BOND: spread_batch_k<1><<<total, 128, 0, st>>>(descs, start, nj); break;
-    case BK_SPREAD_FIB: spread_batch_k<2><<<total, 128, 0, st>>>(descs, start, nj); break;
-    case BK_INTERP: interp_batch_k<<<total, 128, 0, st>>>(descs, start, nj); break;
+    case BK_FIBRIN: fibrin_batch_k<<<total, mt, 0, st>>>(descs, start, nj); break;
+    case BK_SPREAD_ELEM: spread_batch_k<0><<<total, mt, 0, st>>>(descs, start, nj); break;
+    case BK_SPREAD_BOND: spread_batch_k<1><<<total, mt, 0, st>>>(descs, start, nj); break;
+    case BK_SPREAD_FIB: spread_batch_k<2><<<total, mt, 0, st>>>(descs, start, nj); break;
+    case BK_INTERP: interp_batch_k<<<total, mt, 0, st>>>(descs, start, nj); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

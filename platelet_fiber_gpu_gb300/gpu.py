@@ -78,6 +78,8 @@ def lib():
         L.pfgpu_batch_bytes_in_use.restype = C.c_size_t
         L.pfgpu_batch_bytes_in_use.argtypes = [vp]
         L.pfgpu_batch_num_jobs.argtypes = [vp]
+        L.pfgpu_batch_shape.argtypes = [vp, ip, ip]
+        L.pfgpu_batch_set_shape.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.pfgpu_batch_destroy.argtypes = [vp]
         L.pfgpu_detach_uniform.restype = C.c_double
         L.pfgpu_detach_uniform.argtypes = [C.c_uint64, C.c_int64]
@@ -276,6 +278,29 @@ class Batch:
         check(lib().pfgpu_batch_retire(self.h, slot))
         self._scenes.pop(slot, None)
         self._c.pop(slot, None)
+
+    def shape(self):
+        """(lbm_rows, list_per_sm, marker_threads), state) of the fused step:
+        state 0 while the autotuner measures candidates, 1 once fixed, -1
+        when the batch does not use the fused step."""
+        sh = (C.c_int * 3)()
+        st = C.c_int(0)
+        check(lib().pfgpu_batch_shape(self.h, sh, C.byref(st)))
+        return (sh[0], sh[1], sh[2]), st.value
+
+    def set_shape(self, lbm_rows: int = 0, list_per_sm: int = 0, marker_threads: int = 0):
+        """Forces the fused step's shapes; all zero hands them back to the
+        autotuner."""
+        check(lib().pfgpu_batch_set_shape(self.h, lbm_rows, list_per_sm, marker_threads))
+
+    def tune(self, max_steps: int = 400, chunk: int = 20) -> int:
+        """Steps the batch until the autotuner has fixed the shapes (at most
+        max_steps); returns the steps taken.  The steps advance every job."""
+        taken = 0
+        while taken < max_steps and self.shape()[1] == 0:
+            self.step(chunk)
+            taken += chunk
+        return taken
 
     @property
     def bytes_in_use(self) -> int:

@@ -34,7 +34,11 @@ def run_batched(precision: int, n_jobs: int = 64, steps: int = 1000, seed: int =
         if s is None:
             raise RuntimeError("the job set does not fit the budget")
         slots.append(s)
-    b.step(1)  # captures each job's step graph
+    b.step(1)  # captures the step graph
+    # the autotuner measures its candidate shapes on real steps; they run
+    # before the timed region (every job advances by them)
+    tune_steps = b.tune(max_steps=400, chunk=20)
+    shape, state = b.shape()
     nodes = sum(sc.n_nodes for sc in scenes)
     t0 = time.perf_counter()
     left = steps
@@ -45,7 +49,9 @@ def run_batched(precision: int, n_jobs: int = 64, steps: int = 1000, seed: int =
     dt = time.perf_counter() - t0
     b.close()
     return {"mode": "batched", "precision": precision, "jobs": n_jobs, "steps": steps, "nodes": nodes,
-            "seconds": round(dt, 4), "mlups": round(nodes * steps / dt / 1e6, 1)}
+            "seconds": round(dt, 4), "mlups": round(nodes * steps / dt / 1e6, 1), "tune_steps": tune_steps,
+            "shape": {"lbm_rows": shape[0], "list_per_sm": shape[1], "marker_threads": shape[2],
+                      "state": state}}
 
 
 def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed: int = 4, budget: float = 150e9,

@@ -90,3 +90,22 @@ def test_scene_device_bytes_is_host_arithmetic(lib):
     b64 = gpu.scene_device_bytes(sc, 0)
     assert b16 < b32 < b64
     assert b32 > 2 * 19 * sc.n_nodes * 4
+
+
+def test_batch_shape_validation_without_gpu(lib):
+    """Forcing the fused batch step's shapes is checked on the host: the
+    row count and CTAs per SM in 1..64, marker threads a multiple of 32 up to
+    256; zero hands the shapes back to the autotuner."""
+    h = C.c_void_p()
+    lib.pfgpu_batch_create.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+    lib.pfgpu_batch_set_shape.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+    lib.pfgpu_batch_destroy.argtypes = [C.c_void_p]
+    assert lib.pfgpu_batch_create(1 << 20, C.byref(h)) == 0
+    try:
+        assert lib.pfgpu_batch_set_shape(h, 4, 8, 128) == 0
+        assert lib.pfgpu_batch_set_shape(h, 0, 0, 0) == 0
+        for bad in ((4, 8, 100), (4, 8, 512), (0 - 1, 8, 128), (4, 0, 128), (65, 8, 128)):
+            assert lib.pfgpu_batch_set_shape(h, *bad) == 1, bad
+        assert lib.pfgpu_batch_set_shape(None, 4, 8, 128) == 1
+    finally:
+        lib.pfgpu_batch_destroy(h)

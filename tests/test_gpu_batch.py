@@ -104,3 +104,65 @@ def test_fused_batch_matches_standalone(gpu, prec, tol, monkeypatch):
         ref.close()
     fused.close()
     plain.close()
+
+
+@pytest.mark.parametrize("shape", [(1, 2, 64), (16, 16, 256), (2, 4, 96)], ids=["r1l2t64", "r16l16t256", "r2l4t96"])
+def test_forced_shapes_match_standalone(gpu, shape):
+    """Every block/tile shape of the fused step computes the same updates:
+    a batch forced to a shape matches the jobs stepped alone."""
+    scenes = _fused_scenes()
+    b = gpu.Batch(16 << 30)
+    slots = [b.admit(sc, 1) for sc in scenes]
+    b.set_shape(*shape)
+    assert b.shape() == (shape, 1)
+    b.step(5)
+    for sc, s in zip(scenes, slots):
+        ref = gpu.Job(sc, 1)
+        ref.step(5)
+        got = b.job(s)
+        a, r = got.lattice()["fIN"], ref.lattice()["fIN"]
+        assert np.abs(a - r).max() / np.abs(r).max() < 1e-5
+        if sc.n_platelets:
+            np.testing.assert_array_equal(got.bonds()["rec_state"], ref.bonds()["rec_state"])
+        ref.close()
+    b.close()
+
+
+def test_autotuner_fixes_a_shape_and_caches_it(gpu, tmp_path, monkeypatch):
+    """The autotuner measures candidate shapes on the batch's own steps
+    (coordinate descent over the three axes), then runs the fastest; the jobs
+    advance by exactly the steps asked for and match the same jobs stepped
+    alone; the class's result is reused by a new batch and written to
+    PFGPU_TUNE_CACHE."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("PFGPU_TUNE_CACHE", str(cache))
+    scenes = [W.batch_job(7, 2), W.batch_job(9, 0)]
+    b = gpu.Batch(16 << 30)
+    slots = [b.admit(sc, 1) for sc in scenes]
+    shape, state = b.shape()
+    assert state == 0 and shape == (8, 8, 128)  # the default runs between trials
+    taken = b.tune(max_steps=600, chunk=30)
+    shape, state = b.shape()
+    assert state == 1, taken
+    assert shape[0] in (1, 2, 4, 8, 16, 32, 64) and shape[1] in (2, 4, 8, 16, 32, 64)
+    assert shape[2] in (32, 64, 128, 256)
+    b.step(4)
+    for sc, s in zip(scenes, slots):
+        ref = gpu.Job(sc, 1)
+        ref.step(taken + 4)
+        got = b.job(s)
+        assert got.steps == taken + 4
+        a, r = got.lattice()["fIN"], ref.lattice()["fIN"]
+        assert np.abs(a - r).max() / np.abs(r).max() < 1e-4
+        if sc.n_platelets:
+            np.testing.assert_array_equal(got.bonds()["rec_state"], ref.bonds()["rec_state"])
+        ref.close()
+    b2 = gpu.Batch(16 << 30)
+    for sc in scenes:
+        b2.admit(sc, 1)
+    assert b2.shape() == (shape, 1)
+    b2.close()
+    b.close()
+    line = cache.read_text().split()
+    assert [int(v) for v in line[1:4]] == list(shape)
