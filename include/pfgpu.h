@@ -150,6 +150,11 @@ const char *pfgpu_profile_phase_name(int i);
 /* Copies state back in scene layouts; any pointer may be NULL. */
 int pfgpu_job_get_lattice(pfgpu_job *job, double *fIN, double *fOUT, double *rho, double *u /*[3][N]*/,
                           double *F /*[3][N]*/);
+/* Density and velocity (the units of pfgpu_job_get_lattice's rho and u) at
+ * every stride-th node in x, y and z, computed on the device: float arrays
+ * [dims[2]][dims[1]][dims[0]], dims[i] = ceil(n_i / stride).  NULL arrays are
+ * skipped (all NULL: only dims).  Feeds pfgpu_write_vti. */
+int pfgpu_job_get_fields(pfgpu_job *job, int stride, float *rho, float *ux, float *uy, float *uz, int dims[3]);
 int pfgpu_job_get_elements(pfgpu_job *job, double *X, double *Y, double *RY, double *Z,
                            double *V /*[3][P*E]*/, double *F /*[3][P*E]*/);
 int pfgpu_job_get_bonds(pfgpu_job *job, int *rec_state /*[P][n_rec][3]*/, int *vwf /*[4][ny][nx]*/,
@@ -194,6 +199,14 @@ int pfgpu_output_frame(pfgpu_output *out);
 /* Appends "<step * dt>, <seed>" to cellsPauseTime.dat (gpuSEM_LB.c:1533)
  * and closes the files. */
 int pfgpu_output_close(pfgpu_output *out, int seed);
+/* The reference driver's writeVTK (gpuSEM_LB.c:1631-1709, outputSave at
+ * :1618): <directory>/<filename>_<t, 7 digits>.vti, VTK ImageData with ASCII
+ * Float32 "Density" and 3-component "Velocity" point data, "%.4e " per value
+ * and one line per x row; host arrays [nz][ny][nx].  `spacing` is the node
+ * stride of downsampled fields (1: the reference's Spacing "1 1 1").  The
+ * directory is created if missing.  Host-only. */
+int pfgpu_write_vti(int t, int nx, int ny, int nz, int spacing, const float *rho, int write_rho, const float *ux,
+                    const float *uy, const float *uz, int write_vel, const char *directory, const char *filename);
 void pfgpu_job_destroy(pfgpu_job *job);
 
 /* Device bytes a job with this scene and precision would allocate. */

@@ -218,6 +218,9 @@ cudaError_t lattice_near(Lattice& L, Control* ctl, int from_mark, cudaStream_t s
 // far pass counter: sync (far_step = step) or advance after a far pass
 cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st);
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
+// density and velocity at every stride-th node (float [mz][my][mx] planes)
+cudaError_t lattice_fields(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
+                           cudaStream_t st);
 // fIN [19][N], fOUT [19][N], rho [N], u [3][N], F [3][N] (double, device)
 cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* fIN, double* fOUT, double* rho,
                              double* u, double* F, cudaStream_t st);

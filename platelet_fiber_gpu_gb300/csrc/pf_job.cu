@@ -849,6 +849,35 @@ int pfgpu_job_get_lattice(pfgpu_job* j, double* fIN, double* fOUT, double* rho, 
   return PFGPU_OK;
 }
 
+int pfgpu_job_get_fields(pfgpu_job* j, int stride, float* rho, float* ux, float* uy, float* uz, int dims[3]) {
+  if (!j || stride < 1) return set_error(PFGPU_ERR_INVALID, "bad job or stride");
+  const int mx = (j->L.k.nx + stride - 1) / stride, my = (j->L.k.ny + stride - 1) / stride,
+            mz = (j->L.k.nz + stride - 1) / stride;
+  if (dims) {
+    dims[0] = mx;
+    dims[1] = my;
+    dims[2] = mz;
+  }
+  if (!rho && !ux) return PFGPU_OK;
+  if (ux && (!uy || !uz)) return set_error(PFGPU_ERR_INVALID, "ux given without uy, uz");
+  CK(cudaStreamSynchronize(j->s0));
+  Control c;
+  CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+  const size_t M = (size_t)mx * my * mz;
+  float* d = nullptr;
+  CK(cudaMalloc(&d, 4 * M * sizeof(float)));
+  cudaError_t e = lattice_fields(j->L, c.step, stride, rho ? d : nullptr, ux ? d + M : nullptr,
+                                 ux ? d + 2 * M : nullptr, ux ? d + 3 * M : nullptr, j->s0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(j->s0);
+  if (e == cudaSuccess && rho) e = cudaMemcpy(rho, d, M * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && ux) e = cudaMemcpy(ux, d + M, M * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && ux) e = cudaMemcpy(uy, d + 2 * M, M * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && ux) e = cudaMemcpy(uz, d + 3 * M, M * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  CK(e);
+  return PFGPU_OK;
+}
+
 int pfgpu_job_get_elements(pfgpu_job* j, double* X, double* Y, double* RY, double* Z, double* V, double* F) {
   if (!j) return set_error(PFGPU_ERR_INVALID, "bad job");
   CK(cudaStreamSynchronize(j->s0));

@@ -846,6 +846,34 @@ __global__ void download_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, con
   }
 }
 
+// Density and velocity (the units of download_k's u) at every stride-th
+// node in x, y and z, as float planes [mz][my][mx] for the VTK dump.
+template <class S, class R>
+__global__ void fields_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, const R4<R>* ubuf, int apply_bc,
+                         int use_ubuf, int stride, int mx, int my, int mz, float* rho, float* ux, float* uy,
+                         float* uz) {
+  const size_t m = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= (size_t)mx * my * mz) return;
+  const int x = (int)(m % mx) * stride, y = (int)((m / mx) % my) * stride, z = (int)(m / ((size_t)mx * my)) * stride;
+  const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
+  R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
+  ld_force<R>(Fsrc, n, Fx, Fy, Fz);
+  R drho, vx, vy, vz;
+  if (use_ubuf) {
+    ld_u<R>(ubuf, n, drho, vx, vy, vz);
+  } else {
+    R g[Q];
+    gather<S, R>(k, gsrc, x, y, z, g);
+    node_state<R>(k, g, z, apply_bc != 0, Fx, Fy, Fz, drho, vx, vy, vz);
+  }
+  if (rho) rho[m] = (float)(1.0 + (double)drho);
+  if (ux) {
+    ux[m] = (float)((double)vx * k.C);
+    uy[m] = (float)((double)vy * k.C);
+    uz[m] = (float)((double)vz * k.C);
+  }
+}
+
 // f*_d(x) = fIN_d(x + c_d) so that the first pull reproduces fIN; through a
 // bounce-back face f*_d(x) = fIN_opp(d)(x).  Also loads the initial force of
 // the step before the first (flags its bricks) and (rho, u/C) for the first
@@ -1039,6 +1067,30 @@ cudaError_t download_impl(Lattice& L, long long step, double* fIN, double* fOUT,
   return cudaGetLastError();
 }
 template <class S, class R>
+cudaError_t fields_impl(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
+                        cudaStream_t st) {
+  const void* gsrc;
+  const void* Fs;
+  int apply_bc = 1, use_ubuf = 0;
+  if (step == 0) {
+    gsrc = L.g[0];
+    Fs = L.F[1];
+    apply_bc = 0;
+    use_ubuf = 1;
+  } else {
+    const int last = (int)((step - 1) & 1);
+    gsrc = last ? L.g[0] : L.g[1];
+    Fs = L.F[last];
+  }
+  const int mx = (L.k.nx + stride - 1) / stride, my = (L.k.ny + stride - 1) / stride,
+            mz = (L.k.nz + stride - 1) / stride;
+  const size_t M = (size_t)mx * my * mz;
+  fields_k<S, R><<<(unsigned)((M + 255) / 256), 256, 0, st>>>(L.k, (const S*)gsrc, (const R4<R>*)Fs,
+                                                              (const R4<R>*)L.ubuf, apply_bc, use_ubuf, stride, mx,
+                                                              my, mz, rho, ux, uy, uz);
+  return cudaGetLastError();
+}
+template <class S, class R>
 cudaError_t conservation_impl(Lattice& L, long long step, double* out, cudaStream_t st) {
   const size_t N = (size_t)L.k.N;
   const void* gsrc = step == 0 ? L.g[0] : (((step - 1) & 1) ? L.g[0] : L.g[1]);
@@ -1141,6 +1193,15 @@ cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* f
     case PF_PREC_FP64: return download_impl<double, double>(L, step, fIN, fOUT, rho, u, F, st);
     case PF_PREC_FP32: return download_impl<float, float>(L, step, fIN, fOUT, rho, u, F, st);
     case PF_PREC_FP16: return download_impl<__half, float>(L, step, fIN, fOUT, rho, u, F, st);
+  }
+  return cudaErrorInvalidValue;
+}
+cudaError_t lattice_fields(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
+                           cudaStream_t st) {
+  switch (L.precision) {
+    case PF_PREC_FP64: return fields_impl<double, double>(L, step, stride, rho, ux, uy, uz, st);
+    case PF_PREC_FP32: return fields_impl<float, float>(L, step, stride, rho, ux, uy, uz, st);
+    case PF_PREC_FP16: return fields_impl<__half, float>(L, step, stride, rho, ux, uy, uz, st);
   }
   return cudaErrorInvalidValue;
 }

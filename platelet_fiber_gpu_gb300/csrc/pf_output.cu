@@ -12,6 +12,9 @@
 // Values are doubles as the reference writes them (PFGPU_OUT_FP64) or floats
 // (PFGPU_OUT_FP32): four floats per element is the 16-byte record
 // convBtoXYZ.py splits from `od -f` lines.  Host-only code.
+#include <sys/stat.h>
+#include <sys/types.h>
+
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -142,3 +145,55 @@ int pfgpu_output_close(pfgpu_output* o, int seed) {
 }
 
 }  // extern "C"
+
+// writeVTK of the reference driver (gpuSEM_LB.c:1631-1709): the same file
+// name pattern, XML header and value layout; Spacing carries the stride of
+// downsampled fields.
+extern "C" int pfgpu_write_vti(int t, int nx, int ny, int nz, int spacing, const float* rho, int write_rho,
+                               const float* ux, const float* uy, const float* uz, int write_vel,
+                               const char* directory, const char* filename) {
+  if (nx < 1 || ny < 1 || nz < 1 || spacing < 1 || !directory || !filename || (write_rho && !rho) ||
+      (write_vel && (!ux || !uy || !uz)))
+    return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_write_vti: bad arguments");
+  mkdir(directory, 0777);
+  char name[4096];
+  snprintf(name, sizeof name, "%s/%s_%07d.vti", directory, filename, t);
+  FILE* f = fopen(name, "w");
+  if (!f) return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_write_vti: cannot open the .vti file");
+  fprintf(f, "<?xml version=\"1.0\"?>\n");
+  fprintf(f, "<!-- gpuLBMflow ND ACMS -->\n");
+  fprintf(f, "<VTKFile type=\"ImageData\" version=\"0.1\" byte_order=\"LittleEndian\">\n");
+  fprintf(f, "  <ImageData WholeExtent=\"0 %d 0 %d 0 %d\" Origin=\"0 0 0\" Spacing=\"%d %d %d\">\n", nx - 1,
+          ny - 1, nz - 1, spacing, spacing, spacing);
+  fprintf(f, "  <Piece Extent=\"0 %d 0 %d 0 %d\">\n", nx - 1, ny - 1, nz - 1);
+  fprintf(f, "    <PointData Scalars=\"scalars\">\n");
+  const size_t row = (size_t)nx;
+  if (write_rho) {
+    fprintf(f, "      <DataArray type=\"Float32\" Name=\"Density\" NumberOfComponents=\"1\" format=\"ascii\">\n");
+    for (size_t r = 0; r < (size_t)ny * nz; ++r) {
+      for (size_t x = 0; x < row; ++x) fprintf(f, "%.4e ", rho[r * row + x]);
+      fprintf(f, "\n");
+    }
+    fprintf(f, "      </DataArray>\n");
+  }
+  if (write_vel) {
+    fprintf(f, "      <DataArray type=\"Float32\" Name=\"Velocity\" NumberOfComponents=\"3\" format=\"ascii\">\n");
+    for (size_t r = 0; r < (size_t)ny * nz; ++r) {
+      for (size_t x = 0; x < row; ++x) {
+        const size_t i = r * row + x;
+        fprintf(f, "%.4e %.4e %.4e ", ux[i], uy[i], uz[i]);
+      }
+      fprintf(f, "\n");
+    }
+    fprintf(f, "      </DataArray>\n");
+  }
+  fprintf(f, "    </PointData>\n");
+  fprintf(f, "    <CellData>\n");
+  fprintf(f, "    </CellData>\n");
+  fprintf(f, "  </Piece>\n");
+  fprintf(f, "  </ImageData>\n");
+  fprintf(f, "</VTKFile>\n");
+  const bool ok = !ferror(f);
+  if (fclose(f) != 0 || !ok) return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_write_vti: write failed");
+  return PFGPU_OK;
+}

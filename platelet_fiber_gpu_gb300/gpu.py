@@ -57,6 +57,10 @@ def lib():
         L.pfgpu_job_lbm_kernel.restype = C.c_char_p
         L.pfgpu_job_lbm_kernel.argtypes = [vp]
         L.pfgpu_output_open.argtypes = [vp, C.c_char_p, C.c_int, C.POINTER(vp)]
+        fp = C.POINTER(C.c_float)
+        L.pfgpu_job_get_fields.argtypes = [vp, C.c_int, fp, fp, fp, fp, ip]
+        L.pfgpu_write_vti.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, fp, C.c_int, fp, fp, fp, C.c_int,
+                                      C.c_char_p, C.c_char_p]
         L.pfgpu_output_frame.argtypes = [vp]
         L.pfgpu_output_close.argtypes = [vp, C.c_int]
         L.pfgpu_job_profile.argtypes = [vp, C.c_int, dp]
@@ -164,6 +168,26 @@ class Job:
         check(lib().pfgpu_job_get_lattice(self.h, _p(a), _p(b), _p(rho), _p(u), _p(F)))
         return dict(fIN=a, fOUT=b, rho=rho, u=u, F=F)
 
+    def fields(self, stride: int = 1):
+        """Density and velocity at every stride-th node, computed on the
+        device: float32 arrays rho [mz, my, mx] and u [3, mz, my, mx]."""
+        dims = (C.c_int * 3)()
+        check(lib().pfgpu_job_get_fields(self.h, stride, None, None, None, None, dims))
+        mx, my, mz = dims
+        rho = np.zeros((mz, my, mx), dtype=np.float32)
+        u = np.zeros((3, mz, my, mx), dtype=np.float32)
+        check(lib().pfgpu_job_get_fields(self.h, stride, _p(rho, C.c_float), _p(u[0], C.c_float),
+                                         _p(u[1], C.c_float), _p(u[2], C.c_float), dims))
+        return dict(rho=rho, u=u)
+
+    def write_vti(self, t: int, directory, filename: str = "LBMflow", stride: int = 1, write_rho: bool = True,
+                  write_vel: bool = True):
+        """The reference driver's VTK dump of this job's fields (downsampled
+        by `stride` on the device)."""
+        f = self.fields(stride)
+        write_vti(t, f["rho"], f["u"], directory, filename, spacing=stride, write_rho=write_rho,
+                  write_vel=write_vel)
+
     def elements(self):
         PE = self.scene.n_platelets * self.scene.n_elem
         X, Y, RY, Z = (np.zeros(PE) for _ in range(4))
@@ -240,6 +264,20 @@ class _BatchJob(Job):
 
     def close(self):
         self.h = None
+
+
+def write_vti(t: int, rho, u, directory, filename: str = "LBMflow", spacing: int = 1, write_rho: bool = True,
+              write_vel: bool = True):
+    """pfgpu_write_vti: rho [nz, ny, nx] and u [3, nz, ny, nx] float32 host
+    arrays to <directory>/<filename>_<t:07d>.vti (host-only)."""
+    rho = np.ascontiguousarray(rho, dtype=np.float32)
+    u = np.ascontiguousarray(u, dtype=np.float32)
+    nz, ny, nx = rho.shape
+    assert u.shape == (3, nz, ny, nx)
+    fp = C.c_float
+    check(lib().pfgpu_write_vti(int(t), nx, ny, nz, int(spacing), _p(rho, fp), int(write_rho), _p(u[0], fp),
+                                _p(u[1], fp), _p(u[2], fp), int(write_vel), str(directory).encode(),
+                                filename.encode()))
 
 
 class Batch:

@@ -62,3 +62,36 @@ def test_output_frames(gpu, tmp_path, fp32):
         assert n == 3
         xyz = read_xyz(tmp_path / "xyzFiles" / "pos_2.xyz")
         np.testing.assert_allclose(xyz, _positions(frames[2])[:, :3], rtol=1e-6)
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "fp32", "fp16"])
+def test_fields_and_vti(gpu, tmp_path, prec):
+    """pfgpu_job_get_fields (density and velocity computed on the device at
+    every stride-th node) agrees with the full lattice download rounded to
+    float, before the first step and after some; stride 2 is the subsample of
+    stride 1; the job's VTK dump holds those values at "%.4e"."""
+    import xml.etree.ElementTree as ET
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small()
+    j = gpu.Job(sc, prec)
+    for steps in (0, 5):
+        j.step(steps)
+        full = j.lattice(fIN=False)
+        shape = (sc.nz, sc.ny, sc.nx)
+        f1 = j.fields(1)
+        np.testing.assert_array_equal(f1["rho"], full["rho"].reshape(shape).astype(np.float32))
+        np.testing.assert_array_equal(f1["u"], full["u"].reshape((3,) + shape).astype(np.float32))
+        f2 = j.fields(2)
+        np.testing.assert_array_equal(f2["rho"], f1["rho"][::2, ::2, ::2])
+        np.testing.assert_array_equal(f2["u"], f1["u"][:, ::2, ::2, ::2])
+    j.write_vti(5, tmp_path / "Output", stride=2)
+    root = ET.parse(tmp_path / "Output" / "LBMflow_0000005.vti").getroot()
+    img = root.find("ImageData")
+    mz, my, mx = f2["rho"].shape
+    assert img.get("WholeExtent") == "0 %d 0 %d 0 %d" % (mx - 1, my - 1, mz - 1)
+    assert img.get("Spacing") == "2 2 2"
+    arrays = {a.get("Name"): np.array(a.text.split(), dtype=np.float64) for a in img.iter("DataArray")}
+    np.testing.assert_allclose(arrays["Density"], f2["rho"].ravel(), rtol=6e-5)
+    vel = np.stack([f2["u"][i].ravel() for i in range(3)], axis=1).ravel()
+    np.testing.assert_allclose(arrays["Velocity"], vel, rtol=6e-5, atol=1e-30)
+    j.close()
