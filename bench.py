@@ -59,6 +59,7 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.n0 = 0
 
     def __enter__(self):
         try:
@@ -67,6 +68,12 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the sampler is live before the timed region starts; samples
+            # taken before it are left out of the summary
+            t_end = time.time() + 3.0
+            while not self.lines and time.time() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.n0 = len(self.lines)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -77,6 +84,11 @@ class ClockSampler:
 
     def __exit__(self, *exc):
         if self.proc:
+            # a timed region shorter than the sampling interval still gets
+            # the sample that closes it
+            t_end = time.time() + 0.5
+            while len(self.lines) <= self.n0 and time.time() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=2)
@@ -87,7 +99,7 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[getattr(self, "n0", 0):]:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 8:
                 continue
