@@ -35,7 +35,7 @@ typedef enum pfgpu_status {
   PFGPU_ERR_NOMEM = 3,        /* device allocation failed or budget exceeded */
   PFGPU_ERR_UNSUPPORTED = 4,  /* valid input the GPU path does not implement */
   PFGPU_ERR_DEVICE = 5,       /* a kernel reported an error status */
-  PFGPU_DONE = 6              /* the platelet detached (reference semLB.cu:451-455) */
+  PFGPU_DONE = 6              /* the platelet detached (reference semLB.cu:451-455) or the job reached its stop step */
 } pfgpu_status;
 
 /* ------------------------------------------------------------ scene */
@@ -171,6 +171,11 @@ int pfgpu_job_get_cells(pfgpu_job *job, int *cell_of, int *counts, int *members,
 /* FP64 conservation sums over the lattice: mass and x/y/z momentum. */
 int pfgpu_job_conservation(pfgpu_job *job, double out[4]);
 int64_t pfgpu_job_step_count(const pfgpu_job *job);
+/* The job stops by itself after completing step stop_step (0: never): later
+ * steps do nothing and pfgpu_job_sync returns PFGPU_DONE, as after a
+ * detachment.  A stop step at or before the current step stops it at once; a
+ * later one lets a job stopped this way run on. */
+int pfgpu_job_set_stop(pfgpu_job *job, int64_t stop_step);
 size_t pfgpu_job_device_bytes(const pfgpu_job *job);
 /* Kernel launches one coupled step issues (graph nodes). */
 int pfgpu_job_launches_per_step(const pfgpu_job *job);
@@ -231,6 +236,10 @@ int pfgpu_batch_admit(pfgpu_batch *b, const pf_scene *scene, int precision, doub
  * status turns PFGPU_DONE (retire it). */
 int pfgpu_batch_step(pfgpu_batch *b, int nsteps);
 int pfgpu_batch_status(pfgpu_batch *b, int slot);
+/* pfgpu_job_set_stop for the job in `slot`: a served job is admitted with the
+ * step count it asked for and leaves the fused step when it reaches it, so a
+ * batch step can run a whole chunk of steps whatever the other jobs need. */
+int pfgpu_batch_set_stop(pfgpu_batch *b, int slot, int64_t stop_step);
 int pfgpu_batch_retire(pfgpu_batch *b, int slot);
 pfgpu_job *pfgpu_batch_job(pfgpu_batch *b, int slot);
 /* The fused step's shapes: shape[0] row segments per CTA of the unflagged

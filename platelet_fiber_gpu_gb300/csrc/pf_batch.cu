@@ -26,6 +26,16 @@ using namespace pf;
 
 extern "C" int pfgpu_job_enqueue(pfgpu_job* j, int nsteps);
 extern "C" int pfgpu_job_batch_desc_(pfgpu_job* j, BatchDesc* d, int* precision, int* fast);
+extern "C" int pfgpu_job_control_status_(const pfgpu_job* j, const Control* c);
+
+namespace {
+// every job's control block into one array (one copy to the host reads the
+// status of the whole batch)
+__global__ void gather_controls_k(const BatchDesc* d, int nj, Control* out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nj) out[j] = *d[j].ctl;
+}
+}  // namespace
 
 struct pfgpu_batch {
   size_t budget = 0, in_use = 0;
@@ -48,6 +58,8 @@ struct pfgpu_batch {
     int njobs = 0, sms = 0;
     long long nodes = 0;     // lattice nodes of all jobs (one step's node updates)
     BatchDesc* d_desc = nullptr;
+    Control* d_ctl = nullptr;  // gathered control blocks (device) and their host copy
+    Control* h_ctl = nullptr;
     // shapes with a CTA offset table on the device; `running` is the one
     // the step graph uses
     std::vector<BatchTune> shapes;
@@ -73,9 +85,13 @@ void fused_release(pfgpu_batch::Fused& f) {
   if (f.graph) cudaGraphExecDestroy(f.graph);
   if (f.d_desc) cudaFree(f.d_desc);
   if (f.d_start) cudaFree(f.d_start);
+  if (f.d_ctl) cudaFree(f.d_ctl);
+  if (f.h_ctl) cudaFreeHost(f.h_ctl);
   f.graph = nullptr;
   f.d_desc = nullptr;
   f.d_start = nullptr;
+  f.d_ctl = nullptr;
+  f.h_ctl = nullptr;
   f.valid = false;
   f.usable = false;
   f.exploring = false;
@@ -251,6 +267,8 @@ int fused_plan(pfgpu_batch* b) {
   BK_CK(cudaMalloc(&f.d_desc, sizeof(BatchDesc) * nj));
   BK_CK(cudaMalloc(&f.d_start, sizeof(int) * (size_t)kMaxShapes * BK_COUNT * (nj + 1)));
   BK_CK(cudaMemcpy(f.d_desc, f.descs.data(), sizeof(BatchDesc) * nj, cudaMemcpyHostToDevice));
+  BK_CK(cudaMalloc(&f.d_ctl, sizeof(Control) * nj));
+  BK_CK(cudaMallocHost(&f.h_ctl, sizeof(Control) * nj));
   if (!f.st[0]) {
     int lo = 0, hi = 0;
     BK_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
@@ -409,11 +427,16 @@ int pfgpu_batch_step(pfgpu_batch* b, int nsteps) {
     auto& f = b->fused;
     const int rc = fused_steps(b, nsteps);
     if (rc) return rc;
+    const int nj = f.njobs;
+    gather_controls_k<<<(nj + 127) / 128, 128, 0, f.st[0]>>>(f.d_desc, nj, f.d_ctl);
+    BK_CK(cudaGetLastError());
+    BK_CK(cudaMemcpyAsync(f.h_ctl, f.d_ctl, sizeof(Control) * nj, cudaMemcpyDeviceToHost, f.st[0]));
+    BK_CK(cudaStreamSynchronize(f.st[0]));
     int first_err = PFGPU_OK;
     bool changed = false;
-    for (int i : f.order) {
-      auto& s = b->slots[i];
-      const int rc = pfgpu_job_sync(s.job);
+    for (int q = 0; q < nj; ++q) {
+      auto& s = b->slots[f.order[q]];
+      const int rc = pfgpu_job_control_status_(s.job, &f.h_ctl[q]);
       if (rc == PFGPU_DONE) {
         s.status = PFGPU_DONE;
         changed = true;
@@ -437,6 +460,25 @@ int pfgpu_batch_step(pfgpu_batch* b, int nsteps) {
       else if (rc && !first_err) first_err = rc;
     }
   return first_err;
+}
+
+// The job in `slot` stops by itself after step stop_step (0: never); its
+// status turns PFGPU_DONE at the end of the batch step that reached it.
+int pfgpu_batch_set_stop(pfgpu_batch* b, int slot, int64_t stop_step) {
+  if (!b) return report_error(PFGPU_ERR_INVALID, "bad batch");
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].job)
+    return report_error(PFGPU_ERR_INVALID, "no job in this slot");
+  auto& s = b->slots[slot];
+  int rc = pfgpu_job_set_stop(s.job, stop_step);
+  if (rc) return rc;
+  rc = pfgpu_job_sync(s.job);
+  const int st = rc == PFGPU_DONE ? PFGPU_DONE : (rc ? s.status : PFGPU_OK);
+  if (st != s.status) {
+    s.status = st;
+    b->fused.valid = false;
+  }
+  return rc == PFGPU_DONE ? PFGPU_OK : rc;
 }
 
 int pfgpu_batch_status(pfgpu_batch* b, int slot) {

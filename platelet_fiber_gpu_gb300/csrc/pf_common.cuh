@@ -52,7 +52,7 @@ enum : uint32_t {
 // between steps.  Graph replays read the step counter from here.
 struct Control {
   long long step;         // coupled steps completed
-  int done;               // platelet detached (semLB.cu:451-455)
+  int done;               // 1: platelet detached (semLB.cu:451-455); 2: stop step reached
   int first;              // next LBM step is the first after an upload
   int total_bond;         // sum of bond counts of the last bond pass
   unsigned int err;       // ERR_* bits
@@ -65,6 +65,8 @@ struct Control {
   // whether that step is the first after an upload
   int far_first;
   long long far_step;
+  // the step after which the job stops by itself (done = 2; 0: never)
+  long long stop;
 };
 
 // ------------------------------------------------------------- Philox

@@ -600,15 +600,18 @@ static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
   return PFGPU_OK;
 }
 
-static int check_control(pfgpu_job* j) {
-  Control c;
-  CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+static int control_status(const Control& c) {
   if (c.err) {
     char buf[128];
     snprintf(buf, sizeof buf, "device error bits 0x%x", c.err);
     return set_error(PFGPU_ERR_DEVICE, buf);
   }
   return c.done ? PFGPU_DONE : PFGPU_OK;
+}
+static int check_control(pfgpu_job* j) {
+  Control c;
+  CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+  return control_status(c);
 }
 
 extern "C" {
@@ -816,6 +819,23 @@ int pfgpu_job_sync(pfgpu_job* j) {
   CK(cudaStreamSynchronize(j->s0));
   return check_control(j);
 }
+
+int pfgpu_job_set_stop(pfgpu_job* j, int64_t stop_step) {
+  if (!j || stop_step < 0) return set_error(PFGPU_ERR_INVALID, "bad job or stop step");
+  CK(cudaStreamSynchronize(j->s0));
+  Control c;
+  CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
+  c.stop = stop_step;
+  // a job stopped at its old stop step runs on to a later one
+  if (c.done == 2 && (stop_step == 0 || stop_step > c.step)) c.done = 0;
+  if (c.done == 0 && stop_step > 0 && c.step >= stop_step) c.done = 2;
+  CK(cudaMemcpy(j->ctl, &c, sizeof c, cudaMemcpyHostToDevice));
+  return PFGPU_OK;
+}
+
+// status of a job from a copy of its control block (batch steps read all
+// jobs' blocks with one copy)
+int pfgpu_job_control_status_(const pfgpu_job* j, const Control* c) { return j ? control_status(*c) : PFGPU_ERR_INVALID; }
 
 int64_t pfgpu_job_step_count(const pfgpu_job* j) {
   if (!j) return -1;

@@ -506,6 +506,7 @@ __device__ __forceinline__ void close_step(const PlateletConst& pk, Control* ctl
       // kernel then runs with no threads and totalBond stays at zero)
       if (!pk.nrec || !pk.P) ctl->total_bond = 0;
       if (detach_rate > 0 && ctl->total_bond == 0 && detach_uniform(seed, s) < detach_rate) ctl->done = 1;
+      if (!ctl->done && ctl->stop > 0 && s >= ctl->stop) ctl->done = 2;
       *done_blocks = 0u;
     }
   }

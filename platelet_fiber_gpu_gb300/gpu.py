@@ -83,6 +83,8 @@ def lib():
         L.pfgpu_batch_bytes_in_use.argtypes = [vp]
         L.pfgpu_batch_num_jobs.argtypes = [vp]
         L.pfgpu_batch_shape.argtypes = [vp, ip, ip]
+        L.pfgpu_batch_set_stop.argtypes = [vp, C.c_int, C.c_int64]
+        L.pfgpu_job_set_stop.argtypes = [vp, C.c_int64]
         L.pfgpu_batch_set_shape.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.pfgpu_batch_destroy.argtypes = [vp]
         L.pfgpu_detach_uniform.restype = C.c_double
@@ -131,6 +133,11 @@ class Job:
     def step(self, n: int = 1, graph: bool = True) -> int:
         f = lib().pfgpu_job_step_graph if graph else lib().pfgpu_job_step
         return check(f(self.h, int(n)), allow_done=True)
+
+    def set_stop(self, stop_step: int):
+        """The job stops by itself after step stop_step (0: never): later
+        steps do nothing and step() returns PFGPU_DONE."""
+        check(lib().pfgpu_job_set_stop(self.h, int(stop_step)))
 
     def profile(self, n: int) -> dict:
         """Per-phase device time (ms, summed over n serialised steps)."""
@@ -308,6 +315,11 @@ class Batch:
 
     def status(self, slot: int) -> int:
         return check(lib().pfgpu_batch_status(self.h, slot), allow_done=True)
+
+    def set_stop(self, slot: int, stop_step: int):
+        """The job stops by itself after step stop_step (0: never); its status
+        turns PFGPU_DONE at the end of the batch step that reached it."""
+        check(lib().pfgpu_batch_set_stop(self.h, slot, int(stop_step)))
 
     def job(self, slot: int) -> Job:
         return _BatchJob(self._scenes[slot], lib().pfgpu_batch_job(self.h, slot))

@@ -6,7 +6,8 @@
   together for a fixed number of steps; reports aggregate MLUPS.
 `run_served`  -- jobs arriving as a Poisson process with a requested step
   count each, admitted against a device-memory budget as they arrive
-  (continuous batching: jobs join and leave between batch steps); reports
+  (continuous batching: jobs join between batch steps of `chunk` steps and
+  leave by themselves when they reach their step count); reports
   aggregate MLUPS over the makespan and the p50 / p99 job latency
   (arrival to completion).
 
@@ -74,6 +75,9 @@ def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed:
     latencies = []
     work = 0
     i = 0
+    host = {"admit": 0.0, "step": 0.0, "retire": 0.0}
+    calls = 0
+    live_sum = 0
     t0 = time.perf_counter()
     while i < len(arrivals) or waiting or live:
         now = time.perf_counter() - t0
@@ -81,34 +85,45 @@ def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed:
             waiting.append(arrivals[i])
             i += 1
         still = []
+        ta = time.perf_counter()
         for a in waiting:
             sc = scenes[a[1]]
             s = b.admit(sc, precision)
             if s is None:
                 still.append(a)
                 continue
+            # the job leaves the fused step by itself after its requested steps
+            b.set_stop(s, a[2])
             live[s] = [a[0], a[2], sc.n_nodes, a[2]]
         waiting = still
+        host["admit"] += time.perf_counter() - ta
         if not live:
             if i < len(arrivals):
                 time.sleep(max(0.0, arrivals[i][0] - (time.perf_counter() - t0)))
             continue
-        k = min(chunk, min(v[1] for v in live.values()))
-        b.step(k)
+        ts = time.perf_counter()
+        b.step(chunk)
+        calls += 1
+        live_sum += len(live)
+        tr = time.perf_counter()
+        host["step"] += tr - ts
         for s in list(live):
-            live[s][1] -= k
-            if live[s][1] <= 0 or b.status(s) != 0:
+            live[s][1] -= chunk
+            if b.status(s) != 0:
                 arr, _, n, req = live.pop(s)
                 work += n * req
                 latencies.append(time.perf_counter() - t0 - arr)
                 b.retire(s)
+        host["retire"] += time.perf_counter() - tr
     span = time.perf_counter() - t0
     b.close()
     lat = np.array(latencies) if latencies else np.zeros(1)
     return {"mode": "served", "precision": precision, "jobs": len(arrivals), "rate_per_s": rate,
             "duration_s": duration, "makespan_s": round(span, 3), "mlups": round(work / span / 1e6, 1),
             "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
-            "latency_p99_s": round(float(np.percentile(lat, 99)), 4), "scene_pool": pool}
+            "latency_p99_s": round(float(np.percentile(lat, 99)), 4), "scene_pool": pool,
+            "host_s": {k: round(v, 3) for k, v in host.items()}, "step_calls": calls,
+            "mean_live_jobs": round(live_sum / max(1, calls), 1)}
 
 
 def main():

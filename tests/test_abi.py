@@ -107,5 +107,9 @@ def test_batch_shape_validation_without_gpu(lib):
         for bad in ((4, 8, 100), (4, 8, 512), (0 - 1, 8, 128), (4, 0, 128), (65, 8, 128)):
             assert lib.pfgpu_batch_set_shape(h, *bad) == 1, bad
         assert lib.pfgpu_batch_set_shape(None, 4, 8, 128) == 1
+        lib.pfgpu_batch_set_stop.argtypes = [C.c_void_p, C.c_int, C.c_int64]
+        assert lib.pfgpu_batch_set_stop(h, 0, 5) == 1  # no job in the slot
+        lib.pfgpu_job_set_stop.argtypes = [C.c_void_p, C.c_int64]
+        assert lib.pfgpu_job_set_stop(None, 5) == 1
     finally:
         lib.pfgpu_batch_destroy(h)

@@ -166,3 +166,45 @@ def test_autotuner_fixes_a_shape_and_caches_it(gpu, tmp_path, monkeypatch):
     b.close()
     line = cache.read_text().split()
     assert [int(v) for v in line[1:4]] == list(shape)
+
+
+def test_stop_steps(gpu):
+    """A job given a stop step halts there by itself (later steps do nothing,
+    the status reads done) and matches the same job stepped exactly that far;
+    a later stop step lets it run on.  In a fused batch, jobs with different
+    stop steps leave the batch step by themselves."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small(seed=3)
+    j = gpu.Job(sc, 1)
+    j.set_stop(5)
+    assert j.step(9) == gpu.PFGPU_DONE
+    assert j.steps == 5
+    ref = gpu.Job(sc, 1)
+    ref.step(5)
+    # float atomics in the spreading: equal to rounding, not bit for bit
+    a, r = j.lattice()["fIN"], ref.lattice()["fIN"]
+    assert np.abs(a - r).max() / np.abs(r).max() < 1e-6
+    assert np.abs(j.elements()["X"] - ref.elements()["X"]).max() < 1e-9
+    j.set_stop(8)
+    assert j.step(2) == 0 and j.steps == 7
+    assert j.step(5) == gpu.PFGPU_DONE and j.steps == 8
+    j.close()
+    ref.close()
+
+    scenes = _fused_scenes()
+    b = gpu.Batch(16 << 30)
+    slots = [b.admit(s, 1) for s in scenes]
+    stops = [3, 6, 0, 4]
+    for s, t in zip(slots, stops):
+        b.set_stop(s, t)
+    b.step(8)
+    for sc, s, t in zip(scenes, slots, stops):
+        got = b.job(s)
+        assert got.steps == (t or 8)
+        assert b.status(s) == (gpu.PFGPU_DONE if t else 0)
+        r = gpu.Job(sc, 1)
+        r.step(t or 8)
+        a, e = got.lattice()["fIN"], r.lattice()["fIN"]
+        assert np.abs(a - e).max() / np.abs(e).max() < 1e-5
+        r.close()
+    b.close()
