@@ -218,6 +218,11 @@ cudaError_t lattice_near(Lattice& L, Control* ctl, int from_mark, cudaStream_t s
 // far pass counter: sync (far_step = step) or advance after a far pass
 cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st);
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
+// initial equilibrium fIN [19][N] and ru [4][N] (device) of a scene given no
+// populations (u_init / rho_init: optional device arrays)
+cudaError_t lattice_equilibrium(int nx, int ny, int nz, int zh, double shear, double dx, double umax, double C0,
+                                const double* u_init, const double* rho_init, double* f, double* ru,
+                                cudaStream_t st);
 // density and velocity at every stride-th node (float [mz][my][mx] planes)
 cudaError_t lattice_fields(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
                            cudaStream_t st);

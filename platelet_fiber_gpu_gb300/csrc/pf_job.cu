@@ -221,40 +221,18 @@ static int validate(const pf_scene* s, int precision) {
 
 // Initial populations and the (rho, u) of the first collision, in the
 // reference's host conventions (gpuSEM_LB.c:1206-1258 and
-// fluid_initGPUKernel, semLB.cu:154-233).
+// fluid_initGPUKernel, semLB.cu:154-233), for a scene that brings its own
+// populations (f_init): (rho, u) from rho_init / u_init when given, else the
+// moments of f_init with the half-force shift and the Zou/He wall
+// velocities.  Scenes without populations start from the equilibrium
+// computed on the device (lattice_equilibrium).
 static void initial_lattice(const pf_scene* s, std::vector<double>& f, std::vector<double>& ru) {
   const size_t N = (size_t)s->nx * s->ny * s->nz;
   const int zh = s->bc[2] == PF_BC_ZOUHE_SHEAR;
   const float* mp = s->params;
   const bool have_ru = s->rho_init && s->u_init;
   ru.assign(4 * N, 0.0);
-  if (s->f_init) {
-    f.assign(s->f_init, s->f_init + 19 * N);
-  } else {
-    f.assign(19 * N, 0.0);
-    const double shear = (double)mp[PF_P_SHEAR];
-    const double umax_d = shear > 0 ? shear * (s->nz - 1) * (double)s->dx : (double)mp[PF_P_UMAX];
-    const float dxdt = s->dx / s->dt;
-    const double C0 = (double)dxdt / umax_d, C02 = C0 * C0;
-    for (int k = 0; k < s->nz; ++k)
-      for (int j = 0; j < s->ny; ++j)
-        for (int i = 0; i < s->nx; ++i) {
-          const size_t n = (size_t)i + (size_t)s->nx * (j + (size_t)s->ny * k);
-          double u[3] = {0, 0, 0}, r = 1.0;
-          if (s->u_init) {
-            u[0] = s->u_init[n]; u[1] = s->u_init[N + n]; u[2] = s->u_init[2 * N + n];
-          } else if (zh) {
-            u[1] = shear * k * (double)s->dx / umax_d;
-          }
-          if (s->rho_init) r = s->rho_init[n];
-          for (int d = 0; d < 19; ++d) {
-            const double cu = 3.0 * (cx(d) * u[0] + cy(d) * u[1] + cz(d) * u[2]);
-            f[d * N + n] = r * wgt(d) * (1.0 + cu / C0 + 0.5 * cu * cu / C02 -
-                                         1.5 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) / C02);
-          }
-          ru[n] = r; ru[N + n] = u[0]; ru[2 * N + n] = u[1]; ru[3 * N + n] = u[2];
-        }
-  }
+  f.assign(s->f_init, s->f_init + 19 * N);
   if (have_ru) {
     for (size_t n = 0; n < N; ++n) {
       ru[n] = s->rho_init[n];
@@ -262,7 +240,7 @@ static void initial_lattice(const pf_scene* s, std::vector<double>& f, std::vect
       ru[2 * N + n] = s->u_init[N + n];
       ru[3 * N + n] = s->u_init[2 * N + n];
     }
-  } else if (s->f_init) {
+  } else {
     float c = s->dx / s->dt;
     c = c / mp[PF_P_UMAX];
     const double C = (double)c;
@@ -709,13 +687,37 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(dalloc(j, &j->done_blocks, 1));
   CKJ(dalloc(j, &j->scratch4, 4));
   {
+    // initial populations: the scene's own (uploaded), else the equilibrium
+    // of the initial flow computed on the device
     std::vector<double> f, ru;
-    initial_lattice(s, f, ru);
-    double *df = nullptr, *dF = nullptr, *dru = nullptr;
-    CKJ(cudaMalloc(&df, f.size() * sizeof(double)));
-    cudaError_t e = cudaMemcpy(df, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&dru, ru.size() * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemcpy(dru, ru.data(), ru.size() * sizeof(double), cudaMemcpyHostToDevice);
+    double *df = nullptr, *dF = nullptr, *dru = nullptr, *dui = nullptr, *dri = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (s->f_init) {
+      initial_lattice(s, f, ru);
+      e = cudaMalloc(&df, f.size() * sizeof(double));
+      if (e == cudaSuccess) e = cudaMemcpy(df, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMalloc(&dru, ru.size() * sizeof(double));
+      if (e == cudaSuccess) e = cudaMemcpy(dru, ru.data(), ru.size() * sizeof(double), cudaMemcpyHostToDevice);
+    } else {
+      e = cudaMalloc(&df, 19 * N * sizeof(double));
+      if (e == cudaSuccess) e = cudaMalloc(&dru, 4 * N * sizeof(double));
+      if (e == cudaSuccess && s->u_init) {
+        e = cudaMalloc(&dui, 3 * N * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemcpy(dui, s->u_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
+      }
+      if (e == cudaSuccess && s->rho_init) {
+        e = cudaMalloc(&dri, N * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemcpy(dri, s->rho_init, N * sizeof(double), cudaMemcpyHostToDevice);
+      }
+      const float* mp = s->params;
+      const double shear = (double)mp[PF_P_SHEAR];
+      const double umax_d = shear > 0 ? shear * (s->nz - 1) * (double)s->dx : (double)mp[PF_P_UMAX];
+      const float dxdt = s->dx / s->dt;
+      const double C0 = (double)dxdt / umax_d;
+      if (e == cudaSuccess)
+        e = lattice_equilibrium(s->nx, s->ny, s->nz, s->bc[2] == PF_BC_ZOUHE_SHEAR, shear, (double)s->dx, umax_d,
+                                C0, dui, dri, df, dru, j->s0);
+    }
     if (e == cudaSuccess && s->F_init) {
       e = cudaMalloc(&dF, 3 * N * sizeof(double));
       if (e == cudaSuccess) e = cudaMemcpy(dF, s->F_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
@@ -726,6 +728,8 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
     cudaFree(df);
     cudaFree(dF);
     cudaFree(dru);
+    cudaFree(dui);
+    cudaFree(dri);
     CKJ(e);
   }
   Control c{};

@@ -907,6 +907,43 @@ __global__ void upload_k(LatticeConst k, S* g, const double* fIN, R4<R>* Fprev, 
   st_u<R>(ubuf, n, (R)(ru[n] - 1.0), (R)(ru[N + n] / k.C), (R)(ru[2 * N + n] / k.C), (R)(ru[3 * N + n] / k.C));
 }
 
+// Initial equilibrium populations fIN[19][N] and (rho, u) ru[4][N] of a
+// scene given no populations: rho = 1 (or rho_init), u = the linear shear
+// profile u_y = shear * z * dx / UMAX of the Zou/He channel (or u_init, or
+// rest).  The FP64 operations and their order are those of the host
+// restatement (round-to-nearest intrinsics, no contraction), so the two agree
+// bit for bit.
+__global__ void equilibrium_k(int nx, int ny, long long N, int zh, double shear, double dx, double umax,
+                              double C0, double C02, const double* u_init, const double* rho_init, double* f,
+                              double* ru) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int z = (int)(n / ((long long)nx * ny));
+  double u0 = 0, u1 = 0, u2 = 0, r = 1.0;
+  if (u_init) {
+    u0 = u_init[n];
+    u1 = u_init[N + n];
+    u2 = u_init[2 * N + n];
+  } else if (zh) {
+    u1 = __ddiv_rn(__dmul_rn(__dmul_rn(shear, (double)z), dx), umax);
+  }
+  if (rho_init) r = rho_init[n];
+  const double uu = __dadd_rn(__dadd_rn(__dmul_rn(u0, u0), __dmul_rn(u1, u1)), __dmul_rn(u2, u2));
+  const double tail = __ddiv_rn(__dmul_rn(1.5, uu), C02);
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    const double cu = __dmul_rn(3.0, __dadd_rn(__dadd_rn(__dmul_rn((double)cx(d), u0), __dmul_rn((double)cy(d), u1)),
+                                               __dmul_rn((double)cz(d), u2)));
+    const double in = __dsub_rn(__dadd_rn(__dadd_rn(1.0, __ddiv_rn(cu, C0)), __ddiv_rn(__dmul_rn(__dmul_rn(0.5, cu), cu), C02)),
+                                tail);
+    f[(size_t)d * N + n] = __dmul_rn(__dmul_rn(r, wgt(d)), in);
+  }
+  ru[n] = r;
+  ru[N + n] = u0;
+  ru[2 * N + n] = u1;
+  ru[3 * N + n] = u2;
+}
+
 template <class S, class R>
 __global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
   const size_t N = (size_t)k.N;
@@ -1195,6 +1232,14 @@ cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* f
     case PF_PREC_FP16: return download_impl<__half, float>(L, step, fIN, fOUT, rho, u, F, st);
   }
   return cudaErrorInvalidValue;
+}
+cudaError_t lattice_equilibrium(int nx, int ny, int nz, int zh, double shear, double dx, double umax, double C0,
+                                const double* u_init, const double* rho_init, double* f, double* ru,
+                                cudaStream_t st) {
+  const long long N = (long long)nx * ny * nz;
+  equilibrium_k<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nx, ny, N, zh, shear, dx, umax, C0, C0 * C0, u_init,
+                                                              rho_init, f, ru);
+  return cudaGetLastError();
 }
 cudaError_t lattice_fields(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
                            cudaStream_t st) {
