@@ -223,6 +223,10 @@ cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
 cudaError_t lattice_equilibrium(int nx, int ny, int nz, int zh, double shear, double dx, double umax, double C0,
                                 const double* u_init, const double* rho_init, double* f, double* ru,
                                 cudaStream_t st);
+// (rho, u) ru [4][N] of given initial populations f [19][N] (device; F: the
+// initial force [3][N] or NULL)
+cudaError_t lattice_initial_moments(int nx, int ny, int nz, int zh, double C, double Fo, double dt, double uw,
+                                    const double* f, const double* F, double* ru, cudaStream_t st);
 // density and velocity at every stride-th node (float [mz][my][mx] planes)
 cudaError_t lattice_fields(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
                            cudaStream_t st);

@@ -219,59 +219,6 @@ static int validate(const pf_scene* s, int precision) {
   return PFGPU_OK;
 }
 
-// Initial populations and the (rho, u) of the first collision, in the
-// reference's host conventions (gpuSEM_LB.c:1206-1258 and
-// fluid_initGPUKernel, semLB.cu:154-233), for a scene that brings its own
-// populations (f_init): (rho, u) from rho_init / u_init when given, else the
-// moments of f_init with the half-force shift and the Zou/He wall
-// velocities.  Scenes without populations start from the equilibrium
-// computed on the device (lattice_equilibrium).
-static void initial_lattice(const pf_scene* s, std::vector<double>& f, std::vector<double>& ru) {
-  const size_t N = (size_t)s->nx * s->ny * s->nz;
-  const int zh = s->bc[2] == PF_BC_ZOUHE_SHEAR;
-  const float* mp = s->params;
-  const bool have_ru = s->rho_init && s->u_init;
-  ru.assign(4 * N, 0.0);
-  f.assign(s->f_init, s->f_init + 19 * N);
-  if (have_ru) {
-    for (size_t n = 0; n < N; ++n) {
-      ru[n] = s->rho_init[n];
-      ru[N + n] = s->u_init[n];
-      ru[2 * N + n] = s->u_init[N + n];
-      ru[3 * N + n] = s->u_init[2 * N + n];
-    }
-  } else {
-    float c = s->dx / s->dt;
-    c = c / mp[PF_P_UMAX];
-    const double C = (double)c;
-    float fq = mp[PF_P_F0] / mp[PF_P_RHO0];
-    fq = fq / mp[PF_P_UMAX];
-    fq = fq * mp[PF_P_UNIT];
-    const double Fo = (double)fq;
-    float uwf = mp[PF_P_SHEAR] * (float)(s->nz - 1);
-    uwf = uwf * s->dx;
-    uwf = uwf / mp[PF_P_UMAX];
-    for (size_t n = 0; n < N; ++n) {
-      double r = 0, a = 0, b = 0, cc = 0;
-      for (int d = 0; d < 19; ++d) {
-        const double v = f[d * N + n];
-        r += v; a += cx(d) * v; b += cy(d) * v; cc += cz(d) * v;
-      }
-      const double Fx = s->F_init ? s->F_init[n] : 0, Fy = s->F_init ? s->F_init[N + n] : 0,
-                   Fz = s->F_init ? s->F_init[2 * N + n] : 0;
-      ru[n] = r;
-      ru[N + n] = (a * C + 0.5 * Fo * Fx * (double)s->dt) / r;
-      ru[2 * N + n] = (b * C + 0.5 * Fo * Fy * (double)s->dt) / r;
-      ru[3 * N + n] = (cc * C + 0.5 * Fo * Fz * (double)s->dt) / r;
-      const int k = (int)(n / ((size_t)s->nx * s->ny));
-      if (zh && (k == 0 || k == s->nz - 1)) {
-        ru[N + n] = 0; ru[3 * N + n] = 0;
-        ru[2 * N + n] = k == 0 ? 0.0 : (double)uwf;
-      }
-    }
-  }
-}
-
 static int build_platelets(pfgpu_job* j, const pf_scene* s) {
   Platelets& P = j->Pl;
   PlateletConst& k = P.k;
@@ -689,18 +636,37 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   {
     // initial populations: the scene's own (uploaded), else the equilibrium
     // of the initial flow computed on the device
-    std::vector<double> f, ru;
     double *df = nullptr, *dF = nullptr, *dru = nullptr, *dui = nullptr, *dri = nullptr;
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = cudaMalloc(&df, 19 * N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dru, 4 * N * sizeof(double));
+    if (e == cudaSuccess && s->F_init) {
+      e = cudaMalloc(&dF, 3 * N * sizeof(double));
+      if (e == cudaSuccess) e = cudaMemcpy(dF, s->F_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    const float* mp = s->params;
+    const int zh = s->bc[2] == PF_BC_ZOUHE_SHEAR;
     if (s->f_init) {
-      initial_lattice(s, f, ru);
-      e = cudaMalloc(&df, f.size() * sizeof(double));
-      if (e == cudaSuccess) e = cudaMemcpy(df, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) e = cudaMalloc(&dru, ru.size() * sizeof(double));
-      if (e == cudaSuccess) e = cudaMemcpy(dru, ru.data(), ru.size() * sizeof(double), cudaMemcpyHostToDevice);
+      // the scene's populations; (rho, u) from rho_init / u_init, else their
+      // moments (fluid_initGPUKernel, semLB.cu:154-233)
+      if (e == cudaSuccess) e = cudaMemcpy(df, s->f_init, 19 * N * sizeof(double), cudaMemcpyHostToDevice);
+      if (s->rho_init && s->u_init) {
+        if (e == cudaSuccess) e = cudaMemcpy(dru, s->rho_init, N * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(dru + N, s->u_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
+      } else {
+        float c = s->dx / s->dt;
+        c = c / mp[PF_P_UMAX];
+        float fq = mp[PF_P_F0] / mp[PF_P_RHO0];
+        fq = fq / mp[PF_P_UMAX];
+        fq = fq * mp[PF_P_UNIT];
+        float uwf = mp[PF_P_SHEAR] * (float)(s->nz - 1);
+        uwf = uwf * s->dx;
+        uwf = uwf / mp[PF_P_UMAX];
+        if (e == cudaSuccess)
+          e = lattice_initial_moments(s->nx, s->ny, s->nz, zh, (double)c, (double)fq, (double)s->dt, (double)uwf, df,
+                                      dF, dru, j->s0);
+      }
     } else {
-      e = cudaMalloc(&df, 19 * N * sizeof(double));
-      if (e == cudaSuccess) e = cudaMalloc(&dru, 4 * N * sizeof(double));
+      // the equilibrium of the initial flow (gpuSEM_LB.c:1206-1258)
       if (e == cudaSuccess && s->u_init) {
         e = cudaMalloc(&dui, 3 * N * sizeof(double));
         if (e == cudaSuccess) e = cudaMemcpy(dui, s->u_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
@@ -709,18 +675,12 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
         e = cudaMalloc(&dri, N * sizeof(double));
         if (e == cudaSuccess) e = cudaMemcpy(dri, s->rho_init, N * sizeof(double), cudaMemcpyHostToDevice);
       }
-      const float* mp = s->params;
       const double shear = (double)mp[PF_P_SHEAR];
       const double umax_d = shear > 0 ? shear * (s->nz - 1) * (double)s->dx : (double)mp[PF_P_UMAX];
       const float dxdt = s->dx / s->dt;
       const double C0 = (double)dxdt / umax_d;
       if (e == cudaSuccess)
-        e = lattice_equilibrium(s->nx, s->ny, s->nz, s->bc[2] == PF_BC_ZOUHE_SHEAR, shear, (double)s->dx, umax_d,
-                                C0, dui, dri, df, dru, j->s0);
-    }
-    if (e == cudaSuccess && s->F_init) {
-      e = cudaMalloc(&dF, 3 * N * sizeof(double));
-      if (e == cudaSuccess) e = cudaMemcpy(dF, s->F_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
+        e = lattice_equilibrium(s->nx, s->ny, s->nz, zh, shear, (double)s->dx, umax_d, C0, dui, dri, df, dru, j->s0);
     }
     if (e == cudaSuccess) e = lattice_upload(L, df, dF, dru, j->ctl, j->s0);
     if (e == cudaSuccess) e = lattice_configure(L);

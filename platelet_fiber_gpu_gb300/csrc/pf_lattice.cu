@@ -944,6 +944,35 @@ __global__ void equilibrium_k(int nx, int ny, long long N, int zh, double shear,
   ru[3 * N + n] = u2;
 }
 
+// (rho, u) ru[4][N] of given initial populations f[19][N]: the moments with
+// the half-force shift, the Zou/He walls at rest (bottom) and moving (top),
+// in the operation order of the host restatement (FP64, no contraction).
+__global__ void initial_moments_k(int nx, int ny, int nz, long long N, int zh, double C, double Fo, double dt,
+                                  double uw, const double* f, const double* F, double* ru) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double r = 0, a = 0, b = 0, c = 0;
+  for (int d = 0; d < Q; ++d) {
+    const double v = f[(size_t)d * N + n];
+    r = __dadd_rn(r, v);
+    a = __dadd_rn(a, __dmul_rn((double)cx(d), v));
+    b = __dadd_rn(b, __dmul_rn((double)cy(d), v));
+    c = __dadd_rn(c, __dmul_rn((double)cz(d), v));
+  }
+  const double Fx = F ? F[n] : 0, Fy = F ? F[N + n] : 0, Fz = F ? F[2 * N + n] : 0;
+  const double h = __dmul_rn(0.5, Fo);
+  ru[n] = r;
+  ru[N + n] = __ddiv_rn(__dadd_rn(__dmul_rn(a, C), __dmul_rn(__dmul_rn(h, Fx), dt)), r);
+  ru[2 * N + n] = __ddiv_rn(__dadd_rn(__dmul_rn(b, C), __dmul_rn(__dmul_rn(h, Fy), dt)), r);
+  ru[3 * N + n] = __ddiv_rn(__dadd_rn(__dmul_rn(c, C), __dmul_rn(__dmul_rn(h, Fz), dt)), r);
+  const int z = (int)(n / ((long long)nx * ny));
+  if (zh && (z == 0 || z == nz - 1)) {
+    ru[N + n] = 0;
+    ru[3 * N + n] = 0;
+    ru[2 * N + n] = z == 0 ? 0.0 : uw;
+  }
+}
+
 template <class S, class R>
 __global__ void conservation_k(LatticeConst k, const S* gsrc, double* out) {
   const size_t N = (size_t)k.N;
@@ -1232,6 +1261,12 @@ cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* f
     case PF_PREC_FP16: return download_impl<__half, float>(L, step, fIN, fOUT, rho, u, F, st);
   }
   return cudaErrorInvalidValue;
+}
+cudaError_t lattice_initial_moments(int nx, int ny, int nz, int zh, double C, double Fo, double dt, double uw,
+                                    const double* f, const double* F, double* ru, cudaStream_t st) {
+  const long long N = (long long)nx * ny * nz;
+  initial_moments_k<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nx, ny, nz, N, zh, C, Fo, dt, uw, f, F, ru);
+  return cudaGetLastError();
 }
 cudaError_t lattice_equilibrium(int nx, int ny, int nz, int zh, double shear, double dx, double umax, double C0,
                                 const double* u_init, const double* rho_init, double* f, double* ru,
