@@ -217,6 +217,36 @@ void pfgpu_job_destroy(pfgpu_job *job);
 /* Device bytes a job with this scene and precision would allocate. */
 size_t pfgpu_scene_device_bytes(const pf_scene *scene, int precision);
 
+/* ------------------------------------------------------------ host input */
+/* The reference driver's inputs, read and built on the host (no CUDA call):
+ * the parameter file (ParReader, gpuSEM_LB.c:148-343), the NEU surface mesh
+ * (NEUReader, gpuSEM_LB.c:345-404) and the membrane topology built from it
+ * (gpuSEM_LB.c:846-1055), with CSR tables instead of the dense bondLengths
+ * table and the [node][10] arrays.  Errors return PFGPU_ERR_INVALID with the
+ * reason in pfgpu_last_error (the reference prints and exits). */
+typedef struct pf_parameter_file {
+  char pdb_path[256], psf_path[256], neu_path[256];
+  float dx, dt, sim_time;                  /* DELTA_X, DELTA_T, SIM_TIME */
+  int out_freq, max_cell, max_elem, surf_elem;  /* OUT_FREQ, MAX_CELL, MAX_ELEM, SURF_ELEM */
+  /* HostParam: [0] RECEPTOR, [1] RANDOM_SEED, [2] K_SPRING, [3] Kf0 (not in
+   * the file), [4] Kr0, [5] SHEAR_RATE, [6] INIT_RHO */
+  float host_param[7];
+} pf_parameter_file;
+int pfgpu_read_parameter_file(const char *path, pf_parameter_file *out);
+int pfgpu_neu_counts(const char *path, int *n_sce, int *n_tri);
+/* X, Y, Z [n_sce]; tri3 [n_tri][3] 0-based; bond CSR of the triangle edges:
+ * bond_ptr [n_sce + 1], bond_nbr / bond_len [6 n_tri] (ascending neighbour). */
+int pfgpu_read_neu(const char *path, double *X, double *Y, double *Z, int *tri3, int *bond_ptr, int *bond_nbr,
+                   double *bond_len);
+/* tri6 [n_tri][6] (vertices, then the virtual edge nodes), node_ptr
+ * [n_vert + 3 n_tri + 1] / node_tri [6 n_tri] (triangles of each node; a
+ * vertex's in ring order), ring [3 n_tri] (vertex i's ordered neighbours at
+ * ring[node_ptr[i] + j]), normals [3 (n_vert + 3 n_tri)], S0 [n_tri], the
+ * total rest area and the volume; *n_nodes: vertices + virtual nodes. */
+int pfgpu_build_topology(int n_vert, int n_tri, const int *tri3, const double *X, const double *Y, const double *Z,
+                         int *tri6, int *n_nodes, int *node_ptr, int *node_tri, int *ring, double *normals,
+                         double *S0, double *S0_all, double *V0);
+
 /* ------------------------------------------------------------ batch API */
 /* Continuous batching of independent jobs on one GPU: each admitted job keeps
  * its own device state.  A batch step of FP32 or FP16 jobs is one captured

@@ -57,6 +57,12 @@ def lib():
         L.pfgpu_job_lbm_kernel.restype = C.c_char_p
         L.pfgpu_job_lbm_kernel.argtypes = [vp]
         L.pfgpu_output_open.argtypes = [vp, C.c_char_p, C.c_int, C.POINTER(vp)]
+        dpp = C.POINTER(C.c_double)
+        L.pfgpu_read_parameter_file.argtypes = [C.c_char_p, vp]
+        L.pfgpu_neu_counts.argtypes = [C.c_char_p, ip, ip]
+        L.pfgpu_read_neu.argtypes = [C.c_char_p, dpp, dpp, dpp, ip, ip, ip, dpp]
+        L.pfgpu_build_topology.argtypes = [C.c_int, C.c_int, ip, dpp, dpp, dpp, ip, ip, ip, ip, ip, dpp, dpp, dpp,
+                                           dpp]
         fp = C.POINTER(C.c_float)
         L.pfgpu_job_get_fields.argtypes = [vp, C.c_int, fp, fp, fp, fp, ip]
         L.pfgpu_write_vti.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, fp, C.c_int, fp, fp, fp, C.c_int,
@@ -285,6 +291,68 @@ def write_vti(t: int, rho, u, directory, filename: str = "LBMflow", spacing: int
     check(lib().pfgpu_write_vti(int(t), nx, ny, nz, int(spacing), _p(rho, fp), int(write_rho), _p(u[0], fp),
                                 _p(u[1], fp), _p(u[2], fp), int(write_vel), str(directory).encode(),
                                 filename.encode()))
+
+
+class ParameterFile(C.Structure):
+    """pf_parameter_file (the reference driver's Input/parameter.dat)."""
+    _fields_ = [("pdb_path", C.c_char * 256), ("psf_path", C.c_char * 256), ("neu_path", C.c_char * 256),
+                ("dx", C.c_float), ("dt", C.c_float), ("sim_time", C.c_float), ("out_freq", C.c_int),
+                ("max_cell", C.c_int), ("max_elem", C.c_int), ("surf_elem", C.c_int),
+                ("host_param", C.c_float * 7)]
+
+
+def read_parameter_file(path) -> dict:
+    """pfgpu_read_parameter_file (host-only): the reference's ParReader."""
+    p = ParameterFile()
+    check(lib().pfgpu_read_parameter_file(str(path).encode(), C.addressof(p)))
+    d = {k: getattr(p, k) for k, _ in ParameterFile._fields_}
+    for k in ("pdb_path", "psf_path", "neu_path"):
+        d[k] = d[k].decode()
+    d["host_param"] = list(p.host_param)
+    return d
+
+
+def read_neu(path) -> dict:
+    """pfgpu_read_neu (host-only): vertex coordinates, 0-based triangles and
+    the CSR bond lengths of the triangle edges of a NEU mesh file."""
+    ns, nt = C.c_int(0), C.c_int(0)
+    check(lib().pfgpu_neu_counts(str(path).encode(), C.byref(ns), C.byref(nt)))
+    n, t = ns.value, nt.value
+    X, Y, Z = np.zeros(n), np.zeros(n), np.zeros(n)
+    tri = np.zeros((t, 3), dtype=np.int32)
+    ptr = np.zeros(n + 1, dtype=np.int32)
+    nbr = np.zeros(max(1, 6 * t), dtype=np.int32)
+    ln = np.zeros(max(1, 6 * t))
+    ip = C.c_int
+    check(lib().pfgpu_read_neu(str(path).encode(), _p(X), _p(Y), _p(Z), _p(tri, ip), _p(ptr, ip), _p(nbr, ip),
+                               _p(ln)))
+    m = int(ptr[-1])
+    return dict(X=X, Y=Y, Z=Z, tri=tri, bond_ptr=ptr, bond_nbr=nbr[:m].copy(), bond_len=ln[:m].copy())
+
+
+def build_topology(tri, X, Y, Z) -> dict:
+    """pfgpu_build_topology (host-only): virtual edge nodes, node -> triangle
+    CSR, ordered vertex rings, reference normals, rest areas and volume."""
+    tri = np.ascontiguousarray(np.asarray(tri)[:, :3], dtype=np.int32)
+    X, Y, Z = (np.ascontiguousarray(a, dtype=np.float64) for a in (X, Y, Z))
+    nv, nt = len(X), len(tri)
+    cap = nv + 3 * nt
+    tri6 = np.zeros((nt, 6), dtype=np.int32)
+    ptr = np.zeros(cap + 1, dtype=np.int32)
+    ntri = np.zeros(6 * nt, dtype=np.int32)
+    ring = np.zeros(3 * nt, dtype=np.int32)
+    normals = np.zeros((cap, 3))
+    S0 = np.zeros(nt)
+    S0_all, V0 = C.c_double(0), C.c_double(0)
+    nn = C.c_int(0)
+    ip = C.c_int
+    check(lib().pfgpu_build_topology(nv, nt, _p(tri, ip), _p(X), _p(Y), _p(Z), _p(tri6, ip), C.byref(nn),
+                                     _p(ptr, ip), _p(ntri, ip), _p(ring, ip), _p(normals), _p(S0), C.byref(S0_all),
+                                     C.byref(V0)))
+    n = nn.value
+    ptr = ptr[:n + 1].copy()
+    return dict(tri6=tri6, n_nodes=n, node_ptr=ptr, node_tri=ntri[:ptr[-1]].copy(), ring=ring[:ptr[nv]].copy(),
+                normals=normals[:n].copy(), S0=S0, S0_all=S0_all.value, V0=V0.value)
 
 
 class Batch:

@@ -49,6 +49,14 @@ class PlateletTemplate:
         self.sp_ptr, self.sp_nbr, self.sp_L0 = M.edge_rest_lengths(self.verts, self.tris, self.n_elem)
         self.mean_bond = M.mean_bond_length(self.sp_L0, self.sp_ptr, self.sp_nbr)
 
+    @classmethod
+    def from_neu(cls, path, n_cyto: int, seed: int, axes):
+        """A template whose membrane is the reference's NEU surface mesh (read
+        by libpfgpu's NEU reader); `axes` bound the cytoplasm sampling."""
+        from .gpu import read_neu
+        m = read_neu(path)
+        return cls(np.stack([m["X"], m["Y"], m["Z"]], 1), m["tri"], n_cyto, seed, axes)
+
 
 def _place(scene: Scene, tpl: PlateletTemplate, centers: np.ndarray, ly_um: float):
     P = len(centers)
