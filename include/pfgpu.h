@@ -272,7 +272,7 @@ int pfgpu_batch_status(pfgpu_batch *b, int slot);
 int pfgpu_batch_set_stop(pfgpu_batch *b, int slot, int64_t stop_step);
 int pfgpu_batch_retire(pfgpu_batch *b, int slot);
 pfgpu_job *pfgpu_batch_job(pfgpu_batch *b, int slot);
-/* The fused step's shapes: shape[0] row segments per CTA of the unflagged
+/* The fused step's shapes: shape[0] groups of four bricks per CTA of the unflagged
  * lattice pass, shape[1] CTAs per SM of the near-region list and moments
  * passes, shape[2] threads per CTA of the marker passes.  *state: 0 still
  * tuning, 1 fixed (tuned, forced or tuning off), -1 no fused step. */

@@ -508,7 +508,7 @@ pfgpu_job* pfgpu_batch_job(pfgpu_batch* b, int slot) {
   return b->slots[slot].job;
 }
 
-// The fused step's block and tile shapes: shape[0] row segments per CTA of
+// The fused step's block and tile shapes: shape[0] groups of four bricks per CTA of
 // the unflagged lattice pass, shape[1] CTAs per SM of the list and moments
 // passes, shape[2] threads per CTA of the marker passes.  *state: 0 the
 // autotuner is still measuring candidates (shape is the one running between

@@ -169,7 +169,7 @@ enum BatchKernel : int {
 };
 // Block and tile shapes of a fused batch step (picked by the batch autotuner)
 struct BatchTune {
-  int lbm_rows;        // row segments of kLbmBlock nodes per CTA, unflagged lattice pass
+  int lbm_rows;        // groups of four bricks (kLbmBlock nodes) per CTA, unflagged lattice pass
   int list_per_sm;     // CTAs per SM (shared by the batch) of the near-region list and moments passes
   int marker_threads;  // threads per CTA of the spreading, fibrin and interpolation passes
 };

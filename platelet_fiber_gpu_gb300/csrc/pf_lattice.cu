@@ -296,8 +296,8 @@ __device__ __forceinline__ void zero_bins(int* bin_count, int ncells, Control* c
   if (tid == 0) ctl->occupied = 0;
 }
 
-// Direct-gather step over the lattice, one x-row segment of kLbmBlock nodes
-// per CTA, one force brick per warp.  mode:
+// Direct-gather step over the lattice, one force brick (32 x-nodes of a row)
+// per warp, four consecutive bricks per CTA.  mode:
 //   kPassAll     every brick;
 //   kPassUnflag  bricks not flagged for this step's force (the flagged ones
 //                are left to lbm_list_k, after the spreading);
@@ -310,7 +310,7 @@ __device__ __forceinline__ void zero_bins(int* bin_count, int ncells, Control* c
 //                this step or the previous one).
 enum : int { kPassAll = 0, kPassUnflag = 1, kPassNear = 4, kPassFar = 3 };
 // bid / nblk: the CTA's index and the number of CTAs of this lattice's pass
-// (the launch is one-dimensional: x-row segments, then rows, then planes)
+// (the launch is one-dimensional over groups of four bricks in lattice order)
 template <class S, class R, bool FAST>
 __device__ __forceinline__ void lbm_step_body(const LatticeConst& k, S* gA, S* gB, R4<R>* FA, R4<R>* FB,
                                               R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
@@ -325,27 +325,27 @@ __device__ __forceinline__ void lbm_step_body(const LatticeConst& k, S* gA, S* g
   R4<R>* Fp = par ? FA : FB;
   unsigned* flp = par ? flA : flB;
   const unsigned* flc = par ? flB : flA;
-  const int gx = (k.nx + kLbmBlock - 1) / kLbmBlock;
-  const int yz = bid / gx;
-  const int x = (bid - yz * gx) * kLbmBlock + threadIdx.x, y = yz % k.ny, z = yz / k.ny;
-  const int bxw = x / kBrickX;
-  const bool row_ok = bxw < k.nbx;
-  const int brick = bxw + k.nbx * (y + k.ny * z);
+  // one brick (32 x-nodes of a row) per warp, bricks in lattice order: rows
+  // narrower than a CTA leave no warp idle
+  const int brick = bid * (kLbmBlock / kBrickX) + (int)(threadIdx.x >> 5);
   if (bin_count)
     zero_bins(bin_count, ncells, ctl, (size_t)bid * blockDim.x + threadIdx.x, (size_t)nblk * blockDim.x);
+  if (brick >= k.nbricks) return;  // whole warp
+  const int yz = brick / k.nbx;
+  const int x = (brick - yz * k.nbx) * kBrickX + (int)(threadIdx.x & 31), y = yz % k.ny, z = yz / k.ny;
   // whole warp: one brick
   if (mode == kPassNear || far) {
     const unsigned char* nr = par ? nearB : nearA;
-    const bool is_near = row_ok && nr[brick] != 0;
+    const bool is_near = nr[brick] != 0;
     if (is_near == far) return;
   }
   if (far) {
     if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 0u, 0u, ctl->far_first);
     return;
   }
-  const unsigned fc = row_ok ? flc[brick] : 0u;
+  const unsigned fc = flc[brick];
   if (mode != kPassAll && fc) return;
-  const unsigned fp = row_ok ? flp[brick] : 0u;
+  const unsigned fp = flp[brick];
   if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, fc, fp, ctl->first);
   __syncwarp();
   if ((threadIdx.x & 31) == 0 && fp) flp[brick] = 0;
@@ -780,8 +780,8 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_batch_k(const BatchDesc* d
   cta_copy(s_k, d.L.k);
   __syncthreads();
   const Lattice& L = d.L;
-  // `rows` row segments per CTA (amortizes the per-CTA set-up)
-  const int segs = ((s_k.nx + kLbmBlock - 1) / kLbmBlock) * s_k.ny * s_k.nz;
+  // `rows` groups of four bricks per CTA (amortizes the per-CTA set-up)
+  const int segs = (s_k.nbricks + kLbmBlock / kBrickX - 1) / (kLbmBlock / kBrickX);
   for (int r = (blockIdx.x - start[j]) * rows, e = min(segs, r + rows); r < e; ++r)
     lbm_step_body<S, R, FAST>(s_k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
                               L.flags[0], L.flags[1], nullptr, 0, 1, L.near[0], L.near[1], d.ctl, r, segs);
@@ -1081,7 +1081,7 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
                                      ctl);
     return cudaGetLastError();
   }
-  const unsigned grid = (unsigned)((L.k.nx + kLbmBlock - 1) / kLbmBlock) * L.k.ny * L.k.nz;
+  const unsigned grid = (unsigned)((L.k.nbricks + kLbmBlock / kBrickX - 1) / (kLbmBlock / kBrickX));
   auto kern = fast_lattice(L) ? lbm_step_k<S, R, true> : lbm_step_k<S, R, false>;
   kern<<<grid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
                                    L.flags[0], L.flags[1], bin_count, ncells, part, L.near[0], L.near[1], ctl);

@@ -2830,7 +2830,7 @@ int batch_ctas(const BatchDesc& d, int kind, int sms, int njobs, const BatchTune
       return lk.nz * ((lk.ny + R - 1) / R);
     }
     case BK_LBM_UNFLAGGED:
-      return (((lk.nx + kLbmBlock - 1) / kLbmBlock) * lk.ny * lk.nz + t.lbm_rows - 1) / t.lbm_rows;
+      return ((lk.nbricks + kLbmBlock / kBrickX - 1) / (kLbmBlock / kBrickX) + t.lbm_rows - 1) / t.lbm_rows;
     case BK_MEMBRANE: return PE ? pk.P : 0;
     case BK_BOUNDS: return PE && pk.morse ? pk.P : 0;
     case BK_MORSE: return PE && pk.morse ? pk.P * ((pk.E + 31) / 32) : 0;

@@ -1,6 +1,6 @@
 // pf_tune.cu -- autotuner of the fused batch step's block and tile shapes.
 //
-// A shape (BatchTune) has three axes: row segments per CTA of the unflagged
+// A shape (BatchTune) has three axes: groups of four bricks per CTA of the unflagged
 // lattice pass, CTAs per SM of the near-region list and moments passes, and
 // threads per CTA of the marker passes.  The search is coordinate descent:
 // starting from the default shape, every value of one axis is measured with
