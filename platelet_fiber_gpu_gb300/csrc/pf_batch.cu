@@ -348,11 +348,13 @@ int fused_steps(pfgpu_batch* b, int nsteps) {
       continue;
     }
     const size_t ev = trials.size() * (kTrialSteps + 1);
-    while (b->tev.size() < ev + kTrialSteps + 1) {
+    while (!rc && b->tev.size() < ev + kTrialSteps + 1) {
       cudaEvent_t e = nullptr;
-      BK_CK(cudaEventCreate(&e));
-      b->tev.push_back(e);
+      const cudaError_t ce = cudaEventCreate(&e);
+      if (ce != cudaSuccess) rc = report_error(PFGPU_ERR_CUDA, cudaGetErrorString(ce));
+      else b->tev.push_back(e);
     }
+    if (rc) break;
     cudaGraphExec_t g = nullptr;
     rc = fused_graph(f, s, &g);
     if (rc) break;
