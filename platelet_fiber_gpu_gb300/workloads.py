@@ -19,6 +19,8 @@ Lengths are in microns with the reference's lattice spacing dx = 0.2 um
 """
 from __future__ import annotations
 
+from pathlib import Path
+
 import numpy as np
 
 from . import mesh as M
@@ -246,6 +248,61 @@ def single_large(seed: int = 2, nx=256, ny=128, nz=128, n_platelets=50, n_membra
     _fibrin(sc, n_fib, n_links, 3 * REF_DX, rng, 0.5)
     sc.seed = seed
     sc.meta.update(workload="single_large", shear=shear)
+    return sc
+
+
+def from_reference_inputs(parameter_file, nx: int, ny: int, nz: int, neu_path=None, centers=None,
+                          n_fib: int = 0, n_links: int = 0, n_wall: int = 0) -> Scene:
+    """A scene from the reference driver's own inputs: `Input/parameter.dat`
+    (read by libpfgpu's ParReader restatement) and the NEU surface mesh it
+    names (NEUReader restatement).  The file sets dx, dt, the shear rate, the
+    initial density, the spring constant, Kr0, the receptor total and the seed
+    of the parameter table (gpuSEM_LB.c:1206-1233), the cell count
+    (MAX_CELL) and the elements per cell (MAX_ELEM: the mesh's vertices, then
+    cytoplasm).  Cell positions come from `centers` (um, shape [MAX_CELL][3])
+    or a seeded Poisson-disk placement above the bottom wall; the reference
+    reads them from its PDB file, which this builder does not parse.
+    `neu_path` defaults to the file's NEU_PATH, relative to the directory
+    holding Input/."""
+    from .gpu import read_neu, read_parameter_file
+    par = Path(parameter_file)
+    p = read_parameter_file(par)
+    neu = Path(neu_path) if neu_path is not None else Path(p["neu_path"])
+    if not neu.is_absolute() and not neu.exists():
+        neu = par.resolve().parent.parent / neu
+    hp = p["host_param"]
+    seed = int(hp[1])
+    n_cells = int(p["max_cell"])
+    m = read_neu(neu)
+    verts = np.stack([m["X"], m["Y"], m["Z"]], 1)
+    n_cyto = max(0, int(p["max_elem"]) - len(verts))
+    axes = tuple(float(a) for a in 0.5 * (verts.max(0) - verts.min(0)))
+    tpl = PlateletTemplate(verts, m["tri"], n_cyto, seed, axes)
+    dx, dt = float(p["dx"]), float(p["dt"])
+    params = reference_params(dx=dx, dt=dt, nz=nz, shear=float(hp[5]), rho0=float(hp[6]), k_spring=float(hp[2]),
+                              kr0=float(hp[4]), receptors=float(hp[0]), seed=float(hp[1]),
+                              mean_bond=tpl.mean_bond)
+    sc = Scene(nx=nx, ny=ny, nz=nz, dx=dx, dt=dt, params=params,
+               bc=(BC_PERIODIC, BC_PERIODIC, BC_ZOUHE_SHEAR), ibm_wrap=(1, 1, 0))
+    rng = np.random.default_rng(seed)
+    L = np.array([nx, ny, nz]) * dx
+    if centers is None:
+        rmin = 2 * max(axes[0], axes[1]) + 2 * dx
+        centers = poisson_disk(n_cells, (axes[0], axes[1], axes[2] + 0.05),
+                               (L[0] - axes[0], L[1] - axes[1], L[2] - axes[2] - 0.6), rmin, rng,
+                               fixed_z=axes[2] + 0.05, n_fixed=min(n_wall, n_cells))
+    centers = np.asarray(centers, dtype=np.float64).reshape(-1, 3)
+    if len(centers) != n_cells:
+        raise ValueError(f"{len(centers)} centers for MAX_CELL = {n_cells}")
+    _place(sc, tpl, centers, L[1])
+    n_rec = int(round(float(hp[0]))) // max(1, n_cells)
+    _receptors_random(sc, n_rec, rng)
+    sc.params[P_NUMRECEPTORS] = n_rec * n_cells
+    sc.morse = 1
+    if n_fib:
+        _fibrin(sc, n_fib, n_links, 3 * dx, rng, 0.5)
+    sc.seed = seed
+    sc.meta.update(workload="reference_inputs", parameter_file=str(par), neu=str(neu))
     return sc
 
 

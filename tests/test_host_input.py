@@ -111,3 +111,40 @@ def test_template_from_neu(gpu, tmp_path):
     np.testing.assert_array_equal(a.tris[:, :3], b.tris[:, :3])
     np.testing.assert_array_equal(a.sp_L0, b.sp_L0)
     assert a.mean_bond == b.mean_bond
+
+
+def test_scene_from_reference_inputs(gpu, tmp_path):
+    """A scene built from a parameter file and the NEU mesh it names carries
+    the file's dx, dt, shear, density, spring constant, Kr0, receptor total
+    and seed, MAX_CELL platelets of MAX_ELEM elements (mesh vertices first,
+    then cytoplasm), and passes the library's scene checks."""
+    from platelet_fiber_gpu_gb300 import mesh as M, workloads as W
+    from platelet_fiber_gpu_gb300.scene import P_KR0, P_KSPRING, P_NUMRECEPTORS, P_RHO0, P_SEED, P_SHEAR
+    v, t = M.ellipsoid_icosphere(2, (1.0, 1.0, 0.5))
+    (tmp_path / "Input").mkdir()
+    write_neu(tmp_path / "Input" / "platelet.neu", v, t, np.random.default_rng(1))
+    keys = dict(KEYS)
+    keys.update(MAX_CELL="3", MAX_ELEM=str(len(v) + 40), SURF_ELEM=str(len(t)), RECEPTOR="120")
+    par = tmp_path / "Input" / "parameter.dat"
+    par.write_text("".join(f"{k} {keys[k]}\n" for k, _ in KEYS))
+    sc = W.from_reference_inputs(par, 64, 48, 32)
+    assert (sc.n_platelets, sc.n_elem, sc.n_membrane) == (3, len(v) + 40, len(v))
+    assert sc.dx == np.float32(0.2) or abs(sc.dx - 0.2) < 1e-7
+    p = sc.params
+    assert p[P_SHEAR] == 1000 and p[P_RHO0] == np.float32(1.0239) and p[P_KSPRING] == np.float32(0.05)
+    assert p[P_KR0] == np.float32(3.21) and p[P_SEED] == 1101
+    assert p[P_NUMRECEPTORS] == 120 and sc.n_rec == 40
+    # membrane vertices of the first platelet are the mesh, shifted to its centre
+    X = np.asarray(sc.X).reshape(3, -1)
+    np.testing.assert_allclose(X[0, :len(v)] - X[0, :len(v)].mean(), v[:, 0] - v[:, 0].mean(), atol=1e-12)
+    assert gpu.scene_device_bytes(sc, 1) > 0
+    # the library's scene validation runs on the host before any CUDA call:
+    # without a GPU a valid scene fails only there (PFGPU_ERR_CUDA)
+    import ctypes as C
+    L = gpu.lib()
+    c = sc.to_c()
+    h = C.c_void_p()
+    rc = L.pfgpu_job_create(C.byref(c), 1, 0.0, C.byref(h))
+    assert rc in (0, 2), L.pfgpu_last_error()
+    if rc == 0:
+        L.pfgpu_job_destroy(h)
