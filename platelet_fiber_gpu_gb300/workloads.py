@@ -259,11 +259,12 @@ def from_reference_inputs(parameter_file, nx: int, ny: int, nz: int, neu_path=No
     initial density, the spring constant, Kr0, the receptor total and the seed
     of the parameter table (gpuSEM_LB.c:1206-1233), the cell count
     (MAX_CELL) and the elements per cell (MAX_ELEM: the mesh's vertices, then
-    cytoplasm).  Cell positions come from `centers` (um, shape [MAX_CELL][3])
-    or a seeded Poisson-disk placement above the bottom wall; the reference
-    reads them from its PDB file, which this builder does not parse.
-    `neu_path` defaults to the file's NEU_PATH, relative to the directory
-    holding Input/."""
+    cytoplasm).  Cell positions: `centers` (um, shape [MAX_CELL][3], added to
+    the mesh coordinates), else for one cell the driver's own offset of the
+    mesh, (8.0, 1.5, 0.32) um (gpuSEM_LB.c:811-820; its PDB and PSF readers
+    are commented out at :810, :1060), else a seeded Poisson-disk placement
+    above the bottom wall.  `neu_path` defaults to the file's NEU_PATH,
+    relative to the directory holding Input/."""
     from .gpu import read_neu, read_parameter_file
     par = Path(parameter_file)
     p = read_parameter_file(par)
@@ -286,6 +287,8 @@ def from_reference_inputs(parameter_file, nx: int, ny: int, nz: int, neu_path=No
                bc=(BC_PERIODIC, BC_PERIODIC, BC_ZOUHE_SHEAR), ibm_wrap=(1, 1, 0))
     rng = np.random.default_rng(seed)
     L = np.array([nx, ny, nz]) * dx
+    if centers is None and n_cells == 1:
+        centers = [(8.0, 1.5, 0.32)]
     if centers is None:
         rmin = 2 * max(axes[0], axes[1]) + 2 * dx
         centers = poisson_disk(n_cells, (axes[0], axes[1], axes[2] + 0.05),

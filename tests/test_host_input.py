@@ -148,3 +148,22 @@ def test_scene_from_reference_inputs(gpu, tmp_path):
     assert rc in (0, 2), L.pfgpu_last_error()
     if rc == 0:
         L.pfgpu_job_destroy(h)
+
+
+def test_single_cell_gets_the_drivers_offset(gpu, tmp_path):
+    """One cell: the mesh shifted by the reference driver's (8.0, 1.5, 0.32)
+    um (gpuSEM_LB.c:811-820), RY equal to Y."""
+    from platelet_fiber_gpu_gb300 import mesh as M, workloads as W
+    v, t = M.ellipsoid_icosphere(1, (1.0, 1.0, 0.5))
+    (tmp_path / "Input").mkdir()
+    write_neu(tmp_path / "Input" / "platelet.neu", v, t, np.random.default_rng(2))
+    keys = dict(KEYS)
+    keys.update(MAX_CELL="1", MAX_ELEM=str(len(v)), RECEPTOR="30")
+    par = tmp_path / "Input" / "parameter.dat"
+    par.write_text("".join(f"{k} {keys[k]}\n" for k, _ in KEYS))
+    sc = W.from_reference_inputs(par, 96, 48, 32)
+    X, Y, Z = (np.asarray(a).reshape(-1) for a in (sc.X, sc.Y, sc.Z))
+    np.testing.assert_allclose(X, v[:, 0] + 8.0, atol=1e-12)
+    np.testing.assert_allclose(Y, v[:, 1] + 1.5, atol=1e-12)
+    np.testing.assert_allclose(Z, v[:, 2] + 0.32, atol=1e-12)
+    np.testing.assert_array_equal(np.asarray(sc.RY).reshape(-1), Y)
