@@ -176,3 +176,19 @@ void tune_record(const std::string& key, const BatchTune& t, float ns_per_node) 
 }
 
 }  // namespace pf
+
+// Host hooks for testing the search without a GPU (not part of pfgpu.h):
+// the next shape to measure for a class (returns 0 once the search is done,
+// shape = the best), and recording a measurement.
+extern "C" int pfgpu_tune_next_(const char* key, int shape[3]) {
+  pf::BatchTune t{};
+  const bool more = pf::tune_next(key, {}, &t);
+  if (!more) pf::tune_best(key, &t);
+  shape[0] = t.lbm_rows;
+  shape[1] = t.list_per_sm;
+  shape[2] = t.marker_threads;
+  return more ? 1 : 0;
+}
+extern "C" void pfgpu_tune_record_(const char* key, const int shape[3], float ns_per_node) {
+  pf::tune_record(key, pf::BatchTune{shape[0], shape[1], shape[2]}, ns_per_node);
+}
