@@ -56,12 +56,16 @@ def run_batched(precision: int, n_jobs: int = 64, steps: int = 1000, seed: int =
 
 
 def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed: int = 4, budget: float = 150e9,
-               chunk: int = 50, steps_range=(500, 5000), pool: int = 32) -> dict:
+               chunk: int = 50, steps_range=(500, 5000), pool: int = 32, batch_factory=Batch,
+               scenes=None) -> dict:
     """Poisson arrivals at `rate` per second for `duration` seconds; each job
     is one of `pool` pre-built scenes of the many-job workload with its own
-    requested step count drawn from `steps_range`."""
+    requested step count drawn from `steps_range`.  `batch_factory` and
+    `scenes` replace the GPU batch and the scene pool (host-logic tests)."""
     rng = np.random.default_rng(seed)
-    scenes = [W.batch_job(seed, i) for i in range(pool)]
+    if scenes is None:
+        scenes = [W.batch_job(seed, i) for i in range(pool)]
+    pool = len(scenes)
     arrivals = []
     t = 0.0
     while True:
@@ -69,7 +73,7 @@ def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed:
         if t > duration:
             break
         arrivals.append((t, int(rng.integers(pool)), int(rng.integers(steps_range[0], steps_range[1] + 1))))
-    b = Batch(int(budget))
+    b = batch_factory(int(budget))
     live = {}  # slot -> [arrival, steps left, nodes, requested]
     waiting = []
     latencies = []
@@ -122,7 +126,7 @@ def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed:
             "duration_s": duration, "makespan_s": round(span, 3), "mlups": round(work / span / 1e6, 1),
             "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
             "latency_p99_s": round(float(np.percentile(lat, 99)), 4), "scene_pool": pool,
-            "host_s": {k: round(v, 3) for k, v in host.items()}, "step_calls": calls,
+            "node_steps": int(work), "host_s": {k: round(v, 3) for k, v in host.items()}, "step_calls": calls,
             "mean_live_jobs": round(live_sum / max(1, calls), 1)}
 
 
