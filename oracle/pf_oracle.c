@@ -5,8 +5,9 @@
  * fibrin spring forces and half-way bounce-back walls that the benchmark
  * workloads add.
  *
- * ORACLE / TEST INFRASTRUCTURE ONLY: it is the checker of the CUDA path and
- * the timed CPU baseline.  The product library never links it.
+ * ORACLE / TEST INFRASTRUCTURE ONLY: the tests compare the CUDA path with
+ * it, and the benchmark times it as the CPU baseline.  The product library
+ * never links it.
  *
  * The step follows the reference's launch order (gpuSEM_LB.c:1441-1442 calls
  * sem_invokeGPUKernel_Force, semLB.cu:441-531, then fluid_invokeGPUKernel,

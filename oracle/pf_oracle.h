@@ -1,9 +1,9 @@
 /*
  * pf_oracle.h -- CPU FP64 restatement of the reference's coupled step.
  *
- * ORACLE / TEST INFRASTRUCTURE ONLY.  Tests, the smoke check and the
- * benchmark's CPU-baseline leg call it as the checker and as the timed CPU
- * baseline; the product never links it.
+ * ORACLE / TEST INFRASTRUCTURE ONLY.  Tests and the smoke check compare the
+ * CUDA path with it, the benchmark's CPU-baseline leg times it; the product
+ * never links it.
  */
 #ifndef PF_ORACLE_H
 #define PF_ORACLE_H
