@@ -195,7 +195,7 @@ def run_reference(args, rank):
         "unit": "MLUPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / n * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(args), "timed_steps": n},
+        "config": dict(bench_config(args, scene, args.precision, args.gpus), timed_steps=n),
         "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": f"{n} coupled steps of the full scene after 1 warm-up step (budget "
                                    f"{total_budget:.0f} s); CPU restatement of the reference kernels, FP64, "
@@ -204,6 +204,14 @@ def run_reference(args, rank):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def bench_config(args, scene, prec, world):
+    """The config object of both arms' lines (same keys, same workload)."""
+    return {"workload": workload_name(args), "lattice": [scene.nx, scene.ny, scene.nz], "nodes": scene.n_nodes,
+            "elements": scene.n_platelets * scene.n_elem, "fibrin_nodes": scene.n_fib,
+            "receptors": scene.n_platelets * scene.n_rec, "parallelism": f"replicas x{world}",
+            "l2": "working set > L2 (2 x 19 x N x 4 B populations)", "precision": PREC_NAME[prec]}
 
 
 def workload_name(args):
@@ -281,10 +289,15 @@ def main():
         stream = torch.cuda.current_stream()
         start.record(stream)
         t0 = time.perf_counter()
-        job.step(args.steps, graph=True)  # synchronises the job's stream before returning
+        rc_timed = job.step(args.steps, graph=True)  # synchronises the job's stream before returning
         stop.record(stream)
         barrier_sync()
         wall = time.perf_counter() - t0
+    # every timed step ran: no stop, detachment or device error bit (step()
+    # raises on error bits and returns PFGPU_DONE once the job stopped)
+    if rc_timed != gpu.PFGPU_OK or job.steps != args.warmup + args.steps:
+        raise RuntimeError(f"timed region incomplete: status {rc_timed}, {job.steps} steps of "
+                           f"{args.warmup + args.steps}")
     # the job runs on its own stream and step() returns after it finished, so
     # the host wall time and the event pair bracket the same work
     dev_ms = start.elapsed_time(stop)
@@ -298,28 +311,45 @@ def main():
     job.close()
 
     # ---- end to end through the C ABI from host buffers
-    import ctypes
-    # the caller's host buffers: the initial populations as a drop-in caller
-    # holds them (the equilibrium of the channel flow, made before timing)
+    # the caller's host buffers, in pinned memory as a driver holding its
+    # arrays for the whole run keeps them: the initial populations (the
+    # equilibrium of the channel flow, made before timing) and the arrays the
+    # lattice and element state are read back into
     scene.f_init = None
     j0 = gpu.Job(scene, prec, fp16_scale)
-    scene.f_init = np.ascontiguousarray(j0.lattice(fIN=True)["fIN"])
+    f_host = gpu.pinned((19, N))
+    f_host[:] = j0.lattice(fIN=True)["fIN"]
     j0.close()
+    scene.f_init = f_host
+    lat_out = {"fIN": gpu.pinned((19, N)), "rho": gpu.pinned(N), "u": gpu.pinned((3, N)), "F": gpu.pinned((3, N))}
+    el_out = {"X": gpu.pinned(PE), "Y": gpu.pinned(PE), "RY": gpu.pinned(PE), "Z": gpu.pinned(PE),
+              "V": gpu.pinned((3, PE)), "F": gpu.pinned((3, PE))}
+    for a in (*lat_out.values(), *el_out.values()):
+        a.fill(0.0)
     # every host array the scene hands to pfgpu_job_create, and what
     # pfgpu_job_get_lattice (fIN, rho, u, F) and _get_elements (X, Y, RY, Z,
     # V, F) return
     from platelet_fiber_gpu_gb300.scene import _ARRAY_FIELDS
     h2d_bytes = sum(np.asarray(getattr(scene, f)).nbytes for f in _ARRAY_FIELDS if getattr(scene, f) is not None)
-    d2h_bytes = (19 * N + N + 3 * N + 3 * N) * 8 + (4 * PE + 3 * PE + 3 * PE) * 8
+    d2h_bytes = sum(a.nbytes for a in (*lat_out.values(), *el_out.values()))
     barrier_sync()
     t0 = time.perf_counter()
     j2 = gpu.Job(scene, prec, fp16_scale)
-    j2.step(args.steps, graph=True)
-    L = j2.lattice(fIN=True)
-    E = j2.elements()
+    t1 = time.perf_counter()
+    j2.step(0, graph=True)  # captures and instantiates the step graph
+    t2 = time.perf_counter()
+    rc_e2e = j2.step(args.steps, graph=True)
+    t3 = time.perf_counter()
+    j2.lattice(out=lat_out)
+    j2.elements(out=el_out)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    t4 = time.perf_counter()
+    e2e_s = t4 - t0
+    if rc_e2e != gpu.PFGPU_OK or j2.steps != args.steps:
+        raise RuntimeError(f"end-to-end run incomplete: status {rc_e2e}, {j2.steps} of {args.steps} steps")
     j2.close()
+    e2e_breakdown = {"create_upload": round((t1 - t0) * 1e3, 3), "graph_capture": round((t2 - t1) * 1e3, 3),
+                     "steps": round((t3 - t2) * 1e3, 3), "download": round((t4 - t3) * 1e3, 3)}
     e2e_s = max_over_ranks(e2e_s)
     e2e_value = replica_value(world, N * args.steps, e2e_s)
 
@@ -344,15 +374,13 @@ def main():
         "vs_baseline": None,
         "dtype": PREC_NAME[prec],
         "data": "synthetic",
-        "config": {"workload": workload_name(args), "lattice": [scene.nx, scene.ny, scene.nz], "nodes": N,
-                   "elements": PE, "fibrin_nodes": scene.n_fib, "receptors": scene.n_platelets * scene.n_rec,
-                   "parallelism": f"replicas x{world}", "l2": "working set > L2 (2 x 19 x N x 4 B populations)",
-                   "precision": PREC_NAME[prec]},
+        "config": bench_config(args, scene, prec, world),
         "sem_elem_steps_per_s": round(world * PE / t_step, 1),
         "e2e": {"value": round(e2e_value, 1), "unit": "MLUPS",
                 "h2d_bytes_per_step": int(h2d_bytes / args.steps), "d2h_bytes_per_step": int(d2h_bytes / args.steps),
-                "seconds": round(e2e_s, 4),
-                "what": "pfgpu_job_create from host arrays + K graph steps + pfgpu_job_get_lattice/elements"},
+                "seconds": round(e2e_s, 4), "breakdown_ms": e2e_breakdown,
+                "what": "pfgpu_job_create from pinned host arrays (read in place by the device) + step graph "
+                        "capture + K graph steps + pfgpu_job_get_lattice/elements into pinned host arrays"},
         "roofline": {"bound": "hbm", "kernel": lbm_kernel, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "bytes_per_node": bpn, "launch_ms": round(lbm_ms, 5),

@@ -305,6 +305,15 @@ void pfgpu_batch_destroy(pfgpu_batch *b);
  *   host threads, race on it.  Serialise them.
  * - Nothing needs to start at zero: each call zeroes the scratch's control
  *   word on `stream` and writes every other scratch word before reading it.
+ * - The topology is checked on the device, where the call cannot wait for
+ *   it: a triangle index outside the nodes, node_ntri outside 0..10 or
+ *   unequal to the node's count in tri, a ring or spring entry out of range
+ *   leaves F_out, S_V_out and km_out unwritten, and
+ *   pfgpu_membrane_noalloc_status(stream) then returns PFGPU_ERR_INVALID.
+ *   Call it after the pass when the inputs are not known to be consistent.
+ * - The cached address belongs to the device's primary context: after a
+ *   cudaDeviceReset on that device it is stale, so make no further call on
+ *   that device in the process.
  * Inputs use the pf_scene layouts (device pointers); F_out is [3][P*n_elem]
  * in units of F0, double for PF_PREC_FP64 and float otherwise; S_V_out
  * ([P][2]: area, volume) and km_out ([P][n_membrane]: mean curvature, the
@@ -331,9 +340,21 @@ typedef struct {
 } pf_membrane_args;
 int pfgpu_membrane_forces_noalloc(const pf_membrane_args *args, void *stream);
 size_t pfgpu_membrane_noalloc_scratch_bytes(void);
+/* Waits for `stream` and reports the last pass on the current device:
+ * PFGPU_OK, or PFGPU_ERR_INVALID for rejected inputs (F_out unwritten) or a
+ * platelet too large for the pass.  Allocates nothing. */
+int pfgpu_membrane_noalloc_status(void *stream);
 
 const char *pfgpu_last_error(void);
 int pfgpu_version(void);
+/* Pinned, device-mapped host memory for a caller's arrays (no counterpart in
+ * the reference, whose driver malloc's its host arrays).  Job creation and
+ * the lattice download read and write caller arrays where they lie whenever
+ * the device can reach them -- pinned memory like this, or any host memory
+ * on machines whose GPU walks the host page tables (Grace, NVLink-C2C) --
+ * instead of staging them through device copies.  NULL on failure. */
+void *pfgpu_host_alloc(size_t bytes);
+void pfgpu_host_free(void *p);
 /* Philox-4x32-10 uniforms of the receptor stream (step, receptor) -> (u1, u2),
  * the same values the device draws; for tests and drivers. */
 void pfgpu_receptor_uniforms(uint64_t seed, int64_t step, int64_t receptor, double out[2]);

@@ -33,10 +33,17 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
+def reference_dir() -> Path:
+    """Where the reference's source tree is looked for: $PF_REFERENCE_DIR,
+    else a `reference` directory beside this checkout."""
+    env = os.environ.get("PF_REFERENCE_DIR")
+    return Path(env) if env else ROOT.parent / "reference"
+
+
 def build_refemu() -> Path | None:
     """Builds oracle/_ref/librefemu.so from the reference tree when present."""
     script = HERE / "refemu" / "build_refemu.sh"
-    subprocess.run(["sh", str(script)], check=True)
+    subprocess.run(["sh", str(script)], check=True, env=dict(os.environ, REF_DIR=str(reference_dir())))
     return REFEMU_LIB if REFEMU_LIB.exists() else None
 
 

@@ -3,10 +3,11 @@
 # (LB_kernel.cu, which includes sem_kernel.cu) compiled with g++ through the
 # serial CUDA emulation header, plus the step-loop harness refemu.cpp.
 # Oracle test infrastructure: it reads the reference tree, so it only builds
-# where that tree is present (REF_DIR, default /root/reference).
+# where that tree is present (REF_DIR, default: a `reference` directory
+# beside the repository checkout).
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF_DIR=${REF_DIR:-/root/reference}
+REF_DIR=${REF_DIR:-$HERE/../../../reference}
 OUT="$HERE/../_ref"
 if [ ! -f "$REF_DIR/LB_kernel.cu" ]; then
   echo "reference tree not found at $REF_DIR; skipping refemu build" >&2

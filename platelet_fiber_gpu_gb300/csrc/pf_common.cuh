@@ -46,6 +46,7 @@ enum : uint32_t {
   ERR_MEMBRANE_SIZE = 8u,
   ERR_WAIT_TIMEOUT = 16u,  // a bounded wait on an mbarrier gave up
   ERR_FAR_FLAGGED = 32u,   // a force brick lay in the far region (a marker moved over a node)
+  ERR_INPUT = 64u,         // caller-given device arrays inconsistent (membrane pass without allocation)
 };
 
 // Per-job device-resident control block: written by kernels, read by the host

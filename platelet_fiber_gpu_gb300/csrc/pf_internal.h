@@ -201,8 +201,18 @@ bool fast_gather(const Lattice& L);
 
 // ------------------------------------------------------------------ launchers
 // All launchers enqueue on `st` and return the launch error.
-cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_dev, const double* ru_dev,
-                           Control* ctl, cudaStream_t st);
+// The initial state of a job: the caller's populations f [19][N] (with
+// rho/u [N], [3][N] or their moments), or, with f NULL, the equilibrium of
+// rest / u [3][N] / rho [N] / the Zou/He shear profile; F [3][N] the initial
+// force.  Every pointer may be NULL where optional and must be readable by
+// the device (device memory, pinned or device-accessible host memory).
+struct InitSource {
+  const double *f, *F, *rho, *u;
+  int zh;                  // Zou/He shear walls on z
+  double C, Fo, dt, uw;    // moments of f: lattice speed, force factor, dt, top wall velocity
+  double shear, dx, umax, C0, C02;  // equilibrium of the shear profile
+};
+cudaError_t lattice_init(Lattice& L, const InitSource& src, cudaStream_t st);
 // picks the row-staged or the direct-gather step kernel (host only; call
 // before the first step and outside stream capture)
 cudaError_t lattice_configure(Lattice& L);
@@ -218,15 +228,6 @@ cudaError_t lattice_near(Lattice& L, Control* ctl, int from_mark, cudaStream_t s
 // far pass counter: sync (far_step = step) or advance after a far pass
 cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st);
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
-// initial equilibrium fIN [19][N] and ru [4][N] (device) of a scene given no
-// populations (u_init / rho_init: optional device arrays)
-cudaError_t lattice_equilibrium(int nx, int ny, int nz, int zh, double shear, double dx, double umax, double C0,
-                                const double* u_init, const double* rho_init, double* f, double* ru,
-                                cudaStream_t st);
-// (rho, u) ru [4][N] of given initial populations f [19][N] (device; F: the
-// initial force [3][N] or NULL)
-cudaError_t lattice_initial_moments(int nx, int ny, int nz, int zh, double C, double Fo, double dt, double uw,
-                                    const double* f, const double* F, double* ru, cudaStream_t st);
 // density and velocity at every stride-th node (float [mz][my][mx] planes)
 cudaError_t lattice_fields(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
                            cudaStream_t st);

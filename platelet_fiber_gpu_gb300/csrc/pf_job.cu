@@ -104,6 +104,31 @@ static void destroy(pfgpu_job* j) {
   delete j;
 }
 
+// An address the device can read or write for caller memory: device and
+// managed memory as given, pinned host memory through its mapping, and
+// pageable host memory as given where the GPU walks the host's page tables
+// (ATS over NVLink-C2C on Grace machines).  NULL otherwise, or when
+// PFGPU_HOST_DIRECT=0: the data then goes through a device staging copy.
+static void* device_view(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void*>(p);
+  const char* env = getenv("PFGPU_HOST_DIRECT");
+  if (env && strcmp(env, "0") == 0) return nullptr;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  int dev = 0, pageable = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return pageable ? const_cast<void*>(p) : nullptr;
+}
+
 static size_t store_bytes(int precision) {
   return precision == PF_PREC_FP64 ? 8 : (precision == PF_PREC_FP32 ? 4 : 2);
 }
@@ -563,7 +588,24 @@ size_t pfgpu_scene_device_bytes(const pf_scene* s, int precision) {
     b += nc * (kBinCap * 16 + 4);
   }
   b += (size_t)s->n_fib * 14 * 8;
-  b += 19 * N * 8 + 4 * N * 8 + 3 * N * 8;  // transient upload staging
+  // topology tables (shared by the platelets), fibrin link lists, and the
+  // small per-job buffers (control block, counters, bounds)
+  if (s->n_platelets > 0 && s->n_elem > 0) {
+    const size_t nsp = s->spring_ptr ? (size_t)s->spring_ptr[s->n_elem] : 0;
+    b += (size_t)s->n_tri * 6 * 4 + (size_t)s->n_node * (4 + 40) + (size_t)s->n_membrane * 80 +
+         ((size_t)s->n_elem + 1) * 4 + nsp * 12 + (size_t)s->n_platelets * ((size_t)s->n_tri * 8 + 64);
+  }
+  if (s->n_fib > 0) b += ((size_t)s->n_fib + 1) * 8 + (size_t)s->fib_ptr[s->n_fib] * 12;
+  b += 64 * 1024;
+  // transient staging of the caller's FP64 arrays, where the device cannot
+  // read pageable host memory itself
+  int dev = 0, pageable = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+    cudaGetLastError();
+    pageable = 0;
+  }
+  if (!pageable) b += 19 * N * 8 + 4 * N * 8 + 3 * N * 8;
   return b;
 }
 
@@ -634,62 +676,58 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(dalloc(j, &j->done_blocks, 1));
   CKJ(dalloc(j, &j->scratch4, 4));
   {
-    // initial populations: the scene's own (uploaded), else the equilibrium
-    // of the initial flow computed on the device
-    double *df = nullptr, *dF = nullptr, *dru = nullptr, *dui = nullptr, *dri = nullptr;
-    cudaError_t e = cudaMalloc(&df, 19 * N * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&dru, 4 * N * sizeof(double));
-    if (e == cudaSuccess && s->F_init) {
-      e = cudaMalloc(&dF, 3 * N * sizeof(double));
-      if (e == cudaSuccess) e = cudaMemcpy(dF, s->F_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
-    }
+    // initial populations: the scene's own, else the equilibrium of the
+    // initial flow, built on the device in one pass that reads the caller's
+    // arrays where they lie (no FP64 staging copy where the device can read
+    // them: device, pinned or ATS-visible host memory)
     const float* mp = s->params;
-    const int zh = s->bc[2] == PF_BC_ZOUHE_SHEAR;
+    InitSource src{};
+    src.zh = s->bc[2] == PF_BC_ZOUHE_SHEAR;
+    std::vector<void*> staged;
+    cudaError_t e = cudaSuccess;
+    auto view = [&](const double* h, size_t count) -> const double* {
+      if (!h || e != cudaSuccess) return nullptr;
+      if (const void* v = device_view(h)) return static_cast<const double*>(v);
+      void* d = nullptr;
+      e = cudaMalloc(&d, count * sizeof(double));
+      if (e != cudaSuccess) return nullptr;
+      staged.push_back(d);
+      e = cudaMemcpyAsync(d, h, count * sizeof(double), cudaMemcpyHostToDevice, j->s0);
+      return static_cast<const double*>(d);
+    };
+    src.F = view(s->F_init, 3 * N);
     if (s->f_init) {
-      // the scene's populations; (rho, u) from rho_init / u_init, else their
-      // moments (fluid_initGPUKernel, semLB.cu:154-233)
-      if (e == cudaSuccess) e = cudaMemcpy(df, s->f_init, 19 * N * sizeof(double), cudaMemcpyHostToDevice);
+      src.f = view(s->f_init, 19 * N);
       if (s->rho_init && s->u_init) {
-        if (e == cudaSuccess) e = cudaMemcpy(dru, s->rho_init, N * sizeof(double), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(dru + N, s->u_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
-      } else {
-        float c = s->dx / s->dt;
-        c = c / mp[PF_P_UMAX];
-        float fq = mp[PF_P_F0] / mp[PF_P_RHO0];
-        fq = fq / mp[PF_P_UMAX];
-        fq = fq * mp[PF_P_UNIT];
-        float uwf = mp[PF_P_SHEAR] * (float)(s->nz - 1);
-        uwf = uwf * s->dx;
-        uwf = uwf / mp[PF_P_UMAX];
-        if (e == cudaSuccess)
-          e = lattice_initial_moments(s->nx, s->ny, s->nz, zh, (double)c, (double)fq, (double)s->dt, (double)uwf, df,
-                                      dF, dru, j->s0);
+        src.rho = view(s->rho_init, N);
+        src.u = view(s->u_init, 3 * N);
       }
+      float c = s->dx / s->dt;
+      c = c / mp[PF_P_UMAX];
+      float fq = mp[PF_P_F0] / mp[PF_P_RHO0];
+      fq = fq / mp[PF_P_UMAX];
+      fq = fq * mp[PF_P_UNIT];
+      float uwf = mp[PF_P_SHEAR] * (float)(s->nz - 1);
+      uwf = uwf * s->dx;
+      uwf = uwf / mp[PF_P_UMAX];
+      src.C = (double)c;
+      src.Fo = (double)fq;
+      src.dt = (double)s->dt;
+      src.uw = (double)uwf;
     } else {
-      // the equilibrium of the initial flow (gpuSEM_LB.c:1206-1258)
-      if (e == cudaSuccess && s->u_init) {
-        e = cudaMalloc(&dui, 3 * N * sizeof(double));
-        if (e == cudaSuccess) e = cudaMemcpy(dui, s->u_init, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
-      }
-      if (e == cudaSuccess && s->rho_init) {
-        e = cudaMalloc(&dri, N * sizeof(double));
-        if (e == cudaSuccess) e = cudaMemcpy(dri, s->rho_init, N * sizeof(double), cudaMemcpyHostToDevice);
-      }
-      const double shear = (double)mp[PF_P_SHEAR];
-      const double umax_d = shear > 0 ? shear * (s->nz - 1) * (double)s->dx : (double)mp[PF_P_UMAX];
+      src.u = view(s->u_init, 3 * N);
+      src.rho = view(s->rho_init, N);
+      src.shear = (double)mp[PF_P_SHEAR];
+      src.umax = src.shear > 0 ? src.shear * (s->nz - 1) * (double)s->dx : (double)mp[PF_P_UMAX];
+      src.dx = (double)s->dx;
       const float dxdt = s->dx / s->dt;
-      const double C0 = (double)dxdt / umax_d;
-      if (e == cudaSuccess)
-        e = lattice_equilibrium(s->nx, s->ny, s->nz, zh, shear, (double)s->dx, umax_d, C0, dui, dri, df, dru, j->s0);
+      src.C0 = (double)dxdt / src.umax;
+      src.C02 = src.C0 * src.C0;
     }
-    if (e == cudaSuccess) e = lattice_upload(L, df, dF, dru, j->ctl, j->s0);
+    if (e == cudaSuccess) e = lattice_init(L, src, j->s0);
     if (e == cudaSuccess) e = lattice_configure(L);
     if (e == cudaSuccess) e = cudaStreamSynchronize(j->s0);
-    cudaFree(df);
-    cudaFree(dF);
-    cudaFree(dru);
-    cudaFree(dui);
-    cudaFree(dri);
+    for (void* d : staged) cudaFree(d);
     CKJ(e);
   }
   Control c{};
@@ -814,21 +852,33 @@ int pfgpu_job_get_lattice(pfgpu_job* j, double* fIN, double* fOUT, double* rho, 
   const size_t N = (size_t)j->L.k.N;
   Control c;
   CK(cudaMemcpy(&c, j->ctl, sizeof c, cudaMemcpyDeviceToHost));
-  double *dfi = nullptr, *dfo = nullptr, *dr = nullptr, *du = nullptr, *dF = nullptr;
+  // the download kernel writes each array where it lies when the device can
+  // reach it (device, pinned or ATS-visible host memory), else into a device
+  // staging buffer copied back afterwards
+  struct Out {
+    double* host;
+    size_t count;
+    double* dev;
+    bool staged;
+  };
+  Out o[5] = {{fIN, 19 * N, nullptr, false}, {fOUT, 19 * N, nullptr, false}, {rho, N, nullptr, false},
+              {u, 3 * N, nullptr, false}, {F, 3 * N, nullptr, false}};
   cudaError_t e = cudaSuccess;
-  if (fIN) e = cudaMalloc(&dfi, 19 * N * sizeof(double));
-  if (e == cudaSuccess && fOUT) e = cudaMalloc(&dfo, 19 * N * sizeof(double));
-  if (e == cudaSuccess && rho) e = cudaMalloc(&dr, N * sizeof(double));
-  if (e == cudaSuccess && u) e = cudaMalloc(&du, 3 * N * sizeof(double));
-  if (e == cudaSuccess && F) e = cudaMalloc(&dF, 3 * N * sizeof(double));
-  if (e == cudaSuccess) e = lattice_download(j->L, j->ctl, c.step, dfi, dfo, dr, du, dF, j->s0);
+  for (auto& x : o) {
+    if (!x.host || e != cudaSuccess) continue;
+    x.dev = static_cast<double*>(device_view(x.host));
+    if (!x.dev) {
+      e = cudaMalloc(&x.dev, x.count * sizeof(double));
+      x.staged = e == cudaSuccess;
+    }
+  }
+  if (e == cudaSuccess) e = lattice_download(j->L, j->ctl, c.step, o[0].dev, o[1].dev, o[2].dev, o[3].dev, o[4].dev, j->s0);
+  for (auto& x : o)
+    if (e == cudaSuccess && x.staged)
+      e = cudaMemcpyAsync(x.host, x.dev, x.count * sizeof(double), cudaMemcpyDeviceToHost, j->s0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(j->s0);
-  if (e == cudaSuccess && fIN) e = cudaMemcpy(fIN, dfi, 19 * N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && fOUT) e = cudaMemcpy(fOUT, dfo, 19 * N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && rho) e = cudaMemcpy(rho, dr, N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && u) e = cudaMemcpy(u, du, 3 * N * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && F) e = cudaMemcpy(F, dF, 3 * N * sizeof(double), cudaMemcpyDeviceToHost);
-  cudaFree(dfi); cudaFree(dfo); cudaFree(dr); cudaFree(du); cudaFree(dF);
+  for (auto& x : o)
+    if (x.staged) cudaFree(x.dev);
   CK(e);
   return PFGPU_OK;
 }
@@ -951,6 +1001,20 @@ const char* pfgpu_last_error(void) {
   return g_last_error_global.c_str();
 }
 int pfgpu_version(void) { return 100; }
+
+void* pfgpu_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  const cudaError_t e = cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    set_error(e == cudaErrorMemoryAllocation ? PFGPU_ERR_NOMEM : PFGPU_ERR_CUDA,
+              std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    return nullptr;
+  }
+  return p;
+}
+void pfgpu_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
 
 void pfgpu_receptor_uniforms(uint64_t seed, int64_t step, int64_t receptor, double out[2]) {
   receptor_uniforms(seed, step, receptor, out[0], out[1]);

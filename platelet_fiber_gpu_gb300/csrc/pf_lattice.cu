@@ -874,29 +874,101 @@ __global__ void fields_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, const
   }
 }
 
-// f*_d(x) = fIN_d(x + c_d) so that the first pull reproduces fIN; through a
-// bounce-back face f*_d(x) = fIN_opp(d)(x).  Also loads the initial force of
-// the step before the first (flags its bricks) and (rho, u/C) for the first
-// collision.
+// The device lattice of a new job in one pass over the nodes, every source
+// word read once.  Node x takes its 19 initial populations f_d(x) -- the
+// caller's fIN [19][N] (any address the device reads: device memory, pinned
+// host memory, or pageable host memory where the GPU walks the host page
+// tables), else the equilibrium of the initial flow -- and pushes each to
+// the node that pulls it in the first step: g_d(x - c_d) = f_d(x) - w_d, so
+// that the first pull reproduces fIN; where x + c_d lies beyond a
+// bounce-back face, node x keeps g_d(x) = f_opp(d)(x) - w_d itself.  Every
+// (node, direction) is written once.  (rho, u/C) for the first collision:
+// the caller's rho_init / u_init, else the moments of f with the half-force
+// shift and the Zou/He walls (fluid_initGPUKernel, semLB.cu:154-233), else
+// the equilibrium's own.  The initial force loads into the step-before
+// buffer and flags its bricks.  FP64 operations and their order are those of
+// the host restatements (round-to-nearest intrinsics, no contraction), so
+// FP64 jobs match them bit for bit.
 template <class S, class R>
-__global__ void upload_k(LatticeConst k, S* g, const double* fIN, R4<R>* Fprev, unsigned* flprev, const double* F,
-                         R4<R>* ubuf, const double* ru) {
+__global__ void lattice_init_k(LatticeConst k, InitSource src, S* g, R4<R>* Fprev, unsigned* flprev, R4<R>* ubuf) {
   const size_t N = (size_t)k.N;
   const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   const int x = (int)(n % k.nx), y = (int)((n / k.nx) % k.ny), z = (int)(n / ((size_t)k.nx * k.ny));
+  double f[Q];
+  double r, u0, u1, u2;
+  if (src.f) {
+#pragma unroll
+    for (int d = 0; d < Q; ++d) f[d] = src.f[(size_t)d * N + n];
+    if (src.rho && src.u) {
+      r = src.rho[n];
+      u0 = src.u[n];
+      u1 = src.u[N + n];
+      u2 = src.u[2 * N + n];
+    } else {
+      double a = 0, b = 0, c = 0;
+      r = 0;
+      for (int d = 0; d < Q; ++d) {
+        r = __dadd_rn(r, f[d]);
+        a = __dadd_rn(a, __dmul_rn((double)cx(d), f[d]));
+        b = __dadd_rn(b, __dmul_rn((double)cy(d), f[d]));
+        c = __dadd_rn(c, __dmul_rn((double)cz(d), f[d]));
+      }
+      const double Fx = src.F ? src.F[n] : 0, Fy = src.F ? src.F[N + n] : 0, Fz = src.F ? src.F[2 * N + n] : 0;
+      const double h = __dmul_rn(0.5, src.Fo);
+      u0 = __ddiv_rn(__dadd_rn(__dmul_rn(a, src.C), __dmul_rn(__dmul_rn(h, Fx), src.dt)), r);
+      u1 = __ddiv_rn(__dadd_rn(__dmul_rn(b, src.C), __dmul_rn(__dmul_rn(h, Fy), src.dt)), r);
+      u2 = __ddiv_rn(__dadd_rn(__dmul_rn(c, src.C), __dmul_rn(__dmul_rn(h, Fz), src.dt)), r);
+      if (src.zh && (z == 0 || z == k.nz - 1)) {
+        u0 = 0;
+        u2 = 0;
+        u1 = z == 0 ? 0.0 : src.uw;
+      }
+    }
+  } else {
+    // equilibrium of rest, the caller's u_init / rho_init, or the Zou/He
+    // channel's linear shear profile u_y = shear * z * dx / UMAX
+    // (gpuSEM_LB.c:1206-1258)
+    u0 = 0; u1 = 0; u2 = 0; r = 1.0;
+    if (src.u) {
+      u0 = src.u[n];
+      u1 = src.u[N + n];
+      u2 = src.u[2 * N + n];
+    } else if (src.zh) {
+      u1 = __ddiv_rn(__dmul_rn(__dmul_rn(src.shear, (double)z), src.dx), src.umax);
+    }
+    if (src.rho) r = src.rho[n];
+    const double uu = __dadd_rn(__dadd_rn(__dmul_rn(u0, u0), __dmul_rn(u1, u1)), __dmul_rn(u2, u2));
+    const double tail = __ddiv_rn(__dmul_rn(1.5, uu), src.C02);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      const double cu = __dmul_rn(3.0, __dadd_rn(__dadd_rn(__dmul_rn((double)cx(d), u0), __dmul_rn((double)cy(d), u1)),
+                                                 __dmul_rn((double)cz(d), u2)));
+      const double in = __dsub_rn(
+          __dadd_rn(__dadd_rn(1.0, __ddiv_rn(cu, src.C0)), __ddiv_rn(__dmul_rn(__dmul_rn(0.5, cu), cu), src.C02)), tail);
+      f[d] = __dmul_rn(__dmul_rn(r, wgt(d)), in);
+    }
+  }
+#pragma unroll
   for (int d = 0; d < Q; ++d) {
-    int tx = x + cx(d), ty = y + cy(d), tz = z + cz(d);
-    bool out = false;
-    if (tx < 0 || tx >= k.nx) { if (k.bc[0] == PF_BC_BOUNCEBACK) out = true; else tx = (tx + k.nx) % k.nx; }
-    if (ty < 0 || ty >= k.ny) { if (k.bc[1] == PF_BC_BOUNCEBACK) out = true; else ty = (ty + k.ny) % k.ny; }
-    if (tz < 0 || tz >= k.nz) { if (k.bc[2] == PF_BC_BOUNCEBACK) out = true; else tz = (tz + k.nz) % k.nz; }
-    double f = out ? fIN[(size_t)opp(d) * N + n]
-                   : fIN[(size_t)d * N + (size_t)tx + (size_t)k.nx * ((size_t)ty + (size_t)k.ny * tz)];
-    st<S, R>(g + (size_t)d * N + n, (R)(f - wgt(d)), d, k);
+    // push f_d(x) to x - c_d (periodic unless the face is bounce-back)
+    int tx = x - cx(d), ty = y - cy(d), tz = z - cz(d);
+    bool ok = true;
+    if (tx < 0 || tx >= k.nx) { if (k.bc[0] == PF_BC_BOUNCEBACK) ok = false; else tx = (tx + k.nx) % k.nx; }
+    if (ty < 0 || ty >= k.ny) { if (k.bc[1] == PF_BC_BOUNCEBACK) ok = false; else ty = (ty + k.ny) % k.ny; }
+    if (tz < 0 || tz >= k.nz) { if (k.bc[2] == PF_BC_BOUNCEBACK) ok = false; else tz = (tz + k.nz) % k.nz; }
+    if (ok)
+      st<S, R>(g + (size_t)d * N + (size_t)tx + (size_t)k.nx * ((size_t)ty + (size_t)k.ny * tz), (R)(f[d] - wgt(d)),
+               d, k);
+    // x + c_d beyond a bounce-back face: node x keeps the reflected value
+    const int sx = x + cx(d), sy = y + cy(d), sz = z + cz(d);
+    const bool out = ((sx < 0 || sx >= k.nx) && k.bc[0] == PF_BC_BOUNCEBACK) ||
+                     ((sy < 0 || sy >= k.ny) && k.bc[1] == PF_BC_BOUNCEBACK) ||
+                     ((sz < 0 || sz >= k.nz) && k.bc[2] == PF_BC_BOUNCEBACK);
+    if (out) st<S, R>(g + (size_t)d * N + n, (R)(f[opp(d)] - wgt(d)), d, k);
   }
   R fx = 0, fy = 0, fz = 0;
-  if (F) { fx = (R)F[n]; fy = (R)F[N + n]; fz = (R)F[2 * N + n]; }
+  if (src.F) { fx = (R)src.F[n]; fy = (R)src.F[N + n]; fz = (R)src.F[2 * N + n]; }
   if (fx != 0 || fy != 0 || fz != 0) {
     const int brick = x / kBrickX + k.nbx * (y + k.ny * z);
     flprev[brick] = 1u;
@@ -904,73 +976,7 @@ __global__ void upload_k(LatticeConst k, S* g, const double* fIN, R4<R>* Fprev, 
   R4<R> v;
   v.x = fx; v.y = fy; v.z = fz; v.w = 0;
   Fprev[n] = v;
-  st_u<R>(ubuf, n, (R)(ru[n] - 1.0), (R)(ru[N + n] / k.C), (R)(ru[2 * N + n] / k.C), (R)(ru[3 * N + n] / k.C));
-}
-
-// Initial equilibrium populations fIN[19][N] and (rho, u) ru[4][N] of a
-// scene given no populations: rho = 1 (or rho_init), u = the linear shear
-// profile u_y = shear * z * dx / UMAX of the Zou/He channel (or u_init, or
-// rest).  The FP64 operations and their order are those of the host
-// restatement (round-to-nearest intrinsics, no contraction), so the two agree
-// bit for bit.
-__global__ void equilibrium_k(int nx, int ny, long long N, int zh, double shear, double dx, double umax,
-                              double C0, double C02, const double* u_init, const double* rho_init, double* f,
-                              double* ru) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  const int z = (int)(n / ((long long)nx * ny));
-  double u0 = 0, u1 = 0, u2 = 0, r = 1.0;
-  if (u_init) {
-    u0 = u_init[n];
-    u1 = u_init[N + n];
-    u2 = u_init[2 * N + n];
-  } else if (zh) {
-    u1 = __ddiv_rn(__dmul_rn(__dmul_rn(shear, (double)z), dx), umax);
-  }
-  if (rho_init) r = rho_init[n];
-  const double uu = __dadd_rn(__dadd_rn(__dmul_rn(u0, u0), __dmul_rn(u1, u1)), __dmul_rn(u2, u2));
-  const double tail = __ddiv_rn(__dmul_rn(1.5, uu), C02);
-#pragma unroll
-  for (int d = 0; d < Q; ++d) {
-    const double cu = __dmul_rn(3.0, __dadd_rn(__dadd_rn(__dmul_rn((double)cx(d), u0), __dmul_rn((double)cy(d), u1)),
-                                               __dmul_rn((double)cz(d), u2)));
-    const double in = __dsub_rn(__dadd_rn(__dadd_rn(1.0, __ddiv_rn(cu, C0)), __ddiv_rn(__dmul_rn(__dmul_rn(0.5, cu), cu), C02)),
-                                tail);
-    f[(size_t)d * N + n] = __dmul_rn(__dmul_rn(r, wgt(d)), in);
-  }
-  ru[n] = r;
-  ru[N + n] = u0;
-  ru[2 * N + n] = u1;
-  ru[3 * N + n] = u2;
-}
-
-// (rho, u) ru[4][N] of given initial populations f[19][N]: the moments with
-// the half-force shift, the Zou/He walls at rest (bottom) and moving (top),
-// in the operation order of the host restatement (FP64, no contraction).
-__global__ void initial_moments_k(int nx, int ny, int nz, long long N, int zh, double C, double Fo, double dt,
-                                  double uw, const double* f, const double* F, double* ru) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  double r = 0, a = 0, b = 0, c = 0;
-  for (int d = 0; d < Q; ++d) {
-    const double v = f[(size_t)d * N + n];
-    r = __dadd_rn(r, v);
-    a = __dadd_rn(a, __dmul_rn((double)cx(d), v));
-    b = __dadd_rn(b, __dmul_rn((double)cy(d), v));
-    c = __dadd_rn(c, __dmul_rn((double)cz(d), v));
-  }
-  const double Fx = F ? F[n] : 0, Fy = F ? F[N + n] : 0, Fz = F ? F[2 * N + n] : 0;
-  const double h = __dmul_rn(0.5, Fo);
-  ru[n] = r;
-  ru[N + n] = __ddiv_rn(__dadd_rn(__dmul_rn(a, C), __dmul_rn(__dmul_rn(h, Fx), dt)), r);
-  ru[2 * N + n] = __ddiv_rn(__dadd_rn(__dmul_rn(b, C), __dmul_rn(__dmul_rn(h, Fy), dt)), r);
-  ru[3 * N + n] = __ddiv_rn(__dadd_rn(__dmul_rn(c, C), __dmul_rn(__dmul_rn(h, Fz), dt)), r);
-  const int z = (int)(n / ((long long)nx * ny));
-  if (zh && (z == 0 || z == nz - 1)) {
-    ru[N + n] = 0;
-    ru[3 * N + n] = 0;
-    ru[2 * N + n] = z == 0 ? 0.0 : uw;
-  }
+  st_u<R>(ubuf, n, (R)(r - 1.0), (R)(u0 / k.C), (R)(u1 / k.C), (R)(u2 / k.C));
 }
 
 template <class S, class R>
@@ -1102,10 +1108,10 @@ cudaError_t moments_impl(Lattice& L, Control* ctl, cudaStream_t st) {
   return cudaGetLastError();
 }
 template <class S, class R>
-cudaError_t upload_impl(Lattice& L, const double* fIN, const double* F, const double* ru, cudaStream_t st) {
+cudaError_t init_impl(Lattice& L, const InitSource& src, cudaStream_t st) {
   const size_t N = (size_t)L.k.N;
-  upload_k<S, R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(L.k, (S*)L.g[0], fIN, (R4<R>*)L.F[1], L.flags[1], F,
-                                                              (R4<R>*)L.ubuf, ru);
+  lattice_init_k<S, R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(L.k, src, (S*)L.g[0], (R4<R>*)L.F[1],
+                                                                     L.flags[1], (R4<R>*)L.ubuf);
   return cudaGetLastError();
 }
 template <class S, class R>
@@ -1175,13 +1181,11 @@ cudaError_t conservation_impl(Lattice& L, long long step, double* out, cudaStrea
     default: return cudaErrorInvalidValue;                \
   }
 
-cudaError_t lattice_upload(Lattice& L, const double* fIN_dev, const double* F_dev, const double* ru_dev,
-                           Control* ctl, cudaStream_t st) {
-  (void)ctl;
+cudaError_t lattice_init(Lattice& L, const InitSource& src, cudaStream_t st) {
   switch (L.precision) {
-    case PF_PREC_FP64: return upload_impl<double, double>(L, fIN_dev, F_dev, ru_dev, st);
-    case PF_PREC_FP32: return upload_impl<float, float>(L, fIN_dev, F_dev, ru_dev, st);
-    case PF_PREC_FP16: return upload_impl<__half, float>(L, fIN_dev, F_dev, ru_dev, st);
+    case PF_PREC_FP64: return init_impl<double, double>(L, src, st);
+    case PF_PREC_FP32: return init_impl<float, float>(L, src, st);
+    case PF_PREC_FP16: return init_impl<__half, float>(L, src, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -1261,20 +1265,6 @@ cudaError_t lattice_download(Lattice& L, Control* ctl, long long step, double* f
     case PF_PREC_FP16: return download_impl<__half, float>(L, step, fIN, fOUT, rho, u, F, st);
   }
   return cudaErrorInvalidValue;
-}
-cudaError_t lattice_initial_moments(int nx, int ny, int nz, int zh, double C, double Fo, double dt, double uw,
-                                    const double* f, const double* F, double* ru, cudaStream_t st) {
-  const long long N = (long long)nx * ny * nz;
-  initial_moments_k<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nx, ny, nz, N, zh, C, Fo, dt, uw, f, F, ru);
-  return cudaGetLastError();
-}
-cudaError_t lattice_equilibrium(int nx, int ny, int nz, int zh, double shear, double dx, double umax, double C0,
-                                const double* u_init, const double* rho_init, double* f, double* ru,
-                                cudaStream_t st) {
-  const long long N = (long long)nx * ny * nz;
-  equilibrium_k<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nx, ny, N, zh, shear, dx, umax, C0, C0 * C0, u_init,
-                                                              rho_init, f, ru);
-  return cudaGetLastError();
 }
 cudaError_t lattice_fields(Lattice& L, long long step, int stride, float* rho, float* ux, float* uy, float* uz,
                            cudaStream_t st) {

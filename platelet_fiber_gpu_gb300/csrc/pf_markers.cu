@@ -2519,13 +2519,11 @@ static cudaError_t launch_mem32(const PlateletConst& k, const double* X, const d
                                 const int* vert_local, const int* ring, const int* sp_ptr, const int* sp_nbr,
                                 const double* sp_L0, const double* S0, const double* S0_all, const double* V0,
                                 float* km, double* SV, float* F, Control* ctl, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(membrane32_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMem32MaxSmem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  // the attribute is per device: set on every launch (host-only, cheap), so
+  // a second device or host thread never launches without it
+  const cudaError_t e =
+      cudaFuncSetAttribute(membrane32_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMem32MaxSmem);
+  if (e != cudaSuccess) return e;
   membrane32_k<<<k.P, kMem32Threads, Mem32Layout(k).bytes, st>>>(k, X, Y, RY, Z, tri, node_ntri, node_tri,
                                                                  vert_local, ring, sp_ptr, sp_nbr, sp_L0, S0,
                                                                  S0_all, V0, km, SV, F, ctl);
@@ -2866,13 +2864,9 @@ cudaError_t batch_launch(int kind, const BatchDesc* descs, const int* start, int
       return batch_launch_lattice(kind, descs, start, nj, total, precision, fast, t.lbm_rows, st);
     case BK_FLAG: flag_batch_k<<<total, kFlagThreads, 0, st>>>(descs, start, nj); break;
     case BK_MEMBRANE: {
-      static bool attr = false;
-      if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(membrane_batch_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kMem32MaxSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-      }
+      cudaError_t e = cudaFuncSetAttribute(membrane_batch_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)kMem32MaxSmem);
+      if (e != cudaSuccess) return e;
       membrane_batch_k<<<total, kMem32Threads, smem, st>>>(descs, start, nj);
       break;
     }

@@ -7,6 +7,7 @@
 // call on a device looks up that array's address with cudaGetSymbolAddress
 // (with the device current) and caches it per device.  No cudaMalloc,
 // cudaFree or other allocating routine is called.
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -25,22 +26,58 @@ void* g_addr[kMaxDevices] = {};
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// node -> its triangles in ascending order and the node's local index in
-// each (the job builds the same lists on the host)
-__global__ void node_triangles_k(int T, int NN, int Em, const int* tri, int* node_tri, int* vert_local) {
+// Checks the caller's topology on the device (the job path checks the same
+// on the host before upload) and builds node -> its triangles in ascending
+// order with the node's local index in each.  Thread q covers node q,
+// triangle q and element q.  Any inconsistency -- a triangle index outside
+// the nodes (or a corner outside the membrane), node_ntri outside 0..10 or
+// unequal to the node's count in tri, a ring entry outside the membrane, a
+// spring list outside the elements -- sets ERR_INPUT and done = 3, so the
+// membrane kernels that follow on the stream return at once and read none
+// of the bad indices.
+__global__ void noalloc_topology_k(int T, int NN, int Em, int E, const int* tri, const int* node_ntri,
+                                   const int* ring, const int* sp_ptr, const int* sp_nbr, int* node_tri,
+                                   int* vert_local, Control* ctl) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= NN) return;
-  int cnt = 0;
-  for (int t = 0; t < T && cnt < 10; ++t)
-    for (int i = 0; i < 6; ++i)
-      if (tri[6 * t + i] == q && cnt < 10) {
-        node_tri[10 * q + cnt] = t;
-        if (q < Em) vert_local[10 * q + cnt] = i;
-        ++cnt;
+  bool bad = false;
+  if (q < T)
+    for (int i = 0; i < 6; ++i) {
+      const int v = tri[6 * q + i];
+      if (v < 0 || v >= NN || (i < 3 && v >= Em)) bad = true;
+    }
+  if (q < NN) {
+    int cnt = 0;
+    for (int t = 0; t < T; ++t)
+      for (int i = 0; i < 6; ++i)
+        if (tri[6 * t + i] == q) {
+          if (cnt < 10) {
+            node_tri[10 * q + cnt] = t;
+            if (q < Em) vert_local[10 * q + cnt] = i;
+          }
+          ++cnt;
+        }
+    for (int c = cnt; c < 10; ++c) {
+      node_tri[10 * q + c] = -1;
+      if (q < Em) vert_local[10 * q + c] = -1;
+    }
+    const int nt = node_ntri[q];
+    if (cnt > 10 || nt != cnt) bad = true;
+    if (q < Em && nt >= 0 && nt <= 10)
+      for (int a = 0; a < nt; ++a) {
+        const int r = ring[10 * q + a];
+        if (r < 0 || r >= Em) bad = true;
       }
-  for (int c = cnt; c < 10; ++c) {
-    node_tri[10 * q + c] = -1;
-    if (q < Em) vert_local[10 * q + c] = -1;
+  }
+  if (q < E) {
+    const int b0 = sp_ptr[q], b1 = sp_ptr[q + 1];
+    if ((q == 0 && b0 != 0) || b1 < b0) bad = true;
+    else
+      for (int s = b0; s < b1; ++s)
+        if (sp_nbr[s] < 0 || sp_nbr[s] >= E) bad = true;
+  }
+  if (bad) {
+    atomicOr(&ctl->err, ERR_INPUT);
+    ctl->done = 3;
   }
 }
 
@@ -101,8 +138,12 @@ extern "C" int pfgpu_membrane_forces_noalloc(const pf_membrane_args* a, void* st
   // written before it is read
   e = cudaMemsetAsync(ctl, 0, sizeof(Control), st);
   if (e != cudaSuccess) return report_error(PFGPU_ERR_CUDA, cudaGetErrorString(e));
-  node_triangles_k<<<(unsigned)((NN + 127) / 128), 128, 0, st>>>(a->n_tri, a->n_node, a->n_membrane, a->tri,
-                                                                   node_tri, vert_local);
+  const size_t nthr = std::max(std::max(NN, T), (size_t)a->n_elem);
+  noalloc_topology_k<<<(unsigned)((nthr + 127) / 128), 128, 0, st>>>(
+      a->n_tri, a->n_node, a->n_membrane, a->n_elem, a->tri, a->node_ntri, a->ring, a->spring_ptr, a->spring_nbr,
+      node_tri, vert_local, ctl);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return report_error(PFGPU_ERR_CUDA, cudaGetErrorString(e));
   PlateletConst k{};
   k.P = a->n_platelets; k.E = a->n_elem; k.Em = a->n_membrane; k.T = a->n_tri; k.NN = a->n_node;
   k.mask = a->membrane_forces;
@@ -121,3 +162,32 @@ extern "C" int pfgpu_membrane_forces_noalloc(const pf_membrane_args* a, void* st
 }
 
 extern "C" size_t pfgpu_membrane_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+// Outcome of the last call on the current device: waits for `stream`, then
+// copies the scratch's control word to the host (no allocation) and reports
+// rejected inputs or a platelet too large for the pass.
+extern "C" int pfgpu_membrane_noalloc_status(void* stream) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return report_error(PFGPU_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return report_error(PFGPU_ERR_UNSUPPORTED, "device index out of range");
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_addr_mu);
+    base = g_addr[dev];
+  }
+  if (!base) return report_error(PFGPU_ERR_INVALID, "no membrane pass without allocation was made on this device");
+  e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return report_error(PFGPU_ERR_CUDA, cudaGetErrorString(e));
+  Control c;
+  e = cudaMemcpy(&c, base, sizeof c, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return report_error(PFGPU_ERR_CUDA, cudaGetErrorString(e));
+  if (c.err & ERR_INPUT)
+    return report_error(PFGPU_ERR_INVALID,
+                        "membrane pass without allocation: inconsistent topology (tri, node_ntri, ring or spring "
+                        "arrays); F_out was not written");
+  if (c.err & ERR_MEMBRANE_SIZE)
+    return report_error(PFGPU_ERR_INVALID, "membrane pass without allocation: platelet too large for the pass");
+  if (c.err) return report_error(PFGPU_ERR_CUDA, ("membrane pass error bits " + std::to_string(c.err)).c_str());
+  return PFGPU_OK;
+}

@@ -93,10 +93,37 @@ def lib():
         L.pfgpu_job_set_stop.argtypes = [vp, C.c_int64]
         L.pfgpu_batch_set_shape.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.pfgpu_batch_destroy.argtypes = [vp]
+        L.pfgpu_host_alloc.restype = vp
+        L.pfgpu_host_alloc.argtypes = [C.c_size_t]
+        L.pfgpu_host_free.argtypes = [vp]
         L.pfgpu_detach_uniform.restype = C.c_double
         L.pfgpu_detach_uniform.argtypes = [C.c_uint64, C.c_int64]
         _lib = L
     return _lib
+
+
+class _PinnedOwner:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            lib().pfgpu_host_free(self.ptr)
+        except Exception:
+            pass
+
+
+def pinned(shape, dtype=np.float64) -> np.ndarray:
+    """A numpy array in pinned, device-mapped host memory
+    (pfgpu_host_alloc), freed when the last view of it goes."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    ptr = lib().pfgpu_host_alloc(max(n, 1))
+    if not ptr:
+        raise PfgpuError(3, lib().pfgpu_last_error().decode(errors="replace"))
+    buf = (C.c_byte * max(n, 1)).from_address(ptr)
+    buf._owner = _PinnedOwner(ptr)
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
 
 def _p(a, t=C.c_double):
@@ -173,11 +200,21 @@ class Job:
         written now); fp32: float records for convBtoXYZ.py."""
         return Output(self, directory, fp32)
 
-    def lattice(self, fIN=True, fOUT=False):
+    def lattice(self, fIN=True, fOUT=False, out=None):
+        """fIN, fOUT [19, N], rho [N], u [3, N], F [3, N] (FP64); `out`: the
+        caller's own arrays under those keys (C-contiguous float64, e.g.
+        pinned()), written in place and returned."""
         N = self.scene.n_nodes
-        a = np.zeros((19, N)) if fIN else None
-        b = np.zeros((19, N)) if fOUT else None
-        rho, u, F = np.zeros(N), np.zeros((3, N)), np.zeros((3, N))
+        if out is not None:
+            for k, v in out.items():
+                if v is not None and (v.dtype != np.float64 or not v.flags.c_contiguous):
+                    raise ValueError(f"out[{k!r}] must be C-contiguous float64")
+            a, b = out.get("fIN"), out.get("fOUT")
+            rho, u, F = out.get("rho"), out.get("u"), out.get("F")
+        else:
+            a = np.zeros((19, N)) if fIN else None
+            b = np.zeros((19, N)) if fOUT else None
+            rho, u, F = np.zeros(N), np.zeros((3, N)), np.zeros((3, N))
         check(lib().pfgpu_job_get_lattice(self.h, _p(a), _p(b), _p(rho), _p(u), _p(F)))
         return dict(fIN=a, fOUT=b, rho=rho, u=u, F=F)
 
@@ -201,10 +238,14 @@ class Job:
         write_vti(t, f["rho"], f["u"], directory, filename, spacing=stride, write_rho=write_rho,
                   write_vel=write_vel)
 
-    def elements(self):
+    def elements(self, out=None):
+        """X, Y, RY, Z [PE], V, F [3, PE]; `out`: the caller's arrays."""
         PE = self.scene.n_platelets * self.scene.n_elem
-        X, Y, RY, Z = (np.zeros(PE) for _ in range(4))
-        V, F = np.zeros((3, PE)), np.zeros((3, PE))
+        if out is not None:
+            X, Y, RY, Z, V, F = (out[k] for k in ("X", "Y", "RY", "Z", "V", "F"))
+        else:
+            X, Y, RY, Z = (np.zeros(PE) for _ in range(4))
+            V, F = np.zeros((3, PE)), np.zeros((3, PE))
         check(lib().pfgpu_job_get_elements(self.h, _p(X), _p(Y), _p(RY), _p(Z), _p(V), _p(F)))
         return dict(X=X, Y=Y, RY=RY, Z=Z, V=V, F=F)
 

@@ -7,7 +7,7 @@ the three documented substitutions).  Each fixture stores the complete input
 scene and the reference's state after `nsteps` coupled steps, so the tests
 can rebuild the case without the reference tree.
 
-Run in a checkout that has the reference tree at /root/reference (or REF_DIR):
+Run in a checkout with the reference tree beside it (or at $PF_REFERENCE_DIR):
     python tests/golden/make_golden.py
 """
 from __future__ import annotations

@@ -23,6 +23,9 @@ def test_reference_arm_line():
         assert k in d, k
     assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "MLUPS" and d["higher_is_better"]
     assert "workload" in d["config"] and d["config"]["timed_steps"] >= 1
+    # the same config keys as the GPU arm's line
+    for k in ("lattice", "nodes", "elements", "fibrin_nodes", "receptors", "parallelism", "l2", "precision"):
+        assert k in d["config"], k
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and "stencil-local" in cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
