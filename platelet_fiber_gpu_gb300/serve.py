@@ -57,11 +57,13 @@ def run_batched(precision: int, n_jobs: int = 64, steps: int = 1000, seed: int =
 
 def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed: int = 4, budget: float = 150e9,
                chunk: int = 50, steps_range=(500, 5000), pool: int = 32, batch_factory=Batch,
-               scenes=None) -> dict:
+               scenes=None, on_finish=None) -> dict:
     """Poisson arrivals at `rate` per second for `duration` seconds; each job
     is one of `pool` pre-built scenes of the many-job workload with its own
     requested step count drawn from `steps_range`.  `batch_factory` and
-    `scenes` replace the GPU batch and the scene pool (host-logic tests)."""
+    `scenes` replace the GPU batch and the scene pool (host-logic tests);
+    `on_finish(scene_index, requested_steps, job)` sees each finished job
+    before it leaves the batch (its results are read there)."""
     rng = np.random.default_rng(seed)
     if scenes is None:
         scenes = [W.batch_job(seed, i) for i in range(pool)]
@@ -98,7 +100,7 @@ def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed:
                 continue
             # the job leaves the fused step by itself after its requested steps
             b.set_stop(s, a[2])
-            live[s] = [a[0], a[2], sc.n_nodes, a[2]]
+            live[s] = [a[0], a[2], sc.n_nodes, a[2], a[1]]
         waiting = still
         host["admit"] += time.perf_counter() - ta
         if not live:
@@ -114,9 +116,11 @@ def run_served(precision: int, rate: float = 20.0, duration: float = 10.0, seed:
         for s in list(live):
             live[s][1] -= chunk
             if b.status(s) != 0:
-                arr, _, n, req = live.pop(s)
+                arr, _, n, req, idx = live.pop(s)
                 work += n * req
                 latencies.append(time.perf_counter() - t0 - arr)
+                if on_finish is not None:
+                    on_finish(idx, req, b.job(s))
                 b.retire(s)
         host["retire"] += time.perf_counter() - tr
     span = time.perf_counter() - t0

@@ -319,8 +319,10 @@ def mixed_large(seed: int = 5) -> Scene:
 
 
 def mixed_small(seed: int = 3, nx=40, ny=32, nz=20, n_platelets=3, level=1, n_cyto=12, n_fib=300,
-                n_links=600, n_rec=40, bell=False) -> Scene:
-    """Every feature of single_large on a lattice the oracle steps in seconds."""
+                n_links=600, n_rec=40, bell=False, wall_gap=0.05) -> Scene:
+    """Every feature of single_large on a lattice the oracle steps in seconds.
+    Two platelets sit `wall_gap` um above the bottom wall (receptors within
+    the 0.078 um bond range of it can bind)."""
     rng = np.random.default_rng(seed)
     axes = (0.6, 0.6, 0.3)
     v, t = M.ellipsoid_icosphere(level, axes)
@@ -333,7 +335,7 @@ def mixed_small(seed: int = 3, nx=40, ny=32, nz=20, n_platelets=3, level=1, n_cy
     L = np.array([nx, ny, nz]) * REF_DX
     centers = poisson_disk(n_platelets, (axes[0], axes[1], axes[2] + 0.05),
                            (L[0] - axes[0], L[1] - axes[1], L[2] - axes[2] - 0.3), 2 * axes[0] + 2 * REF_DX,
-                           rng, fixed_z=axes[2] + 0.05, n_fixed=min(2, n_platelets))
+                           rng, fixed_z=axes[2] + wall_gap, n_fixed=min(2, n_platelets))
     _place(sc, tpl, centers, L[1])
     _receptors_random(sc, n_rec, rng)
     if bell:

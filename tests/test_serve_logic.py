@@ -49,6 +49,9 @@ class FakeBatch:
         j = self.jobs[s]
         return DONE if j["stop"] and j["step"] >= j["stop"] else 0
 
+    def job(self, s):
+        return self.jobs[s]
+
     def retire(self, s):
         j = self.jobs.pop(s)
         assert j["step"] == j["stop"]
@@ -87,3 +90,16 @@ def test_requested_steps_set_the_work():
         req.append(int(rng.integers(5, 41)))
     assert r["jobs"] == len(req)
     assert r["node_steps"] == 500 * sum(req)
+
+
+def test_on_finish_sees_each_job_once_at_its_requested_step():
+    """The served loop hands every finished job to on_finish, with its scene
+    index and requested step count, before retiring it."""
+    scenes = [FakeScene(300), FakeScene(700)]
+    seen = []
+    r = serve.run_served(1, rate=300.0, duration=0.05, seed=5, budget=10 ** 9, chunk=10, steps_range=(5, 40),
+                         batch_factory=FakeBatch, scenes=scenes,
+                         on_finish=lambda idx, req, job: seen.append((idx, req, job["step"], job["n"])))
+    assert len(seen) == r["jobs"] >= 3
+    for idx, req, step, n in seen:
+        assert step == req and n == scenes[idx].n_nodes
