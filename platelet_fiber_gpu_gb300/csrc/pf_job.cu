@@ -171,6 +171,7 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
     k.hs[c] = (float)(wc[c] * k.fp16_scale);
     k.hinv[c] = 1.0f / k.hs[c];
   }
+  k.isig = (float)(1.0 / k.fp16_scale);
   k.dtT = s->dt / mp[PF_P_T0];
   k.omega_f = (float)k.omega;
   k.kcoll_f = (float)k.kcoll;

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "pf_internal.h"
 
@@ -89,7 +90,14 @@ __device__ __forceinline__ void ld_u<double>(const D4* U, size_t n, double& a, d
 // Pull the 19 post-stream populations of node (x,y,z) from the post-collision
 // buffer: periodic on periodic and Zou/He axes (the reference streams
 // periodically first), half-way bounce-back through faces of bounce-back axes.
-template <class S, class R>
+// RAW: the stored values as they are (FP16: q, not scaled back to g)
+template <class S, class R, bool RAW>
+__device__ __forceinline__ R ldr(const S* p, int d, const LatticeConst& k) {
+  if constexpr (RAW && std::is_same<S, __half>::value) return __half2float(__ldg(p));
+  else return ld<S, R>(p, d, k);
+}
+
+template <class S, class R, bool RAW = false>
 __device__ __forceinline__ void gather(const LatticeConst& k, const S* __restrict__ gin, int x, int y, int z,
                                        R g[Q]) {
   const int nx = k.nx, ny = k.ny, nz = k.nz;
@@ -111,9 +119,9 @@ __device__ __forceinline__ void gather(const LatticeConst& k, const S* __restric
     const bool out = (cx(d) == 1 && oxm) || (cx(d) == -1 && oxp) || (cy(d) == 1 && oym) ||
                      (cy(d) == -1 && oyp) || (cz(d) == 1 && ozm) || (cz(d) == -1 && ozp);
     if (out) {
-      g[d] = ld<S, R>(gin + (size_t)opp(d) * N + n, opp(d), k);
+      g[d] = ldr<S, R, RAW>(gin + (size_t)opp(d) * N + n, opp(d), k);
     } else {
-      g[d] = ld<S, R>(gin + (size_t)d * N + (size_t)sx + (size_t)nx * ((size_t)sy + (size_t)ny * sz), d, k);
+      g[d] = ldr<S, R, RAW>(gin + (size_t)d * N + (size_t)sx + (size_t)nx * ((size_t)sy + (size_t)ny * sz), d, k);
     }
   }
 }
@@ -121,7 +129,7 @@ __device__ __forceinline__ void gather(const LatticeConst& k, const S* __restric
 // The same pull for lattices without bounce-back faces (every axis periodic
 // or Zou/He, which streams periodically) whose population index 19 N fits
 // 32 bits: no face tests, 32-bit offsets (nine source rows, three columns).
-template <class S, class R>
+template <class S, class R, bool RAW = false>
 __device__ __forceinline__ void gather_fast(const LatticeConst& k, const S* __restrict__ gin, int x, int y, int z,
                                             R g[Q]) {
   const unsigned nx = (unsigned)k.nx, ny = (unsigned)k.ny, nz = (unsigned)k.nz;
@@ -133,7 +141,7 @@ __device__ __forceinline__ void gather_fast(const LatticeConst& k, const S* __re
   for (int d = 0; d < Q; ++d) {
     // pull from x - c: index 0 of each triple is the -1 neighbour
     const unsigned off = (unsigned)d * N + xs[1 - cx(d)] + nx * (ys[1 - cy(d)] + ny * zs[1 - cz(d)]);
-    g[d] = ld<S, R>(gin + off, d, k);
+    g[d] = ldr<S, R, RAW>(gin + off, d, k);
   }
 }
 
@@ -208,6 +216,20 @@ __device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z,
   uz = (jz + hk * Fz) / rho;
 }
 
+// c_d . (a, b, c) from the nonzero components only, in x, y, z order: the
+// products with zero components of the term-by-term form cannot be folded
+// away under IEEE rules (0 * x is not 0 for every x) and cost an FMA each.
+// Equal to the term-by-term sum except for the sign of a zero result.
+template <class R>
+__device__ __forceinline__ R cdot(int d, R a, R b, R c) {
+  R r = (R)0;
+  bool any = false;
+  if (cx(d) != 0) { r = cx(d) > 0 ? a : -a; any = true; }
+  if (cy(d) != 0) { r = any ? (cy(d) > 0 ? r + b : r - b) : (cy(d) > 0 ? b : -b); any = true; }
+  if (cz(d) != 0) { r = any ? (cz(d) > 0 ? r + c : r - c) : (cz(d) > 0 ? c : -c); }
+  return r;
+}
+
 // BGK collision with Guo forcing of one node, in place on the shifted
 // populations (F already scaled to lattice units, om = 1/tau, sf = 1 - om/2):
 //   g_d <- g_d - om (g_d - geq_d) + S_d.
@@ -240,14 +262,83 @@ __device__ __forceinline__ void collide(R g[Q], R drho, R ux, R uy, R uz, R Fx, 
     for (int d = 1; d < Q; ++d) {
       if (opp(d) < d) continue;  // handled with its partner
       const int o = opp(d);
-      const R cu = (R)cx(d) * ux + (R)cy(d) * uy + (R)cz(d) * uz;
-      const R cF = (R)cx(d) * Fx + (R)cy(d) * Fy + (R)cz(d) * Fz;
+      const R cu = cdot<R>(d, ux, uy, uz);
+      const R cF = cdot<R>(d, Fx, Fy, Fz);
       const R even = A + cu * (C * cu + E * cF);
       const R odd = B * cu + D * cF;
       const R w = (R)wgt(d);
       g[d] = omc * g[d] + w * (even + odd);
       g[o] = omc * g[o] + w * (even - odd);
     }
+  }
+}
+
+// One node of the step on the FP16 store's own values q = g / (w_c sigma)
+// (c: the weight class), in place.  Interior nodes: the moments from
+// per-class sums (g = w_c sigma q) and the FP32 collision's polynomial with
+// the weight folded into 1 / sigma,
+//   q_d <- (1 - om) q_d + (A + B cu + C cu^2 + D cF + E cu cF) / sigma,
+// so no per-population scaling on load or store.  The Zou/He planes go
+// through g with the boundary pass of node_state.
+__device__ __forceinline__ void node_q(const LatticeConst& k, float q[Q], int z, int first, size_t n,
+                                       const float4* ubuf, const float4* Fp, unsigned fp, const float4* Fc,
+                                       unsigned fc) {
+  const float om = k.omega_f, sf = 1.0f - 0.5f * om, kc = k.kcoll_f;
+  float Fx = k.body_f[0], Fy = k.body_f[1], Fz = k.body_f[2];
+  if (fc) ld_force<float>(Fc, n, Fx, Fy, Fz);
+  Fx *= kc; Fy *= kc; Fz *= kc;
+  float drho, ux, uy, uz;
+  if (k.bc[2] == PF_BC_ZOUHE_SHEAR && (z == 0 || z == k.nz - 1)) {
+    float g[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) g[d] = q[d] * k.hs[wcls(d)];
+    if (first) {
+      ld_u<float>(ubuf, n, drho, ux, uy, uz);
+    } else {
+      float px = k.body_f[0], py = k.body_f[1], pz = k.body_f[2];
+      if (fp) ld_force<float>(Fp, n, px, py, pz);
+      node_state<float>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
+    }
+    collide<float>(g, drho, ux, uy, uz, Fx, Fy, Fz, om, sf);
+#pragma unroll
+    for (int d = 0; d < Q; ++d) q[d] = g[d] * k.hinv[wcls(d)];
+    return;
+  }
+  if (first) {
+    ld_u<float>(ubuf, n, drho, ux, uy, uz);
+  } else {
+    float px = k.body_f[0], py = k.body_f[1], pz = k.body_f[2];
+    if (fp) ld_force<float>(Fp, n, px, py, pz);
+    const float s1 = k.hs[1], s2 = k.hs[2];
+    const float ax = q[1] + q[2] + q[3] + q[4] + q[5] + q[6];
+    const float dg = q[7] + q[8] + q[9] + q[10] + q[11] + q[12] + q[13] + q[14] + q[15] + q[16] + q[17] + q[18];
+    drho = k.hs[0] * q[0] + s1 * ax + s2 * dg;
+    const float jx = s1 * (q[1] - q[2]) + s2 * ((q[7] + q[8] + q[9] + q[10]) - (q[11] + q[12] + q[13] + q[14]));
+    const float jy = s1 * (q[3] - q[4]) + s2 * ((q[7] + q[11] + q[15] + q[16]) - (q[8] + q[12] + q[17] + q[18]));
+    const float jz = s1 * (q[5] - q[6]) + s2 * ((q[9] + q[13] + q[15] + q[17]) - (q[10] + q[14] + q[16] + q[18]));
+    const float hk = 0.5f * k.kmom_f, rho = 1.0f + drho;
+    ux = (jx + hk * px) / rho;
+    uy = (jy + hk * py) / rho;
+    uz = (jz + hk * pz) / rho;
+  }
+  const float rho = 1.0f + drho;
+  const float usq = ux * ux + uy * uy + uz * uz;
+  const float uF = ux * Fx + uy * Fy + uz * Fz;
+  const float omr = om * rho, is = k.isig;
+  const float A = (om * drho - 1.5f * omr * usq - 3.0f * sf * uF) * is;
+  const float B = 3.0f * omr * is, C = 4.5f * omr * is, D = 3.0f * sf * is, E = 9.0f * sf * is;
+  const float omc = 1.0f - om;
+  q[0] = omc * q[0] + A;
+#pragma unroll
+  for (int d = 1; d < Q; ++d) {
+    if (opp(d) < d) continue;
+    const int o = opp(d);
+    const float cu = cdot<float>(d, ux, uy, uz);
+    const float cF = cdot<float>(d, Fx, Fy, Fz);
+    const float even = A + cu * (C * cu + E * cF);
+    const float odd = B * cu + D * cF;
+    q[d] = omc * q[d] + (even + odd);
+    q[o] = omc * q[o] + (even - odd);
   }
 }
 
@@ -260,6 +351,20 @@ __device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restr
                                          unsigned fc, unsigned fp, int first) {
   const size_t N = (size_t)k.N;
   const size_t n = (size_t)x + (size_t)k.nx * ((size_t)y + (size_t)k.ny * z);
+  if constexpr (std::is_same<S, __half>::value) {
+    float q[Q];
+    if constexpr (FAST) gather_fast<S, R, true>(k, gin, x, y, z, q);
+    else gather<S, R, true>(k, gin, x, y, z, q);
+    node_q(k, q, z, first, n, ubuf, Fp, fp, Fc, fc);
+    S* p = gout + n;
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      *p = __float2half_rn(q[d]);
+      p += N;
+    }
+    if (fp) zero_force<R>(Fp, n);
+    return;
+  }
   R g[Q];
   if constexpr (FAST) gather_fast<S, R>(k, gin, x, y, z, g);
   else gather<S, R>(k, gin, x, y, z, g);
@@ -357,6 +462,202 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_k(LatticeConst k, S* gA, S
                                                         const unsigned char* nearB, Control* ctl) {
   lbm_step_body<S, R, FAST>(k, gA, gB, FA, FB, ubuf, flA, flB, bin_count, ncells, mode, nearA, nearB, ctl,
                             blockIdx.x, gridDim.x);
+}
+
+// ---------------------------------------------------------- vector step
+// The direct-gather step with V consecutive x-nodes per thread and every
+// population plane moved as one aligned V-element vector per thread (8 or 16
+// bytes): FP16 stores V = 4 or 8 halves, FP32 V = 2 or 4 floats.  For a
+// direction with c_x = +1 (-1) the pull needs each node's left (right)
+// neighbour in the same source row: the thread's own vector supplies all
+// but one, the neighbouring lane's vector the last (a warp shuffle), and
+// lanes whose neighbour segment lies in another warp, another row or an
+// idle lane load that one element directly (periodic wrap at the row ends).
+// Per node the arithmetic is lbm_node's, in the same order, so the results
+// are bit-identical to the one-node-per-thread kernel (FP16: node_q on the
+// stored q, two nodes per packed conversion); the populations are
+// overwritten in place (a carry keeps each c_x = +1 input for the next
+// node).  Lattices without bounce-back faces whose nx is a multiple of V.
+template <class S, int V>
+struct VecIO;
+template <int V>
+struct VecIO<float, V> {
+  static constexpr int W = V;  // 32-bit words per vector
+  __device__ static void load(const float* p, unsigned w[W]) {
+    if constexpr (V == 4) {
+      const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+      w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+    } else {
+      const uint2 a = __ldg(reinterpret_cast<const uint2*>(p));
+      w[0] = a.x; w[1] = a.y;
+    }
+  }
+  __device__ static void store(float* p, const unsigned w[W]) {
+    if constexpr (V == 4) *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+    else *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+  }
+  __device__ static unsigned bits(const unsigned w[W], int i) { return w[i]; }
+  __device__ static unsigned load_bits(const float* p) { return __float_as_uint(__ldg(p)); }
+  __device__ static float value(unsigned b) { return __uint_as_float(b); }
+  __device__ static void put(unsigned w[W], int i, float v) { w[i] = __float_as_uint(v); }
+};
+template <int V>
+struct VecIO<__half, V> {
+  static constexpr int W = V / 2;
+  __device__ static void load(const __half* p, unsigned w[W]) {
+    if constexpr (V == 8) {
+      const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+      w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+    } else {
+      const uint2 a = __ldg(reinterpret_cast<const uint2*>(p));
+      w[0] = a.x; w[1] = a.y;
+    }
+  }
+  __device__ static void store(__half* p, const unsigned w[W]) {
+    if constexpr (V == 8) *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+    else *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+  }
+  __device__ static unsigned bits(const unsigned w[W], int i) { return (w[i >> 1] >> (16 * (i & 1))) & 0xffffu; }
+  __device__ static unsigned load_bits(const __half* p) { return (unsigned)__half_as_ushort(__ldg(p)); }
+};
+
+template <class S, int V>
+__device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB, float4* FA, float4* FB,
+                                             float4* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                             int ncells, int mode, Control* ctl, long long seg, long long tid,
+                                             long long tot) {
+  using IO = VecIO<S, V>;
+  constexpr int W = IO::W;
+  if (ctl->done) return;
+  const int par = (int)(ctl->step & 1);
+  const S* __restrict__ gin = par ? gB : gA;
+  S* __restrict__ gout = par ? gA : gB;
+  const float4* Fc = par ? FB : FA;
+  float4* Fp = par ? FA : FB;
+  unsigned* flp = par ? flA : flB;
+  const unsigned* flc = par ? flB : flA;
+  if (bin_count) zero_bins(bin_count, ncells, ctl, (size_t)tid, (size_t)tot);
+  const int lane = threadIdx.x & 31;
+  const unsigned nx = (unsigned)k.nx, ny = (unsigned)k.ny, nz = (unsigned)k.nz;
+  const unsigned spr = nx / V;  // segments per row
+  const long long nseg = k.N / V;
+  const bool valid = seg < nseg;
+  const unsigned row = valid ? (unsigned)(seg / spr) : 0u;
+  const unsigned sx = valid ? (unsigned)(seg - (long long)row * spr) : 0u;
+  const unsigned x0 = sx * V, y = row % ny, z = row / ny;
+  const int brick = (int)(x0 / kBrickX + (unsigned)k.nbx * row);
+  const unsigned fc = valid ? flc[brick] : 0u;
+  const bool active = valid && (mode == kPassAll || !fc);
+  const unsigned am = __ballot_sync(0xffffffffu, active);
+  // the source rows of the pull (periodic / Zou/He axes wrap)
+  const unsigned ys[3] = {y == 0 ? ny - 1 : y - 1, y, y + 1 == ny ? 0u : y + 1};
+  const unsigned zs[3] = {z == 0 ? nz - 1 : z - 1, z, z + 1 == nz ? 0u : z + 1};
+  const unsigned N = (unsigned)k.N;
+  unsigned w[Q][W];
+  if (active) {
+#pragma unroll
+    for (int d = 0; d < Q; ++d) IO::load(gin + ((unsigned)d * N + nx * (ys[1 - cy(d)] + ny * zs[1 - cz(d)]) + x0), w[d]);
+  }
+  // the one element of each x-shifted plane that lies outside the vector:
+  // x0 - 1 for c_x = +1, x0 + V for c_x = -1
+  const bool left_in_warp = lane > 0 && sx > 0 && ((am >> (lane - 1)) & 1u);
+  const bool right_in_warp = lane < 31 && sx + 1 < spr && ((am >> (lane + 1)) & 1u);
+  const unsigned xl = sx == 0 ? nx - 1 : x0 - 1, xr = sx + 1 == spr ? 0u : x0 + V;
+  unsigned edge[Q];
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    if (cx(d) == 0) continue;
+    const unsigned mine = cx(d) == 1 ? IO::bits(w[d], V - 1) : IO::bits(w[d], 0);
+    const unsigned nb = cx(d) == 1 ? __shfl_up_sync(0xffffffffu, mine, 1) : __shfl_down_sync(0xffffffffu, mine, 1);
+    const bool ok = cx(d) == 1 ? left_in_warp : right_in_warp;
+    edge[d] = nb;
+    if (active && !ok)
+      edge[d] = IO::load_bits(gin + ((unsigned)d * N + nx * (ys[1 - cy(d)] + ny * zs[1 - cz(d)]) +
+                                     (cx(d) == 1 ? xl : xr)));
+  }
+  if (!active) return;
+  const unsigned fp = flp[brick];
+  const int first = ctl->first;
+  const unsigned n0 = nx * row + x0;
+  unsigned carry[Q];
+  if constexpr (std::is_same<S, __half>::value) {
+    // two nodes at a time: their outputs share a 32-bit word of each plane
+    // and are packed by one conversion
+#pragma unroll
+    for (int i = 0; i < V; i += 2) {
+      float qa[Q], qb[Q];
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        unsigned ba, bb;
+        if (cx(d) == 0) {
+          ba = IO::bits(w[d], i);
+          bb = IO::bits(w[d], i + 1);
+        } else if (cx(d) == 1) {
+          ba = i == 0 ? edge[d] : carry[d];
+          bb = IO::bits(w[d], i);
+          carry[d] = IO::bits(w[d], i + 1);
+        } else {
+          ba = IO::bits(w[d], i + 1);
+          bb = i + 1 == V - 1 ? edge[d] : IO::bits(w[d], i + 2);
+        }
+        qa[d] = __half2float(__ushort_as_half((unsigned short)ba));
+        qb[d] = __half2float(__ushort_as_half((unsigned short)bb));
+      }
+      node_q(k, qa, (int)z, first, n0 + i, ubuf, Fp, fp, Fc, fc);
+      node_q(k, qb, (int)z, first, n0 + i + 1, ubuf, Fp, fp, Fc, fc);
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        const __half2 h = __floats2half2_rn(qa[d], qb[d]);
+        w[d][i >> 1] = *reinterpret_cast<const unsigned*>(&h);
+      }
+      if (fp) {
+        zero_force<float>(Fp, n0 + i);
+        zero_force<float>(Fp, n0 + i + 1);
+      }
+    }
+  } else {
+    const float kc = k.kcoll_f, om = k.omega_f;
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const unsigned n = n0 + i;
+      float g[Q];
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        unsigned b;
+        if (cx(d) == 0) b = IO::bits(w[d], i);
+        else if (cx(d) == 1) b = i == 0 ? edge[d] : carry[d];
+        else b = i == V - 1 ? edge[d] : IO::bits(w[d], i + 1);
+        if (cx(d) == 1) carry[d] = IO::bits(w[d], i);
+        g[d] = IO::value(b);
+      }
+      float drho, ux, uy, uz;
+      if (first) {
+        ld_u<float>(ubuf, n, drho, ux, uy, uz);
+      } else {
+        float px = k.body_f[0], py = k.body_f[1], pz = k.body_f[2];
+        if (fp) ld_force<float>(Fp, n, px, py, pz);
+        node_state<float>(k, g, (int)z, true, px, py, pz, drho, ux, uy, uz);
+      }
+      float Fx = k.body_f[0], Fy = k.body_f[1], Fz = k.body_f[2];
+      if (fc) ld_force<float>(Fc, n, Fx, Fy, Fz);
+      collide<float>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, 1.0f - 0.5f * om);
+#pragma unroll
+      for (int d = 0; d < Q; ++d) IO::put(w[d], i, g[d]);
+      if (fp) zero_force<float>(Fp, n);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < Q; ++d) IO::store(gout + ((unsigned)d * N + n0), w[d]);
+  __syncwarp(am);
+  if (fp && (x0 % kBrickX) == 0) flp[brick] = 0;
+}
+template <class S, int V>
+__global__ void __launch_bounds__(kLbmBlock) lbm_vec_k(LatticeConst k, S* gA, S* gB, float4* FA, float4* FB,
+                                                       float4* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                                       int ncells, int mode, Control* ctl) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  lbm_vec_body<S, V>(k, gA, gB, FA, FB, ubuf, flA, flB, bin_count, ncells, mode, ctl, t, t,
+                     (long long)gridDim.x * blockDim.x);
 }
 
 // Near region of a step from a per-brick word array (non-zero: set): every
@@ -1062,6 +1363,24 @@ inline bool fast_lattice(const Lattice& L) {
          19ull * (unsigned long long)L.k.N < (1ull << 32) && !getenv("PFGPU_GENERIC_GATHER");
 }
 
+// Nodes per thread of the vector step for this lattice, 0 for the
+// one-node-per-thread kernel: FP32 2, FP16 4 (8-byte vectors; measured
+// faster than 16-byte ones, whose registers halve the resident warps).  The
+// vector step needs a lattice without bounce-back faces and nx a multiple
+// of the width.  PFGPU_LBM_VEC=0 / 2 / 4 / 8 overrides (0: off).
+template <class S>
+int vec_width(const Lattice& L) {
+  if (!fast_lattice(L)) return 0;
+  int V = std::is_same<S, float>::value ? 2 : 4;
+  if (const char* e = getenv("PFGPU_LBM_VEC")) {
+    V = atoi(e);
+    if (V == 8 && std::is_same<S, float>::value) V = 4;
+  }
+  if (V != 2 && V != 4 && V != 8) return 0;
+  if (std::is_same<S, __half>::value && V == 2) V = 4;
+  return (L.k.nx % V == 0) ? V : 0;
+}
+
 // part: 0 the whole lattice, 1 the bricks not flagged for this step's force,
 // 2 the flagged bricks (after the spreading).
 template <class S, class R>
@@ -1086,6 +1405,19 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
                                      L.flags[0], L.flags[1], L.list[0], L.list[1], bin_count, ncells, L.mark,
                                      ctl);
     return cudaGetLastError();
+  }
+  if constexpr (!std::is_same<S, double>::value) {
+    const int V = vec_width<S>(L);
+    if (V > 0 && (part == 0 || part == 1)) {
+      const long long nseg = L.k.N / V;
+      const unsigned vgrid = (unsigned)((nseg + kLbmBlock - 1) / kLbmBlock);
+      void (*kern)(LatticeConst, S*, S*, float4*, float4*, float4*, unsigned*, unsigned*, int*, int, int, Control*);
+      if constexpr (std::is_same<S, float>::value) kern = V == 4 ? lbm_vec_k<S, 4> : lbm_vec_k<S, 2>;
+      else kern = V == 8 ? lbm_vec_k<S, 8> : lbm_vec_k<S, 4>;
+      kern<<<vgrid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (float4*)L.F[0], (float4*)L.F[1],
+                                        (float4*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells, part, ctl);
+      return cudaGetLastError();
+    }
   }
   const unsigned grid = (unsigned)((L.k.nbricks + kLbmBlock / kBrickX - 1) / (kLbmBlock / kBrickX));
   auto kern = fast_lattice(L) ? lbm_step_k<S, R, true> : lbm_step_k<S, R, false>;
