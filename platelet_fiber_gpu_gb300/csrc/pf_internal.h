@@ -47,6 +47,7 @@ struct LatticeConst {
   int bc[3];
   int ibm_wrap[3];
   float dxf, dtf;
+  double inv_dx;      // 1 / (double)dxf, so kernels divide by no double per thread
   double C;           // float-rounded dx/dt/UMAX
   double omega;       // 1/tau
   double kcoll;       // F0/rho0/UMAX*UNIT (double chain) * dt / C
@@ -95,6 +96,7 @@ struct PlateletConst {
   int mask;
   float kspring, ks, kv, kbend, f0, kf0, kr0, numrec;
   double dxd, dtd;
+  double inv_f0;  // 1 / (double)f0
   float dxf, dtf, dtT;
   int bond_model;
   double p_on, p_off;

@@ -172,6 +172,7 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
     k.hinv[c] = 1.0f / k.hs[c];
   }
   k.isig = (float)(1.0 / k.fp16_scale);
+  k.inv_dx = 1.0 / (double)k.dxf;
   k.dtT = s->dt / mp[PF_P_T0];
   k.omega_f = (float)k.omega;
   k.kcoll_f = (float)k.kcoll;
@@ -255,6 +256,7 @@ static int build_platelets(pfgpu_job* j, const pf_scene* s) {
   k.kspring = mp[PF_P_KSPRING]; k.ks = mp[PF_P_KS]; k.kv = mp[PF_P_KV]; k.kbend = mp[PF_P_KBEND] * 1;
   k.f0 = mp[PF_P_F0]; k.kf0 = mp[PF_P_KF0]; k.kr0 = mp[PF_P_KR0]; k.numrec = mp[PF_P_NUMRECEPTORS];
   k.dxd = (double)s->dx; k.dtd = (double)s->dt; k.dxf = s->dx; k.dtf = s->dt; k.dtT = s->dt / mp[PF_P_T0];
+  k.inv_f0 = 1.0 / (double)k.f0;
   k.bond_model = s->bond_model; k.p_on = s->p_on; k.p_off = s->p_off; k.seed = s->seed;
   k.morse = s->morse;
   for (int a = 0; a < 4; ++a) { k.morse_intra[a] = s->morse_intra[a]; k.morse_inter[a] = s->morse_inter[a]; }

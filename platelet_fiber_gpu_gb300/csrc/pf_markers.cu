@@ -82,9 +82,9 @@ struct Stencil<float> {
   }
 };
 template <class R>
-__device__ __forceinline__ int axis_stencil(double x, float dxf, int n, int wrap, int spread, int node[5], int*,
-                                            R w[5]) {
-  return Stencil<R>::axis(x, dxf, 1.0 / (double)dxf, n, wrap, spread, node, w);
+__device__ __forceinline__ int axis_stencil(double x, float dxf, double inv, int n, int wrap, int spread, int node[5],
+                                            int*, R w[5]) {
+  return Stencil<R>::axis(x, dxf, inv, n, wrap, spread, node, w);
 }
 
 // One marker's force onto its stencil nodes (global atomics).
@@ -93,9 +93,9 @@ __device__ __forceinline__ void spread_one(const LatticeConst& lk, R4<R>* Fc, do
                                            R Fy, R Fz) {
   int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
   R wx[5], wy[5], wz[5];
-  const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 1, nxa, rx, wx);
-  const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 1, nya, ry, wy);
-  const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 1, nza, rz, wz);
+  const int cxn = axis_stencil<R>(x, lk.dxf, lk.inv_dx, lk.nx, lk.ibm_wrap[0], 1, nxa, rx, wx);
+  const int cyn = axis_stencil<R>(y, lk.dxf, lk.inv_dx, lk.ny, lk.ibm_wrap[1], 1, nya, ry, wy);
+  const int czn = axis_stencil<R>(z, lk.dxf, lk.inv_dx, lk.nz, 0, 1, nza, rz, wz);
   for (int c = 0; c < czn; ++c)
     for (int b = 0; b < cyn; ++b)
       for (int a = 0; a < cxn; ++a) {
@@ -110,9 +110,9 @@ __device__ __forceinline__ void interp_one(const LatticeConst& lk, const R4<R>* 
                                            R& ax, R& ay, R& az) {
   int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
   R wx[5], wy[5], wz[5];
-  const int cxn = axis_stencil<R>(x, lk.dxf, lk.nx, lk.ibm_wrap[0], 0, nxa, rx, wx);
-  const int cyn = axis_stencil<R>(y, lk.dxf, lk.ny, lk.ibm_wrap[1], 0, nya, ry, wy);
-  const int czn = axis_stencil<R>(z, lk.dxf, lk.nz, 0, 0, nza, rz, wz);
+  const int cxn = axis_stencil<R>(x, lk.dxf, lk.inv_dx, lk.nx, lk.ibm_wrap[0], 0, nxa, rx, wx);
+  const int cyn = axis_stencil<R>(y, lk.dxf, lk.inv_dx, lk.ny, lk.ibm_wrap[1], 0, nya, ry, wy);
+  const int czn = axis_stencil<R>(z, lk.dxf, lk.inv_dx, lk.nz, 0, 0, nza, rz, wz);
   ax = 0; ay = 0; az = 0;
   for (int c = 0; c < czn; ++c)
     for (int b = 0; b < cyn; ++b)
@@ -156,7 +156,7 @@ __device__ __forceinline__ void spread_one<float>(const LatticeConst& lk, R4<flo
                                                   double z, float Fx, float Fy, float Fz) {
   int nxa[4], nya[4], nza[4];
   float wx[4], wy[4], wz[4];
-  const double inv = 1.0 / (double)lk.dxf;
+  const double inv = lk.inv_dx;
   axis4(x, inv, lk.nx, lk.ibm_wrap[0], nxa, wx);
   axis4(y, inv, lk.ny, lk.ibm_wrap[1], nya, wy);
   axis4(z, inv, lk.nz, 0, nza, wz);
@@ -177,7 +177,7 @@ __device__ __forceinline__ void interp_one<float>(const LatticeConst& lk, const 
                                                   double z, float& ax, float& ay, float& az) {
   int nxa[4], nya[4], nza[4];
   float wx[4], wy[4], wz[4];
-  const double inv = 1.0 / (double)lk.dxf;
+  const double inv = lk.inv_dx;
   axis4(x, inv, lk.nx, lk.ibm_wrap[0], nxa, wx);
   axis4(y, inv, lk.ny, lk.ibm_wrap[1], nya, wy);
   axis4(z, inv, lk.nz, 0, nza, wz);
@@ -268,7 +268,7 @@ constexpr int kFlagR = 2;
 // neighbourhood still covers every in-range node the stencil can reach).
 __device__ __forceinline__ void mark_node(const LatticeConst& lk, unsigned* mark, double x, double y, double z,
                                           bool fp64) {
-  const double dxd = (double)lk.dxf, inv = 1.0 / dxd;
+  const double dxd = (double)lk.dxf, inv = lk.inv_dx;
   auto node = [&](double v, int n, int wrap) {
     const double f = floor(fp64 ? v / dxd : v * inv);
     const int i = f < -1e9 ? -1000000000 : (f > 1e9 ? 1000000000 : (int)f);
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(kBoxThreads) spread_box_k(LatticeConst lk, flo
   float* s_fr = reinterpret_cast<float*>(s_b + 3 * kBoxElems);      // [3][kBoxElems] fractions
   const int p = blockIdx.x, base = p * E;
   const bool staged = E <= kBoxElems;
-  const double inv = 1.0 / (double)lk.dxf;
+  const double inv = lk.inv_dx;
   // element forces (kept for the element output) and positions, thread per
   // element
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(kBoxThreads) interp_box_k(LatticeConst lk, Pla
   float* s_fr = reinterpret_cast<float*>(s_b + 3 * kBoxElems);      // [3][kBoxElems] fractions
   const int p = blockIdx.x, base = p * E;
   const bool staged = E <= kBoxElems;
-  const double inv = 1.0 / (double)lk.dxf;
+  const double inv = lk.inv_dx;
   if (!staged) {
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
       const int g = base + e;
@@ -1854,7 +1854,7 @@ __global__ void __launch_bounds__(128) morse_k(PlateletConst k, const double* X,
         }
       }
       if (valid && g >= 0 && g < PE) {
-        const double sc = 1.0 / (double)k.f0;
+        const double sc = k.inv_f0;
         Fm[g] = (double)ax * sc;
         Fm[PE + g] = (double)ay * sc;
         Fm[2 * PE + g] = (double)az * sc;
@@ -2100,7 +2100,7 @@ __device__ __forceinline__ void morse_platelet_k_body(const PlateletConst& k, co
     R sx = 0, sy = 0, sz = 0;
     for (int t = 0; t < kMorseSplit; ++t) { sx += s_part[t][0][lane]; sy += s_part[t][1][lane]; sz += s_part[t][2][lane]; }
     const int g = p * k.E + e;
-    const R sc = (R)(1.0 / (double)k.f0);
+    const R sc = (R)k.inv_f0;
     Fm[g] = (double)(sx * sc);
     Fm[PE + g] = (double)(sy * sc);
     Fm[2 * PE + g] = (double)(sz * sc);
@@ -2763,14 +2763,14 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
         Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
         detach_rate, seed, nullptr, nullptr, nullptr, nullptr);
-  else if (PE + M == 0 || !L.ibm_box)
+  else if (PE + M == 0 || !L.ibm_box) {
     interp_advance_k<float><<<grid, 128, 0, st>>>(
         L.k, pk, (const float4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
         Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
         detach_rate, seed, Pl ? (const float*)Pl->Fmem : nullptr, (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr,
         (Pl && Pl->k.nrec) ? (const float*)Pl->Fbond : nullptr, Pl ? Pl->Ftot : nullptr);
-  else {
+  } else {
     cudaFuncSetAttribute(interp_box_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBoxSmem);
     const int P = Pl ? Pl->k.P : 0, E = Pl ? Pl->k.E : 0;
     const unsigned g2 = (unsigned)(P + (M + kBoxFibrin - 1) / kBoxFibrin);
