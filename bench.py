@@ -127,16 +127,20 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def lbm_traffic_per_node():
-    """DRAM bytes per node-step of the LBM kernel from the committed ncu
-    capture summary (profiles/lbm_step_traffic.json), or None."""
-    p = ROOT / "profiles" / "lbm_step_traffic.json"
+def lattice_traffic(prec: int, kernel: str, nodes: int):
+    """DRAM bytes (read + write) of one step's lattice passes from the
+    committed full-size ncu capture (profiles/lattice_traffic.json), when it
+    was taken of the same kernels, precision and lattice; else None."""
+    p = ROOT / "profiles" / "lattice_traffic.json"
     if not p.exists():
         return None
     try:
-        return json.loads(p.read_text())
+        e = json.loads(p.read_text()).get(PREC_NAME[prec])
     except ValueError:
         return None
+    if not e or e.get("kernel") != kernel or e.get("nodes") != nodes:
+        return None
+    return e["dram_bytes_per_step"]
 
 
 def reduce_max(dist, x: float, device: str) -> float:
@@ -224,6 +228,54 @@ def workload_name(args):
             f"bond p_on/p_off 1e-2/1e-3 per step")
 
 
+def batched_served(args, gpu, plain_f32_mlups, fp16_scale):
+    """The metric's other parts, measured after the headline: the same
+    channel with FP16-shifted populations; the 64-job ensemble (32^3 ..
+    128x64x64 nodes, log-uniform; 1-8 platelets; 1k-5k fibrin nodes) as one
+    autotuned fused batch in FP32 and FP16; and the served loop (Poisson
+    arrivals, 20 jobs/s, requested steps U{500..5000}, 150 GB budget) over a
+    short arrival window, with p50 / p99 time to completion."""
+    import torch
+    from platelet_fiber_gpu_gb300 import serve
+    from platelet_fiber_gpu_gb300 import workloads as W
+    out = {}
+    scene = build_scene(args)
+    job = gpu.Job(scene, 2, fp16_scale)
+    job.step(args.warmup, graph=True)
+    st = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(st)
+    rc = job.step(args.steps, graph=True)
+    b.record(st)
+    torch.cuda.synchronize()
+    if rc != gpu.PFGPU_OK or job.steps != args.warmup + args.steps:
+        raise RuntimeError("FP16 channel run incomplete")
+    ms = a.elapsed_time(b) / args.steps
+    job.close()
+    out["single_f16"] = {"mlups": round(scene.n_nodes / (ms / 1e3) / 1e6, 1), "ms_per_step": round(ms, 4),
+                         "steps": args.steps}
+    scenes = [W.batch_job(3, i) for i in range(64)]
+    bt = {}
+    for prec in (1, 2):
+        r = serve.run_batched(prec, steps=args.batch_steps, scenes=scenes, chunk=50)
+        bt[PREC_NAME[prec]] = {"mlups": r["mlups"], "seconds": r["seconds"], "shape": r["shape"]}
+    bt["jobs"], bt["nodes"], bt["steps"] = 64, sum(sc.n_nodes for sc in scenes), args.batch_steps
+    bt["f16_over_f32"] = round(bt["f16-shifted"]["mlups"] / bt["f32"]["mlups"], 3)
+    out["batched"] = bt
+    sv = {}
+    for prec in (1, 2):
+        r = serve.run_served(prec, rate=20.0, duration=args.served_seconds, scenes=scenes[:32])
+        sv[PREC_NAME[prec]] = {k: r[k] for k in ("mlups", "latency_p50_s", "latency_p99_s", "jobs", "makespan_s",
+                                                  "mean_live_jobs")}
+    sv["rate_per_s"], sv["arrival_window_s"] = 20.0, args.served_seconds
+    out["served"] = sv
+    out["f16_batched_over_plain_f32"] = round(bt["f16-shifted"]["mlups"] / plain_f32_mlups, 3)
+    out["f16_served_over_plain_f32"] = round(sv["f16-shifted"]["mlups"] / plain_f32_mlups, 3)
+    out["target"] = "batched+served FP16-shifted >= 1.6x the plain FP32 channel's aggregate MLUPS"
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -240,6 +292,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--profile-steps", type=int, default=200)
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the FP16 single-channel, batched-ensemble and served runs")
+    ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--served-seconds", type=float, default=8.0)
     ap.add_argument("--workload", default="single_large", choices=["single_large", "plain_small"],
                     help="single_large (the 256x128x128 channel) or plain_small (the 64x32x32 body-force channel)")
     args = ap.parse_args()
@@ -281,7 +337,7 @@ def main():
     job = gpu.Job(scene, prec, fp16_scale)
     job.step(args.warmup, graph=True)
     launches = job.launches_per_step
-    lbm_kernel = "lbm_rows_k" if job.lbm_kernel == "rows" else "lbm_step_k"
+    lbm_kernel = job.lbm_kernel
     barrier_sync()
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
@@ -356,10 +412,7 @@ def main():
     peak, peak_kind = measured_peak()
     bpn = BYTES_PER_NODE[prec]
     achieved = N * bpn / (lbm_ms / 1e3) / 1e9
-    traffic = lbm_traffic_per_node()
-    traffic_per_launch = None
-    if traffic and traffic.get("precision") == prec and traffic.get("kernel", lbm_kernel) == lbm_kernel:
-        traffic_per_launch = traffic["dram_bytes_per_node"] * N
+    traffic_per_launch = lattice_traffic(prec, lbm_kernel, N)
 
     line = {
         "metric": "MLUPS (coupled LBM+IBM+SEM+fibrin step)",
@@ -389,6 +442,8 @@ def main():
         "clocks": clk,
         "gpu_launches": launches * args.steps,
     }
+    if rank == 0 and not args.no_batch and args.workload == "single_large":
+        line["batched_served"] = batched_served(args, gpu, value, fp16_scale)
     if rank == 0 and not args.no_cpu_baseline:
         small = build_scene(args)
         mlups, n, dt = cpu_oracle_rate(small, args.cpu_budget, 1000, os.cpu_count() or 1)

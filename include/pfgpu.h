@@ -179,9 +179,12 @@ int pfgpu_job_set_stop(pfgpu_job *job, int64_t stop_step);
 size_t pfgpu_job_device_bytes(const pfgpu_job *job);
 /* Kernel launches one coupled step issues (graph nodes). */
 int pfgpu_job_launches_per_step(const pfgpu_job *job);
-/* Which collide-stream kernel the job runs: "rows" (rows staged through
- * shared memory by bulk asynchronous copies; needs nx * sizeof(population)
- * to be a multiple of 16 bytes) or "direct" (per-node gathers). */
+/* Which collide-stream kernels the job runs: "lbm_rows_k" (rows staged
+ * through shared memory by bulk asynchronous copies; needs nx *
+ * sizeof(population) to be a multiple of 16 bytes), "lbm_vec_k+lbm_list_k"
+ * (FP32/FP16 without bounce-back faces: several x-nodes per thread with
+ * vector loads, the force bricks one node per thread) or
+ * "lbm_step_k+lbm_list_k" (one node per thread). */
 const char *pfgpu_job_lbm_kernel(const pfgpu_job *job);
 
 /* ---- element output dumps ----------------------------------------------

@@ -219,6 +219,8 @@ cudaError_t lattice_init(Lattice& L, const InitSource& src, cudaStream_t st);
 // picks the row-staged or the direct-gather step kernel (host only; call
 // before the first step and outside stream capture)
 cudaError_t lattice_configure(Lattice& L);
+// the kernels of the lattice passes this job runs (for reports)
+const char* lattice_pass_name(const Lattice& L);
 // part 0: the whole lattice; 1: bricks not flagged for this step's force
 // (may run while the forces are computed); 2: the flagged bricks (after the
 // spreading); 3: the far region of step far_step (near[] clear); 4: the

@@ -991,7 +991,7 @@ size_t pfgpu_job_device_bytes(const pfgpu_job* j) { return j ? j->bytes : 0; }
 int pfgpu_job_launches_per_step(const pfgpu_job* j) { return j ? j->launches_per_step : 0; }
 const char* pfgpu_job_lbm_kernel(const pfgpu_job* j) {
   if (!j) return "";
-  return j->L.rows_stages > 0 ? "rows" : "direct";
+  return lattice_pass_name(j->L);
 }
 void pfgpu_job_destroy(pfgpu_job* j) {
   if (j && j->s0) cudaStreamSynchronize(j->s0);

@@ -1572,6 +1572,14 @@ cudaError_t batch_launch_lattice(int kind, const BatchDesc* d, const int* start,
   return cudaErrorInvalidValue;
 }
 
+const char* lattice_pass_name(const Lattice& L) {
+  if (L.rows_stages > 0) return "lbm_rows_k";
+  int v = 0;
+  if (L.precision == PF_PREC_FP32) v = vec_width<float>(L);
+  else if (L.precision == PF_PREC_FP16) v = vec_width<__half>(L);
+  return v ? "lbm_vec_k+lbm_list_k" : "lbm_step_k+lbm_list_k";
+}
+
 cudaError_t lattice_configure(Lattice& L) {
   switch (L.precision) {
     case PF_PREC_FP64: rows_config<double, double>(L); return cudaSuccess;

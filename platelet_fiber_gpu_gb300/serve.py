@@ -26,8 +26,11 @@ from .gpu import Batch
 
 
 def run_batched(precision: int, n_jobs: int = 64, steps: int = 1000, seed: int = 3, budget: float = 150e9,
-                chunk: int = 100) -> dict:
-    scenes = [W.batch_job(seed, i) for i in range(n_jobs)]
+                chunk: int = 100, scenes=None) -> dict:
+    """`scenes`: the job set (default: n_jobs jobs of workloads.batch_job)."""
+    if scenes is None:
+        scenes = [W.batch_job(seed, i) for i in range(n_jobs)]
+    n_jobs = len(scenes)
     b = Batch(int(budget))
     slots = []
     for sc in scenes:

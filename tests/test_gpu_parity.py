@@ -210,7 +210,7 @@ def test_row_staged_and_direct_lbm_kernels_agree(gpu, scene, prec, tol, monkeypa
     a = gpu.Job(sc, prec)
     monkeypatch.delenv("PFGPU_LBM_KERNEL")
     b = gpu.Job(sc, prec)
-    assert a.lbm_kernel == "rows" and b.lbm_kernel == "direct"
+    assert a.lbm_kernel == "lbm_rows_k" and b.lbm_kernel != "lbm_rows_k"
     a.step(12)
     b.step(12)
     assert rel_max(a.lattice()["fIN"], b.lattice()["fIN"]) < tol
