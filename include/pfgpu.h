@@ -177,6 +177,17 @@ int64_t pfgpu_job_step_count(const pfgpu_job *job);
  * later one lets a job stopped this way run on. */
 int pfgpu_job_set_stop(pfgpu_job *job, int64_t stop_step);
 size_t pfgpu_job_device_bytes(const pfgpu_job *job);
+/* State snapshots, for checkpoint / resume, preemption and migration of
+ * served jobs (the reference keeps its state on the host between the copy
+ * calls, semLB.cu:154-296, 979-1000).  pfgpu_job_save writes the job's whole
+ * device state (every population, force and flag buffer, element, fibrin and
+ * bond state, the control block with the step counter) into `buf`, which
+ * holds pfgpu_job_state_bytes(job) bytes; pfgpu_job_restore loads a snapshot
+ * into a job created from a scene of the same sizes and precision and
+ * rejects any other with PFGPU_ERR_INVALID.  Both wait for the job's work. */
+size_t pfgpu_job_state_bytes(const pfgpu_job *job);
+int pfgpu_job_save(pfgpu_job *job, void *buf, size_t bytes);
+int pfgpu_job_restore(pfgpu_job *job, const void *buf, size_t bytes);
 /* Kernel launches one coupled step issues (graph nodes). */
 int pfgpu_job_launches_per_step(const pfgpu_job *job);
 /* Which collide-stream kernels the job runs: "lbm_rows_k" (rows staged
@@ -369,8 +380,9 @@ typedef struct pfgpu_uniform_source {
 } pfgpu_uniform_source;
 
 /* ------------------------------------------------------------ drop-in names
- * Signatures of semLB.cu:111, :154, :303, :534, :562, :597, :667, :705, :749,
- * :865, :441, :979, :1005 (host array layouts of gpuSEM_LB.c). */
+ * Signatures of semLB.cu:111, :154, :303, :534 (fluid), :749, :865, :441,
+ * :979, :1005 (SEM), :562, :609, :669, :708 (fibrin); host array layouts of
+ * gpuSEM_LB.c. */
 void *fluid_allocGPUKernel(void *model, float dt, float dx, int width, int height, int depth);
 void fluid_initGPUKernel(void *model, void *g, int aFlag, float *hostParameters, void **fIN, void **fOUT,
                          void *ux, void *uy, void *uz, void *rho, void *obstacle, void *Fx, void *Fy,
@@ -380,6 +392,11 @@ void fluid_releaseGPUKernel(void *model, void *g);
 
 void *sem_allocGPUKernel(void *model, int maxCells, int maxElements, int SurfElem, int newnode,
                          int numReceptorsPerElem, float dt, double S0_all, float *hostSEMparameters);
+/* node_share_Elem and N are accepted and not read: the node -> triangle
+ * lists are built from triElem, and nodal normals are recomputed from the
+ * positions each step.  The reference uploads both (semLB.cu:939-943) but
+ * its kernels read neither outside commented-out code (sem_kernel.cu:743,
+ * 856, 1513). */
 void sem_initGPUKernel(void *model, void *g, int numOfCells, int *numOfElements, int SurfElem,
                        int numReceptorsPerElem, void *hostX_Ref, void *hostY_Ref, void *hostZ_Ref,
                        void *hostX, void *hostY, void *hostRY, void *hostZ, void *hostVX, void *hostVY,

@@ -57,6 +57,7 @@ struct LatticeConst {
   double fp16_scale;  // sigma of the FP16 store
   float hs[3], hinv[3];  // w * sigma and 1 / (w * sigma) for w = 1/3, 1/18, 1/36 (FP16 store)
   float isig;            // 1 / sigma (FP16 store)
+  unsigned long long wait_ns;  // limit of a bounded device wait (1 s; PFGPU_WAIT_LIMIT_NS for tests)
   float dtT;          // dt / T0 (float, sem_kernel.cu:2106): position update factor
   // the float roundings of omega, kcoll, kmom, body, uw: reduced-precision
   // kernels read these instead of converting from double per thread (FP64

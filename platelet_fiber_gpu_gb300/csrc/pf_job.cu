@@ -69,6 +69,7 @@ struct pfgpu_job {
   uint64_t seed = 0;
   size_t bytes = 0;
   std::vector<void*> allocs;
+  std::vector<size_t> alloc_bytes;  // size of each allocation (the state snapshot's layout)
   int launches_per_step = 0;
 };
 
@@ -79,6 +80,7 @@ static cudaError_t dalloc(pfgpu_job* j, T** p, size_t count) {
   cudaError_t e = cudaMalloc((void**)p, bytes);
   if (e == cudaSuccess) {
     j->allocs.push_back(*p);
+    j->alloc_bytes.push_back(bytes);
     j->bytes += bytes;
     cudaMemset(*p, 0, bytes);
   }
@@ -173,6 +175,11 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
   }
   k.isig = (float)(1.0 / k.fp16_scale);
   k.inv_dx = 1.0 / (double)k.dxf;
+  // bounded device waits give up after 1 s; PFGPU_WAIT_LIMIT_NS shortens
+  // the limit (0: give up at the first unfinished wait) so that tests can
+  // run the give-up path
+  k.wait_ns = 1000000000ull;
+  if (const char* w = getenv("PFGPU_WAIT_LIMIT_NS")) k.wait_ns = strtoull(w, nullptr, 10);
   k.dtT = s->dt / mp[PF_P_T0];
   k.omega_f = (float)k.omega;
   k.kcoll_f = (float)k.kcoll;
@@ -989,6 +996,81 @@ int pfgpu_job_conservation(pfgpu_job* j, double out[4]) {
 
 size_t pfgpu_job_device_bytes(const pfgpu_job* j) { return j ? j->bytes : 0; }
 int pfgpu_job_launches_per_step(const pfgpu_job* j) { return j ? j->launches_per_step : 0; }
+// ------------------------------------------------------- state snapshots
+// A snapshot is the byte image of every device buffer of the job, in
+// allocation order, after a header: magic, format version, precision,
+// buffer count and each buffer's size.  Buffers hold the whole state
+// (populations of both parities, forces, moments, brick flags and lists,
+// occupancy, element and fibrin state, bonds and vWF slots, the control
+// block with the step counter and stop step), so a job restored from it
+// continues exactly as the saved one would.  A job only accepts a snapshot
+// of the same layout: created from the same scene sizes and precision.
+namespace {
+constexpr char kSnapMagic[8] = {'P', 'F', 'G', 'J', 'O', 'B', 'S', '1'};
+constexpr uint32_t kSnapVersion = 1;
+size_t snapshot_header_bytes(const pfgpu_job* j) { return 8 + 4 + 4 + 8 + 8 * j->allocs.size(); }
+}  // namespace
+
+size_t pfgpu_job_state_bytes(const pfgpu_job* j) {
+  if (!j) return 0;
+  size_t b = snapshot_header_bytes(j);
+  for (size_t n : j->alloc_bytes) b += n;
+  return b;
+}
+
+int pfgpu_job_save(pfgpu_job* j, void* buf, size_t bytes) {
+  if (!j || !buf) return set_error(PFGPU_ERR_INVALID, "pfgpu_job_save: NULL job or buffer");
+  if (bytes < pfgpu_job_state_bytes(j)) return set_error(PFGPU_ERR_INVALID, "pfgpu_job_save: buffer too small");
+  CK(cudaStreamSynchronize(j->s0));
+  unsigned char* p = static_cast<unsigned char*>(buf);
+  std::memcpy(p, kSnapMagic, 8);
+  const uint32_t ver = kSnapVersion, prec = (uint32_t)j->precision;
+  const uint64_t n = j->allocs.size();
+  std::memcpy(p + 8, &ver, 4);
+  std::memcpy(p + 12, &prec, 4);
+  std::memcpy(p + 16, &n, 8);
+  for (size_t i = 0; i < n; ++i) {
+    const uint64_t b = j->alloc_bytes[i];
+    std::memcpy(p + 24 + 8 * i, &b, 8);
+  }
+  size_t off = snapshot_header_bytes(j);
+  for (size_t i = 0; i < n; ++i) {
+    CK(cudaMemcpy(p + off, j->allocs[i], j->alloc_bytes[i], cudaMemcpyDeviceToHost));
+    off += j->alloc_bytes[i];
+  }
+  return PFGPU_OK;
+}
+
+int pfgpu_job_restore(pfgpu_job* j, const void* buf, size_t bytes) {
+  if (!j || !buf) return set_error(PFGPU_ERR_INVALID, "pfgpu_job_restore: NULL job or buffer");
+  const unsigned char* p = static_cast<const unsigned char*>(buf);
+  if (bytes < snapshot_header_bytes(j) || std::memcmp(p, kSnapMagic, 8) != 0)
+    return set_error(PFGPU_ERR_INVALID, "pfgpu_job_restore: not a job snapshot");
+  uint32_t ver = 0, prec = 0;
+  uint64_t n = 0;
+  std::memcpy(&ver, p + 8, 4);
+  std::memcpy(&prec, p + 12, 4);
+  std::memcpy(&n, p + 16, 8);
+  if (ver != kSnapVersion) return set_error(PFGPU_ERR_INVALID, "pfgpu_job_restore: snapshot format version differs");
+  if (prec != (uint32_t)j->precision || n != j->allocs.size())
+    return set_error(PFGPU_ERR_INVALID, "pfgpu_job_restore: snapshot of a job of another precision or layout");
+  for (size_t i = 0; i < n; ++i) {
+    uint64_t b = 0;
+    std::memcpy(&b, p + 24 + 8 * i, 8);
+    if (b != j->alloc_bytes[i])
+      return set_error(PFGPU_ERR_INVALID, "pfgpu_job_restore: snapshot of a job of other sizes");
+  }
+  if (bytes < pfgpu_job_state_bytes(j)) return set_error(PFGPU_ERR_INVALID, "pfgpu_job_restore: snapshot truncated");
+  CK(cudaStreamSynchronize(j->s0));
+  size_t off = snapshot_header_bytes(j);
+  for (size_t i = 0; i < n; ++i) {
+    CK(cudaMemcpy(j->allocs[i], p + off, j->alloc_bytes[i], cudaMemcpyHostToDevice));
+    off += j->alloc_bytes[i];
+  }
+  j->far_ready = false;
+  return PFGPU_OK;
+}
+
 const char* pfgpu_job_lbm_kernel(const pfgpu_job* j) {
   if (!j) return "";
   return lattice_pass_name(j->L);

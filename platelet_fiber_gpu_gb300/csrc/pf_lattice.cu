@@ -804,13 +804,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 // Wait for phase `parity` of a stage barrier: the waiting thread is
 // suspended in the barrier (up to kWaitSliceNs per try) instead of spinning;
-// false if the phase has not completed after kWaitLimitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
+// false if the phase has not completed after limit_ns (0: one test without
+// waiting, the test setting that makes the give-up path run).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, unsigned long long limit_ns) {
   if (mbar_try_wait(b, parity)) return true;
+  if (limit_ns == 0) return false;
   const unsigned long long t0 = global_ns();
   for (;;) {
     if (mbar_try_wait_hint(b, parity, kWaitSliceNs)) return true;
-    if (global_ns() - t0 > kWaitLimitNs) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* b) {
@@ -1005,24 +1007,25 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     const int nr = min(rpt, rows - r0);
     const unsigned fc = fc_next, fp = fp_next;
     flags_of(i + 1, fc_next, fp_next);
-    if (!mbar_wait(&s_full[s], (unsigned)((i / stages) & 1))) { failed = true; break; }
+    if (!mbar_wait(&s_full[s], (unsigned)((i / stages) & 1), k.wait_ns)) { failed = true; break; }
     if (has_node && rr0 < nr)
       node(sbuf + (size_t)s * Q * DS + H + rr0 * RS + x0, x0, r0 + rr0, s_info[s][rr0], fc, fp);
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&s_empty[s])) : "memory");
     if (warp == 0 && issued < my_tiles) {
       // stage s is free once every warp has arrived on its empty barrier
-      if (!mbar_wait(&s_empty[s], (unsigned)((i / stages) & 1))) { failed = true; break; }
+      if (!mbar_wait(&s_empty[s], (unsigned)((i / stages) & 1), k.wait_ns)) { failed = true; break; }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(issued++);
     }
   }
   if (failed) {
     if (lane == 0) atomicOr(&ctl->err, ERR_WAIT_TIMEOUT);
-    // let the copies this CTA issued land before it exits
-    // (tiles i .. issued-1 are the latest users of their stages)
+    // let the copies this CTA issued land before it exits (tiles
+    // i .. issued-1 are the latest users of their stages); always with the
+    // full limit, whatever the stage waits were given
     if (warp == 0)
-      for (int j = i; j < issued; ++j) mbar_wait(&s_full[j % stages], (unsigned)((j / stages) & 1));
+      for (int j = i; j < issued; ++j) mbar_wait(&s_full[j % stages], (unsigned)((j / stages) & 1), kWaitLimitNs);
     return;
   }
   if (bin_count) zero_bins(bin_count, ncells, ctl, (size_t)blockIdx.x * blockDim.x + threadIdx.x,

@@ -93,6 +93,10 @@ def lib():
         L.pfgpu_job_set_stop.argtypes = [vp, C.c_int64]
         L.pfgpu_batch_set_shape.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.pfgpu_batch_destroy.argtypes = [vp]
+        L.pfgpu_job_state_bytes.restype = C.c_size_t
+        L.pfgpu_job_state_bytes.argtypes = [vp]
+        L.pfgpu_job_save.argtypes = [vp, vp, C.c_size_t]
+        L.pfgpu_job_restore.argtypes = [vp, vp, C.c_size_t]
         L.pfgpu_host_alloc.restype = vp
         L.pfgpu_host_alloc.argtypes = [C.c_size_t]
         L.pfgpu_host_free.argtypes = [vp]
@@ -166,6 +170,18 @@ class Job:
     def step(self, n: int = 1, graph: bool = True) -> int:
         f = lib().pfgpu_job_step_graph if graph else lib().pfgpu_job_step
         return check(f(self.h, int(n)), allow_done=True)
+
+    def save(self) -> np.ndarray:
+        """Snapshot of the job's whole device state (pfgpu_job_save)."""
+        n = int(lib().pfgpu_job_state_bytes(self.h))
+        buf = np.empty(n, dtype=np.uint8)
+        check(lib().pfgpu_job_save(self.h, buf.ctypes.data_as(C.c_void_p), n))
+        return buf
+
+    def restore(self, snapshot: np.ndarray):
+        """Loads a snapshot of a job of the same scene sizes and precision."""
+        snap = np.ascontiguousarray(snapshot, dtype=np.uint8)
+        check(lib().pfgpu_job_restore(self.h, snap.ctypes.data_as(C.c_void_p), snap.nbytes))
 
     def set_stop(self, stop_step: int):
         """The job stops by itself after step stop_step (0: never): later

@@ -2,8 +2,19 @@
 driven the way the reference driver drives them (gpuSEM_LB.c:1285-1304,
 1433-1454): host arrays in the reference's layouts, per step
 sem_invokeGPUKernel_Force then fluid_invokeGPUKernel, then the copy calls.
-The result must match the golden vectors of the reference kernels as
-closely as the job API does (FP64)."""
+
+- FP64 (the default): the golden vectors of the reference kernels to 1e-13,
+  as closely as the job API.
+- node_share_Elem and N are accepted and not read (the reference uploads
+  them, semLB.cu:939-943, but its kernels use neither outside commented-out
+  code, sem_kernel.cu:743,856,1513): poisoned arrays give the same result.
+- FP32 handles (pfgpu_set_default_precision): the golden vectors within the
+  FP32 tolerances of the job API's own golden test.
+- A fibrin handle in the reference's tmp_fiber_GPUgrids layouts
+  (GPUDefines.h:170-200: NodeType, N_Conn_at_Node, Link_at_Node padded with
+  -100, lAdjVer, linkLengths0), attached to the fluid handle: fibrin and
+  element positions equal the job API's and the oracle's for the same scene.
+"""
 import ctypes as C
 from pathlib import Path
 
@@ -37,6 +48,13 @@ def lib():
     L.sem_invokeGPUKernel_Force.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), vp, C.c_double]
     L.sem_copyGPUKernel.argtypes = [vp, vp] + [vp] * 10 + [C.c_int]
     L.sem_releaseGPUKernel.argtypes = [vp, vp]
+    L.fiber_allocGPUKernel.restype = vp
+    L.fiber_allocGPUKernel.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp]
+    L.fiber_init_GPUKernel.argtypes = [vp, vp] + [vp] * 19
+    L.fiber_copy_GPUKernel.argtypes = [vp, vp] + [vp] * 12
+    L.fiber_release_GPUKernel.argtypes = [vp, vp]
+    L.pfgpu_fluid_attach_fiber.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double]
+    L.pfgpu_set_default_precision.argtypes = [C.c_int, C.c_double]
     return L
 
 
@@ -44,12 +62,35 @@ def _ptr(a):
     return a.ctypes.data_as(vp)
 
 
-def test_reference_api_reproduces_golden(lib):
+def _fiber_arrays(sc):
+    """The scene's fibrin mesh in tmp_fiber_GPUgrids host layouts; each
+    node's links in the order of the scene's own neighbour lists."""
+    links = np.asarray(sc.meta["fib_links"], dtype=np.int32)
+    M, L = sc.n_fib, len(links)
+    per = [[] for _ in range(M)]
+    for l, (a, b) in enumerate(links):
+        per[a].append(l)
+        per[b].append(l)
+    K = max(len(p) for p in per)
+    lan = np.full((M, K), -100, dtype=np.int32)
+    for m, p in enumerate(per):
+        lan[m, :len(p)] = p
+    nconn = np.array([len(p) for p in per], dtype=np.int32)
+    l0 = np.zeros(L)
+    ptr, nbr, csr_l0 = sc.fib_ptr, sc.fib_nbr, sc.fib_L0
+    for m in range(M):
+        for q, l in zip(range(ptr[m], ptr[m + 1]), per[m]):
+            a, b = links[l]
+            assert nbr[q] == (b if a == m else a)
+            l0[l] = csr_l0[q]
+    return dict(M=M, L=L, K=K, type=np.ascontiguousarray(sc.fib_fixed, dtype=np.int32), nconn=nconn, lan=lan,
+                adj=np.ascontiguousarray(links), l0=l0)
+
+
+def drive(lib, sc, n, poison=False, fiber=False):
+    """Runs `sc` for n steps through the reference entry points; returns
+    the downloaded lattice, elements and (with fiber) fibrin state."""
     from platelet_fiber_gpu_gb300 import mesh as M
-    from platelet_fiber_gpu_gb300.scene import scene_from_dict
-    d = np.load(GOLDEN / "ref_wall.npz")
-    sc = scene_from_dict(d)
-    n = int(d["nsteps"])
     N, E, T, NN = sc.n_nodes, sc.n_elem, sc.n_tri, sc.n_node
     R = sc.n_rec // T
     params = np.ascontiguousarray(sc.params, dtype=np.float32)
@@ -80,8 +121,12 @@ def test_reference_api_reproduces_golden(lib):
     tri = np.ascontiguousarray(sc.tri, dtype=np.int32)
     r1 = np.ascontiguousarray(np.asarray(sc.rec_r1, dtype=np.float32).reshape(T, R))
     r2 = np.ascontiguousarray(np.asarray(sc.rec_r2, dtype=np.float32).reshape(T, R))
-    share = -np.ones((NN, 10), dtype=np.int32)
-    Nn = np.zeros((NN, 3))
+    if poison:
+        share = np.full((NN, 10), 123456789, dtype=np.int32)
+        Nn = np.full((NN, 3), np.nan)
+    else:
+        share = -np.ones((NN, 10), dtype=np.int32)
+        Nn = np.zeros((NN, 3))
     ntri = np.ascontiguousarray(sc.node_ntri, dtype=np.int32)
     ring = np.zeros((E, 10), dtype=np.int32)
     ring[:sc.n_membrane] = sc.ring
@@ -94,6 +139,19 @@ def test_reference_api_reproduces_golden(lib):
                           _ptr(Z), *[_ptr(a) for a in zeros], _ptr(etype), _ptr(bonds), _ptr(tri), _ptr(r1),
                           _ptr(r2), _ptr(share), _ptr(Nn), _ptr(ntri), _ptr(ring), _ptr(S0), float(sc.V0[0]),
                           _ptr(rb), _ptr(rnd))
+    fg = None
+    if fiber:
+        fa = _fiber_arrays(sc)
+        Mf = fa["M"]
+        fx, fy, fz = (np.ascontiguousarray(np.asarray(a, dtype=np.float64)) for a in (sc.fib_X, sc.fib_Y, sc.fib_Z))
+        z3 = [np.zeros(Mf) for _ in range(9)]
+        fg = lib.fiber_allocGPUKernel(None, Mf, fa["L"], fa["K"], float(sc.dt), None)
+        assert fg
+        lib.fiber_init_GPUKernel(None, fg, _ptr(fa["type"]), _ptr(fa["nconn"]), _ptr(fa["lan"]), _ptr(fa["adj"]),
+                                 _ptr(fa["l0"]), _ptr(fa["l0"]), _ptr(fa["l0"]), _ptr(fx), _ptr(z3[0]), _ptr(fx),
+                                 _ptr(z3[1]), _ptr(fy), _ptr(fy), _ptr(z3[2]), _ptr(z3[3]), _ptr(fz), _ptr(fz),
+                                 _ptr(z3[4]), _ptr(z3[5]))
+        assert lib.pfgpu_fluid_attach_fiber(g, fg, int(sc.fib_law), float(sc.fib_k), float(sc.fib_mass)) == 0
     src = UniformSource(sc.seed)
     done, totalT = C.c_int(0), C.c_int(0)
     for _ in range(n):
@@ -104,14 +162,84 @@ def test_reference_api_reproduces_golden(lib):
                             _ptr(Fx), _ptr(Fy), _ptr(Fz), _ptr(vwf))
     out = [np.zeros(E) for _ in range(10)]
     lib.sem_copyGPUKernel(None, s, *[_ptr(a) for a in out], n)
-    fIN = np.stack(fin).reshape(d["out.fIN"].shape)
-    rel = np.abs(fIN - d["out.fIN"]).max() / np.abs(d["out.fIN"]).max()
-    assert rel < 1e-13
-    u_ref = np.stack([d["out.ux"], d["out.uy"], d["out.uz"]]).reshape(3, -1)
-    u_got = np.stack([ux, uy, uz])
-    assert np.linalg.norm(u_got - u_ref) / np.linalg.norm(u_ref) < 1e-10
-    for got, key in zip(out[:4], ("X", "Y", "RY", "Z")):
-        assert np.abs(got - d[f"out.{key}"].reshape(-1)).max() < 1e-13
-    np.testing.assert_array_equal(vwf, d["out.vwf"])
+    res = dict(fIN=np.stack(fin), u=np.stack([ux, uy, uz]), rho=rho, X=out[0], Y=out[1], RY=out[2], Z=out[3],
+               vwf=vwf)
+    if fiber:
+        fo = [np.zeros(Mf) for _ in range(12)]
+        lib.fiber_copy_GPUKernel(None, fg, *[_ptr(a) for a in fo])
+        res["fib"] = dict(X=fo[0], VX=fo[1], FX=fo[3], Y=fo[4], Z=fo[8], FY=fo[7], FZ=fo[11])
+        lib.fiber_release_GPUKernel(None, fg)
     lib.sem_releaseGPUKernel(None, s)
     lib.fluid_releaseGPUKernel(None, g)
+    return res
+
+
+def _golden():
+    from platelet_fiber_gpu_gb300.scene import scene_from_dict
+    d = np.load(GOLDEN / "ref_wall.npz")
+    return scene_from_dict(d), int(d["nsteps"]), d
+
+
+@pytest.mark.parametrize("poison", [False, True], ids=["plain", "poisoned_share_and_N"])
+def test_reference_api_reproduces_golden(lib, poison):
+    sc, n, d = _golden()
+    r = drive(lib, sc, n, poison=poison)
+    fIN = r["fIN"].reshape(d["out.fIN"].shape)
+    assert np.abs(fIN - d["out.fIN"]).max() / np.abs(d["out.fIN"]).max() < 1e-13
+    u_ref = np.stack([d["out.ux"], d["out.uy"], d["out.uz"]]).reshape(3, -1)
+    assert np.linalg.norm(r["u"] - u_ref) / np.linalg.norm(u_ref) < 1e-10
+    for key in ("X", "Y", "RY", "Z"):
+        assert np.abs(r[key] - d[f"out.{key}"].reshape(-1)).max() < 1e-13
+    np.testing.assert_array_equal(r["vwf"], d["out.vwf"])
+
+
+def test_reference_api_fp32_handles(lib):
+    """pfgpu_set_default_precision(PF_PREC_FP32): later fluid handles run the
+    FP32 store; the golden vectors within the FP32 tolerances (velocity
+    relative L2 1e-4 after the fixture's steps, positions 1e-7), vWF slots
+    bit for bit."""
+    sc, n, d = _golden()
+    assert lib.pfgpu_set_default_precision(1, 0.0) == 0
+    try:
+        r = drive(lib, sc, n)
+    finally:
+        lib.pfgpu_set_default_precision(0, 0.0)
+    u_ref = np.stack([d["out.ux"], d["out.uy"], d["out.uz"]]).reshape(3, -1)
+    assert np.linalg.norm(r["u"] - u_ref) / np.linalg.norm(u_ref) < 1e-4
+    pos = np.stack([r["X"], r["Y"], r["Z"]])
+    pos_ref = np.stack([d["out.X"], d["out.Y"], d["out.Z"]]).reshape(3, -1)
+    assert np.linalg.norm(pos - pos_ref) / np.linalg.norm(pos_ref) < 1e-7
+    np.testing.assert_array_equal(r["vwf"], d["out.vwf"])
+
+
+def test_reference_api_with_fibrin_handle(lib):
+    """The golden channel with a 60-node / 120-link Hookean fibrin mesh on
+    the bottom wall, driven through fiber_allocGPUKernel ->
+    fiber_init_GPUKernel -> pfgpu_fluid_attach_fiber -> per-step invokes ->
+    fiber_copy_GPUKernel: the same state as the job API and the oracle."""
+    from oracle import binding as ob
+    from platelet_fiber_gpu_gb300 import gpu
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc, _, _ = _golden()
+    W._fibrin(sc, 60, 120, 3 * sc.dx, np.random.default_rng(11), 0.5)
+    n = 12
+    r = drive(lib, sc, n, fiber=True)
+    j = gpu.Job(sc, 0)
+    j.step(n)
+    Fj, Ej, Lj = j.fibrin(), j.elements(), j.lattice()
+    j.close()
+    o = ob.Oracle(sc)
+    o.step(n)
+    Fo, Eo = o.fibrin(), o.elements()
+    o.close()
+    assert sc.fib_fixed.any() and not sc.fib_fixed.all()
+    for ref in (Fj, Fo):
+        for k in ("X", "Y", "Z"):
+            assert np.abs(r["fib"][k] - ref[k]).max() < 1e-12
+    assert np.abs(r["fib"]["X"] - sc.fib_X).max() > 0  # the free nodes moved
+    for k in ("X", "Y", "Z"):
+        assert np.abs(r[k] - Ej[k]).max() < 1e-12
+        assert np.abs(r[k] - Eo[k]).max() < 1e-12
+    assert np.abs(r["fIN"] - Lj["fIN"]).max() / np.abs(Lj["fIN"]).max() < 1e-12
+    fF = np.stack([r["fib"]["FX"], r["fib"]["FY"], r["fib"]["FZ"]])
+    assert np.linalg.norm(fF - Fj["F"]) <= 1e-9 * np.linalg.norm(Fj["F"])
