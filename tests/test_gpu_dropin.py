@@ -96,14 +96,15 @@ def drive(lib, sc, n, poison=False, fiber=False):
     params = np.ascontiguousarray(sc.params, dtype=np.float32)
     pf = params.ctypes.data_as(C.POINTER(C.c_float))
     # fluid handle: fIN/fOUT as 19 separate [lz][ly][lx] buffers
-    f = np.ascontiguousarray(np.asarray(sc.f_init, dtype=np.float64).reshape(19, N))
-    fin = [np.ascontiguousarray(f[k]) for k in range(19)]
+    # the caller's own arrays (copies: the download writes into them)
+    f = np.array(np.asarray(sc.f_init, dtype=np.float64).reshape(19, N))
+    fin = [np.array(f[k]) for k in range(19)]
     fout = [np.zeros(N) for _ in range(19)]
     fin_p = (vp * 19)(*[_ptr(a) for a in fin])
     fout_p = (vp * 19)(*[_ptr(a) for a in fout])
     u = np.asarray(sc.u_init, dtype=np.float64).reshape(3, N)
-    ux, uy, uz = (np.ascontiguousarray(u[k]) for k in range(3))
-    rho = np.ascontiguousarray(np.asarray(sc.rho_init, dtype=np.float64).reshape(N))
+    ux, uy, uz = (np.array(u[k]) for k in range(3))
+    rho = np.array(np.asarray(sc.rho_init, dtype=np.float64).reshape(N))
     obst = np.zeros(N, dtype=np.float32)
     Fx, Fy, Fz = np.zeros(N), np.zeros(N), np.zeros(N)
     vwf = -np.ones((4, sc.ny, sc.nx), dtype=np.int32)
