@@ -215,8 +215,15 @@ int pfgpu_output_open(pfgpu_job *job, const char *dir, int mode, pfgpu_output **
 /* Appends one frame at the job's current step: positions to cellsPos.data
  * and a row per element to each table (gpuSEM_LB.c:1464-1494). */
 int pfgpu_output_frame(pfgpu_output *out);
+/* The same files from the caller's host arrays, as the reference driver
+ * writes them after sem_copyGPUKernel: X, RY, Z [P * E] and V, F [3][P * E]
+ * (platelet-major, the job API's layout); each frame names its step. */
+int pfgpu_output_open_arrays(const char *dir, int mode, int P, int E, double dt, const double *X, const double *RY,
+                             const double *Z, const double *V, const double *F, pfgpu_output **out);
+int pfgpu_output_frame_arrays(pfgpu_output *out, long long step, const double *X, const double *RY, const double *Z,
+                              const double *V, const double *F);
 /* Appends "<step * dt>, <seed>" to cellsPauseTime.dat (gpuSEM_LB.c:1533)
- * and closes the files. */
+ * and closes the files (step: the job's, or the last frame's). */
 int pfgpu_output_close(pfgpu_output *out, int seed);
 /* The reference driver's writeVTK (gpuSEM_LB.c:1631-1709, outputSave at
  * :1618): <directory>/<filename>_<t, 7 digits>.vti, VTK ImageData with ASCII

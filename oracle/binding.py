@@ -79,6 +79,8 @@ def lib():
         L.pfo_ibm_phi.restype = C.c_double
         L.pfo_ibm_phi.argtypes = [C.c_double]
         L.pfo_feq.argtypes = [C.c_double, dp, C.c_double, dp]
+        L.pfo_wlc_force.restype = C.c_double
+        L.pfo_wlc_force.argtypes = [C.c_double, C.c_double, C.c_double]
         _lib = L
     return _lib
 
@@ -192,3 +194,8 @@ class Oracle:
         nc = np.zeros(3, dtype=np.int32)
         lib().pfo_get_cells(self.h, _p(cell_of, C.c_int), _p(order, C.c_int), _p(nc, C.c_int))
         return cell_of, order, nc
+
+
+def wlc_force(l0: float, l: float, mass: float) -> float:
+    """The oracle's worm-like-chain link force (fiber.cpp:710-733)."""
+    return float(lib().pfo_wlc_force(l0, l, mass))

@@ -743,6 +743,7 @@ static double wlc_force(double l0, double l, double mass) {
   double IP1 = 0.25 * 1.0 / (tl * tl) - 0.25 + (l - l0) / l0;
   return -CC * IP1 / mass;
 }
+double pfo_wlc_force(double l0, double l, double mass) { return wlc_force(l0, l, mass); }
 static void fibrin_forces(pfo_sim *s) {
 #pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int ni = 0; ni < s->M; ++ni) {

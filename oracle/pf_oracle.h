@@ -41,6 +41,8 @@ long long pfo_step_count(const pfo_sim *s);
 /* Philox-4x32-10 uniforms of the injected receptor/detach streams. */
 void pfo_receptor_uniforms(uint64_t seed, int64_t step, int64_t receptor, double out[2]);
 double pfo_detach_uniform(uint64_t seed, int64_t step);
+/* the worm-like-chain link force law (fiber.cpp:710-733) */
+double pfo_wlc_force(double l0, double l, double mass);
 void pfo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 /* Single-operator entry points used by known-answer tests. */

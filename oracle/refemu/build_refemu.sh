@@ -18,3 +18,13 @@ g++ -O2 -std=c++17 -fPIC -shared -w -fno-fast-math -ffp-contract=off \
     -x c++ -I"$HERE/stub" -I"$HERE" -I"$REF_DIR" \
     "$HERE/refemu.cpp" -o "$OUT/librefemu.so"
 echo "built $OUT/librefemu.so"
+# the driver's host code with stub GPU entry points (refhost_driver.c)
+gcc -O1 -std=gnu11 -fPIC -shared -w -fno-fast-math -ffp-contract=off \
+    -I"$HERE/stub" -I"$HERE" -I"$REF_DIR" \
+    "$HERE/refhost_driver.c" -o "$OUT/librefhost_driver.so" -lm
+echo "built $OUT/librefhost_driver.so"
+# the fibrin code's worm-like-chain law (refhost_fiber.cpp)
+g++ -O1 -std=c++17 -fPIC -shared -w -fno-fast-math -ffp-contract=off \
+    -I"$HERE/stub" -I"$HERE" -I"$REF_DIR" \
+    "$HERE/refhost_fiber.cpp" "$REF_DIR/network.cpp" -o "$OUT/librefhost_fiber.so"
+echo "built $OUT/librefhost_fiber.so"

@@ -25,7 +25,8 @@
 extern "C" void pfgpu_job_elem_dims_(const pfgpu_job* j, int* P, int* E, double* dt);
 
 struct pfgpu_output {
-  pfgpu_job* job = nullptr;
+  pfgpu_job* job = nullptr;  // NULL: the caller hands the arrays to every frame
+  long long step = 0;        // the last frame's step (arrays mode)
   int mode = PFGPU_OUT_FP64;
   int P = 0, E = 0;
   double dt = 0;
@@ -64,6 +65,60 @@ bool put4(const pfgpu_output* o, FILE* fp, double a, double b, double c) {
 
 }  // namespace
 
+namespace {
+int open_files(pfgpu_output* o, const char* dir) {
+  for (int i = 0; i < 7; ++i) {
+    const std::string path = std::string(dir) + "/" + kNames[i];
+    o->f[i] = fopen(path.c_str(), i == kPause ? "a+" : "wb+");
+    if (!o->f[i]) {
+      close_all(o);
+      return pf::report_error(PFGPU_ERR_INVALID, ("pfgpu_output_open: cannot open " + path).c_str());
+    }
+  }
+  return PFGPU_OK;
+}
+// initial frame (gpuSEM_LB.c:1376-1407): all three binaries, timestep 0
+bool write_initial(pfgpu_output* o) {
+  const size_t PE = (size_t)o->P * o->E;
+  for (int i = kPosA; i <= kForceA; ++i) fprintf(o->f[i], "Timestep       ElemID        X         Y         Z\n");
+  bool ok = true;
+  for (int p = 0; p < o->P; ++p)
+    for (int e = 0; e < o->E; ++e) {
+      const size_t g = (size_t)p * o->E + e;
+      ok = ok && put4(o, o->f[kPos], o->X[g], o->RY[g], o->Z[g]);
+      fprintf(o->f[kPosA], "0      %d    %e   %e   %e\n ", e, o->X[g], o->RY[g], o->Z[g]);
+      ok = ok && put4(o, o->f[kVel], o->V[g], o->V[PE + g], o->V[2 * PE + g]);
+      fprintf(o->f[kVelA], "0      %d    %e   %e   %e\n ", e, o->V[g], o->V[PE + g], o->V[2 * PE + g]);
+      ok = ok && put4(o, o->f[kForce], o->F[g], o->F[PE + g], o->F[2 * PE + g]);
+      fprintf(o->f[kForceA], "0      %d    %e   %e   %e\n ", e, o->F[g], o->F[PE + g], o->F[2 * PE + g]);
+    }
+  return ok;
+}
+// gpuSEM_LB.c:1464-1494: positions to the binary dump, all three tables
+bool write_frame(pfgpu_output* o, long long t) {
+  const size_t PE = (size_t)o->P * o->E;
+  bool ok = true;
+  for (int p = 0; p < o->P; ++p)
+    for (int e = 0; e < o->E; ++e) {
+      const size_t g = (size_t)p * o->E + e;
+      ok = ok && put4(o, o->f[kPos], o->X[g], o->RY[g], o->Z[g]);
+      fprintf(o->f[kPosA], "%lld      %d  %e  %e  %e\n ", t, e, o->X[g], o->RY[g], o->Z[g]);
+      fprintf(o->f[kVelA], "%lld      %d  %e  %e  %e\n ", t, e, o->V[g], o->V[PE + g], o->V[2 * PE + g]);
+      fprintf(o->f[kForceA], "%lld      %d  %e  %e  %e\n ", t, e, o->F[g], o->F[PE + g], o->F[2 * PE + g]);
+    }
+  for (int i = 0; i < 6; ++i) fflush(o->f[i]);
+  return ok;
+}
+void take(pfgpu_output* o, const double* X, const double* RY, const double* Z, const double* V, const double* F) {
+  const size_t PE = (size_t)o->P * o->E;
+  o->X.assign(X, X + PE);
+  o->RY.assign(RY, RY + PE);
+  o->Z.assign(Z, Z + PE);
+  o->V.assign(V, V + 3 * PE);
+  o->F.assign(F, F + 3 * PE);
+}
+}  // namespace
+
 extern "C" {
 
 int pfgpu_output_open(pfgpu_job* job, const char* dir, int mode, pfgpu_output** out) {
@@ -77,66 +132,63 @@ int pfgpu_output_open(pfgpu_job* job, const char* dir, int mode, pfgpu_output** 
   const size_t PE = (size_t)o->P * o->E;
   o->X.resize(PE); o->Y.resize(PE); o->RY.resize(PE); o->Z.resize(PE);
   o->V.resize(3 * PE); o->F.resize(3 * PE);
-  for (int i = 0; i < 7; ++i) {
-    const std::string path = std::string(dir) + "/" + kNames[i];
-    o->f[i] = fopen(path.c_str(), i == kPause ? "a+" : "wb+");
-    if (!o->f[i]) {
-      close_all(o);
-      delete o;
-      return pf::report_error(PFGPU_ERR_INVALID, ("pfgpu_output_open: cannot open " + path).c_str());
-    }
-  }
-  int rc = fetch(o);
+  int rc = open_files(o, dir);
+  if (rc == PFGPU_OK) rc = fetch(o);
+  if (rc == PFGPU_OK && !write_initial(o)) rc = pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_open: write failed");
   if (rc) {
     close_all(o);
     delete o;
     return rc;
   }
-  // initial frame (gpuSEM_LB.c:1376-1407): all three binaries, timestep 0
-  for (int i = kPosA; i <= kForceA; ++i) fprintf(o->f[i], "Timestep       ElemID        X         Y         Z\n");
-  bool ok = true;
-  for (int p = 0; p < o->P; ++p)
-    for (int e = 0; e < o->E; ++e) {
-      const size_t g = (size_t)p * o->E + e;
-      ok = ok && put4(o, o->f[kPos], o->X[g], o->RY[g], o->Z[g]);
-      fprintf(o->f[kPosA], "0      %d    %e   %e   %e\n ", e, o->X[g], o->RY[g], o->Z[g]);
-      ok = ok && put4(o, o->f[kVel], o->V[g], o->V[PE + g], o->V[2 * PE + g]);
-      fprintf(o->f[kVelA], "0      %d    %e   %e   %e\n ", e, o->V[g], o->V[PE + g], o->V[2 * PE + g]);
-      ok = ok && put4(o, o->f[kForce], o->F[g], o->F[PE + g], o->F[2 * PE + g]);
-      fprintf(o->f[kForceA], "0      %d    %e   %e   %e\n ", e, o->F[g], o->F[PE + g], o->F[2 * PE + g]);
-    }
-  if (!ok) {
+  *out = o;
+  return PFGPU_OK;
+}
+
+int pfgpu_output_open_arrays(const char* dir, int mode, int P, int E, double dt, const double* X, const double* RY,
+                             const double* Z, const double* V, const double* F, pfgpu_output** out) {
+  if (!dir || !out || (mode != PFGPU_OUT_FP64 && mode != PFGPU_OUT_FP32) || P < 0 || E < 0 || !X || !RY || !Z ||
+      !V || !F)
+    return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_open_arrays: bad arguments");
+  *out = nullptr;
+  pfgpu_output* o = new pfgpu_output;
+  o->mode = mode;
+  o->P = P;
+  o->E = E;
+  o->dt = dt;
+  take(o, X, RY, Z, V, F);
+  int rc = open_files(o, dir);
+  if (rc == PFGPU_OK && !write_initial(o))
+    rc = pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_open_arrays: write failed");
+  if (rc) {
     close_all(o);
     delete o;
-    return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_open: write failed");
+    return rc;
   }
   *out = o;
   return PFGPU_OK;
 }
 
 int pfgpu_output_frame(pfgpu_output* o) {
-  if (!o) return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_frame: NULL handle");
+  if (!o || !o->job) return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_frame: NULL or arrays-mode handle");
   int rc = fetch(o);
   if (rc) return rc;
   const long long t = (long long)pfgpu_job_step_count(o->job);
-  const size_t PE = (size_t)o->P * o->E;
-  bool ok = true;
-  // gpuSEM_LB.c:1464-1494: positions to the binary dump, all three tables
-  for (int p = 0; p < o->P; ++p)
-    for (int e = 0; e < o->E; ++e) {
-      const size_t g = (size_t)p * o->E + e;
-      ok = ok && put4(o, o->f[kPos], o->X[g], o->RY[g], o->Z[g]);
-      fprintf(o->f[kPosA], "%lld      %d  %e  %e  %e\n ", t, e, o->X[g], o->RY[g], o->Z[g]);
-      fprintf(o->f[kVelA], "%lld      %d  %e  %e  %e\n ", t, e, o->V[g], o->V[PE + g], o->V[2 * PE + g]);
-      fprintf(o->f[kForceA], "%lld      %d  %e  %e  %e\n ", t, e, o->F[g], o->F[PE + g], o->F[2 * PE + g]);
-    }
-  for (int i = 0; i < 6; ++i) fflush(o->f[i]);
-  return ok ? PFGPU_OK : pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_frame: write failed");
+  return write_frame(o, t) ? PFGPU_OK : pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_frame: write failed");
+}
+
+int pfgpu_output_frame_arrays(pfgpu_output* o, long long step, const double* X, const double* RY, const double* Z,
+                              const double* V, const double* F) {
+  if (!o || o->job || !X || !RY || !Z || !V || !F)
+    return pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_frame_arrays: bad arguments");
+  take(o, X, RY, Z, V, F);
+  o->step = step;
+  return write_frame(o, step) ? PFGPU_OK
+                              : pf::report_error(PFGPU_ERR_INVALID, "pfgpu_output_frame_arrays: write failed");
 }
 
 int pfgpu_output_close(pfgpu_output* o, int seed) {
   if (!o) return PFGPU_OK;
-  const long long t = (long long)pfgpu_job_step_count(o->job);
+  const long long t = o->job ? (long long)pfgpu_job_step_count(o->job) : o->step;
   // totalT * dt in the reference: int times float, in float
   fprintf(o->f[kPause], "%e, %d\n", (double)((float)t * (float)o->dt), seed);
   close_all(o);

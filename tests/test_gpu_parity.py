@@ -382,3 +382,24 @@ def test_invalid_scene_rejected_on_host(gpu):
     with pytest.raises(gpu.PfgpuError) as e:
         gpu.Job(sc, 1)
     assert e.value.code == 1
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
+def test_worm_like_chain_fibrin_vs_oracle(gpu, prec):
+    """Fibrin links under the worm-like-chain law (fiber.cpp:710-733, pinned
+    to the reference's own function in test_host_pins.py): FP64 link forces
+    and positions as the oracle's; FP32 positions within the FP32 bound (its
+    forces lose digits where 0.25/tl^2 - 0.25 cancels near the rest length)."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small()
+    sc.fib_law = 1
+    sc.fib_mass = 1e-6
+    r = _run_both(gpu, sc, 20, prec)
+    if prec == 0:
+        assert rel_l2(r["Fg"]["F"], r["Fo"]["F"]) < 1e-9
+        assert np.abs(r["Fg"]["X"] - r["Fo"]["X"]).max() < 1e-12
+    else:
+        pos = np.stack([r["Fg"]["X"], r["Fg"]["Y"], r["Fg"]["Z"]])
+        pos_o = np.stack([r["Fo"]["X"], r["Fo"]["Y"], r["Fo"]["Z"]])
+        assert rel_l2(pos, pos_o) < 1e-7
+    assert np.abs(r["Fo"]["F"]).max() > 0
