@@ -178,19 +178,27 @@ def poisson_disk(n: int, lo, hi, rmin: float, rng, fixed_z=None, n_fixed=0, max_
 
 # ---------------------------------------------------------------- workloads
 def reference_case(seed: int = 7, nx=16, ny=20, nz=10, level=1, R=2, center=None,
-                   kf0=3.0e4, kr0=1.5e4) -> Scene:
+                   kf0=3.0e4, kr0=1.5e4, mesh=None) -> Scene:
     """The reference's own path at test size (bond rates stressed so that
-    binding happens within tens of steps)."""
+    binding happens within tens of steps).  `mesh`: (vertices, triangles)
+    of the platelet surface, e.g. the reference's own NEU mesh; default a
+    level-`level` icosphere ellipsoid 0.6 x 0.6 x 0.3 um."""
     rng = np.random.default_rng(seed)
-    v, t = M.ellipsoid_icosphere(level, axes=(0.6, 0.6, 0.3))
-    tpl = PlateletTemplate(v, t, 0, seed, (0.6, 0.6, 0.3))
+    if mesh is None:
+        v, t = M.ellipsoid_icosphere(level, axes=(0.6, 0.6, 0.3))
+        half_z = 0.3
+    else:
+        v, t = np.asarray(mesh[0], dtype=np.float64), np.asarray(mesh[1], dtype=np.int32)
+        half_z = float(0.5 * (v[:, 2].max() - v[:, 2].min()))
+    axes = tuple(float(a) for a in 0.5 * (v.max(0) - v.min(0)))
+    tpl = PlateletTemplate(v, t, 0, seed, axes)
     T = len(t)
     params = reference_params(dx=REF_DX, dt=REF_DT, nz=nz, shear=300.0, receptors=2 * R * T,
                               mean_bond=tpl.mean_bond, kf0=kf0, kr0=kr0)
     sc = Scene(nx=nx, ny=ny, nz=nz, dx=REF_DX, dt=REF_DT, params=params,
                bc=(BC_PERIODIC, BC_PERIODIC, BC_ZOUHE_SHEAR), ibm_wrap=(0, 1, 0))
     if center is None:
-        center = (nx * REF_DX / 2, ny * REF_DX / 2, 0.3 + 0.05)
+        center = (nx * REF_DX / 2, ny * REF_DX / 2, half_z + 0.05)
     _place(sc, tpl, np.array([center]), ny * REF_DX)
     _receptors_per_triangle(sc, R, rng)
     sc.bond_model = BOND_BELL

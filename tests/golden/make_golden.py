@@ -145,19 +145,49 @@ CASES = {
     # platelet straddling the periodic y seam's stencils and the bounded low-x edge
     "ref_edges": dict(seed=11, nx=14, ny=16, nz=9, level=1, R=1, nsteps=30,
                       center=(0.45, 0.62, 0.35)),
+    # the reference's own 958-vertex platelet mesh 0.02 um above the wall:
+    # about 150 receptors bind in the first step, some of them to two vWF
+    # sites (the two-bond branch of the bond kernel); no unbinding (Kr0 = 0),
+    # so no receptor drops from two bonds to one (the stored-site path whose
+    # out-of-bounds read the CUDA path fixes)
+    "ref_mesh958": dict(seed=5, nx=16, ny=16, nz=8, level=1, R=1, nsteps=25, mesh="958", two_bonds=True,
+                        gap=0.02, kr0=0.0),
 }
 
 
-def make(name: str, seed, nx, ny, nz, level, R, nsteps, center=None):
+def reference_mesh958():
+    """The reference's own 958-vertex / 1912-triangle platelet surface
+    (Input/Platelet_Mesh_958.neu of its archive), read by libpfgpu's NEU
+    reader from a temporary extraction."""
+    import tarfile
+    import tempfile
+    from platelet_fiber_gpu_gb300 import build, gpu
+    build.build()
+    with tarfile.open(ob.reference_dir() / "gpu_20151203.tar.gz") as tf, tempfile.TemporaryDirectory() as d:
+        path = Path(d) / "mesh.neu"
+        path.write_bytes(tf.extractfile(tf.getmember("./Input/Platelet_Mesh_958.neu")).read())
+        m = gpu.read_neu(path)
+    return np.stack([m["X"], m["Y"], m["Z"]], 1), m["tri"]
+
+
+def make(name: str, seed, nx, ny, nz, level, R, nsteps, center=None, mesh=None, two_bonds=False, gap=None,
+         kf0=3.0e4, kr0=1.5e4):
+    msh = reference_mesh958() if mesh == "958" else None
     for attempt in range(50):
         s = seed + 1000 * attempt
-        sc = W.reference_case(seed=s, nx=nx, ny=ny, nz=nz, level=level, R=R, center=center)
+        c = center
+        if c is None and gap is not None:
+            c = (nx * W.REF_DX / 2, ny * W.REF_DX / 2, 0.5 * (msh[0][:, 2].max() - msh[0][:, 2].min()) + gap)
+        sc = W.reference_case(seed=s, nx=nx, ny=ny, nz=nz, level=level, R=R, center=c, mesh=msh, kf0=kf0, kr0=kr0)
         out = run_reference(sc, nsteps)
         # a receptor that drops from 2 bonds to 1 leaves the reference's stored
         # site at -1 (sem_kernel.cu:1937-1942); pick a seed whose run never does
         if int(out["lost_site_step"]) >= 0:
             continue
         if out["total_bond"].max() == 0:
+            continue
+        # the two-bond branch of sem_kernel.cu:1999-2030 must be taken
+        if two_bonds and not (out["rec_state"][..., 2] > 1).any():
             continue
         break
     else:
@@ -179,5 +209,6 @@ def make(name: str, seed, nx, ny, nz, level, R, nsteps, center=None):
 
 
 if __name__ == "__main__":
-    for n, kw in CASES.items():
-        make(n, **kw)
+    names = sys.argv[1:] or list(CASES)
+    for n in names:
+        make(n, **CASES[n])

@@ -41,7 +41,7 @@ def golden(name):
     return scene_from_dict(d), int(d["nsteps"]), d
 
 
-@pytest.mark.parametrize("name", ["ref_wall", "ref_edges"])
+@pytest.mark.parametrize("name", ["ref_wall", "ref_edges", "ref_mesh958"])
 def test_fp64_matches_reference_kernels(gpu, name):
     sc, n, d = golden(name)
     j = gpu.Job(sc, 0)
@@ -62,9 +62,10 @@ def test_fp64_matches_reference_kernels(gpu, name):
     j.close()
 
 
+@pytest.mark.parametrize("name", ["ref_wall", "ref_mesh958"])
 @pytest.mark.parametrize("prec,tol", [(1, 1e-4), (2, 2e-3)])
-def test_reduced_precision_vs_reference_kernels(gpu, prec, tol):
-    sc, n, d = golden("ref_wall")
+def test_reduced_precision_vs_reference_kernels(gpu, prec, tol, name):
+    sc, n, d = golden(name)
     j = gpu.Job(sc, prec, 0.0)
     j.step(n)
     L, E, B = j.lattice(), j.elements(), j.bonds()
