@@ -73,30 +73,62 @@ struct pfgpu_job {
   int launches_per_step = 0;
 };
 
+// Job buffers come from the device's stream-ordered memory pool, in order on
+// the job's stream s0: the pool keeps up to kPoolKeepBytes of freed memory
+// mapped, so a job created after another was destroyed (a served loop, a
+// restart) reuses its memory instead of mapping new pages.  Every job-creation
+// operation is queued on s0 (allocation, zero fill, uploads, the initial
+// lattice), so host-side set-up overlaps the device work and one
+// synchronisation ends the creation.
+constexpr unsigned long long kPoolKeepBytes = 32ull << 30;
+static void keep_pool_memory() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    unsigned long long keep = kPoolKeepBytes;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
+  done[dev] = true;
+}
+
 template <class T>
-static cudaError_t dalloc(pfgpu_job* j, T** p, size_t count) {
+static cudaError_t dalloc(pfgpu_job* j, T** p, size_t count, bool zero = true) {
   size_t bytes = count * sizeof(T);
   if (bytes == 0) bytes = sizeof(T);
-  cudaError_t e = cudaMalloc((void**)p, bytes);
+  cudaError_t e = cudaMallocAsync((void**)p, bytes, j->s0);
   if (e == cudaSuccess) {
     j->allocs.push_back(*p);
     j->alloc_bytes.push_back(bytes);
     j->bytes += bytes;
-    cudaMemset(*p, 0, bytes);
+    if (zero) e = cudaMemsetAsync(*p, 0, bytes, j->s0);
   }
   return e;
 }
 template <class T>
 static cudaError_t dupload(pfgpu_job* j, T** p, const T* src, size_t count) {
-  cudaError_t e = dalloc(j, p, count);
-  if (e == cudaSuccess && src && count) e = cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice);
+  cudaError_t e = dalloc(j, p, count, !(src && count));
+  if (e == cudaSuccess && src && count)
+    e = cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, j->s0);
   return e;
 }
 
 static void destroy(pfgpu_job* j) {
   if (!j) return;
   if (j->graph) cudaGraphExecDestroy(j->graph);
-  for (void* p : j->allocs) cudaFree(p);
+  if (j->s0) {
+    cudaStreamSynchronize(j->s0);
+    for (void* p : j->allocs) cudaFreeAsync(p, j->s0);
+    cudaStreamSynchronize(j->s0);
+  }
   cudaStream_t ss[6] = {j->s0, j->s1, j->s2, j->s3, j->sL, j->sF};
   for (cudaStream_t s : ss)
     if (s) cudaStreamDestroy(s);
@@ -638,6 +670,7 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
       return fail(e_ == cudaErrorMemoryAllocation ? PFGPU_ERR_NOMEM : PFGPU_ERR_CUDA);          \
     }                                                                                           \
   } while (0)
+  keep_pool_memory();
   int prio_low = 0, prio_high = 0;
   CKJ(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
   CKJ(cudaStreamCreateWithPriority(&j->s0, cudaStreamNonBlocking, prio_high));
@@ -670,8 +703,10 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   }
   const size_t N = (size_t)L.k.N;
   const size_t sb = store_bytes(precision), rb = real_bytes(precision);
-  CKJ(dalloc(j, (char**)&L.g[0], 19 * N * sb));
-  CKJ(dalloc(j, (char**)&L.g[1], 19 * N * sb));
+  // populations: the initial-state pass writes every word of g[0], the
+  // first step every word of g[1]
+  CKJ(dalloc(j, (char**)&L.g[0], 19 * N * sb, false));
+  CKJ(dalloc(j, (char**)&L.g[1], 19 * N * sb, false));
   CKJ(dalloc(j, (char**)&L.F[0], 4 * N * rb));
   CKJ(dalloc(j, (char**)&L.F[1], 4 * N * rb));
   CKJ(dalloc(j, (char**)&L.ubuf, 4 * N * rb));
@@ -685,6 +720,26 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(dalloc(j, &j->ctl, 1));
   CKJ(dalloc(j, &j->done_blocks, 1));
   CKJ(dalloc(j, &j->scratch4, 4));
+  Control c{};
+  c.step = 0;
+  c.done = 0;
+  c.first = 1;
+  c.total_bond = 1;  // sem_initGPUKernel, semLB.cu:880
+  CKJ(cudaMemcpyAsync(j->ctl, &c, sizeof c, cudaMemcpyHostToDevice, j->s0));
+  if (s->n_platelets > 0 && s->n_elem > 0) {
+    j->has_pl = true;
+    rc = build_platelets(j, s);
+    if (rc) return fail(rc);
+    j->Pl.mem_items = membrane_items(j->Pl.k);
+    CKJ(bin_elements(j->Pl, j->ctl, j->s0));
+  }
+  if (s->n_fib > 0) {
+    j->has_fb = true;
+    rc = build_fibrin(j, s);
+    if (rc) return fail(rc);
+  }
+  // the initial lattice last: uploads from pageable host memory wait for the
+  // stream, so the long initial-state pass goes after the small uploads
   {
     // initial populations: the scene's own, else the equilibrium of the
     // initial flow, built on the device in one pass that reads the caller's
@@ -699,7 +754,7 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
       if (!h || e != cudaSuccess) return nullptr;
       if (const void* v = device_view(h)) return static_cast<const double*>(v);
       void* d = nullptr;
-      e = cudaMalloc(&d, count * sizeof(double));
+      e = cudaMallocAsync(&d, count * sizeof(double), j->s0);
       if (e != cudaSuccess) return nullptr;
       staged.push_back(d);
       e = cudaMemcpyAsync(d, h, count * sizeof(double), cudaMemcpyHostToDevice, j->s0);
@@ -736,27 +791,10 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
     }
     if (e == cudaSuccess) e = lattice_init(L, src, j->s0);
     if (e == cudaSuccess) e = lattice_configure(L);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(j->s0);
-    for (void* d : staged) cudaFree(d);
+    // the caller's arrays may be read by the device until the end of the
+    // creation, which waits for s0; staging copies go back to the pool
+    for (void* d : staged) cudaFreeAsync(d, j->s0);
     CKJ(e);
-  }
-  Control c{};
-  c.step = 0;
-  c.done = 0;
-  c.first = 1;
-  c.total_bond = 1;  // sem_initGPUKernel, semLB.cu:880
-  CKJ(cudaMemcpy(j->ctl, &c, sizeof c, cudaMemcpyHostToDevice));
-  if (s->n_platelets > 0 && s->n_elem > 0) {
-    j->has_pl = true;
-    rc = build_platelets(j, s);
-    if (rc) return fail(rc);
-    j->Pl.mem_items = membrane_items(j->Pl.k);
-    CKJ(bin_elements(j->Pl, j->ctl, j->s0));
-  }
-  if (s->n_fib > 0) {
-    j->has_fb = true;
-    rc = build_fibrin(j, s);
-    if (rc) return fail(rc);
   }
   CKJ(mark_markers(j->L, j->has_pl ? &j->Pl : nullptr, j->has_fb ? &j->Fb : nullptr, j->s0));
   CKJ(cudaStreamSynchronize(j->s0));
