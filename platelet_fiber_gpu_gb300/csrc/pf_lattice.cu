@@ -508,62 +508,50 @@ struct VecIO<__half, V> {
     if constexpr (V == 8) {
       const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
       w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
-    } else {
+    } else if constexpr (V == 4) {
       const uint2 a = __ldg(reinterpret_cast<const uint2*>(p));
       w[0] = a.x; w[1] = a.y;
+    } else {
+      w[0] = __ldg(reinterpret_cast<const unsigned*>(p));
     }
   }
   __device__ static void store(__half* p, const unsigned w[W]) {
     if constexpr (V == 8) *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
-    else *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+    else if constexpr (V == 4) *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+    else *reinterpret_cast<unsigned*>(p) = w[0];
   }
   __device__ static unsigned bits(const unsigned w[W], int i) { return (w[i >> 1] >> (16 * (i & 1))) & 0xffffu; }
   __device__ static unsigned load_bits(const __half* p) { return (unsigned)__half_as_ushort(__ldg(p)); }
 };
 
+// The pull of one V-node segment (row, sx) for every population plane:
+// vector loads from the source rows, and for the x-shifted planes the one
+// element outside the vector, from the lane holding the neighbouring segment
+// of the same row (warp shuffle) or loaded directly.  Every lane of the warp
+// calls it; lanes without `active` load nothing.
 template <class S, int V>
-__device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB, float4* FA, float4* FB,
-                                             float4* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
-                                             int ncells, int mode, Control* ctl, long long seg, long long tid,
-                                             long long tot) {
+__device__ __forceinline__ void vec_pull(const LatticeConst& k, const S* __restrict__ gin, bool active,
+                                         unsigned row, unsigned sx, unsigned w[Q][VecIO<S, V>::W],
+                                         unsigned edge[Q]) {
   using IO = VecIO<S, V>;
-  constexpr int W = IO::W;
-  if (ctl->done) return;
-  const int par = (int)(ctl->step & 1);
-  const S* __restrict__ gin = par ? gB : gA;
-  S* __restrict__ gout = par ? gA : gB;
-  const float4* Fc = par ? FB : FA;
-  float4* Fp = par ? FA : FB;
-  unsigned* flp = par ? flA : flB;
-  const unsigned* flc = par ? flB : flA;
-  if (bin_count) zero_bins(bin_count, ncells, ctl, (size_t)tid, (size_t)tot);
   const int lane = threadIdx.x & 31;
-  const unsigned nx = (unsigned)k.nx, ny = (unsigned)k.ny, nz = (unsigned)k.nz;
-  const unsigned spr = nx / V;  // segments per row
-  const long long nseg = k.N / V;
-  const bool valid = seg < nseg;
-  const unsigned row = valid ? (unsigned)(seg / spr) : 0u;
-  const unsigned sx = valid ? (unsigned)(seg - (long long)row * spr) : 0u;
-  const unsigned x0 = sx * V, y = row % ny, z = row / ny;
-  const int brick = (int)(x0 / kBrickX + (unsigned)k.nbx * row);
-  const unsigned fc = valid ? flc[brick] : 0u;
-  const bool active = valid && (mode == kPassAll || !fc);
   const unsigned am = __ballot_sync(0xffffffffu, active);
+  const unsigned nx = (unsigned)k.nx, ny = (unsigned)k.ny, nz = (unsigned)k.nz, N = (unsigned)k.N;
+  const unsigned spr = nx / V, x0 = sx * V, y = row % ny, z = row / ny;
   // the source rows of the pull (periodic / Zou/He axes wrap)
   const unsigned ys[3] = {y == 0 ? ny - 1 : y - 1, y, y + 1 == ny ? 0u : y + 1};
   const unsigned zs[3] = {z == 0 ? nz - 1 : z - 1, z, z + 1 == nz ? 0u : z + 1};
-  const unsigned N = (unsigned)k.N;
-  unsigned w[Q][W];
   if (active) {
 #pragma unroll
     for (int d = 0; d < Q; ++d) IO::load(gin + ((unsigned)d * N + nx * (ys[1 - cy(d)] + ny * zs[1 - cz(d)]) + x0), w[d]);
   }
-  // the one element of each x-shifted plane that lies outside the vector:
-  // x0 - 1 for c_x = +1, x0 + V for c_x = -1
-  const bool left_in_warp = lane > 0 && sx > 0 && ((am >> (lane - 1)) & 1u);
-  const bool right_in_warp = lane < 31 && sx + 1 < spr && ((am >> (lane + 1)) & 1u);
+  // the lane before (after) holds the segment to the left (right) when it
+  // is active and on the same row
+  const unsigned prow = __shfl_up_sync(0xffffffffu, row, 1), psx = __shfl_up_sync(0xffffffffu, sx, 1);
+  const unsigned nrow = __shfl_down_sync(0xffffffffu, row, 1), nsx = __shfl_down_sync(0xffffffffu, sx, 1);
+  const bool left_in_warp = lane > 0 && ((am >> (lane - 1)) & 1u) && prow == row && psx + 1 == sx;
+  const bool right_in_warp = lane < 31 && ((am >> (lane + 1)) & 1u) && nrow == row && nsx == sx + 1;
   const unsigned xl = sx == 0 ? nx - 1 : x0 - 1, xr = sx + 1 == spr ? 0u : x0 + V;
-  unsigned edge[Q];
 #pragma unroll
   for (int d = 0; d < Q; ++d) {
     if (cx(d) == 0) continue;
@@ -575,10 +563,29 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
       edge[d] = IO::load_bits(gin + ((unsigned)d * N + nx * (ys[1 - cy(d)] + ny * zs[1 - cz(d)]) +
                                      (cx(d) == 1 ? xl : xr)));
   }
-  if (!active) return;
-  const unsigned fp = flp[brick];
-  const int first = ctl->first;
-  const unsigned n0 = nx * row + x0;
+}
+
+// The stored bits of population d at node i of the segment, after the pull
+// (c_x = +1: the left neighbour, c_x = -1: the right one).  `carry` keeps the
+// c_x = +1 inputs of the previous node once a node's outputs overwrite w.
+template <class S, int V>
+__device__ __forceinline__ unsigned vec_in(const unsigned w[Q][VecIO<S, V>::W], const unsigned edge[Q],
+                                           const unsigned carry[Q], int d, int i) {
+  using IO = VecIO<S, V>;
+  if (cx(d) == 0) return IO::bits(w[d], i);
+  if (cx(d) == 1) return i == 0 ? edge[d] : carry[d];
+  return i == V - 1 ? edge[d] : IO::bits(w[d], i + 1);
+}
+
+// Collide-and-store of a pulled segment (node n0 .. n0+V-1 at height z):
+// lbm_node's arithmetic per node, outputs written back over w and stored as
+// vectors; clears the previous force of the segment's nodes.
+template <class S, int V>
+__device__ __forceinline__ void vec_collide_store(const LatticeConst& k, S* __restrict__ gout, unsigned w[Q][VecIO<S, V>::W],
+                                                  const unsigned edge[Q], unsigned n0, unsigned z, const float4* Fc,
+                                                  float4* Fp, const float4* ubuf, unsigned fc, unsigned fp, int first) {
+  using IO = VecIO<S, V>;
+  const unsigned N = (unsigned)k.N;
   unsigned carry[Q];
   if constexpr (std::is_same<S, __half>::value) {
     // two nodes at a time: their outputs share a 32-bit word of each plane
@@ -588,17 +595,13 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
       float qa[Q], qb[Q];
 #pragma unroll
       for (int d = 0; d < Q; ++d) {
-        unsigned ba, bb;
-        if (cx(d) == 0) {
-          ba = IO::bits(w[d], i);
-          bb = IO::bits(w[d], i + 1);
-        } else if (cx(d) == 1) {
-          ba = i == 0 ? edge[d] : carry[d];
+        const unsigned ba = vec_in<S, V>(w, edge, carry, d, i);
+        unsigned bb;
+        if (cx(d) == 1) {
           bb = IO::bits(w[d], i);
           carry[d] = IO::bits(w[d], i + 1);
         } else {
-          ba = IO::bits(w[d], i + 1);
-          bb = i + 1 == V - 1 ? edge[d] : IO::bits(w[d], i + 2);
+          bb = vec_in<S, V>(w, edge, carry, d, i + 1);
         }
         qa[d] = __half2float(__ushort_as_half((unsigned short)ba));
         qb[d] = __half2float(__ushort_as_half((unsigned short)bb));
@@ -623,10 +626,7 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
       float g[Q];
 #pragma unroll
       for (int d = 0; d < Q; ++d) {
-        unsigned b;
-        if (cx(d) == 0) b = IO::bits(w[d], i);
-        else if (cx(d) == 1) b = i == 0 ? edge[d] : carry[d];
-        else b = i == V - 1 ? edge[d] : IO::bits(w[d], i + 1);
+        const unsigned b = vec_in<S, V>(w, edge, carry, d, i);
         if (cx(d) == 1) carry[d] = IO::bits(w[d], i);
         g[d] = IO::value(b);
       }
@@ -648,9 +648,45 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
   }
 #pragma unroll
   for (int d = 0; d < Q; ++d) IO::store(gout + ((unsigned)d * N + n0), w[d]);
+}
+
+// The step over the whole lattice (kPassAll) or the bricks without force
+// (kPassUnflag): segment `seg` of the lattice in lattice order.
+template <class S, int V>
+__device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB, float4* FA, float4* FB,
+                                             float4* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
+                                             int ncells, int mode, Control* ctl, long long seg, long long tid,
+                                             long long tot) {
+  using IO = VecIO<S, V>;
+  if (ctl->done) return;
+  const int par = (int)(ctl->step & 1);
+  const S* __restrict__ gin = par ? gB : gA;
+  S* __restrict__ gout = par ? gA : gB;
+  const float4* Fc = par ? FB : FA;
+  float4* Fp = par ? FA : FB;
+  unsigned* flp = par ? flA : flB;
+  const unsigned* flc = par ? flB : flA;
+  if (bin_count) zero_bins(bin_count, ncells, ctl, (size_t)tid, (size_t)tot);
+  const unsigned nx = (unsigned)k.nx;
+  const unsigned spr = nx / V;  // segments per row
+  const long long nseg = k.N / V;
+  const bool valid = seg < nseg;
+  const unsigned row = valid ? (unsigned)(seg / spr) : 0u;
+  const unsigned sx = valid ? (unsigned)(seg - (long long)row * spr) : 0u;
+  const unsigned x0 = sx * V;
+  const int brick = (int)(x0 / kBrickX + (unsigned)k.nbx * row);
+  const unsigned fc = valid ? flc[brick] : 0u;
+  const bool active = valid && (mode == kPassAll || !fc);
+  unsigned w[Q][IO::W], edge[Q];
+  vec_pull<S, V>(k, gin, active, row, sx, w, edge);
+  const unsigned am = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  const unsigned fp = flp[brick];
+  vec_collide_store<S, V>(k, gout, w, edge, nx * row + x0, row / (unsigned)k.ny, Fc, Fp, ubuf, fc, fp, ctl->first);
   __syncwarp(am);
   if (fp && (x0 % kBrickX) == 0) flp[brick] = 0;
 }
+
 template <class S, int V>
 __global__ void __launch_bounds__(kLbmBlock) lbm_vec_k(LatticeConst k, S* gA, S* gB, float4* FA, float4* FB,
                                                        float4* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
@@ -1380,7 +1416,6 @@ int vec_width(const Lattice& L) {
     if (V == 8 && std::is_same<S, float>::value) V = 4;
   }
   if (V != 2 && V != 4 && V != 8) return 0;
-  if (std::is_same<S, __half>::value && V == 2) V = 4;
   return (L.k.nx % V == 0) ? V : 0;
 }
 
@@ -1416,7 +1451,7 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
       const unsigned vgrid = (unsigned)((nseg + kLbmBlock - 1) / kLbmBlock);
       void (*kern)(LatticeConst, S*, S*, float4*, float4*, float4*, unsigned*, unsigned*, int*, int, int, Control*);
       if constexpr (std::is_same<S, float>::value) kern = V == 4 ? lbm_vec_k<S, 4> : lbm_vec_k<S, 2>;
-      else kern = V == 8 ? lbm_vec_k<S, 8> : lbm_vec_k<S, 4>;
+      else kern = V == 8 ? lbm_vec_k<S, 8> : (V == 4 ? lbm_vec_k<S, 4> : lbm_vec_k<S, 2>);
       kern<<<vgrid, kLbmBlock, 0, st>>>(L.k, (S*)L.g[0], (S*)L.g[1], (float4*)L.F[0], (float4*)L.F[1],
                                         (float4*)L.ubuf, L.flags[0], L.flags[1], bin_count, ncells, part, ctl);
       return cudaGetLastError();

@@ -48,7 +48,8 @@ def _run(gpu, sc, prec, width, steps):
 
 
 @pytest.mark.parametrize("dims", [(40, 32, 20), (256, 8, 12), (48, 10, 9)], ids=["40", "256", "48"])
-@pytest.mark.parametrize("prec,width", [(1, 2), (1, 4), (2, 4), (2, 8)], ids=["f32v2", "f32v4", "f16v4", "f16v8"])
+@pytest.mark.parametrize("prec,width", [(1, 2), (1, 4), (2, 2), (2, 4), (2, 8)],
+                         ids=["f32v2", "f32v4", "f16v2", "f16v4", "f16v8"])
 def test_vector_step_bit_identical_without_markers(gpu, prec, width, dims):
     sc = _lattice_only(*dims)
     ref = _run(gpu, sc, prec, 0, 7)
