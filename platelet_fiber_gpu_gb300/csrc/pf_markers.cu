@@ -2146,6 +2146,57 @@ __device__ __forceinline__ void fibrin_k_body(int M, int law, double kk, double 
   F[M + ni] = (double)fy;
   F[2 * M + ni] = (double)fz;
 }
+// Reduced precision with four lanes per fibrin node: lane c takes the node's
+// links c, c+4, ... (the per-link arithmetic of fibrin_k_body), the lanes'
+// sums are added as (s0 + s1) + (s2 + s3).  The per-node loop is a chain of
+// dependent loads (link list, neighbour position); four short chains in
+// flight instead of one long one.
+constexpr int kFibLanes = 4;
+__global__ void __launch_bounds__(128) fibrin4_k(int M, int law, double kk, double mass, const double* X,
+                                                 const double* Y, const double* Z, const int* ptr, const int* nbr,
+                                                 const double* L0, double* F, const Control* ctl) {
+  if (ctl->done) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ni = t / kFibLanes, c = t % kFibLanes;
+  const bool live = ni < M;
+  float fx = 0, fy = 0, fz = 0;
+  if (live) {
+    const double xi = X[ni], yi = Y[ni], zi = Z[ni];
+    const int q1 = ptr[ni + 1];
+    for (int q = ptr[ni] + c; q < q1; q += kFibLanes) {
+      const int o = nbr[q];
+      const float d0 = (float)(xi - X[o]), d1 = (float)(yi - Y[o]), d2 = (float)(zi - Z[o]);
+      const float len = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+      if (len < 1.0e-13f) continue;
+      const float l0 = (float)L0[q];
+      float wf;
+      if (law == PF_FIB_WLC) {
+        const float En = (float)(1.3806503 * 1e-8 * 10);
+        const float CC = En / l0;
+        const float tl = 1.0f - (len - l0) / l0;
+        const float IP1 = 0.25f * 1.0f / (tl * tl) - 0.25f + (len - l0) / l0;
+        wf = -CC * IP1 / (float)mass;
+      } else {
+        wf = (float)kk * (len - l0);
+      }
+      fx -= wf * d0 / len;
+      fy -= wf * d1 / len;
+      fz -= wf * d2 / len;
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < kFibLanes; o <<= 1) {
+    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+  }
+  if (live && c == 0) {
+    F[ni] = (double)fx;
+    F[M + ni] = (double)fy;
+    F[2 * M + ni] = (double)fz;
+  }
+}
+
 template <class R>
 __global__ void fibrin_k(int M, int law, double kk, double mass, const double* X, const double* Y, const double* Z,
                          const int* ptr, const int* nbr, const double* L0, double* F, const Control* ctl) {
@@ -2632,8 +2683,8 @@ cudaError_t fibrin_forces(Fibrin& Fb, int precision, Control* ctl, cudaStream_t 
     fibrin_k<double><<<(Fb.M + 127) / 128, 128, 0, st>>>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr,
                                                          Fb.nbr, Fb.L0, Fb.F, ctl);
   else
-    fibrin_k<float><<<(Fb.M + 127) / 128, 128, 0, st>>>(Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr,
-                                                        Fb.nbr, Fb.L0, Fb.F, ctl);
+    fibrin4_k<<<(unsigned)(((long long)Fb.M * kFibLanes + 127) / 128), 128, 0, st>>>(
+        Fb.M, Fb.law, Fb.k, Fb.mass, Fb.X, Fb.Y, Fb.Z, Fb.ptr, Fb.nbr, Fb.L0, Fb.F, ctl);
   return cudaGetLastError();
 }
 
