@@ -39,11 +39,33 @@ typedef enum pfgpu_status {
 } pfgpu_status;
 
 /* ------------------------------------------------------------ scene */
-enum { PF_BC_PERIODIC = 0, PF_BC_BOUNCEBACK = 1, PF_BC_ZOUHE_SHEAR = 2 };
+/* PF_BC_INOUT (y only, with Zou/He shear walls on z and periodic x): the
+ * velocity inlet at y=0 and outlet at y=ny-1 of the reference's
+ * fluid3d_in_out_flow_boundary_kernel (LB_kernel.cu:78-392, commented out
+ * there): the shear profile u = (0, uw z/(nz-1), 0) on both planes, Zou/He
+ * unknowns on the interior of each plane, the equilibrium at unit density on
+ * the plane's rows next to its edges (x = 1, nx-2; z = 1, nz-2).  Streaming
+ * is periodic in y before the planes are rewritten, as the reference's is. */
+enum { PF_BC_PERIODIC = 0, PF_BC_BOUNCEBACK = 1, PF_BC_ZOUHE_SHEAR = 2, PF_BC_INOUT = 3 };
 enum { PF_PREC_FP64 = 0, PF_PREC_FP32 = 1, PF_PREC_FP16 = 2 };
 enum { PF_BOND_BELL = 0, PF_BOND_CONSTANT = 1 };
 enum { PF_FIB_HOOKE = 0, PF_FIB_WLC = 1 };
-enum { PF_MEM_SPRING = 1, PF_MEM_WALL = 2, PF_MEM_AREAVOL = 4, PF_MEM_BEND = 8, PF_MEM_ALL = 15 };
+/* How fibrin nodes meet the fluid.  MARKER: immersed markers (link forces
+ * spread into the lattice, nodes moved with the interpolated velocity).
+ * PENALTY: the reference's fibrin FSI design (fiber_LB_Fsi_force /
+ * Flow_vel_at_position, fiber.cpp:501-814, with the network's damped
+ * kick-drift-kick, network.cpp:445-513,839-881): each node carries its own
+ * velocity, the fluid pulls it with the penalty force kappa rho (u - V) and
+ * receives the reaction. */
+enum { PF_FIBCPL_MARKER = 0, PF_FIBCPL_PENALTY = 1 };
+/* PF_MEM_ALL: the membrane chain the reference runs (semLB.cu:510-523).
+ * PF_MEM_FEMBEND adds the reference's disabled FEM bending chain
+ * (sem_calculate_K_kernel, sem_calculate_q_kernel, sem_bending_force_kernel,
+ * sem_kernel.cu:1129-1497) in the slot its commented-out launches hold
+ * (semLB.cu:518-520, between the curvature and the area/volume forces).
+ * Single jobs only: the batch API and the no-allocation entry point refuse it. */
+enum { PF_MEM_SPRING = 1, PF_MEM_WALL = 2, PF_MEM_AREAVOL = 4, PF_MEM_BEND = 8, PF_MEM_ALL = 15,
+       PF_MEM_FEMBEND = 16 };
 
 /* Indices into pf_scene.params: the reference's model parameter table
  * (sem_kernel.cu:58-76, filled at gpuSEM_LB.c:1206-1233). */
@@ -120,6 +142,12 @@ typedef struct pf_scene {
   /* injected uniform stream and detachment */
   uint64_t seed;                /* Philox-4x32-10 key of the receptor/detach uniforms */
   double detach_rate;           /* gama of semLB.cu:451 (0 = never detach) */
+
+  /* fibrin coupling (PF_FIBCPL_*; PENALTY only reads the three below) */
+  int fib_coupling;
+  double fib_gamma;             /* friction rate of the kick, per lattice step (0 = none) */
+  double fib_node_mass;         /* node mass in lattice units (1 = the fluid in one lattice cell) */
+  double fib_kappa;             /* penalty stiffness (1 = the reference's rho (u - V) / dt) */
 } pf_scene;
 
 /* ------------------------------------------------------------ job API */

@@ -126,6 +126,7 @@ struct pfo_sim {
   int M;
   double *fX, *fY, *fZ, *fVX, *fVY, *fVZ, *fFX, *fFY, *fFZ, *fL0;
   int *ffix, *fptr, *fnbr;
+  double *fsX, *fsY, *fsZ; /* penalty coupling: lattice force on each node this step */
   long long step;
   int done;
 };
@@ -162,6 +163,7 @@ void pfo_feq(double rho, const double u[3], double C, double out[19]) {
 double pfo_ibm_phi(double r) { return 0.25 * (1.0 + cos(0.5 * PI_REF * r)); }
 
 static int zouhe(const pfo_sim *s) { return s->sc.bc[2] == PF_BC_ZOUHE_SHEAR; }
+static int penalty(const pfo_sim *s) { return s->sc.fib_coupling == PF_FIBCPL_PENALTY; }
 
 /* wall velocity of the moving plate in units of UMAX (LB_kernel.cu:640) */
 static double top_wall_uy(const pfo_sim *s) {
@@ -170,6 +172,8 @@ static double top_wall_uy(const pfo_sim *s) {
   v = v / s->mp[PF_P_UMAX];
   return (double)v;
 }
+
+static void fib_flow_at(const pfo_sim *s, double x, double y, double z, double u[3], double *rho);
 
 /* ------------------------------------------------------------------ create */
 pfo_sim *pfo_create(const pf_scene *sc, int ibm_bruteforce) {
@@ -351,6 +355,19 @@ pfo_sim *pfo_create(const pf_scene *sc, int ibm_bruteforce) {
   int nfl = (sc->fib_ptr && M) ? sc->fib_ptr[M] : 0;
   s->fnbr = (int *)xdup(sc->fib_nbr, (size_t)nfl * sizeof(int));
   s->fL0 = (double *)xdup(sc->fib_L0, (size_t)nfl * sizeof(double));
+  s->fsX = (double *)xcalloc(M, sizeof(double));
+  s->fsY = (double *)xcalloc(M, sizeof(double));
+  s->fsZ = (double *)xcalloc(M, sizeof(double));
+  if (sc->fib_coupling == PF_FIBCPL_PENALTY)
+    for (int m = 0; m < s->M; ++m) {
+      /* initial node velocity: the flow's at the node (cpu_init_fiber_LB,
+       * fiber.cpp:815-910, interpolates it trilinearly; here with the
+       * coupling's own stencil); fixed nodes rest */
+      if (s->ffix[m]) continue;
+      double u[3], r;
+      fib_flow_at(s, s->fX[m], s->fY[m], s->fZ[m], u, &r);
+      s->fVX[m] = u[0]; s->fVY[m] = u[1]; s->fVZ[m] = u[2];
+    }
   return s;
 }
 
@@ -361,7 +378,7 @@ void pfo_destroy(pfo_sim *s) {
                s->Z, s->VX, s->VY, s->VZ, s->FX, s->FY, s->FZ, s->nodeN, s->Kapa, s->km, s->S,
                s->nelem, s->SV, s->rec_tri, s->rec_state, s->vwf, s->r1, s->r2, s->cell_of,
                s->cell_start, s->cell_order, s->fX, s->fY, s->fZ, s->fVX, s->fVY, s->fVZ, s->fFX,
-               s->fFY, s->fFZ, s->fL0, s->ffix, s->fptr, s->fnbr};
+               s->fFY, s->fFZ, s->fL0, s->ffix, s->fptr, s->fnbr, s->fsX, s->fsY, s->fsZ};
   for (size_t i = 0; i < sizeof p / sizeof p[0]; ++i) free(p[i]);
   free(s);
 }
@@ -422,6 +439,134 @@ static void p2_grad(double s_, double t_, double dNds[6], double dNdt[6]) {
 
 static double nrm3(double a, double b, double c) { return sqrt(a * a + b * b + c * c); }
 
+/* The reference's disabled FEM bending chain, in the slot of its
+ * commented-out launches (semLB.cu:518-520): after the curvature tensors
+ * (divided by the node's triangle count and symmetrised, as
+ * sem_calculate_m_kernel leaves them) and before the area/volume forces.
+ *  1. sem_calculate_K_kernel (sem_kernel.cu:1129-1235): per triangle and
+ *     each of its 6 nodes i, for each column l of the curvature tensors, the
+ *     3x3 system rows (dx/ds, dx/dt, n_i) with right-hand sides
+ *     (dKapa_l/ds, dKapa_l/dt, 0) is solved; row k of the solution, entry j,
+ *     is added to K[node i][j][k][l].
+ *  2. sem_calculate_q_kernel (:1237-1306): K divided by the node's triangle
+ *     count, traceK_i = sum_j K[j][j][i], q_j = sum_i traceK_i (I - n n)_ij.
+ *  3. sem_bending_force_kernel (:1308-1497): per triangle, edge tangents t
+ *     and the in-plane normals b = t x n at the 6 nodes, line loads
+ *     f = (b . q) n, Simpson's rule along the three sides; the total goes to
+ *     each of the 3 vertices divided by S[vertex id] and F0.  S is the
+ *     per-triangle area array, so the divisor is the area of the triangle
+ *     whose index equals the vertex id: kept as the reference wrote it. */
+static void fem_bending(pfo_sim *s, int p, const double *X, const double *Y, const double *Z, const double *nN,
+                        const double *Kp, const double *S, double *FX, double *FY, double *FZ, double F0) {
+  const int T = s->T, NN = s->NN;
+  double *K = (double *)xcalloc((size_t)NN * 27, sizeof(double));
+  double *q = (double *)xcalloc((size_t)NN * 3, sizeof(double));
+  (void)p;
+  for (int t = 0; t < T; ++t) {
+    const int *nd = s->tri + 6 * t;
+    double c[6][3];
+    for (int i = 0; i < 3; ++i) { c[i][0] = X[nd[i]]; c[i][1] = Y[nd[i]]; c[i][2] = Z[nd[i]]; }
+    for (int i = 0; i < 3; ++i) {
+      c[3][i] = 0.5 * (c[0][i] + c[1][i]);
+      c[4][i] = 0.5 * (c[0][i] + c[2][i]);
+      c[5][i] = 0.5 * (c[1][i] + c[2][i]);
+    }
+    for (int i = 0; i < 6; ++i) {
+      double gs[6], gt[6];
+      p2_grad(QN_ST[i][0], QN_ST[i][1], gs, gt);
+      for (int l = 0; l < 3; ++l) {
+        double a1[3], a2[3], a3[3], a4[3], a5[3], a6[3], Ke[3][3];
+        for (int j = 0; j < 3; ++j) {
+          a1[j] = c[0][j] * gs[0] + c[1][j] * gs[1] + c[2][j] * gs[2] + c[3][j] * gs[3] + c[4][j] * gs[4] +
+                  c[5][j] * gs[5];
+          a3[j] = c[0][j] * gt[0] + c[1][j] * gt[1] + c[2][j] * gt[2] + c[3][j] * gt[3] + c[4][j] * gt[4] +
+                  c[5][j] * gt[5];
+          a2[j] = 0;
+          a4[j] = 0;
+          for (int m = 0; m < 6; ++m) a2[j] += Kp[9 * nd[m] + j * 3 + l] * gs[m];
+          for (int m = 0; m < 6; ++m) a4[j] += Kp[9 * nd[m] + j * 3 + l] * gt[m];
+          a5[j] = nN[3 * nd[i] + j];
+          a6[j] = 0;
+        }
+        solve_rows(Ke, a1, a2, a3, a4, a5, a6);
+        double *kr = K + 27 * nd[i];
+        for (int k = 0; k < 3; ++k)
+          for (int j = 0; j < 3; ++j) kr[j * 9 + k * 3 + l] += Ke[k][j];
+      }
+    }
+  }
+  for (int v = 0; v < NN; ++v) {
+    double *kr = K + 27 * v;
+    const double *n = nN + 3 * v;
+    const int cnt = s->node_ntri[v];
+    if (cnt <= 0) continue;
+    for (int m = 0; m < 27; ++m) kr[m] /= cnt;
+    for (int i = 0; i < 3; ++i) {
+      const double tr = kr[i] + kr[12 + i] + kr[24 + i];
+      for (int j = 0; j < 3; ++j) q[3 * v + j] += tr * ((i == j ? 1.0 : 0.0) - n[i] * n[j]);
+    }
+  }
+  for (int t = 0; t < T; ++t) {
+    const int *nd = s->tri + 6 * t;
+    double c[3][3], nv[6][3], tv[6][3], L[3], b[6][6], f[6][6], F[3];
+    for (int i = 0; i < 3; ++i) { c[i][0] = X[nd[i]]; c[i][1] = Y[nd[i]]; c[i][2] = Z[nd[i]]; }
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 3; ++j) nv[i][j] = nN[3 * nd[i] + j];
+    for (int j = 0; j < 3; ++j) {
+      tv[0][j] = c[0][j] - c[1][j];
+      tv[1][j] = c[1][j] - c[2][j];
+      tv[2][j] = c[2][j] - c[0][j];
+    }
+    for (int i = 0; i < 3; ++i) L[i] = nrm3(tv[i][0], tv[i][1], tv[i][2]);
+    for (int j = 0; j < 3; ++j) {
+      tv[3][j] = tv[0][j] / L[0];
+      tv[4][j] = tv[2][j] / L[2];
+      tv[5][j] = tv[1][j] / L[1];
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) tv[i][j] /= L[i];
+    /* b_i = t_i x n_i at every node; the vertices also along the other side
+     * that meets them (t2 at vertex 0, t0 at vertex 1, t1 at vertex 2) */
+    static const int other[3] = {2, 0, 1};
+    for (int i = 0; i < 6; ++i) {
+      b[i][0] = tv[i][1] * nv[i][2] - tv[i][2] * nv[i][1];
+      b[i][1] = tv[i][2] * nv[i][0] - tv[i][0] * nv[i][2];
+      b[i][2] = tv[i][0] * nv[i][1] - tv[i][1] * nv[i][0];
+      const double nb = nrm3(b[i][0], b[i][1], b[i][2]);
+      for (int j = 0; j < 3; ++j) b[i][j] /= nb;
+    }
+    for (int i = 0; i < 3; ++i) {
+      const double *o = tv[other[i]];
+      b[i][3] = o[1] * nv[i][2] - o[2] * nv[i][1];
+      b[i][4] = o[2] * nv[i][0] - o[0] * nv[i][2];
+      b[i][5] = o[0] * nv[i][1] - o[1] * nv[i][0];
+      const double nb = nrm3(b[i][3], b[i][4], b[i][5]);
+      for (int j = 3; j < 6; ++j) b[i][j] /= nb;
+    }
+    for (int i = 0; i < 6; ++i) {
+      const double *qq = q + 3 * nd[i];
+      const double bq = b[i][0] * qq[0] + b[i][1] * qq[1] + b[i][2] * qq[2];
+      const double bq2 = i < 3 ? b[i][3] * qq[0] + b[i][4] * qq[1] + b[i][5] * qq[2] : 0.0;
+      for (int j = 0; j < 3; ++j) {
+        f[i][j] = bq * nv[i][j];
+        if (i < 3) f[i][j + 3] = bq2 * nv[i][j];
+      }
+    }
+    for (int j = 0; j < 3; ++j)
+      F[j] = 0.5 * ((1 / 3.0 * (f[0][j] + f[1][j + 3]) + 4.0 / 3.0 * f[3][j]) * L[0] +
+                    (1 / 3.0 * (f[1][j] + f[2][j + 3]) + 4.0 / 3.0 * f[5][j]) * L[1] +
+                    (1 / 3.0 * (f[2][j] + f[0][j + 3]) + 4.0 / 3.0 * f[4][j]) * L[2]);
+    for (int i = 0; i < 3; ++i) {
+      const double Sv = S[nd[i]];
+      FX[nd[i]] += F[0] / Sv / F0;
+      FY[nd[i]] += F[1] / Sv / F0;
+      FZ[nd[i]] += F[2] / Sv / F0;
+    }
+  }
+  free(K);
+  free(q);
+}
+
 /* One platelet's membrane force pass: sem_Force_kernel (:320-513),
  * sem_calculate_A_kernel (:724-872), sem_surface_tension_kernel (:874-948),
  * sem_calculate_Kapa_kernel (:950-1055), sem_calculate_m_kernel (:1057-1128),
@@ -466,7 +611,7 @@ static void membrane_forces(pfo_sim *s, int p) {
       }
     }
   }
-  if (!(mask & (PF_MEM_AREAVOL | PF_MEM_BEND))) {
+  if (!(mask & (PF_MEM_AREAVOL | PF_MEM_BEND | PF_MEM_FEMBEND))) {
     s->SV[2 * p] = 0; s->SV[2 * p + 1] = 0;
     return;
   }
@@ -543,6 +688,7 @@ static void membrane_forces(pfo_sim *s, int p) {
   }
   s->SV[2 * p] = S_all;
   s->SV[2 * p + 1] = V;
+  if (mask & PF_MEM_FEMBEND) fem_bending(s, p, X, Y, Z, nN, Kp, S, FX, FY, FZ, F0);
   /* area and volume penalty forces */
   if (mask & PF_MEM_AREAVOL) {
     const double Ks = (double)s->mp[PF_P_KS], Kv = (double)s->mp[PF_P_KV];
@@ -921,6 +1067,102 @@ static void interp_marker(const pfo_sim *s, double x, double y, double z, double
   *vx = a0; *vy = a1; *vz = a2;
 }
 
+/* ------------------------------------------------ fibrin penalty coupling */
+/* Flow_vel_at_position (fiber.cpp:753-814): flow velocity and density at a
+ * fibrin node, summed over the stencil with the IBM kernel
+ * phi(r) = (1 + cos(pi r / 2)) / 4, |r| < 2 (r in lattice spacings), nodes
+ * of the Zou/He wall planes (the obstacle nodes there) skipped, weights not
+ * renormalised.  The text's DH1D (fiber.cpp:82-103) is that kernel with two
+ * slips, fixed here: its non-zero branch computes the value without
+ * returning it, and its callers pass distances already divided by dx. */
+static void fib_flow_at(const pfo_sim *s, double x, double y, double z, double u[3], double *rho) {
+  stw ax[5], ay[5], az[5];
+  int nxs = axis_stencil(x, s->dx, s->nx, s->sc.ibm_wrap[0], 0, ax);
+  int nys = axis_stencil(y, s->dx, s->ny, s->sc.ibm_wrap[1], 0, ay);
+  int nzs = axis_stencil(z, s->dx, s->nz, 0, 0, az);
+  const int walls = zouhe(s);
+  double a0 = 0, a1 = 0, a2 = 0, r = 0;
+  for (int c = 0; c < nzs; ++c) {
+    if (walls && (az[c].node == 0 || az[c].node == s->nz - 1)) continue;
+    for (int b = 0; b < nys; ++b)
+      for (int a = 0; a < nxs; ++a) {
+        double delta = ax[a].w * ay[b].w * az[c].w;
+        size_t n = (size_t)ax[a].node + (size_t)s->nx * (ay[b].node + (size_t)s->ny * az[c].node);
+        a0 += s->ux[n] * delta; a1 += s->uy[n] * delta; a2 += s->uz[n] * delta;
+        r += s->rho[n] * delta;
+      }
+  }
+  u[0] = a0; u[1] = a1; u[2] = a2;
+  *rho = r;
+}
+
+/* reference nodal force -> lattice force: F0/rho0/UMAX*1e12 * dt / C */
+static double fib_force_scale(const pfo_sim *s) {
+  const double Kd = (double)s->mp[PF_P_F0] / (double)s->mp[PF_P_RHO0] / (double)s->mp[PF_P_UMAX] *
+                    (double)s->mp[PF_P_UNIT];
+  return Kd * (double)s->dt / lattice_C(s);
+}
+
+/* fiber_LB_Fsi_force (fiber.cpp:501-600): the penalty force
+ * kappa rho (u - V) / dt on each node (lattice units; u and V in units of
+ * UMAX, so divided by C), and its reaction spread into the lattice force
+ * with the marker stencil.  The text adds +rho (u - V)/dt to the fluid
+ * populations, which pushes the fluid away from the node's velocity; the
+ * reaction (momentum exchange) is used here. */
+static void fibrin_penalty(pfo_sim *s) {
+  const double C = lattice_C(s), kc = fib_force_scale(s), kap = s->sc.fib_kappa;
+  for (int m = 0; m < s->M; ++m) {
+    double u[3], r;
+    fib_flow_at(s, s->fX[m], s->fY[m], s->fZ[m], u, &r);
+    const double f0 = kap * r * (u[0] - s->fVX[m]) / C;
+    const double f1 = kap * r * (u[1] - s->fVY[m]) / C;
+    const double f2 = kap * r * (u[2] - s->fVZ[m]) / C;
+    s->fsX[m] = f0; s->fsY[m] = f1; s->fsZ[m] = f2;
+    spread_marker(s, s->fX[m], s->fY[m], s->fZ[m], -f0 / kc, -f1 / kc, -f2 / kc);
+  }
+}
+
+/* network::solverkick (network.cpp:839-881) over half a lattice step:
+ * v <- e^{-gamma/2} v + a (1 - e^{-gamma/2}) / gamma (a/2 for gamma = 0),
+ * a = (link force + penalty force) / node mass in lattice units; fixed
+ * nodes rest. */
+static void fibrin_kick(pfo_sim *s) {
+  const double C = lattice_C(s), kc = fib_force_scale(s), F0 = (double)s->mp[PF_P_F0];
+  const double g = s->sc.fib_gamma, mass = s->sc.fib_node_mass;
+  const double vdt = exp(-0.5 * g), fdt = g > 0 ? (1.0 - vdt) / g : 0.5;
+  double *V[3] = {s->fVX, s->fVY, s->fVZ}, *F[3] = {s->fFX, s->fFY, s->fFZ}, *P[3] = {s->fsX, s->fsY, s->fsZ};
+  for (int m = 0; m < s->M; ++m)
+    for (int a = 0; a < 3; ++a) {
+      if (s->ffix[m]) { V[a][m] = 0; continue; }
+      const double acc = (F[a][m] / F0 * kc + P[a][m]) / mass;
+      V[a][m] = (vdt * (V[a][m] / C) + acc * fdt) * C;
+    }
+}
+
+/* network::Solve (network.cpp:445-513): kick, drift of the free nodes, link
+ * forces at the new positions, kick (the penalty force held over the step) */
+static void fibrin_integrate(pfo_sim *s) {
+  float dtT = s->dt / s->mp[PF_P_T0];
+  double Lx = s->nx * (double)s->dx, Ly = s->ny * (double)s->dx;
+  fibrin_kick(s);
+  for (int m = 0; m < s->M; ++m) {
+    if (s->ffix[m]) continue;
+    s->fX[m] += s->fVX[m] * dtT;
+    if (s->sc.ibm_wrap[0]) {
+      if (s->fX[m] > Lx) s->fX[m] -= Lx;
+      else if (s->fX[m] < 0) s->fX[m] += Lx;
+    }
+    s->fY[m] += s->fVY[m] * dtT;
+    if (s->sc.ibm_wrap[1]) {
+      if (s->fY[m] > Ly) s->fY[m] -= Ly;
+      else if (s->fY[m] < 0) s->fY[m] += Ly;
+    }
+    s->fZ[m] += s->fVZ[m] * dtT;
+  }
+  fibrin_forces(s);
+  fibrin_kick(s);
+}
+
 /* Node-centric loops of fluid3d_force_distribute_kernel and
  * fluid3d_velocity_distribute_kernel (LB_kernel.cu:1419-1642), including the
  * y-image pass for j<2 || j>ly-2; only for the reference's axis set
@@ -1078,6 +1320,63 @@ static void zouhe_bc(pfo_sim *s) {
   }
 }
 
+/* The velocity inlet (y=0) and outlet (y=ly-1) of
+ * fluid3d_in_out_flow_boundary_kernel (LB_kernel.cu:78-392, commented out in
+ * the reference; its launch slot is after the wall kernels and before the
+ * moments, semLB.cu:412-418).  Interior nodes of the two planes only
+ * (0 < i < lx-1, 0 < k < lz-1); the prescribed velocity is the shear
+ * profile (0, uw k/(lz-1), 0).  Rows next to the plane's edges
+ * (i = 1, lx-2; k = 1, lz-2) are reset to the equilibrium at INIT_RHO = 1
+ * (:120-153); the others get Zou/He unknowns (:155-246 inlet, :289-389
+ * outlet).  Corrected slips of the text: the inlet's f11 is built from f8
+ * (the text reads f9), and the outlet computes its own Nyx, Nyz (the text
+ * uses variables set only on the inlet branch).  The moments pass then
+ * recomputes density and velocity there (these nodes are not obstacles). */
+static void inout_bc(pfo_sim *s) {
+  const size_t N = s->N;
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const double C = lattice_C(s), uw = top_wall_uy(s);
+  double *f = s->fIN;
+  for (int k = 1; k < nz - 1; ++k)
+    for (int side = 0; side < 2; ++side) {
+      const int j = side ? ny - 1 : 0;
+      for (int i = 1; i < nx - 1; ++i) {
+        size_t n = (size_t)i + (size_t)nx * (j + (size_t)ny * k);
+#define FI(d) f[(size_t)(d)*N + n]
+        const double ux = 0.0, uy = uw * k / (nz - 1), uz = 0.0;
+        if (i == 1 || i == nx - 2 || k == 1 || k == nz - 2) {
+          for (int d = 0; d < 19; ++d) {
+            double cu = 3.0 * (CX[d] * ux + CY[d] * uy + CZ[d] * uz);
+            FI(d) = 1.0 * W19[d] * (1.0 + cu / C + 0.5 * cu * cu / (C * C) -
+                                    1.5 * (ux * ux + uy * uy + uz * uz) / (C * C));
+          }
+          continue;
+        }
+        const double inplane = FI(1) + FI(2) + FI(5) + FI(6) + FI(9) + FI(10) + FI(13) + FI(14) + FI(0);
+        if (side == 0) {
+          double rho = 1.0 / (1.0 - uy / C) * (inplane + 2.0 * (FI(4) + FI(8) + FI(12) + FI(17) + FI(18)));
+          double Nyx = 0.5 * (FI(1) + FI(9) + FI(10) - FI(2) - FI(13) - FI(14)) - 1.0 / 3.0 * rho * ux / C;
+          double Nyz = 0.5 * (FI(5) + FI(9) + FI(13) - FI(6) - FI(10) - FI(14)) - 1.0 / 3.0 * rho * uz / C;
+          FI(3) = FI(4) + 1.0 / 3.0 * rho * uy / C;
+          FI(7) = FI(12) + 1.0 / 6.0 * rho * (uy + ux) / C - Nyx;
+          FI(11) = FI(8) + 1.0 / 6.0 * rho * (uy - ux) / C + Nyx;
+          FI(15) = FI(18) + 1.0 / 6.0 * rho * (uy + uz) / C - Nyz;
+          FI(16) = FI(17) + 1.0 / 6.0 * rho * (uy - uz) / C + Nyz;
+        } else {
+          double rho = 1.0 / (1.0 + uy / C) * (inplane + 2.0 * (FI(3) + FI(7) + FI(11) + FI(15) + FI(16)));
+          double Nyx = 0.5 * (FI(1) + FI(9) + FI(10) - FI(2) - FI(13) - FI(14)) - 1.0 / 3.0 * rho * ux / C;
+          double Nyz = 0.5 * (FI(5) + FI(9) + FI(13) - FI(6) - FI(10) - FI(14)) - 1.0 / 3.0 * rho * uz / C;
+          FI(4) = FI(3) - 1.0 / 3.0 * rho * uy / C;
+          FI(12) = FI(7) + 1.0 / 6.0 * rho * (-uy - ux) / C + Nyx;
+          FI(8) = FI(11) + 1.0 / 6.0 * rho * (-uy + ux) / C - Nyx;
+          FI(18) = FI(15) + 1.0 / 6.0 * rho * (-uy - uz) / C + Nyz;
+          FI(17) = FI(16) + 1.0 / 6.0 * rho * (-uy + uz) / C - Nyz;
+        }
+#undef FI
+      }
+    }
+}
+
 /* fluid3d_velocity_density_kernel (LB_kernel.cu:1108-1199); the Zou/He
  * planes are obstacle nodes there (gpuSEM_LB.c:1150-1156) and keep the
  * boundary values. */
@@ -1127,7 +1426,7 @@ static void advance_positions(pfo_sim *s) {
     s->RY[g] += s->VY[g] * dtT;
     s->Z[g] += s->VZ[g] * dtT;
   }
-  for (int m = 0; m < s->M; ++m) {
+  for (int m = 0; m < s->M && !penalty(s); ++m) {
     if (s->ffix[m]) continue;
     s->fX[m] += s->fVX[m] * dtT;
     if (s->sc.ibm_wrap[0]) {
@@ -1175,7 +1474,9 @@ int pfo_step(pfo_sim *s, int nsteps) {
     } else {
       for (size_t g = 0; g < PE; ++g) spread_marker(s, s->X[g], s->Y[g], s->Z[g], s->FX[g], s->FY[g], s->FZ[g]);
     }
-    {
+    if (penalty(s)) {
+      fibrin_penalty(s);
+    } else {
       const double F0 = (double)s->mp[PF_P_F0];
       for (int m = 0; m < s->M; ++m)
         spread_marker(s, s->fX[m], s->fY[m], s->fZ[m], s->fFX[m] / F0, s->fFY[m] / F0, s->fFZ[m] / F0);
@@ -1187,6 +1488,7 @@ int pfo_step(pfo_sim *s, int nsteps) {
     collide(s);
     stream(s);
     if (zouhe(s)) zouhe_bc(s);
+    if (s->sc.bc[1] == PF_BC_INOUT) inout_bc(s);
     moments(s);
     if (brute_ok(s)) {
       brute_pass(s, 0);
@@ -1195,9 +1497,12 @@ int pfo_step(pfo_sim *s, int nsteps) {
       for (long long g = 0; g < (long long)PE; ++g)
         interp_marker(s, s->X[g], s->Y[g], s->Z[g], &s->VX[g], &s->VY[g], &s->VZ[g]);
     }
+    if (!penalty(s)) {
 #pragma omp parallel for num_threads(g_threads) schedule(static)
-    for (int m = 0; m < s->M; ++m) interp_marker(s, s->fX[m], s->fY[m], s->fZ[m], &s->fVX[m], &s->fVY[m], &s->fVZ[m]);
+      for (int m = 0; m < s->M; ++m) interp_marker(s, s->fX[m], s->fY[m], s->fZ[m], &s->fVX[m], &s->fVY[m], &s->fVZ[m]);
+    }
     advance_positions(s);
+    if (penalty(s)) fibrin_integrate(s);
     s->step++;
   }
   return s->done;

@@ -128,6 +128,7 @@ typedef struct refemu_case {
   double *km_out;              /* [newnode] out (may be null) */
   double *S_all_V_out;         /* [nsteps][2] out (may be null) */
   int first_lost_site_step;    /* out: first step after which a bonded receptor has site -1, or -1 */
+  int fem_bend;                /* in: also launch the FEM bending chain the reference comments out */
 } refemu_case;
 
 int refemu_run(refemu_case *c) {
@@ -321,6 +322,12 @@ int refemu_run(refemu_case *c) {
     launch(dim3(bpgNode), dim3(32), [&] { sem_surface_tension_kernel(gs); });
     launch(dim3(bpgFEM), dim3(32), [&] { sem_calculate_Kapa_kernel(gs); });
     launch(dim3(bpgNode), dim3(32), [&] { sem_calculate_m_kernel(gs); });
+    if (c->fem_bend) {
+      /* the three launches commented out at semLB.cu:518-520, in their slot */
+      launch(dim3(bpgFEM), dim3(32), [&] { sem_calculate_K_kernel(gs); });
+      launch(dim3(bpgNode), dim3(32), [&] { sem_calculate_q_kernel(gs); });
+      launch(dim3(bpgFEM), dim3(32), [&] { sem_bending_force_kernel(gs); });
+    }
     launch(dim3(bpgFEM), dim3(32), [&] { sem_ForceAreaVol_kernel(gs); });
     launch(dim3(bpgSEM), dim3(32), [&] { sem_Laplace_Kapa_kernel(gs); });
     if (c->S_all_V_out) {

@@ -128,6 +128,7 @@ struct Platelets {
   // membrane scratch (Real)
   void *nN = nullptr, *nelem = nullptr, *S = nullptr, *km = nullptr;
   double* SV = nullptr;  // [P][2]
+  void* fem = nullptr;   // Real [P][NN*12 + T*4]: FEM bending chain (PF_MEM_FEMBEND only)
   bool mem_items = false;  // FP32 membrane through the item-parallel kernel
   // receptors
   int *rec_tri = nullptr, *rec_state = nullptr, *vwf = nullptr;

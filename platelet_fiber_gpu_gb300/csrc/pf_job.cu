@@ -230,8 +230,19 @@ static int validate(const pf_scene* s, int precision) {
     return set_error(PFGPU_ERR_UNSUPPORTED, "Zou/He shear walls are only supported on z");
   if (s->bc[2] == PF_BC_ZOUHE_SHEAR && (s->bc[0] == PF_BC_BOUNCEBACK || s->bc[1] == PF_BC_BOUNCEBACK))
     return set_error(PFGPU_ERR_UNSUPPORTED, "Zou/He z walls need periodic x and y");
+  for (int a = 0; a < 3; ++a)
+    if (s->bc[a] < PF_BC_PERIODIC || s->bc[a] > PF_BC_INOUT) return set_error(PFGPU_ERR_INVALID, "unknown boundary kind");
+  if (s->bc[0] == PF_BC_INOUT || s->bc[2] == PF_BC_INOUT)
+    return set_error(PFGPU_ERR_UNSUPPORTED, "the inflow/outflow planes are only supported on y");
+  if (s->bc[1] == PF_BC_INOUT && (s->bc[2] != PF_BC_ZOUHE_SHEAR || s->bc[0] != PF_BC_PERIODIC || s->nx < 3 ||
+                                  s->nz < 3 || s->ny < 2))
+    return set_error(PFGPU_ERR_UNSUPPORTED, "inflow/outflow on y needs Zou/He shear walls on z, periodic x");
   if (s->n_platelets < 0 || s->n_elem < 0 || s->n_fib < 0 || s->n_rec < 0)
     return set_error(PFGPU_ERR_INVALID, "negative count");
+  if (s->membrane_forces & ~(PF_MEM_ALL | PF_MEM_FEMBEND))
+    return set_error(PFGPU_ERR_INVALID, "unknown membrane force bits");
+  if (s->n_fib > 0 && s->fib_coupling != PF_FIBCPL_MARKER)
+    return set_error(PFGPU_ERR_UNSUPPORTED, "fibrin coupling: only PF_FIBCPL_MARKER");
   if (s->n_platelets > 0) {
     if (!s->X || !s->Y || !s->RY || !s->Z) return set_error(PFGPU_ERR_INVALID, "element positions missing");
     if (s->n_membrane > s->n_elem) return set_error(PFGPU_ERR_INVALID, "n_membrane > n_elem");
@@ -361,6 +372,11 @@ static int build_platelets(pfgpu_job* j, const pf_scene* s) {
   CK(dalloc(j, (char**)&P.S, (size_t)k.P * k.T * rb));
   CK(dalloc(j, (char**)&P.km, (size_t)k.P * k.Em * rb));
   CK(dalloc(j, &P.SV, (size_t)k.P * 2));
+  if (k.mask & PF_MEM_FEMBEND) {
+    // the chain divides by S[vertex id] of the per-triangle area array
+    if (k.Em > k.T) return set_error(PFGPU_ERR_INVALID, "FEM bending needs at least as many triangles as vertices");
+    CK(dalloc(j, (char**)&P.fem, (size_t)k.P * ((size_t)k.NN * 12 + (size_t)k.T * 4) * rb));
+  }
   // receptors and wall sites
   const size_t NR = (size_t)k.P * k.nrec;
   CK(dupload(j, &P.rec_tri, s->rec_tri, NR));
@@ -617,6 +633,8 @@ size_t pfgpu_scene_device_bytes(const pf_scene* s, int precision) {
   const size_t PE = (size_t)s->n_platelets * s->n_elem;
   b += PE * (4 * 8 + 6 * 8 + 3 * 8 + 6 * rb);
   b += (size_t)s->n_platelets * ((size_t)s->n_node * 3 + (size_t)s->n_tri * 4 + s->n_membrane) * rb;
+  if (s->membrane_forces & PF_MEM_FEMBEND)
+    b += (size_t)s->n_platelets * ((size_t)s->n_node * 12 + (size_t)s->n_tri * 4) * rb;
   const size_t NR = (size_t)s->n_platelets * s->n_rec;
   b += NR * 64 + 4 * (size_t)s->nx * s->ny * 4;
   if (s->morse) {

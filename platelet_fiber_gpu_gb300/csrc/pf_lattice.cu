@@ -178,6 +178,50 @@ __device__ __forceinline__ R zouhe_top(R g[Q], R uw) {
   return drho;
 }
 
+// Velocity inlet (y=0) / outlet (y=ny-1) of LB_kernel.cu:78-392 at an
+// interior node (0 < x < nx-1, 0 < z < nz-1) of those planes, on shifted
+// populations in lattice units: u = (0, uw z/(nz-1), 0).  Rows next to the
+// plane's edges: the equilibrium at unit density (the reference's
+// re-initialisation).  Elsewhere Zou/He: the density from the in-plane and
+// outgoing populations (their weights add up to one, so
+// rho = (1 + G) / (1 -+ uy)), the unknowns from their opposites plus the
+// momentum terms and the transverse corrections Nyx, Nyz.  Two slips of the
+// reference's text are corrected: the inlet's f11 is built from f8 (the
+// text reads f9), and the outlet computes its own Nyx, Nyz (the text uses
+// values set only on the inlet branch).  The moments of the node are then
+// taken from these populations as everywhere else.
+template <class R>
+__device__ __forceinline__ void inout_y(const LatticeConst& k, R g[Q], int x, int y, int z) {
+  const R uy = kv<R>(k.uw, k.uw_f) * (R)z / (R)(k.nz - 1);
+  if (x == 1 || x == k.nx - 2 || z == 1 || z == k.nz - 2) {
+    const R usq = uy * uy;
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      const R cu = (R)cy(d) * uy;
+      g[d] = (R)wgt(d) * ((R)3 * cu + (R)4.5 * cu * cu - (R)1.5 * usq);
+    }
+    return;
+  }
+  const R inplane = g[1] + g[2] + g[5] + g[6] + g[9] + g[10] + g[13] + g[14] + g[0];
+  const R Nyx = (R)0.5 * (g[1] + g[9] + g[10] - g[2] - g[13] - g[14]);
+  const R Nyz = (R)0.5 * (g[5] + g[9] + g[13] - g[6] - g[10] - g[14]);
+  if (y == 0) {
+    const R rho = ((R)1 + inplane + (R)2 * (g[4] + g[8] + g[12] + g[17] + g[18])) / ((R)1 - uy);
+    g[3] = g[4] + (R)(1.0 / 3.0) * rho * uy;
+    g[7] = g[12] + (R)(1.0 / 6.0) * rho * uy - Nyx;
+    g[11] = g[8] + (R)(1.0 / 6.0) * rho * uy + Nyx;
+    g[15] = g[18] + (R)(1.0 / 6.0) * rho * uy - Nyz;
+    g[16] = g[17] + (R)(1.0 / 6.0) * rho * uy + Nyz;
+  } else {
+    const R rho = ((R)1 + inplane + (R)2 * (g[3] + g[7] + g[11] + g[15] + g[16])) / ((R)1 + uy);
+    g[4] = g[3] - (R)(1.0 / 3.0) * rho * uy;
+    g[12] = g[7] - (R)(1.0 / 6.0) * rho * uy + Nyx;
+    g[8] = g[11] - (R)(1.0 / 6.0) * rho * uy - Nyx;
+    g[18] = g[15] - (R)(1.0 / 6.0) * rho * uy + Nyz;
+    g[17] = g[16] - (R)(1.0 / 6.0) * rho * uy - Nyz;
+  }
+}
+
 template <class R>
 __device__ __forceinline__ void moments(const R g[Q], R& drho, R& jx, R& jy, R& jz) {
   drho = 0; jx = 0; jy = 0; jz = 0;
@@ -194,9 +238,20 @@ __device__ __forceinline__ void moments(const R g[Q], R& drho, R& jx, R& jy, R& 
 // (boundary values on the Zou/He planes, half-force corrected moments
 // elsewhere).  drho is carried separately: rounding 1 + drho in FP32 would
 // put ~6e-8 of noise into the density every step.
+// Whether linear node n of plane z is an interior node of an inflow/outflow
+// plane.
+__device__ __forceinline__ bool on_inout(const LatticeConst& k, size_t n, int z) {
+  if (k.bc[1] != PF_BC_INOUT || z == 0 || z == k.nz - 1) return false;
+  const int y = (int)((n / (size_t)k.nx) % (size_t)k.ny);
+  if (y != 0 && y != k.ny - 1) return false;
+  const int x = (int)(n % (size_t)k.nx);
+  return x > 0 && x < k.nx - 1;
+}
 template <class R>
-__device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z, bool apply_bc, R Fx, R Fy,
-                                           R Fz, R& drho, R& ux, R& uy, R& uz) {
+__device__ __forceinline__ void node_state(const LatticeConst& k, R g[Q], int z, size_t n, bool apply_bc, R Fx,
+                                           R Fy, R Fz, R& drho, R& ux, R& uy, R& uz) {
+  if (apply_bc && on_inout(k, n, z))
+    inout_y<R>(k, g, (int)(n % (size_t)k.nx), (int)((n / (size_t)k.nx) % (size_t)k.ny), z);
   if (apply_bc && k.bc[2] == PF_BC_ZOUHE_SHEAR && z == 0) {
     drho = zouhe_bottom(g);
     ux = 0; uy = 0; uz = 0;
@@ -288,7 +343,7 @@ __device__ __forceinline__ void node_q(const LatticeConst& k, float q[Q], int z,
   if (fc) ld_force<float>(Fc, n, Fx, Fy, Fz);
   Fx *= kc; Fy *= kc; Fz *= kc;
   float drho, ux, uy, uz;
-  if (k.bc[2] == PF_BC_ZOUHE_SHEAR && (z == 0 || z == k.nz - 1)) {
+  if ((k.bc[2] == PF_BC_ZOUHE_SHEAR && (z == 0 || z == k.nz - 1)) || on_inout(k, n, z)) {
     float g[Q];
 #pragma unroll
     for (int d = 0; d < Q; ++d) g[d] = q[d] * k.hs[wcls(d)];
@@ -297,7 +352,7 @@ __device__ __forceinline__ void node_q(const LatticeConst& k, float q[Q], int z,
     } else {
       float px = k.body_f[0], py = k.body_f[1], pz = k.body_f[2];
       if (fp) ld_force<float>(Fp, n, px, py, pz);
-      node_state<float>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
+      node_state<float>(k, g, z, n, true, px, py, pz, drho, ux, uy, uz);
     }
     collide<float>(g, drho, ux, uy, uz, Fx, Fy, Fz, om, sf);
 #pragma unroll
@@ -376,7 +431,7 @@ __device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restr
   } else {
     R px = kv<R>(k.body[0], k.body_f[0]), py = kv<R>(k.body[1], k.body_f[1]), pz = kv<R>(k.body[2], k.body_f[2]);
     if (fp) ld_force<R>(Fp, n, px, py, pz);
-    node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
+    node_state<R>(k, g, z, n, true, px, py, pz, drho, ux, uy, uz);
   }
   R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
   if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
@@ -636,7 +691,7 @@ __device__ __forceinline__ void vec_collide_store(const LatticeConst& k, S* __re
       } else {
         float px = k.body_f[0], py = k.body_f[1], pz = k.body_f[2];
         if (fp) ld_force<float>(Fp, n, px, py, pz);
-        node_state<float>(k, g, (int)z, true, px, py, pz, drho, ux, uy, uz);
+        node_state<float>(k, g, (int)z, (size_t)n, true, px, py, pz, drho, ux, uy, uz);
       }
       float Fx = k.body_f[0], Fy = k.body_f[1], Fz = k.body_f[2];
       if (fc) ld_force<float>(Fc, n, Fx, Fy, Fz);
@@ -1000,7 +1055,7 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
     } else {
       R px = kv<R>(k.body[0], k.body_f[0]), py = kv<R>(k.body[1], k.body_f[1]), pz = kv<R>(k.body[2], k.body_f[2]);
       if (fp) ld_force<R>(Fp, n, px, py, pz);
-      node_state<R>(k, g, z, true, px, py, pz, drho, ux, uy, uz);
+      node_state<R>(k, g, z, n, true, px, py, pz, drho, ux, uy, uz);
     }
     R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
     if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
@@ -1097,7 +1152,7 @@ __device__ __forceinline__ void moments_body(const LatticeConst& k, const S* gA,
     R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
     ld_force<R>(Fc, n, Fx, Fy, Fz);
     R drho, ux, uy, uz;
-    node_state<R>(k, g, z, true, Fx, Fy, Fz, drho, ux, uy, uz);
+    node_state<R>(k, g, z, n, true, Fx, Fy, Fz, drho, ux, uy, uz);
     st_u<R>(ubuf, n, drho, ux, uy, uz);
   }
 }
@@ -1167,7 +1222,7 @@ __global__ void download_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, con
   if (use_ubuf) {
     ld_u<R>(ubuf, n, drho, ux, uy, uz);
   } else {
-    node_state<R>(k, g, z, apply_bc != 0, Fx, Fy, Fz, drho, ux, uy, uz);
+    node_state<R>(k, g, z, n, apply_bc != 0, Fx, Fy, Fz, drho, ux, uy, uz);
   }
   for (int d = 0; d < Q; ++d) {
     if (fIN) fIN[(size_t)d * N + n] = (double)g[d] + wgt(d);
@@ -1204,7 +1259,7 @@ __global__ void fields_k(LatticeConst k, const S* gsrc, const R4<R>* Fsrc, const
   } else {
     R g[Q];
     gather<S, R>(k, gsrc, x, y, z, g);
-    node_state<R>(k, g, z, apply_bc != 0, Fx, Fy, Fz, drho, vx, vy, vz);
+    node_state<R>(k, g, z, n, apply_bc != 0, Fx, Fy, Fz, drho, vx, vy, vz);
   }
   if (rho) rho[m] = (float)(1.0 + (double)drho);
   if (ux) {

@@ -946,6 +946,147 @@ __device__ __forceinline__ R nrm3(R a, R b, R c) {
   return sqrt(a * a + b * b + c * c);
 }
 
+// Derivatives of the quadratic 6-node triangle's shape functions at its
+// node li, (s, t) = (0,0) (1,0) (0,1) (.5,0) (0,.5) (.5,.5):
+// N0 = (1-s-t)(1-2s-2t), N1 = s(2s-1), N2 = t(2t-1), N3 = 4s(1-s-t),
+// N4 = 4t(1-s-t), N5 = 4st (the table of sem_kernel.cu:92-100).
+template <class R>
+__device__ __forceinline__ void p2_grad(int li, R gs[6], R gt[6]) {
+  const R s_ = (li == 1) ? (R)1 : (li == 3 || li == 5) ? (R)0.5 : (R)0;
+  const R t_ = (li == 2) ? (R)1 : (li == 4 || li == 5) ? (R)0.5 : (R)0;
+  gs[0] = 4 * s_ + 4 * t_ - 3; gs[1] = 4 * s_ - 1; gs[2] = 0;
+  gs[3] = -8 * s_ - 4 * t_ + 4; gs[4] = -4 * t_; gs[5] = 4 * t_;
+  gt[0] = 4 * t_ + 4 * s_ - 3; gt[1] = 0; gt[2] = 4 * t_ - 1;
+  gt[3] = -4 * s_; gt[4] = -8 * t_ - 4 * s_ + 4; gt[5] = 4 * s_;
+}
+// Position of node v among a triangle's 6 nodes (6 if absent).
+__device__ __forceinline__ int local_of(const int* nd, int v) {
+  int i = 0;
+  while (i < 6 && nd[i] != v) ++i;
+  return i;
+}
+
+// FEM bending chain, the reference's sem_calculate_K_kernel and
+// sem_calculate_q_kernel (sem_kernel.cu:1129-1306), one thread per node,
+// gathering over the node's triangles in ascending order (the order of the
+// reference's atomics under a serial schedule).  Per triangle and column l
+// of the nodes' curvature tensors the 3x3 system with rows (dx/ds, dx/dt,
+// n) and right-hand sides (dKapa_l/ds, dKapa_l/dt, 0) is solved; q needs
+// only the diagonal K[j][j][l] of the accumulated third-order tensor:
+// traceK_l = sum_j K[j][j][l] / count, q = (I - n n) traceK.
+template <class R, class Pos>
+__device__ __forceinline__ void fem_q(int NN, int Em, const int* tri, const int* node_ntri, const int* node_tri,
+                                      const int* vert_local, const R* nNp, const R* kap, R* qv, Pos P3) {
+  for (int v = threadIdx.x; v < NN; v += blockDim.x) {
+    const int cnt = node_ntri[v];
+    R Kd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [j][l]
+    for (int j = 0; j < cnt; ++j) {
+      const int t = node_tri[10 * v + j];
+      const int* nd = tri + 6 * t;
+      const int li = v < Em ? vert_local[10 * v + j] : local_of(nd, v);
+      R c[6][3];
+      P3(nd[0], c[0]); P3(nd[1], c[1]); P3(nd[2], c[2]);
+      for (int i = 0; i < 3; ++i) {
+        c[3][i] = (R)0.5 * (c[0][i] + c[1][i]);
+        c[4][i] = (R)0.5 * (c[0][i] + c[2][i]);
+        c[5][i] = (R)0.5 * (c[1][i] + c[2][i]);
+      }
+      R gs[6], gt[6];
+      p2_grad<R>(li, gs, gt);
+      R a1[3], a3[3];
+      for (int d = 0; d < 3; ++d) {
+        a1[d] = c[0][d] * gs[0] + c[1][d] * gs[1] + c[2][d] * gs[2] + c[3][d] * gs[3] + c[4][d] * gs[4] +
+                c[5][d] * gs[5];
+        a3[d] = c[0][d] * gt[0] + c[1][d] * gt[1] + c[2][d] * gt[2] + c[3][d] * gt[3] + c[4][d] * gt[4] +
+                c[5][d] * gt[5];
+      }
+      for (int l = 0; l < 3; ++l) {
+        R g[3][6];
+        for (int d = 0; d < 3; ++d) {
+          R a2 = 0, a4 = 0;
+          for (int m = 0; m < 6; ++m) a2 += kap[9 * nd[m] + 3 * d + l] * gs[m];
+          for (int m = 0; m < 6; ++m) a4 += kap[9 * nd[m] + 3 * d + l] * gt[m];
+          g[0][d] = a1[d]; g[1][d] = a3[d]; g[2][d] = nNp[3 * nd[li] + d];
+          g[0][3 + d] = a2; g[1][3 + d] = a4; g[2][3 + d] = 0;
+        }
+        gauss36<R>(g);
+        // diagonal entries A[d][d] of the solution rows
+        const R A22 = g[2][5];
+        const R A11 = g[1][4] - g[2][4] * g[1][2];
+        const R A0_2 = g[2][3];
+        const R A0_1 = g[1][3] - A0_2 * g[1][2];
+        const R A00 = g[0][3] - A0_2 * g[0][2] - A0_1 * g[0][1];
+        Kd[0][l] += A00;
+        Kd[1][l] += A11;
+        Kd[2][l] += A22;
+      }
+    }
+    R qq[3] = {0, 0, 0};
+    if (cnt > 0) {
+      const R n[3] = {nNp[3 * v], nNp[3 * v + 1], nNp[3 * v + 2]};
+      for (int i = 0; i < 3; ++i) {
+        const R tr = Kd[0][i] / (R)cnt + Kd[1][i] / (R)cnt + Kd[2][i] / (R)cnt;
+        for (int j = 0; j < 3; ++j) qq[j] += tr * ((i == j ? (R)1 : (R)0) - n[i] * n[j]);
+      }
+    }
+    qv[3 * v] = qq[0]; qv[3 * v + 1] = qq[1]; qv[3 * v + 2] = qq[2];
+  }
+}
+
+// The reference's sem_bending_force_kernel (sem_kernel.cu:1308-1497), one
+// thread per triangle: unit side tangents t, in-plane normals b = t x n at
+// the six nodes (the vertices also along their second side), line loads
+// f = (b . q) n and Simpson's rule along the sides.  The load goes to
+// ft[t]; the vertices gather it.
+template <class R, class Pos>
+__device__ __forceinline__ void fem_loads(int T, const int* tri, const R* nNp, const R* qv, R* ft, Pos P3) {
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    const int* nd = tri + 6 * t;
+    R c[3][3], nv[6][3], tv[6][3], L[3], f[6][6];
+    P3(nd[0], c[0]); P3(nd[1], c[1]); P3(nd[2], c[2]);
+    for (int i = 0; i < 6; ++i)
+      for (int d = 0; d < 3; ++d) nv[i][d] = nNp[3 * nd[i] + d];
+    for (int d = 0; d < 3; ++d) {
+      tv[0][d] = c[0][d] - c[1][d];
+      tv[1][d] = c[1][d] - c[2][d];
+      tv[2][d] = c[2][d] - c[0][d];
+    }
+    for (int i = 0; i < 3; ++i) L[i] = nrm3(tv[i][0], tv[i][1], tv[i][2]);
+    for (int d = 0; d < 3; ++d) {
+      tv[3][d] = tv[0][d] / L[0];
+      tv[4][d] = tv[2][d] / L[2];
+      tv[5][d] = tv[1][d] / L[1];
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int d = 0; d < 3; ++d) tv[i][d] /= L[i];
+    for (int i = 0; i < 6; ++i) {
+      R b[3];
+      b[0] = tv[i][1] * nv[i][2] - tv[i][2] * nv[i][1];
+      b[1] = tv[i][2] * nv[i][0] - tv[i][0] * nv[i][2];
+      b[2] = tv[i][0] * nv[i][1] - tv[i][1] * nv[i][0];
+      const R nb = nrm3(b[0], b[1], b[2]);
+      for (int d = 0; d < 3; ++d) b[d] /= nb;
+      const R* q = qv + 3 * nd[i];
+      const R bq = b[0] * q[0] + b[1] * q[1] + b[2] * q[2];
+      for (int d = 0; d < 3; ++d) f[i][d] = bq * nv[i][d];
+      if (i < 3) {
+        const R* o = tv[i == 0 ? 2 : i - 1];  // t2 at vertex 0, t0 at 1, t1 at 2
+        b[0] = o[1] * nv[i][2] - o[2] * nv[i][1];
+        b[1] = o[2] * nv[i][0] - o[0] * nv[i][2];
+        b[2] = o[0] * nv[i][1] - o[1] * nv[i][0];
+        const R nb2 = nrm3(b[0], b[1], b[2]);
+        for (int d = 0; d < 3; ++d) b[d] /= nb2;
+        const R bq2 = b[0] * q[0] + b[1] * q[1] + b[2] * q[2];
+        for (int d = 0; d < 3; ++d) f[i][d + 3] = bq2 * nv[i][d];
+      }
+    }
+    for (int d = 0; d < 3; ++d)
+      ft[3 * t + d] = (R)0.5 * (((R)(1 / 3.0) * (f[0][d] + f[1][d + 3]) + (R)(4.0 / 3.0) * f[3][d]) * L[0] +
+                                ((R)(1 / 3.0) * (f[1][d] + f[2][d + 3]) + (R)(4.0 / 3.0) * f[5][d]) * L[1] +
+                                ((R)(1 / 3.0) * (f[2][d] + f[0][d + 3]) + (R)(4.0 / 3.0) * f[4][d]) * L[2]);
+  }
+}
+
 // One CTA per platelet: springs + wall, triangle areas/normals and the global
 // area/volume (FP64 sums), nodal normals, curvature tensor and mean
 // curvature at the vertices, area/volume penalty and bending forces.  Every
@@ -958,7 +1099,7 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
                                                   const int* vert_local, const int* ring, const int* sp_ptr,
                                                   const int* sp_nbr, const double* sp_L0, const double* S0,
                                                   const double* S0_all, const double* V0, R* nN, R* nelem, R* S,
-                                                  R* kmv, double* SV, R* Fmem, Control* ctl) {
+                                                  R* kmv, double* SV, R* Fmem, Control* ctl, R* fem) {
   if (ctl->done) return;
   const int p = blockIdx.x;
   const int E = k.E, Em = k.Em, T = k.T, NN = k.NN, PE = k.P * k.E;
@@ -991,6 +1132,14 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
   R* nep = nelem + (size_t)p * T * 3;
   R* Sp = S + (size_t)p * T;
   R* kmp = kmv + (size_t)p * Em;
+  // FEM bending chain (mask PF_MEM_FEMBEND): per platelet the symmetrised
+  // curvature tensors of all nodes [NN][9], the q vectors [NN][3], the
+  // triangles' bending loads [T][3] and areas [T]
+  const bool use_fem = (k.mask & PF_MEM_FEMBEND) && fem;
+  R* kapp = use_fem ? fem + (size_t)p * ((size_t)NN * 12 + (size_t)T * 4) : nullptr;
+  R* qvp = kapp ? kapp + (size_t)NN * 9 : nullptr;
+  R* ftp = kapp ? qvp + (size_t)NN * 3 : nullptr;
+  R* arp = kapp ? ftp + (size_t)T * 3 : nullptr;
   __shared__ double s_a[512], s_b[512];
   __shared__ int s_i[512];
   __shared__ double s_Sall, s_V;
@@ -1059,7 +1208,7 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
     Fmem[PE + base + e] = fy;
     Fmem[2 * PE + base + e] = fz;
   }
-  if (!(k.mask & (PF_MEM_AREAVOL | PF_MEM_BEND))) {
+  if (!(k.mask & (PF_MEM_AREAVOL | PF_MEM_BEND)) && !use_fem) {
     if (threadIdx.x == 0) { SV[2 * p] = 0; SV[2 * p + 1] = 0; }
     return;
   }
@@ -1084,6 +1233,7 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
     const R St = (R)0.5 * nn;
     const R S0e = (R)S0[(size_t)p * T + t];
     Sp[t] = (St - S0e) / S0e;
+    if (arp) arp[t] = St;
     nep[3 * t] = n[0]; nep[3 * t + 1] = n[1]; nep[3 * t + 2] = n[2];
     pa += (double)St;
     pv += (double)((R)(1 / 3.0) * (cc[0] * n[0] + cc[1] * n[1] + cc[2] * n[2]) * St);
@@ -1122,14 +1272,16 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
   }
   __syncthreads();
   // curvature tensor at each vertex from its triangles (6-node element),
-  // mean curvature km = tr/2 of the node average
-  for (int v = threadIdx.x; v < Em; v += blockDim.x) {
+  // mean curvature km = tr/2 of the node average; with the FEM chain at the
+  // mid-side nodes too, and the symmetrised node averages kept
+  const int ncurv = use_fem ? NN : Em;
+  for (int v = threadIdx.x; v < ncurv; v += blockDim.x) {
     const int cnt = node_ntri[v];
     R K[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int j = 0; j < cnt; ++j) {
       const int t = node_tri[10 * v + j];
-      const int li = vert_local[10 * v + j];
       const int* nd = tri + 6 * t;
+      const int li = v < Em ? vert_local[10 * v + j] : local_of(nd, v);
       R c[6][3], nv[6][3];
       P3(nd[0], c[0]); P3(nd[1], c[1]); P3(nd[2], c[2]);
       for (int i = 0; i < 3; ++i) {
@@ -1139,9 +1291,8 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
       }
       for (int i = 0; i < 6; ++i)
         for (int d = 0; d < 3; ++d) nv[i][d] = nNp[3 * nd[i] + d];
-      const R s_ = li == 1 ? (R)1 : (R)0, t_ = li == 2 ? (R)1 : (R)0;
-      const R gs[6] = {4 * s_ + 4 * t_ - 3, 4 * s_ - 1, 0, -8 * s_ - 4 * t_ + 4, -4 * t_, 4 * t_};
-      const R gt[6] = {4 * t_ + 4 * s_ - 3, 0, 4 * t_ - 1, -4 * s_, -8 * t_ - 4 * s_ + 4, 4 * s_};
+      R gs[6], gt[6];
+      p2_grad<R>(li, gs, gt);
       R a1[3], a2[3], a3[3], a4[3];
       for (int d = 0; d < 3; ++d) {
         a1[d] = c[0][d] * gs[0] + c[1][d] * gs[1] + c[2][d] * gs[2] + c[3][d] * gs[3] + c[4][d] * gs[4] +
@@ -1168,17 +1319,41 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) K[a * 3 + b] += A[b][a];
     }
-    R km = 0;
-    if (cnt > 0) km = (R)0.5 * (K[0] / (R)cnt + K[4] / (R)cnt + K[8] / (R)cnt);
-    kmp[v] = km;
+    if (v < Em) {
+      R km = 0;
+      if (cnt > 0) km = (R)0.5 * (K[0] / (R)cnt + K[4] / (R)cnt + K[8] / (R)cnt);
+      kmp[v] = km;
+    }
+    if (kapp)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          kapp[9 * v + 3 * a + b] = cnt > 0 ? (R)0.5 * (K[a * 3 + b] / (R)cnt + K[b * 3 + a] / (R)cnt) : (R)0;
   }
   __syncthreads();
+  if (use_fem) {
+    fem_q<R>(NN, Em, tri, node_ntri, node_tri, vert_local, nNp, kapp, qvp, P3);
+    __syncthreads();
+    fem_loads<R>(T, tri, nNp, qvp, ftp, P3);
+    __syncthreads();
+  }
   // area/volume penalty (sem_kernel.cu:1640-1749) and bending
   // (:1499-1638) at each vertex
   const double Sall = s_Sall, Vol = s_V;
   for (int v = threadIdx.x; v < Em; v += blockDim.x) {
     R fx = Fmem[base + v], fy = Fmem[PE + base + v], fz = Fmem[2 * PE + base + v];
     const int cnt = node_ntri[v];
+    if (use_fem) {
+      // each triangle's load to its vertices, divided by S[vertex id]: the
+      // area of the triangle whose index is the vertex id
+      // (sem_kernel.cu:1484-1495)
+      const R Sv = arp[v];
+      for (int j = 0; j < cnt; ++j) {
+        const int t = node_tri[10 * v + j];
+        fx += ftp[3 * t] / Sv / F0;
+        fy += ftp[3 * t + 1] / Sv / F0;
+        fz += ftp[3 * t + 2] / Sv / F0;
+      }
+    }
     if (k.mask & PF_MEM_AREAVOL) {
       const R Ks = (R)k.ks, Kv = (R)k.kv;
       const R sglob = (R)((Sall - S0_all[p]) / S0_all[p]);
@@ -2562,6 +2737,7 @@ int membrane_threads() { return 512; }
 constexpr size_t kMem32MaxSmem = 200u << 10;
 bool membrane_items(const PlateletConst& k) {
   if (getenv("PFGPU_MEMBRANE_PER_VERTEX")) return false;
+  if (k.mask & PF_MEM_FEMBEND) return false;  // the FEM chain is in the per-vertex kernel only
   return Mem32Layout(k).bytes <= kMem32MaxSmem && k.E < (1 << 26);
 }
 
@@ -2592,12 +2768,12 @@ cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStre
     membrane_k<double><<<k.P, 512, 0, st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
                                             Pl.vert_local, Pl.ring, Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0,
                                             Pl.S0_all, Pl.V0, (double*)Pl.nN, (double*)Pl.nelem, (double*)Pl.S,
-                                            (double*)Pl.km, Pl.SV, (double*)Pl.Fmem, ctl);
+                                            (double*)Pl.km, Pl.SV, (double*)Pl.Fmem, ctl, (double*)Pl.fem);
   else
     membrane_k<float><<<k.P, 512, (size_t)k.E * 4 * sizeof(float), st>>>(k, Pl.X, Pl.Y, Pl.RY, Pl.Z, Pl.tri, Pl.node_ntri, Pl.node_tri,
                                            Pl.vert_local, Pl.ring, Pl.sp_ptr, Pl.sp_nbr, Pl.sp_L0, Pl.S0,
                                            Pl.S0_all, Pl.V0, (float*)Pl.nN, (float*)Pl.nelem, (float*)Pl.S,
-                                           (float*)Pl.km, Pl.SV, (float*)Pl.Fmem, ctl);
+                                           (float*)Pl.km, Pl.SV, (float*)Pl.Fmem, ctl, (float*)Pl.fem);
   return cudaGetLastError();
 }
 
@@ -2616,11 +2792,11 @@ cudaError_t membrane_forces_raw(const PlateletConst& k, int precision, const dou
   if (precision == PF_PREC_FP64)
     membrane_k<double><<<k.P, 512, 0, st>>>(k, X, Y, RY, Z, tri, node_ntri, node_tri, vert_local, ring, sp_ptr,
                                             sp_nbr, sp_L0, S0, S0_all, V0, (double*)nN, (double*)nelem, (double*)S,
-                                            (double*)km, SV, (double*)F, ctl);
+                                            (double*)km, SV, (double*)F, ctl, nullptr);
   else
     membrane_k<float><<<k.P, 512, (size_t)k.E * 4 * sizeof(float), st>>>(
         k, X, Y, RY, Z, tri, node_ntri, node_tri, vert_local, ring, sp_ptr, sp_nbr, sp_L0, S0, S0_all, V0,
-        (float*)nN, (float*)nelem, (float*)S, (float*)km, SV, (float*)F, ctl);
+        (float*)nN, (float*)nelem, (float*)S, (float*)km, SV, (float*)F, ctl, nullptr);
   return cudaGetLastError();
 }
 

@@ -93,6 +93,8 @@ extern "C" int pfgpu_membrane_forces_noalloc(const pf_membrane_args* a, void* st
     return report_error(PFGPU_ERR_INVALID, "membrane args: bad counts");
   if (a->precision < PF_PREC_FP64 || a->precision > PF_PREC_FP16)
     return report_error(PFGPU_ERR_INVALID, "membrane args: bad precision");
+  if (a->membrane_forces & ~PF_MEM_ALL)
+    return report_error(PFGPU_ERR_INVALID, "membrane args: only the PF_MEM_ALL terms (no FEM bending chain)");
   if (!a->X || !a->Y || !a->RY || !a->Z || !a->tri || !a->node_ntri || !a->ring || !a->spring_ptr || !a->S0 ||
       !a->S0_all || !a->V0 || !a->F_out)
     return report_error(PFGPU_ERR_INVALID, "membrane args: missing device array");

@@ -14,10 +14,17 @@ from dataclasses import dataclass, field
 import numpy as np
 
 BC_PERIODIC, BC_BOUNCEBACK, BC_ZOUHE_SHEAR = 0, 1, 2
+# velocity inlet at y=0 / outlet at y=ny-1 with the shear profile (y only)
+BC_INOUT = 3
 PREC_FP64, PREC_FP32, PREC_FP16 = 0, 1, 2
 BOND_BELL, BOND_CONSTANT = 0, 1
 FIB_HOOKE, FIB_WLC = 0, 1
+# fibrin nodes as immersed markers, or with their own velocity and the
+# penalty coupling of the reference's fibrin FSI design
+FIBCPL_MARKER, FIBCPL_PENALTY = 0, 1
 MEM_SPRING, MEM_WALL, MEM_AREAVOL, MEM_BEND, MEM_ALL = 1, 2, 4, 8, 15
+# the reference's disabled FEM bending chain, added to the chain it runs
+MEM_FEMBEND = 16
 
 P_NUMRECEPTORS, P_SEED, P_KSPRING, P_KF0, P_KR0, P_SHEAR, P_RHO0, P_L0, P_T0, P_M0, P_F0, \
     P_UMAX, P_NU, P_TAU, P_P0, P_CL, P_UNIT, P_KS, P_KV, P_KBEND = range(20)
@@ -50,6 +57,8 @@ class PfScene(C.Structure):
         ("fib_fixed", _ip), ("fib_ptr", _ip), ("fib_nbr", _ip), ("fib_L0", _dp),
         ("fib_law", C.c_int), ("fib_k", C.c_double), ("fib_mass", C.c_double),
         ("seed", C.c_uint64), ("detach_rate", C.c_double),
+        ("fib_coupling", C.c_int), ("fib_gamma", C.c_double), ("fib_node_mass", C.c_double),
+        ("fib_kappa", C.c_double),
     ]
 
 
@@ -175,6 +184,10 @@ class Scene:
     fib_mass: float = 1.0
     seed: int = 1
     detach_rate: float = 0.0
+    fib_coupling: int = FIBCPL_MARKER
+    fib_gamma: float = 0.0
+    fib_node_mass: float = 1.0
+    fib_kappa: float = 1.0
     meta: dict = field(default_factory=dict)
 
     @property
@@ -243,6 +256,8 @@ class Scene:
         s.fib_law, s.fib_k, s.fib_mass = self.fib_law, self.fib_k, self.fib_mass
         s.seed = int(self.seed) & ((1 << 64) - 1)
         s.detach_rate = self.detach_rate
+        s.fib_coupling, s.fib_gamma = self.fib_coupling, self.fib_gamma
+        s.fib_node_mass, s.fib_kappa = self.fib_node_mass, self.fib_kappa
         s._keep = a  # noqa: SLF001 -- keeps the arrays referenced by the pointers alive
         return s
 
@@ -252,7 +267,8 @@ _ARRAY_FIELDS = ("params", "f_init", "u_init", "F_init", "rho_init", "tri", "nod
                  "rec_state", "vwf", "fib_X", "fib_Y", "fib_Z", "fib_fixed", "fib_ptr", "fib_nbr", "fib_L0")
 _SCALAR_FIELDS = ("nx", "ny", "nz", "dx", "dt", "bc", "ibm_wrap", "body_force", "n_platelets", "n_elem",
                   "n_membrane", "membrane_forces", "n_rec", "bond_model", "p_on", "p_off", "morse",
-                  "morse_intra", "morse_inter", "n_fib", "fib_law", "fib_k", "fib_mass", "seed", "detach_rate")
+                  "morse_intra", "morse_inter", "n_fib", "fib_law", "fib_k", "fib_mass", "seed", "detach_rate",
+                  "fib_coupling", "fib_gamma", "fib_node_mass", "fib_kappa")
 
 
 def scene_to_dict(sc: Scene, prefix: str = "scene.") -> dict:
@@ -270,6 +286,8 @@ def scene_to_dict(sc: Scene, prefix: str = "scene.") -> dict:
 def scene_from_dict(d, prefix: str = "scene.") -> Scene:
     kw = {}
     for k in _SCALAR_FIELDS:
+        if (prefix + k) not in d:
+            continue  # written before the field existed: the default
         v = np.asarray(d[prefix + k])
         kw[k] = tuple(v.tolist()) if v.ndim else v.item()
     for k in _ARRAY_FIELDS:

@@ -24,7 +24,7 @@ from pathlib import Path
 import numpy as np
 
 from . import mesh as M
-from .scene import (BC_BOUNCEBACK, BC_PERIODIC, BC_ZOUHE_SHEAR, BOND_BELL, BOND_CONSTANT, FIB_HOOKE,
+from .scene import (BC_BOUNCEBACK, BC_INOUT, BC_PERIODIC, BC_ZOUHE_SHEAR, BOND_BELL, BOND_CONSTANT, FIB_HOOKE,
                     MEM_ALL, P_KF0, P_KR0, P_NUMRECEPTORS, Scene, force_to_lattice, reference_params)
 
 REF_DX = 0.2
@@ -357,6 +357,17 @@ def mixed_small(seed: int = 3, nx=40, ny=32, nz=20, n_platelets=3, level=1, n_cy
     _fibrin(sc, n_fib, n_links, 3 * REF_DX, rng, 0.5)
     sc.seed = seed
     sc.meta.update(workload="mixed_small")
+    return sc
+
+
+def inflow_small(seed: int = 3, **kw) -> Scene:
+    """mixed_small with the y axis open: the velocity inlet at y=0 and outlet
+    at y=ny-1 (BC_INOUT, the reference's in/out-flow planes) carrying the
+    same shear profile as the initial flow, and no IBM wrap across them."""
+    sc = mixed_small(seed=seed, **kw)
+    sc.bc = (BC_PERIODIC, BC_INOUT, BC_ZOUHE_SHEAR)
+    sc.ibm_wrap = (1, 0, 0)
+    sc.meta.update(workload="inflow_small")
     return sc
 
 

@@ -24,7 +24,7 @@ sys.path.insert(0, str(ROOT))
 from oracle import binding as ob  # noqa: E402
 from platelet_fiber_gpu_gb300 import mesh as M  # noqa: E402
 from platelet_fiber_gpu_gb300 import workloads as W  # noqa: E402
-from platelet_fiber_gpu_gb300.scene import P_SHEAR, scene_to_dict  # noqa: E402
+from platelet_fiber_gpu_gb300.scene import MEM_ALL, MEM_FEMBEND, P_SHEAR, scene_to_dict  # noqa: E402
 
 CX = np.array([0, 1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0], dtype=np.float64)
 CY = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1], dtype=np.float64)
@@ -45,7 +45,8 @@ class RefCase(C.Structure):
                 ("r1", fp), ("r2", fp), ("node_nbrElemNum", ip), ("node_nbr_nodes", ip), ("Nref", dp),
                 ("S0", dp), ("S0_all", C.c_double), ("V0", C.c_double), ("receptBond", ip),
                 ("nsteps", C.c_int), ("uniforms", dp), ("totalBond_per_step", ip), ("traj", dp),
-                ("km_out", dp), ("S_all_V_out", dp), ("first_lost_site_step", C.c_int)]
+                ("km_out", dp), ("S_all_V_out", dp), ("first_lost_site_step", C.c_int),
+                ("fem_bend", C.c_int)]
 
 
 def _p(a, t=C.c_double):
@@ -129,6 +130,7 @@ def run_reference(sc, nsteps: int):
     c.receptBond = _p(rb, C.c_int)
     c.nsteps, c.uniforms = nsteps, _p(uni)
     c.totalBond_per_step, c.traj, c.km_out, c.S_all_V_out = _p(tb, C.c_int), _p(traj), _p(km), _p(sv)
+    c.fem_bend = 1 if int(sc.membrane_forces) & MEM_FEMBEND else 0
     if lib.refemu_run(C.byref(c)) != 0:
         raise RuntimeError("refemu_run failed")
     rec_state = np.stack([rb[0].T.reshape(-1), rb[1].T.reshape(-1), rb[2].T.reshape(-1)], 1)[None]
@@ -152,6 +154,9 @@ CASES = {
     # out-of-bounds read the CUDA path fixes)
     "ref_mesh958": dict(seed=5, nx=16, ny=16, nz=8, level=1, R=1, nsteps=25, mesh="958", two_bonds=True,
                         gap=0.02, kr0=0.0),
+    # the FEM bending chain the reference comments out (semLB.cu:518-520),
+    # launched in its slot on top of the membrane chain it runs
+    "ref_fembend": dict(seed=13, nx=16, ny=20, nz=10, level=1, R=2, nsteps=20, mem=MEM_ALL | MEM_FEMBEND),
 }
 
 
@@ -171,7 +176,7 @@ def reference_mesh958():
 
 
 def make(name: str, seed, nx, ny, nz, level, R, nsteps, center=None, mesh=None, two_bonds=False, gap=None,
-         kf0=3.0e4, kr0=1.5e4):
+         kf0=3.0e4, kr0=1.5e4, mem=MEM_ALL):
     msh = reference_mesh958() if mesh == "958" else None
     for attempt in range(50):
         s = seed + 1000 * attempt
@@ -179,6 +184,7 @@ def make(name: str, seed, nx, ny, nz, level, R, nsteps, center=None, mesh=None, 
         if c is None and gap is not None:
             c = (nx * W.REF_DX / 2, ny * W.REF_DX / 2, 0.5 * (msh[0][:, 2].max() - msh[0][:, 2].min()) + gap)
         sc = W.reference_case(seed=s, nx=nx, ny=ny, nz=nz, level=level, R=R, center=c, mesh=msh, kf0=kf0, kr0=kr0)
+        sc.membrane_forces = mem
         out = run_reference(sc, nsteps)
         # a receptor that drops from 2 bonds to 1 leaves the reference's stored
         # site at -1 (sem_kernel.cu:1937-1942); pick a seed whose run never does

@@ -68,6 +68,16 @@ def test_host_validation_without_gpu(lib):
     assert lib.fluid_allocGPUKernel(None, 1e-8, 0.2, 0, 4, 4) is None
     lib.pfgpu_membrane_forces_noalloc.argtypes = [C.c_void_p, C.c_void_p]
     assert lib.pfgpu_membrane_forces_noalloc(None, None) == 1
+    # membrane force bits outside PF_MEM_ALL | PF_MEM_FEMBEND
+    odd = W.mixed_small()
+    odd.membrane_forces = 64
+    co = odd.to_c()
+    assert lib.pfgpu_job_create(C.byref(co), 1, 0.0, C.byref(h)) == 1
+    assert b"membrane force bits" in lib.pfgpu_last_error()
+    # the no-allocation entry point has no scratch for the FEM bending chain
+    args = (C.c_int * 7)(1, 8, 4, 4, 6, 0, 15 | 16)
+    assert lib.pfgpu_membrane_forces_noalloc(C.cast(args, C.c_void_p), None) == 1
+    assert b"FEM" in lib.pfgpu_last_error()
 
 
 def test_receptor_uniforms_match_oracle(lib):

@@ -84,3 +84,56 @@ def test_body_force_poiseuille_profile():
     # sqrt(3/16); at tau = 0.8 the node next to the wall sits ~2% low
     np.testing.assert_allclose(ux, ana, rtol=3e-2)
     np.testing.assert_allclose(ux[2:-2], ana[2:-2], rtol=6e-3)
+
+
+def test_inflow_outflow_planes_hold_the_shear_profile():
+    """The y inlet/outlet planes (BC_INOUT) of a marker-free shear channel:
+    on every node of the planes' interior (0 < x < nx-1, 0 < z < nz-1) the
+    moments after the step are exactly the prescribed u = (0, uw z/(nz-1), 0)
+    -- Zou/He rebuilds the unknowns so that the momentum is rho u, and the
+    rows next to the edges are reset to the equilibrium at unit density."""
+    sc = W.inflow_small()
+    sc.n_platelets = 0
+    sc.n_fib = 0
+    o = ob.Oracle(sc)
+    o.step(30)
+    L = o.lattice()
+    nx, ny, nz = sc.nx, sc.ny, sc.nz
+    u = [L["u"][a].reshape(nz, ny, nx) for a in range(3)]
+    rho = L["rho"].reshape(nz, ny, nx)
+    uw = u[1][-1, ny // 2, nx // 2]
+    prof = uw * np.arange(nz) / (nz - 1)
+    for j in (0, ny - 1):
+        np.testing.assert_allclose(u[1][1:-1, j, 1:-1], np.broadcast_to(prof[1:-1, None], (nz - 2, nx - 2)),
+                                   rtol=0, atol=1e-11 * uw)
+        np.testing.assert_allclose(u[0][1:-1, j, 1:-1], 0, atol=1e-11 * uw)
+        np.testing.assert_allclose(u[2][1:-1, j, 1:-1], 0, atol=1e-11 * uw)
+        for edge in (rho[1, j, 1:-1], rho[-2, j, 1:-1], rho[1:-1, j, 1], rho[1:-1, j, -2]):
+            np.testing.assert_allclose(edge, 1.0, rtol=0, atol=1e-14)
+    # the flow inside differs from the periodic channel's only through the planes
+    per = W.mixed_small()
+    per.n_platelets = 0
+    per.n_fib = 0
+    op = ob.Oracle(per)
+    op.step(30)
+    assert np.abs(L["u"][1] - op.lattice()["u"][1]).max() > 1e-6 * uw
+
+
+def test_inflow_outflow_planes_differ_from_periodic_with_markers():
+    """With platelets and fibrin the open y planes change the flow (the
+    disturbance no longer re-enters at the other end), while the planes'
+    interior still carries the prescribed profile up to the half-force
+    correction of nearby markers."""
+    sc = W.inflow_small()
+    o = ob.Oracle(sc)
+    o.step(30)
+    per = ob.Oracle(W.mixed_small())
+    per.step(30)
+    L, Lp = o.lattice(), per.lattice()
+    nx, ny, nz = sc.nx, sc.ny, sc.nz
+    uy = L["u"][1].reshape(nz, ny, nx)
+    uw = uy[-1, ny // 2, nx // 2]
+    prof = uw * np.arange(nz) / (nz - 1)
+    for j in (0, ny - 1):
+        assert np.abs(uy[2:-2, j, 2:-2] - prof[2:-2, None]).max() < 1e-3 * uw
+    assert np.abs(L["u"][1] - Lp["u"][1]).max() > 1e-3 * uw
