@@ -1105,21 +1105,27 @@ static double fib_force_scale(const pfo_sim *s) {
 
 /* fiber_LB_Fsi_force (fiber.cpp:501-600): the penalty force
  * kappa rho (u - V) / dt on each node (lattice units; u and V in units of
- * UMAX, so divided by C), and its reaction spread into the lattice force
- * with the marker stencil.  The text adds +rho (u - V)/dt to the fluid
- * populations, which pushes the fluid away from the node's velocity; the
- * reaction (momentum exchange) is used here. */
+ * UMAX, so divided by C) from the flow of this step's moments at the node.
+ * The fluid receives the reaction in the next step's force (spread then,
+ * at the node's position then): fibrin_penalty_spread.  The text adds
+ * +rho (u - V)/dt to the fluid populations, which pushes the fluid away from
+ * the node's velocity; the reaction (momentum exchange) is used here. */
 static void fibrin_penalty(pfo_sim *s) {
-  const double C = lattice_C(s), kc = fib_force_scale(s), kap = s->sc.fib_kappa;
+  const double C = lattice_C(s), kap = s->sc.fib_kappa;
   for (int m = 0; m < s->M; ++m) {
     double u[3], r;
     fib_flow_at(s, s->fX[m], s->fY[m], s->fZ[m], u, &r);
-    const double f0 = kap * r * (u[0] - s->fVX[m]) / C;
-    const double f1 = kap * r * (u[1] - s->fVY[m]) / C;
-    const double f2 = kap * r * (u[2] - s->fVZ[m]) / C;
-    s->fsX[m] = f0; s->fsY[m] = f1; s->fsZ[m] = f2;
-    spread_marker(s, s->fX[m], s->fY[m], s->fZ[m], -f0 / kc, -f1 / kc, -f2 / kc);
+    s->fsX[m] = kap * r * (u[0] - s->fVX[m]) / C;
+    s->fsY[m] = kap * r * (u[1] - s->fVY[m]) / C;
+    s->fsZ[m] = kap * r * (u[2] - s->fVZ[m]) / C;
   }
+}
+/* the previous step's penalty reaction onto the lattice force, with the
+ * marker stencil, in reference force units (lattice force / scale) */
+static void fibrin_penalty_spread(pfo_sim *s) {
+  const double kc = fib_force_scale(s);
+  for (int m = 0; m < s->M; ++m)
+    spread_marker(s, s->fX[m], s->fY[m], s->fZ[m], -s->fsX[m] / kc, -s->fsY[m] / kc, -s->fsZ[m] / kc);
 }
 
 /* network::solverkick (network.cpp:839-881) over half a lattice step:
@@ -1475,7 +1481,7 @@ int pfo_step(pfo_sim *s, int nsteps) {
       for (size_t g = 0; g < PE; ++g) spread_marker(s, s->X[g], s->Y[g], s->Z[g], s->FX[g], s->FY[g], s->FZ[g]);
     }
     if (penalty(s)) {
-      fibrin_penalty(s);
+      fibrin_penalty_spread(s);
     } else {
       const double F0 = (double)s->mp[PF_P_F0];
       for (int m = 0; m < s->M; ++m)
@@ -1502,7 +1508,10 @@ int pfo_step(pfo_sim *s, int nsteps) {
       for (int m = 0; m < s->M; ++m) interp_marker(s, s->fX[m], s->fY[m], s->fZ[m], &s->fVX[m], &s->fVY[m], &s->fVZ[m]);
     }
     advance_positions(s);
-    if (penalty(s)) fibrin_integrate(s);
+    if (penalty(s)) {
+      fibrin_penalty(s);
+      fibrin_integrate(s);
+    }
     s->step++;
   }
   return s->done;

@@ -151,6 +151,16 @@ struct Fibrin {
   int *fixed = nullptr, *ptr = nullptr, *nbr = nullptr;
   double* L0 = nullptr;
   size_t bytes = 0;
+  // penalty coupling (PF_FIBCPL_PENALTY): node force of the step in lattice
+  // units [3][M], and its reaction in reference force units, spread in the
+  // next step [3][M]
+  int coupling = PF_FIBCPL_MARKER;
+  double gamma = 0, node_mass = 1, kappa = 1;
+  double f0 = 1;  // the reference's force unit F0 (link forces are in it)
+  double *Ffsi = nullptr, *Fs = nullptr;
+  // the force the lattice receives at the nodes: the link forces (markers)
+  // or the penalty reaction
+  const double* spread_force() const { return coupling == PF_FIBCPL_PENALTY ? Fs : F; }
 };
 
 // ------------------------------------------------------------------ batches
@@ -246,6 +256,13 @@ cudaError_t lattice_conservation(Lattice& L, long long step, double* out4_dev, c
 cudaError_t membrane_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
 cudaError_t morse_forces(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
 cudaError_t fibrin_forces(Fibrin& Fb, int precision, Control* ctl, cudaStream_t st);
+// Penalty coupling, after the step's moments and before the position update:
+// the node forces from the flow at the nodes, then the damped kick-drift-kick
+// with the link forces recomputed at the new positions (sets the nodes'
+// occupancy bits of the next step).
+cudaError_t fibrin_penalty_step(Lattice& L, Fibrin& Fb, int precision, double F0, Control* ctl, cudaStream_t st);
+// initial node velocity of the penalty coupling: the flow at the node
+cudaError_t fibrin_penalty_init(Lattice& L, Fibrin& Fb, cudaStream_t st);
 cudaError_t bond_pass(Platelets& Pl, int precision, Control* ctl, cudaStream_t st);
 // occupancy bits of the current marker positions (once, after an upload;
 // the position update sets them for the following step)

@@ -241,8 +241,14 @@ static int validate(const pf_scene* s, int precision) {
     return set_error(PFGPU_ERR_INVALID, "negative count");
   if (s->membrane_forces & ~(PF_MEM_ALL | PF_MEM_FEMBEND))
     return set_error(PFGPU_ERR_INVALID, "unknown membrane force bits");
-  if (s->n_fib > 0 && s->fib_coupling != PF_FIBCPL_MARKER)
-    return set_error(PFGPU_ERR_UNSUPPORTED, "fibrin coupling: only PF_FIBCPL_MARKER");
+  if (s->n_fib > 0) {
+    if (s->fib_coupling != PF_FIBCPL_MARKER && s->fib_coupling != PF_FIBCPL_PENALTY)
+      return set_error(PFGPU_ERR_INVALID, "unknown fibrin coupling");
+    if (s->fib_coupling == PF_FIBCPL_PENALTY &&
+        !(s->fib_node_mass > 0 && s->fib_gamma >= 0 && s->fib_kappa >= 0 && std::isfinite(s->fib_gamma) &&
+          std::isfinite(s->fib_kappa) && std::isfinite(s->fib_node_mass)))
+      return set_error(PFGPU_ERR_INVALID, "penalty coupling needs node mass > 0, gamma >= 0, kappa >= 0");
+  }
   if (s->n_platelets > 0) {
     if (!s->X || !s->Y || !s->RY || !s->Z) return set_error(PFGPU_ERR_INVALID, "element positions missing");
     if (s->n_membrane > s->n_elem) return set_error(PFGPU_ERR_INVALID, "n_membrane > n_elem");
@@ -416,6 +422,15 @@ static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
   CK(dupload(j, &F.ptr, s->fib_ptr, M + 1));
   CK(dupload(j, &F.nbr, s->fib_nbr, (size_t)nl));
   CK(dupload(j, &F.L0, s->fib_L0, (size_t)nl));
+  F.f0 = (double)s->params[PF_P_F0];
+  F.coupling = s->fib_coupling;
+  if (F.coupling == PF_FIBCPL_PENALTY) {
+    F.gamma = s->fib_gamma;
+    F.node_mass = s->fib_node_mass;
+    F.kappa = s->fib_kappa;
+    CK(dalloc(j, &F.Ffsi, 3 * M));
+    CK(dalloc(j, &F.Fs, 3 * M));
+  }
   return PFGPU_OK;
 }
 
@@ -462,6 +477,10 @@ static int far_prologue(pfgpu_job* j) {
   j->far_ready = true;
   return PFGPU_OK;
 }
+
+// fibrin nodes the interpolation moves (markers); penalty-coupled nodes
+// move with their own velocity
+static Fibrin* marker_fibrin(Fibrin* Fb) { return Fb && Fb->coupling == PF_FIBCPL_MARKER ? Fb : nullptr; }
 
 static int enqueue_step(pfgpu_job* j) {
   Platelets* Pl = j->has_pl ? &j->Pl : nullptr;
@@ -545,7 +564,11 @@ static int enqueue_step(pfgpu_job* j) {
   }
   CK(lattice_step_part(j->L, j->ctl, 2, bins, ncells, j->s0));
   CK(lattice_moments_active(j->L, j->ctl, j->s0));
-  CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
+  if (Fb && Fb->coupling == PF_FIBCPL_PENALTY) {
+    CK(fibrin_penalty_step(j->L, *Fb, j->precision, Pl ? (double)Pl->k.f0 : 1.0, j->ctl, j->s0));
+    launches += 4;
+  }
+  CK(interp_advance(j->L, Pl, marker_fibrin(Fb), j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
   launches += 3;
   if (pipe) CK(cudaStreamWaitEvent(j->s0, j->ev_far, 0));
   j->launches_per_step = launches;
@@ -590,7 +613,10 @@ static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
     }
     CK(rec(t, 6, 1));
     CK(rec(t, 7, 0)); if (markers) CK(lattice_moments_active(j->L, j->ctl, s)); CK(rec(t, 7, 1));
-    CK(rec(t, 8, 0)); CK(interp_advance(j->L, Pl, Fb, j->ctl, j->detach_rate, j->seed, j->done_blocks, s));
+    CK(rec(t, 8, 0));
+    if (Fb && Fb->coupling == PF_FIBCPL_PENALTY)
+      CK(fibrin_penalty_step(j->L, *Fb, j->precision, Pl ? (double)Pl->k.f0 : 1.0, j->ctl, s));
+    CK(interp_advance(j->L, Pl, marker_fibrin(Fb), j->ctl, j->detach_rate, j->seed, j->done_blocks, s));
     CK(rec(t, 8, 1));
   }
   CK(cudaStreamSynchronize(s));
@@ -648,6 +674,7 @@ size_t pfgpu_scene_device_bytes(const pf_scene* s, int precision) {
     b += nc * (kBinCap * 16 + 4);
   }
   b += (size_t)s->n_fib * 14 * 8;
+  if (s->fib_coupling == PF_FIBCPL_PENALTY) b += (size_t)s->n_fib * 6 * 8;
   // topology tables (shared by the platelets), fibrin link lists, and the
   // small per-job buffers (control block, counters, bounds)
   if (s->n_platelets > 0 && s->n_elem > 0) {
@@ -815,6 +842,7 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
     CKJ(e);
   }
   CKJ(mark_markers(j->L, j->has_pl ? &j->Pl : nullptr, j->has_fb ? &j->Fb : nullptr, j->s0));
+  if (j->has_fb && j->Fb.coupling == PF_FIBCPL_PENALTY) CKJ(fibrin_penalty_init(j->L, j->Fb, j->s0));
   CKJ(cudaStreamSynchronize(j->s0));
   *out = j;
   return PFGPU_OK;
@@ -1170,6 +1198,7 @@ cudaStream_t pfgpu_job_stream_(pfgpu_job* j) { return j->s0; }
 int pfgpu_job_batch_desc_(pfgpu_job* j, BatchDesc* d, int* precision, int* fast) {
   if (j->precision == PF_PREC_FP64 || j->L.ibm_box || j->pipeline) return 0;
   if (j->has_pl && (!j->Pl.mem_items || (j->Pl.k.morse && morse_uses_cells(j->Pl.k)))) return 0;
+  if (j->has_fb && j->Fb.coupling != PF_FIBCPL_MARKER) return 0;
   d->L = j->L;
   d->Pl = j->has_pl ? j->Pl : Platelets();
   d->Fb = j->has_fb ? j->Fb : Fibrin();

@@ -2864,6 +2864,141 @@ cudaError_t fibrin_forces(Fibrin& Fb, int precision, Control* ctl, cudaStream_t 
   return cudaGetLastError();
 }
 
+// ------------------------------------------------ fibrin penalty coupling
+// Flow at a fibrin node (fiber.cpp:753-814, its DH1D kernel restated as the
+// IBM kernel the markers use): velocity (lattice units) and density summed
+// with the stencil weights over the moments buffer, nodes of the Zou/He wall
+// planes skipped, weights not renormalised.
+template <class R>
+__device__ __forceinline__ void fib_flow(const LatticeConst& lk, const R4<R>* ubuf, double x, double y, double z,
+                                         double u[3], double& rho) {
+  int nxa[5], nya[5], nza[5], rx[5], ry[5], rz[5];
+  R wx[5], wy[5], wz[5];
+  const int cxn = axis_stencil<R>(x, lk.dxf, lk.inv_dx, lk.nx, lk.ibm_wrap[0], 0, nxa, rx, wx);
+  const int cyn = axis_stencil<R>(y, lk.dxf, lk.inv_dx, lk.ny, lk.ibm_wrap[1], 0, nya, ry, wy);
+  const int czn = axis_stencil<R>(z, lk.dxf, lk.inv_dx, lk.nz, 0, 0, nza, rz, wz);
+  const bool walls = lk.bc[2] == PF_BC_ZOUHE_SHEAR;
+  R a0 = 0, a1 = 0, a2 = 0, r = 0;
+  for (int c = 0; c < czn; ++c) {
+    if (walls && (nza[c] == 0 || nza[c] == lk.nz - 1)) continue;
+    for (int b = 0; b < cyn; ++b)
+      for (int a = 0; a < cxn; ++a) {
+        const R delta = wx[a] * wy[b] * wz[c];
+        const size_t n = (size_t)nxa[a] + (size_t)lk.nx * ((size_t)nya[b] + (size_t)lk.ny * nza[c]);
+        const R4<R> v = ubuf[n];
+        a0 += v.y * delta; a1 += v.z * delta; a2 += v.w * delta;
+        r += ((R)1 + v.x) * delta;
+      }
+  }
+  u[0] = (double)a0; u[1] = (double)a1; u[2] = (double)a2;
+  rho = (double)r;
+}
+
+// Node force kappa rho (u - V) (lattice units; V is kept in the element
+// velocity units, V/C in lattice units) and its reaction for the next
+// step's spreading, in reference force units (lattice force * F0 / kc).
+template <class R>
+__global__ void __launch_bounds__(128) fibrin_fsi_k(LatticeConst lk, int M, const double* X, const double* Y,
+                                                    const double* Z, const double* V, const R4<R>* ubuf,
+                                                    double kappa, double F0, double* Ffsi, double* Fs,
+                                                    const Control* ctl) {
+  if (ctl->done) return;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  double u[3], rho;
+  fib_flow<R>(lk, ubuf, X[m], Y[m], Z[m], u, rho);
+  const double C = lk.C, kc = lk.kcoll;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double f = kappa * rho * (u[a] - V[(size_t)a * M + m] / C);
+    Ffsi[(size_t)a * M + m] = f;
+    Fs[(size_t)a * M + m] = -f / kc * F0;
+  }
+}
+
+// network::solverkick (network.cpp:839-881) over half a lattice step on the
+// node velocity in lattice units: v <- e^{-g/2} v + a (1 - e^{-g/2}) / g
+// (a/2 for g = 0), a = (link force * kc / F0 + penalty force) / mass; fixed
+// nodes rest.  Phase 0 then drifts the free nodes (the position update of
+// the markers); phase 1 sets the occupancy bits of the next step.
+__global__ void __launch_bounds__(128) fibrin_kick_k(LatticeConst lk, int M, int phase, double* X, double* Y,
+                                                     double* Z, double* V, const int* fixed, const double* F,
+                                                     const double* Ffsi, double F0, double mass, double gamma,
+                                                     unsigned* mark, const Control* ctl, bool fp64) {
+  if (ctl->done) return;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  const double C = lk.C, kc = lk.kcoll;
+  const double vdt = exp(-0.5 * gamma), fdt = gamma > 0 ? (1.0 - vdt) / gamma : 0.5;
+  const bool fx = fixed[m] != 0;
+  double v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const size_t i = (size_t)a * M + m;
+    if (fx) {
+      v[a] = 0;
+    } else {
+      const double acc = (F[i] / F0 * kc + Ffsi[i]) / mass;
+      v[a] = (vdt * (V[i] / C) + acc * fdt) * C;
+    }
+    V[i] = v[a];
+  }
+  double x = X[m], y = Y[m], z = Z[m];
+  if (phase == 0) {
+    if (fx) return;
+    const float dtT = lk.dtT;
+    const double Lx = (double)lk.nx * (double)lk.dxf, Ly = (double)lk.ny * (double)lk.dxf;
+    x += v[0] * dtT;
+    if (lk.ibm_wrap[0]) { if (x > Lx) x -= Lx; else if (x < 0) x += Lx; }
+    y += v[1] * dtT;
+    if (lk.ibm_wrap[1]) { if (y > Ly) y -= Ly; else if (y < 0) y += Ly; }
+    z += v[2] * dtT;
+    X[m] = x; Y[m] = y; Z[m] = z;
+    return;
+  }
+  mark_node(lk, mark + (size_t)((int)(ctl->step & 1) ^ 1) * lk.nbricks, x, y, z, fp64);
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) fibrin_vinit_k(LatticeConst lk, int M, const double* X, const double* Y,
+                                                      const double* Z, double* V, const int* fixed,
+                                                      const R4<R>* ubuf) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  double u[3] = {0, 0, 0}, rho = 0;
+  if (!fixed[m]) fib_flow<R>(lk, ubuf, X[m], Y[m], Z[m], u, rho);
+  for (int a = 0; a < 3; ++a) V[(size_t)a * M + m] = u[a] * lk.C;
+}
+
+cudaError_t fibrin_penalty_step(Lattice& L, Fibrin& Fb, int precision, double F0, Control* ctl, cudaStream_t st) {
+  if (Fb.M == 0) return cudaSuccess;
+  const unsigned grid = (Fb.M + 127) / 128;
+  const bool fp64 = precision == PF_PREC_FP64;
+  if (fp64)
+    fibrin_fsi_k<double><<<grid, 128, 0, st>>>(L.k, Fb.M, Fb.X, Fb.Y, Fb.Z, Fb.V, (const D4*)L.ubuf, Fb.kappa, F0,
+                                               Fb.Ffsi, Fb.Fs, ctl);
+  else
+    fibrin_fsi_k<float><<<grid, 128, 0, st>>>(L.k, Fb.M, Fb.X, Fb.Y, Fb.Z, Fb.V, (const float4*)L.ubuf, Fb.kappa,
+                                              F0, Fb.Ffsi, Fb.Fs, ctl);
+  fibrin_kick_k<<<grid, 128, 0, st>>>(L.k, Fb.M, 0, Fb.X, Fb.Y, Fb.Z, Fb.V, Fb.fixed, Fb.F, Fb.Ffsi, Fb.f0,
+                                      Fb.node_mass, Fb.gamma, L.mark, ctl, fp64);
+  cudaError_t e = fibrin_forces(Fb, precision, ctl, st);
+  if (e != cudaSuccess) return e;
+  fibrin_kick_k<<<grid, 128, 0, st>>>(L.k, Fb.M, 1, Fb.X, Fb.Y, Fb.Z, Fb.V, Fb.fixed, Fb.F, Fb.Ffsi, Fb.f0,
+                                      Fb.node_mass, Fb.gamma, L.mark, ctl, fp64);
+  return cudaGetLastError();
+}
+
+cudaError_t fibrin_penalty_init(Lattice& L, Fibrin& Fb, cudaStream_t st) {
+  if (Fb.M == 0) return cudaSuccess;
+  const unsigned grid = (Fb.M + 127) / 128;
+  if (L.precision == PF_PREC_FP64)
+    fibrin_vinit_k<double><<<grid, 128, 0, st>>>(L.k, Fb.M, Fb.X, Fb.Y, Fb.Z, Fb.V, Fb.fixed, (const D4*)L.ubuf);
+  else
+    fibrin_vinit_k<float><<<grid, 128, 0, st>>>(L.k, Fb.M, Fb.X, Fb.Y, Fb.Z, Fb.V, Fb.fixed, (const float4*)L.ubuf);
+  return cudaGetLastError();
+}
+
 cudaError_t bond_pass(Platelets& Pl, int precision, Control* ctl, cudaStream_t st) {
   const PlateletConst& k = Pl.k;
   const int NR = k.P * k.nrec;
@@ -2909,14 +3044,14 @@ cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
         L.k, (float4*)L.F[0], (float4*)L.F[1], PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? (float*)Pl->Fmem : nullptr, (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr,
         (Pl && Pl->k.nrec) ? (float*)Pl->Fbond : nullptr, Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr,
-        Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr, Fb ? Fb->F : nullptr, F0, ctl);
+        Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr, Fb ? Fb->spread_force() : nullptr, F0, ctl);
   else if (L.precision == PF_PREC_FP64)
     spread_k<double><<<grid, 128, 0, st>>>(
         L.k, (D4*)L.F[0], (D4*)L.F[1], PE, Pl ? Pl->X : nullptr,
         Pl ? Pl->Y : nullptr, Pl ? Pl->Z : nullptr, Pl ? (double*)Pl->Fmem : nullptr,
         (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr, (Pl && Pl->k.nrec) ? (double*)Pl->Fbond : nullptr,
         Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr,
-        Fb ? Fb->F : nullptr, F0, ctl);
+        Fb ? Fb->spread_force() : nullptr, F0, ctl);
   else {
     // FP32: one CTA per platelet box, then the fibrin nodes
     cudaFuncSetAttribute(spread_box_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBoxSmem);
@@ -2926,7 +3061,7 @@ cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
         L.k, (float4*)L.F[0], (float4*)L.F[1], P, E, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? (float*)Pl->Fmem : nullptr, (Pl && Pl->k.morse) ? Pl->Fmorse : nullptr,
         (Pl && Pl->k.nrec) ? (float*)Pl->Fbond : nullptr, Pl ? Pl->Ftot : nullptr, M, Fb ? Fb->X : nullptr,
-        Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr, Fb ? Fb->F : nullptr, F0, ctl);
+        Fb ? Fb->Y : nullptr, Fb ? Fb->Z : nullptr, Fb ? Fb->spread_force() : nullptr, F0, ctl);
   }
   return cudaGetLastError();
 }
@@ -2938,7 +3073,7 @@ cudaError_t spread_part(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, int
     if (!Fb || Fb->M == 0) return cudaSuccess;
     const double F0 = Pl ? (double)Pl->k.f0 : 1.0;
     spread_part_k<<<(Fb->M + 127) / 128, 128, 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], Fb->M, Fb->X, Fb->Y,
-                                                       Fb->Z, nullptr, Fb->F, F0, ctl);
+                                                       Fb->Z, nullptr, Fb->spread_force(), F0, ctl);
     return cudaGetLastError();
   }
   const int PE = Pl ? Pl->k.P * Pl->k.E : 0;

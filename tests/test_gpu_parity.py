@@ -173,6 +173,31 @@ def test_inflow_outflow_planes_vs_oracle(gpu, prec):
         assert np.abs(uy[2:-2, j, 2:-2] - prof[2:-2, None]).max() < 1e-3 * prof[-1]
 
 
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "fp32", "fp16"])
+def test_fibrin_penalty_coupling_vs_oracle(gpu, prec):
+    """Fibrin nodes with their own velocity (the reference's fibrin FSI
+    design: penalty force from the flow at the node, reaction into the
+    lattice, damped kick-drift-kick, fiber.cpp:501-814 and
+    network.cpp:445-513,839-881) against the oracle, with friction."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    from platelet_fiber_gpu_gb300.scene import FIBCPL_PENALTY
+    sc = W.mixed_small()
+    sc.fib_coupling = FIBCPL_PENALTY
+    sc.fib_gamma = 0.05
+    sc.fib_node_mass = 2.0
+    r = _run_both(gpu, sc, 20, prec)
+    if prec == 0:
+        assert rel_max(r["Lg"]["fIN"], r["Lo"]["fIN"]) < 1e-12
+        assert rel_l2(r["Fg"]["X"], r["Fo"]["X"]) < 1e-14
+        assert rel_l2(r["Fg"]["V"], r["Fo"]["V"]) < 1e-10
+        assert rel_l2(r["Fg"]["F"], r["Fo"]["F"]) < 1e-9
+    else:
+        assert rel_l2(r["Lg"]["u"], r["Lo"]["u"]) < (2e-5 if prec == 1 else 1e-3)
+        assert rel_l2(r["Fg"]["X"], r["Fo"]["X"]) < 1e-7
+        assert rel_l2(r["Fg"]["V"], r["Fo"]["V"]) < (1e-4 if prec == 1 else 2e-3)
+    np.testing.assert_array_equal(r["Bg"]["rec_state"], r["Bo"]["rec_state"])
+
+
 def test_fp32_plain_channel_1000_steps(gpu):
     """The plain FP32 method on the 64x32x32 body-force channel with one
     600-element platelet and a 200-node fibrin mesh: velocity, density and

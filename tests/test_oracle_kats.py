@@ -137,3 +137,64 @@ def test_inflow_outflow_planes_differ_from_periodic_with_markers():
     for j in (0, ny - 1):
         assert np.abs(uy[2:-2, j, 2:-2] - prof[2:-2, None]).max() < 1e-3 * uw
     assert np.abs(L["u"][1] - Lp["u"][1]).max() > 1e-3 * uw
+
+
+def _lone_fibrin_node(fixed: int, gamma: float):
+    """Shear channel with one fibrin node (no links) mid-height, penalty
+    coupled."""
+    from platelet_fiber_gpu_gb300.scene import FIBCPL_PENALTY
+    sc = W.mixed_small()
+    sc.n_platelets = 0
+    nx, ny, nz, dx = sc.nx, sc.ny, sc.nz, sc.dx
+    sc.n_fib = 1
+    sc.fib_X = np.array([nx * dx / 2 + 0.013])
+    sc.fib_Y = np.array([ny * dx / 2 + 0.021])
+    sc.fib_Z = np.array([nz * dx / 2 + 0.007])
+    sc.fib_fixed = np.array([fixed], dtype=np.int32)
+    sc.fib_ptr = np.array([0, 0], dtype=np.int32)
+    sc.fib_nbr = np.zeros(0, dtype=np.int32)
+    sc.fib_L0 = np.zeros(0)
+    sc.fib_coupling = FIBCPL_PENALTY
+    sc.fib_gamma = gamma
+    return sc
+
+
+def test_penalty_free_node_follows_the_flow():
+    """A free node without links starts with the flow's velocity and keeps
+    it: the penalty force stays near zero and the flow is undisturbed."""
+    sc = _lone_fibrin_node(0, 0.0)
+    o = ob.Oracle(sc)
+    ref = W.mixed_small()
+    ref.n_platelets = 0
+    ref.n_fib = 0
+    o0 = ob.Oracle(ref)
+    o.step(40)
+    o0.step(40)
+    F = o.fibrin()
+    uy0 = o0.lattice()["u"][1]
+    # the linear shear profile at the node's height (wall speed uy0.max())
+    expect = uy0.max() * (sc.fib_Z[0] / sc.dx) / (sc.nz - 1)
+    assert abs(F["V"][1, 0] - expect) < 1e-2 * uy0.max()
+    assert np.abs(o.lattice()["u"] - o0.lattice()["u"]).max() < 1e-6 * uy0.max()
+    assert abs(F["Y"][0] - sc.fib_Y[0]) > 0
+
+
+def test_penalty_fixed_node_drags_the_flow():
+    """A fixed node holds still and slows the flow around it (the reaction of
+    the penalty force), more so than far from it."""
+    sc = _lone_fibrin_node(1, 0.0)
+    o = ob.Oracle(sc)
+    ref = W.mixed_small()
+    ref.n_platelets = 0
+    ref.n_fib = 0
+    o0 = ob.Oracle(ref)
+    o.step(40)
+    o0.step(40)
+    F = o.fibrin()
+    assert F["Y"][0] == sc.fib_Y[0] and np.all(F["V"] == 0)
+    nx, ny, nz = sc.nx, sc.ny, sc.nz
+    du = (o.lattice()["u"][1] - o0.lattice()["u"][1]).reshape(nz, ny, nx)
+    i, j, k = (int(sc.fib_X[0] / sc.dx), int(sc.fib_Y[0] / sc.dx), int(sc.fib_Z[0] / sc.dx))
+    near = du[k, j, i]
+    assert near < 0
+    assert abs(near) > 10 * abs(du[k, (j + ny // 2) % ny, (i + nx // 2) % nx])
