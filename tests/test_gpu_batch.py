@@ -208,3 +208,39 @@ def test_stop_steps(gpu):
         assert np.abs(a - e).max() / np.abs(e).max() < 1e-5
         r.close()
     b.close()
+
+
+def test_next_path_options_in_a_batch(gpu):
+    """Jobs with the reference's "next" code paths (FEM bending chain, y
+    inflow/outflow planes, fibrin penalty coupling) share a batch with a
+    plain job: the batch steps the three through their own graphs and the
+    plain ones fused, and every job ends where it ends alone."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    from platelet_fiber_gpu_gb300.scene import FIBCPL_PENALTY, MEM_ALL, MEM_FEMBEND
+    fem = W.mixed_small(seed=3)
+    fem.membrane_forces = MEM_ALL | MEM_FEMBEND
+    inout = W.inflow_small(seed=4)
+    pen = W.mixed_small(seed=5)
+    pen.fib_coupling = FIBCPL_PENALTY
+    pen.fib_gamma = 0.02
+    plain = W.mixed_small(seed=6)
+    scenes = [fem, inout, pen, plain]
+    b = gpu.Batch(16 << 30)
+    slots = [b.admit(sc, 1) for sc in scenes]
+    assert None not in slots
+    b.step(5)
+    b.step(3)
+    for sc, s in zip(scenes, slots):
+        ref = gpu.Job(sc, 1)
+        ref.step(8)
+        got = b.job(s)
+        assert got.steps == 8
+        a, r = got.lattice()["fIN"], ref.lattice()["fIN"]
+        assert np.abs(a - r).max() / np.abs(r).max() < 1e-5
+        ea, er = got.elements(), ref.elements()
+        for k in ("X", "Y", "Z"):
+            assert np.abs(ea[k] - er[k]).max() < 1e-6
+        assert np.abs(got.fibrin()["X"] - ref.fibrin()["X"]).max() < 1e-6
+        np.testing.assert_array_equal(got.bonds()["rec_state"], ref.bonds()["rec_state"])
+        ref.close()
+    b.close()

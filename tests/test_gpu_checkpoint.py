@@ -25,14 +25,24 @@ def _state(j, sc):
         E, B = j.elements(), j.bonds()
         out.update(X=E["X"], Y=E["Y"], Z=E["Z"], RY=E["RY"], rec=B["rec_state"], vwf=B["vwf"])
     if sc.n_fib:
-        out["fX"] = j.fibrin()["X"]
+        F = j.fibrin()
+        out["fX"] = F["X"]
+        out["fV"] = F["V"]
     return out
 
 
 def _scene(kind):
     from platelet_fiber_gpu_gb300 import workloads as W
+    from platelet_fiber_gpu_gb300.scene import FIBCPL_PENALTY
     if kind == "full":
         return W.mixed_small()
+    if kind == "penalty":
+        # fibrin nodes with their own velocity: the node velocities and the
+        # pending penalty reaction are part of the state
+        sc = W.mixed_small()
+        sc.fib_coupling = FIBCPL_PENALTY
+        sc.fib_gamma = 0.05
+        return sc
     sc = W.mixed_small(n_fib=300 if kind == "fibrin" else 0, n_links=600 if kind == "fibrin" else 0)
     sc.n_platelets = 0
     sc.n_rec = 0
@@ -42,8 +52,10 @@ def _scene(kind):
 
 
 @pytest.mark.parametrize("kind,prec,exact", [("fibrin", 0, False), ("lattice", 1, True), ("lattice", 2, True),
-                                             ("full", 0, False), ("full", 1, False), ("full", 2, False)],
-                         ids=["fibrin-fp64", "lattice-fp32", "lattice-fp16", "full-fp64", "full-fp32", "full-fp16"])
+                                             ("full", 0, False), ("full", 1, False), ("full", 2, False),
+                                             ("penalty", 1, False)],
+                         ids=["fibrin-fp64", "lattice-fp32", "lattice-fp16", "full-fp64", "full-fp32", "full-fp16",
+                              "penalty-fp32"])
 def test_restore_resumes_the_saved_job(gpu, kind, prec, exact):
     sc = _scene(kind)
     a = gpu.Job(sc, prec)
