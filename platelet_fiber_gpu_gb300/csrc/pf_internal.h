@@ -270,9 +270,11 @@ cudaError_t mark_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, cudaStream_t st)
 // flags (and lists) the force bricks every marker's stencil can reach this
 // step, before any force exists; spread_markers then only adds forces
 // check_near: every flagged brick must lie in near[step parity] (pipelined
-// schedule), else ERR_FAR_FLAGGED
+// schedule), else ERR_FAR_FLAGGED.  with_prev: the list of the flagged-brick
+// pass also holds the bricks flagged in the previous step (the schedule whose
+// lattice pass over the other bricks is the quiet pass, part 5)
 cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st,
-                         bool check_near = false);
+                         bool check_near = false, bool with_prev = false);
 cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st);
 // Reduced precision with per-marker spreading: each force part is spread
 // as soon as it exists (part 0: element membrane + Morse forces, 1: bond

@@ -438,9 +438,12 @@ static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
 //   fork -> s1 membrane | s2 Morse | s3 fibrin
 //           s0 flag the force bricks of this step (from the marker
 //              positions), then bonds
-//           sL (after the flags) the lattice pass over the unflagged bricks
-//   join -> s0: spread, lattice pass over the flagged bricks, moments at the
-//       flagged bricks, interpolation + advance.
+//           sL the lattice pass over the bricks without force in the
+//              previous step (the quiet pass: it needs no flag of this step;
+//              the few bricks that gain a force now are done again after
+//              the spreading)
+//   join -> s0: spread, lattice pass over the bricks flagged in this step or
+//       the previous one, moments there, interpolation + advance.
 // The force kernels are latency-bound and occupy few SMs; the memory-bound
 // lattice pass fills the rest.  It runs at low stream priority, so the force
 // kernels' blocks, enqueued first, are dispatched before its blocks take the
@@ -500,9 +503,13 @@ static int enqueue_step(pfgpu_job* j) {
   CK(cudaStreamWaitEvent(j->s1, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s2, j->ev_fork, 0));
   CK(cudaStreamWaitEvent(j->s3, j->ev_fork, 0));
-  CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0, pipe));
+  // serial schedule: the lattice pass over the bricks without force in the
+  // previous step starts at the fork, beside the flagging (part 5);
+  // pipelined: the unflagged near bricks after the flags (part 4)
+  const bool quiet = !pipe;
+  CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0, pipe, quiet));
   CK(cudaEventRecord(j->ev_flag, j->s0));
-  CK(cudaStreamWaitEvent(j->sL, j->ev_flag, 0));
+  CK(cudaStreamWaitEvent(j->sL, quiet ? j->ev_fork : j->ev_flag, 0));
   launches += 2;
   if (pipe) {
     CK(cudaStreamWaitEvent(j->sF, j->ev_flag, 0));
@@ -541,7 +548,7 @@ static int enqueue_step(pfgpu_job* j) {
       launches++;
     }
   }
-  CK(lattice_step_part(j->L, j->ctl, pipe ? 4 : 1, nullptr, 0, j->sL));
+  CK(lattice_step_part(j->L, j->ctl, pipe ? 4 : (quiet ? 5 : 1), nullptr, 0, j->sL));
   launches++;
   CK(cudaEventRecord(j->evL, j->sL));
   if (pipe) {
@@ -592,7 +599,7 @@ static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
   const bool cells = Pl && Pl->k.morse && morse_uses_cells(Pl->k);
   const bool markers = Pl || Fb;
   for (int t = 0; t < nsteps; ++t) {
-    CK(rec(t, 0, 0)); if (markers) CK(flag_markers(j->L, Pl, Fb, j->ctl, s)); CK(rec(t, 0, 1));
+    CK(rec(t, 0, 0)); if (markers) CK(flag_markers(j->L, Pl, Fb, j->ctl, s, false, true)); CK(rec(t, 0, 1));
     CK(rec(t, 1, 0)); if (Pl) CK(membrane_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 1, 1));
     CK(rec(t, 2, 0)); if (Pl && Pl->k.morse) CK(morse_forces(*Pl, j->precision, j->ctl, s)); CK(rec(t, 2, 1));
     CK(rec(t, 3, 0)); if (Fb) CK(fibrin_forces(*Fb, j->precision, j->ctl, s)); CK(rec(t, 3, 1));
@@ -606,7 +613,7 @@ static int profile_steps(pfgpu_job* j, int nsteps, double* ms) {
     CK(rec(t, 5, 1));
     CK(rec(t, 6, 0));
     if (markers) {
-      CK(lattice_step_part(j->L, j->ctl, 1, nullptr, 0, s));
+      CK(lattice_step_part(j->L, j->ctl, 5, nullptr, 0, s));
       CK(lattice_step_part(j->L, j->ctl, 2, cells ? Pl->bin_count : nullptr, cells ? Pl->ncells : 0, s));
     } else {
       CK(lattice_step_part(j->L, j->ctl, 0, nullptr, 0, s));

@@ -468,7 +468,15 @@ __device__ __forceinline__ void zero_bins(int* bin_count, int ncells, Control* c
 //                takes its parity and first-step flag from far_step /
 //                far_first, and has no force (no far brick is flagged in
 //                this step or the previous one).
-enum : int { kPassAll = 0, kPassUnflag = 1, kPassNear = 4, kPassFar = 3 };
+//   kPassQuiet   bricks without force in the previous step (flags of the
+//                previous step, known when the step starts), taken as
+//                without force in this step too; bricks that gain a force in
+//                this step are computed again by lbm_list_k, whose list holds
+//                the bricks flagged in this step or the previous one.  So
+//                this pass waits for no flagging; a marker moves far less
+//                than a node per step, and the bricks computed twice are the
+//                few a stencil enters in this step.
+enum : int { kPassAll = 0, kPassUnflag = 1, kPassNear = 4, kPassFar = 3, kPassQuiet = 5 };
 // bid / nblk: the CTA's index and the number of CTAs of this lattice's pass
 // (the launch is one-dimensional over groups of four bricks in lattice order)
 template <class S, class R, bool FAST>
@@ -501,6 +509,11 @@ __device__ __forceinline__ void lbm_step_body(const LatticeConst& k, S* gA, S* g
   }
   if (far) {
     if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 0u, 0u, ctl->far_first);
+    return;
+  }
+  if (mode == kPassQuiet) {
+    if (flp[brick]) return;
+    if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 0u, 0u, ctl->first);
     return;
   }
   const unsigned fc = flc[brick];
@@ -730,8 +743,9 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
   const unsigned sx = valid ? (unsigned)(seg - (long long)row * spr) : 0u;
   const unsigned x0 = sx * V;
   const int brick = (int)(x0 / kBrickX + (unsigned)k.nbx * row);
-  const unsigned fc = valid ? flc[brick] : 0u;
-  const bool active = valid && (mode == kPassAll || !fc);
+  const bool quiet = mode == kPassQuiet;
+  const unsigned fc = (valid && !quiet) ? flc[brick] : 0u;
+  const bool active = valid && (quiet ? flp[brick] == 0u : (mode == kPassAll || !fc));
   unsigned w[Q][IO::W], edge[Q];
   vec_pull<S, V>(k, gin, active, row, sx, w, edge);
   const unsigned am = __ballot_sync(0xffffffffu, active);
@@ -1501,7 +1515,7 @@ cudaError_t step_impl(Lattice& L, Control* ctl, int part, int* bin_count, int nc
   }
   if constexpr (!std::is_same<S, double>::value) {
     const int V = vec_width<S>(L);
-    if (V > 0 && (part == 0 || part == 1)) {
+    if (V > 0 && (part == 0 || part == 1 || part == kPassQuiet)) {
       const long long nseg = L.k.N / V;
       const unsigned vgrid = (unsigned)((nseg + kLbmBlock - 1) / kLbmBlock);
       void (*kern)(LatticeConst, S*, S*, float4*, float4*, float4*, unsigned*, unsigned*, int*, int, int, Control*);

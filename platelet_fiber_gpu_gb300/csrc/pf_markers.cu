@@ -336,13 +336,15 @@ __host__ __device__ inline int flag_rows(int nbx) {
 }
 __device__ __forceinline__ void flag_k_body(const LatticeConst& lk, const unsigned* mark, unsigned* flA,
                                                        unsigned* flB, int* lA, int* lB, const unsigned char* nearA,
-                                                       const unsigned char* nearB, int hi, Control* ctl, int bid, int nblk) {
+                                                       const unsigned char* nearB, int hi, Control* ctl, int bid, int nblk,
+                                                       bool with_prev = false) {
   if (ctl->done) return;
   __shared__ unsigned s_z[kFlagWords];  // OR over the planes, rows y0-2 .. y0+R+1
   __shared__ unsigned s_yz[kFlagWords];  // OR over the rows too, rows y0 .. y0+R-1
   const int par = (int)(ctl->step & 1);
   const unsigned* mk = mark + (size_t)par * lk.nbricks;
   unsigned* fl = par ? flB : flA;
+  const unsigned* flprev = par ? flA : flB;  // the previous step's flags
   int* list = par ? lB : lA;
   const unsigned char* nr = par ? nearB : nearA;
   const int lane = threadIdx.x & 31;
@@ -383,7 +385,7 @@ __device__ __forceinline__ void flag_k_body(const LatticeConst& lk, const unsign
   for (int i0 = 0; i0 < outs; i0 += kFlagThreads) {
     const int i = i0 + threadIdx.x;
     const int bx = i % nbx, y = y0 + i / nbx;
-    bool f = false;
+    bool f = false, listed = false;
     int w = 0;
     if (i < outs && y < lk.ny) {
       const int rowbase = i - bx;
@@ -396,20 +398,24 @@ __device__ __forceinline__ void flag_k_body(const LatticeConst& lk, const unsign
         fl[w] = 1u;
         if (nr && !nr[w]) atomicOr(&ctl->err, ERR_FAR_FLAGGED);
       }
+      // with_prev: the flagged-brick pass also takes the bricks that had a
+      // force in the previous step (the quiet pass leaves them out)
+      listed = f || (with_prev && flprev[w] != 0u);
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    const unsigned bal = __ballot_sync(0xffffffffu, listed);
     if (bal) {
       int base = 0;
       if (lane == 0) base = atomicAdd(&ctl->active_count[par], __popc(bal));
       base = __shfl_sync(0xffffffffu, base, 0);
-      if (f) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
+      if (listed) list[base + __popc(bal & ((1u << lane) - 1u))] = w;
     }
   }
 }
 __global__ void __launch_bounds__(kFlagThreads) flag_k(LatticeConst lk, const unsigned* mark, unsigned* flA,
                                                        unsigned* flB, int* lA, int* lB, const unsigned char* nearA,
-                                                       const unsigned char* nearB, int hi, Control* ctl) {
-  flag_k_body(lk, mark, flA, flB, lA, lB, nearA, nearB, hi, ctl, blockIdx.x, gridDim.x);
+                                                       const unsigned char* nearB, int hi, Control* ctl,
+                                                       bool with_prev) {
+  flag_k_body(lk, mark, flA, flB, lA, lB, nearA, nearB, hi, ctl, blockIdx.x, gridDim.x, with_prev);
 }
 
 // ------------------------------------------------------- interp + advance
@@ -984,6 +990,7 @@ __device__ __forceinline__ void fem_q(int NN, int Em, const int* tri, const int*
       const int t = node_tri[10 * v + j];
       const int* nd = tri + 6 * t;
       const int li = v < Em ? vert_local[10 * v + j] : local_of(nd, v);
+      if (li > 5) continue;  // not a node of t: the lists are built from tri, so never
       R c[6][3];
       P3(nd[0], c[0]); P3(nd[1], c[1]); P3(nd[2], c[2]);
       for (int i = 0; i < 3; ++i) {
@@ -1282,6 +1289,7 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
       const int t = node_tri[10 * v + j];
       const int* nd = tri + 6 * t;
       const int li = v < Em ? vert_local[10 * v + j] : local_of(nd, v);
+      if (li > 5) continue;  // not a node of t: the lists are built from tri, so never
       R c[6][3], nv[6][3];
       P3(nd[0], c[0]); P3(nd[1], c[1]); P3(nd[2], c[2]);
       for (int i = 0; i < 3; ++i) {
@@ -3033,6 +3041,14 @@ size_t bond_scratch_bytes(int NR) {
   return (size_t)NR * sizeof(RecTmp) + (size_t)NR * sizeof(int) + 16 + ops * sizeof(unsigned long long) + 64;
 }
 
+// Threads per CTA of the per-marker spreading and interpolation launches:
+// one warp.  These kernels are bound by scattered L1/L2 accesses, not by
+// warps; one-warp CTAs spread the markers evenly over the SMs (30,000
+// elements make 235 CTAs of 128 threads, one or two per SM, but 938 of 32).
+// Measured on the 256x128x128 channel: spreading 41.3 -> 39.3 us,
+// interpolation 25.0 -> 24.3 us, the step 0.5 % faster than with 128.
+static int marker_block() { return 32; }
+
 cudaError_t spread_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st) {
   const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
   const int M = Fb ? Fb->M : 0;
@@ -3072,7 +3088,7 @@ cudaError_t spread_part(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, int
   if (part == 2) {
     if (!Fb || Fb->M == 0) return cudaSuccess;
     const double F0 = Pl ? (double)Pl->k.f0 : 1.0;
-    spread_part_k<<<(Fb->M + 127) / 128, 128, 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], Fb->M, Fb->X, Fb->Y,
+    spread_part_k<<<(Fb->M + marker_block() - 1) / marker_block(), marker_block(), 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], Fb->M, Fb->X, Fb->Y,
                                                        Fb->Z, nullptr, Fb->spread_force(), F0, ctl);
     return cudaGetLastError();
   }
@@ -3080,7 +3096,7 @@ cudaError_t spread_part(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, int
   if (PE == 0 || (part == 1 && !Pl->k.nrec)) return cudaSuccess;
   const float* Fa = (const float*)(part == 0 ? Pl->Fmem : Pl->Fbond);
   const double* Fd = part == 0 && Pl->k.morse ? Pl->Fmorse : nullptr;
-  spread_part_k<<<(PE + 127) / 128, 128, 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], PE, Pl->X, Pl->Y, Pl->Z,
+  spread_part_k<<<(PE + marker_block() - 1) / marker_block(), marker_block(), 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], PE, Pl->X, Pl->Y, Pl->Z,
                                                   Fa, Fd, 1.0, ctl);
   return cudaGetLastError();
 }
@@ -3096,7 +3112,8 @@ cudaError_t mark_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, cudaStream_t st)
   return cudaGetLastError();
 }
 
-cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st, bool check_near) {
+cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cudaStream_t st, bool check_near,
+                         bool with_prev) {
   const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
   const int M = Fb ? Fb->M : 0;
   if (PE + M == 0) return cudaSuccess;
@@ -3104,7 +3121,7 @@ cudaError_t flag_markers(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, cu
   if ((R + 2 * kFlagR) * L.k.nbx > kFlagWords) return cudaErrorInvalidValue;  // rows wider than 131072 nodes
   flag_k<<<L.k.nz * ((L.k.ny + R - 1) / R), kFlagThreads, 0, st>>>(L.k, L.mark, L.flags[0], L.flags[1], L.list[0], L.list[1],
                                            check_near ? L.near[0] : nullptr, check_near ? L.near[1] : nullptr,
-                                           L.precision == PF_PREC_FP64 ? kFlagR : kFlagR - 1, ctl);
+                                           L.precision == PF_PREC_FP64 ? kFlagR : kFlagR - 1, ctl, with_prev);
   return cudaGetLastError();
 }
 
@@ -3112,7 +3129,8 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
                            uint64_t seed, unsigned* done_blocks, cudaStream_t st) {
   const int PE = Pl ? Pl->k.P * Pl->k.E : 0;
   const int M = Fb ? Fb->M : 0;
-  const unsigned grid = (PE + M + 127) / 128 > 0 ? (PE + M + 127) / 128 : 1;
+  const int mb = marker_block();
+  const unsigned grid = (PE + M + mb - 1) / mb > 0 ? (PE + M + mb - 1) / mb : 1;
   PlateletConst pk{};
   if (Pl) pk = Pl->k;
   // elements are binned every step only when the Morse pass uses the cell list
@@ -3120,13 +3138,13 @@ cudaError_t interp_advance(Lattice& L, Platelets* Pl, Fibrin* Fb, Control* ctl, 
   int* bc = cells ? Pl->bin_count : nullptr;
   float4* bn = cells ? (float4*)Pl->bin : nullptr;
   if (L.precision == PF_PREC_FP64)
-    interp_advance_k<double><<<grid, 128, 0, st>>>(
+    interp_advance_k<double><<<grid, mb, 0, st>>>(
         L.k, pk, (const D4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
         Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
         detach_rate, seed, nullptr, nullptr, nullptr, nullptr);
   else if (PE + M == 0 || !L.ibm_box) {
-    interp_advance_k<float><<<grid, 128, 0, st>>>(
+    interp_advance_k<float><<<grid, mb, 0, st>>>(
         L.k, pk, (const float4*)L.ubuf, PE, Pl ? Pl->X : nullptr, Pl ? Pl->Y : nullptr, Pl ? Pl->RY : nullptr,
         Pl ? Pl->Z : nullptr, Pl ? Pl->V : nullptr, M, Fb ? Fb->X : nullptr, Fb ? Fb->Y : nullptr,
         Fb ? Fb->Z : nullptr, Fb ? Fb->V : nullptr, Fb ? Fb->fixed : nullptr, bc, bn, L.mark, ctl, done_blocks,
