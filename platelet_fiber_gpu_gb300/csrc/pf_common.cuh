@@ -68,6 +68,14 @@ struct Control {
   long long far_step;
   // the step after which the job stops by itself (done = 2; 0: never)
   long long stop;
+  // quiet lattice pass (bricks without force in the previous step): the
+  // step it computes, whether that step is the first after an upload, and
+  // whether to skip it (the job was done when the pass was scheduled).  Set
+  // by the flagged-brick pass of the step before (the pass then runs ahead,
+  // beside that step's moments and interpolation) or by the prologue.
+  long long qstep;
+  int qfirst;
+  int qskip;
 };
 
 // ------------------------------------------------------------- Philox

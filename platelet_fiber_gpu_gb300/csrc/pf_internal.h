@@ -243,6 +243,9 @@ cudaError_t lattice_step_part(Lattice& L, Control* ctl, int part, int* bin_count
 // or from the occupancy bits into near[this parity] (from_mark 1)
 cudaError_t lattice_near(Lattice& L, Control* ctl, int from_mark, cudaStream_t st);
 // far pass counter: sync (far_step = step) or advance after a far pass
+// sets the quiet pass (part 5) to compute the current step (before a quiet
+// pass that no flagged-brick pass of the step before scheduled)
+cudaError_t lattice_quiet_prologue(Control* ctl, cudaStream_t st);
 cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st);
 cudaError_t lattice_moments_active(Lattice& L, Control* ctl, cudaStream_t st);
 // density and velocity at every stride-th node (float [mz][my][mx] planes)

@@ -484,9 +484,9 @@ __device__ __forceinline__ void lbm_step_body(const LatticeConst& k, S* gA, S* g
                                               R4<R>* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
                                               int ncells, int mode, const unsigned char* nearA,
                                               const unsigned char* nearB, Control* ctl, int bid, int nblk) {
-  if (ctl->done) return;
-  const bool far = mode == kPassFar;
-  const int par = (int)((far ? ctl->far_step : ctl->step) & 1);
+  const bool far = mode == kPassFar, quiet = mode == kPassQuiet;
+  if (quiet ? ctl->qskip != 0 : ctl->done != 0) return;
+  const int par = (int)((far ? ctl->far_step : (quiet ? ctl->qstep : ctl->step)) & 1);
   const S* __restrict__ gin = par ? gB : gA;
   S* __restrict__ gout = par ? gA : gB;
   const R4<R>* Fc = par ? FB : FA;
@@ -511,9 +511,9 @@ __device__ __forceinline__ void lbm_step_body(const LatticeConst& k, S* gA, S* g
     if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 0u, 0u, ctl->far_first);
     return;
   }
-  if (mode == kPassQuiet) {
+  if (quiet) {
     if (flp[brick]) return;
-    if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 0u, 0u, ctl->first);
+    if (x < k.nx) lbm_node<S, R, FAST>(k, gin, gout, Fc, Fp, ubuf, x, y, z, 0u, 0u, ctl->qfirst);
     return;
   }
   const unsigned fc = flc[brick];
@@ -726,8 +726,9 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
                                              int ncells, int mode, Control* ctl, long long seg, long long tid,
                                              long long tot) {
   using IO = VecIO<S, V>;
-  if (ctl->done) return;
-  const int par = (int)(ctl->step & 1);
+  const bool quiet = mode == kPassQuiet;
+  if (quiet ? ctl->qskip != 0 : ctl->done != 0) return;
+  const int par = (int)((quiet ? ctl->qstep : ctl->step) & 1);
   const S* __restrict__ gin = par ? gB : gA;
   S* __restrict__ gout = par ? gA : gB;
   const float4* Fc = par ? FB : FA;
@@ -743,7 +744,6 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
   const unsigned sx = valid ? (unsigned)(seg - (long long)row * spr) : 0u;
   const unsigned x0 = sx * V;
   const int brick = (int)(x0 / kBrickX + (unsigned)k.nbx * row);
-  const bool quiet = mode == kPassQuiet;
   const unsigned fc = (valid && !quiet) ? flc[brick] : 0u;
   const bool active = valid && (quiet ? flp[brick] == 0u : (mode == kPassAll || !fc));
   unsigned w[Q][IO::W], edge[Q];
@@ -751,7 +751,8 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
   const unsigned am = __ballot_sync(0xffffffffu, active);
   if (!active) return;
   const unsigned fp = flp[brick];
-  vec_collide_store<S, V>(k, gout, w, edge, nx * row + x0, row / (unsigned)k.ny, Fc, Fp, ubuf, fc, fp, ctl->first);
+  vec_collide_store<S, V>(k, gout, w, edge, nx * row + x0, row / (unsigned)k.ny, Fc, Fp, ubuf, fc, fp,
+                          quiet ? ctl->qfirst : ctl->first);
   __syncwarp(am);
   if (fp && (x0 % kBrickX) == 0) flp[brick] = 0;
 }
@@ -811,6 +812,14 @@ __device__ __forceinline__ void lbm_list_body(const LatticeConst& k, S* gA, S* g
                                               R4<R>* ubuf, unsigned* flA, unsigned* flB, const int* lA,
                                               const int* lB, int* bin_count, int ncells, unsigned* mark,
                                               Control* ctl, int bid, int nblk) {
+  // the quiet pass of the next step may run as soon as this pass is done
+  // (it reads this step's output, written by now, and skips the bricks
+  // flagged in this step)
+  if (bid == 0 && threadIdx.x == 0) {
+    ctl->qstep = ctl->step + 1;
+    ctl->qfirst = 0;
+    ctl->qskip = ctl->done;
+  }
   if (ctl->done) return;
   const int par = (int)(ctl->step & 1);
   const S* __restrict__ gin = par ? gB : gA;
@@ -1646,6 +1655,16 @@ cudaError_t lattice_near(Lattice& L, Control* ctl, int from_mark, cudaStream_t s
   const int rx = from_mark ? 2 : 1, ry = from_mark ? 4 : 2, rz = from_mark ? 4 : 2;
   near_bricks_k<<<(nb + 255) / 256, 256, 0, st>>>(L.k, L.flags[0], L.flags[1], L.mark, L.near[0], L.near[1],
                                                   from_mark, rx, ry, rz, ctl);
+  return cudaGetLastError();
+}
+// the quiet pass of the current step, when no flagged-brick pass scheduled it
+__global__ void quiet_prologue_k(Control* ctl) {
+  ctl->qstep = ctl->step;
+  ctl->qfirst = ctl->first;
+  ctl->qskip = ctl->done;
+}
+cudaError_t lattice_quiet_prologue(Control* ctl, cudaStream_t st) {
+  quiet_prologue_k<<<1, 1, 0, st>>>(ctl);
   return cudaGetLastError();
 }
 cudaError_t lattice_far_counter(Control* ctl, int sync, cudaStream_t st) {
