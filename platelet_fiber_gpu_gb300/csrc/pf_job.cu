@@ -456,11 +456,11 @@ static int build_fibrin(pfgpu_job* j, const pf_scene* s) {
 //           sL the lattice pass over the bricks without force in the
 //              previous step (the quiet pass: it needs no flag of this step;
 //              the few bricks that gain a force now are done again after
-//              the spreading) -- FP16 only: FP32 and FP64 run it ahead,
-//              below
+//              the spreading) -- with PFGPU_QUIET_AHEAD=0 only; by
+//              default it runs ahead, below
 //   join -> s0: spread, lattice pass over the bricks flagged in this step or
 //       the previous one, moments there, interpolation + advance.
-//   Quiet pass ahead (FP32, FP64): the quiet pass of step t+1 needs only
+//   Quiet pass ahead (the default): the quiet pass of step t+1 needs only
 //   step t's output, complete once step t's flagged-brick pass is done, so
 //   it runs then on sL, beside step t's moments and interpolation, and the
 //   next step's force kernels run alone.  Its parity and first-step flag
@@ -800,13 +800,11 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   CKJ(cudaEventCreateWithFlags(&j->ev_list, cudaEventDisableTiming));
   CKJ(cudaEventCreateWithFlags(&j->ev_q, cudaEventDisableTiming));
   {
-    // measured on the 256x128x128 channel: FP32 0.2126 -> 0.2069 ms per
-    // step with the quiet pass ahead; FP16 0.1826 -> 0.1832 (its lattice
-    // pass is issue-bound and slows the tail it runs beside), so FP16 keeps
-    // the pass at the fork.  PFGPU_QUIET_AHEAD=0/1 overrides.
+    // measured on the 256x128x128 channel with eight-step graphs: FP32
+    // 0.2126 -> 0.1998 ms per step with the quiet pass ahead, FP16
+    // 0.1822 -> 0.1755.  PFGPU_QUIET_AHEAD=0/1 overrides.
     const char* qa = getenv("PFGPU_QUIET_AHEAD");
-    const bool dflt = precision != PF_PREC_FP16;
-    j->quiet_ahead = !j->pipeline && (qa ? strcmp(qa, "1") == 0 : dflt);
+    j->quiet_ahead = !j->pipeline && (qa ? strcmp(qa, "1") == 0 : true);
     const char* gk = getenv("PFGPU_GRAPH_STEPS");
     if (gk && atoi(gk) >= 1 && atoi(gk) <= 64) j->graph_k = atoi(gk);
   }
