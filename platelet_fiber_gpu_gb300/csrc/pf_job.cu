@@ -847,6 +847,8 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
   c.step = 0;
   c.done = 0;
   c.first = 1;
+  c.qstep = 0;  // the quiet pass's counters describe the first step
+  c.qfirst = 1;
   c.total_bond = 1;  // sem_initGPUKernel, semLB.cu:880
   CKJ(cudaMemcpyAsync(j->ctl, &c, sizeof c, cudaMemcpyHostToDevice, j->s0));
   if (s->n_platelets > 0 && s->n_elem > 0) {
@@ -976,9 +978,11 @@ int pfgpu_job_step_graph(pfgpu_job* j, int nsteps) {
     int rc = capture_steps(j, 1, &j->graph);
     if (rc) return rc;
   }
-  // k-step graphs only where a step's quiet pass runs ahead of it
+  // k-step graphs only where a step's quiet pass runs ahead of it; both
+  // graphs are captured on the first call (also with nsteps = 0), so no
+  // later call pays for a capture
   const int k = j->quiet_ahead ? j->graph_k : 1;
-  if (k > 1 && nsteps >= k && !j->graphK) {
+  if (k > 1 && !j->graphK) {
     int rc = capture_steps(j, k, &j->graphK);
     if (rc) return rc;
   }
