@@ -123,9 +123,12 @@ int fused_enqueue(pfgpu_batch::Fused& f, int s) {
   };
   BK_CK(cudaEventRecord(fork, s0));
   for (cudaStream_t st : {s1, s2, s3, sL}) BK_CK(cudaStreamWaitEvent(st, fork, 0));
+  // the quiet lattice pass (bricks without force in the previous step)
+  // needs no flag of this step: sL starts at the fork; the flagging lists
+  // the bricks flagged in this step or the previous one for the flagged-
+  // brick pass
   BK_CK(launch(BK_FLAG, s0));
-  BK_CK(cudaEventRecord(flag, s0));
-  BK_CK(cudaStreamWaitEvent(sL, flag, 0));
+  (void)flag;
   BK_CK(launch(BK_MEMBRANE, s1));
   BK_CK(launch(BK_BOUNDS, s2));
   BK_CK(launch(BK_MORSE, s2));

@@ -1202,7 +1202,8 @@ __global__ void __launch_bounds__(kLbmBlock) lbm_step_batch_k(const BatchDesc* d
   const int segs = (s_k.nbricks + kLbmBlock / kBrickX - 1) / (kLbmBlock / kBrickX);
   for (int r = (blockIdx.x - start[j]) * rows, e = min(segs, r + rows); r < e; ++r)
     lbm_step_body<S, R, FAST>(s_k, (S*)L.g[0], (S*)L.g[1], (R4<R>*)L.F[0], (R4<R>*)L.F[1], (R4<R>*)L.ubuf,
-                              L.flags[0], L.flags[1], nullptr, 0, 1, L.near[0], L.near[1], d.ctl, r, segs);
+                              L.flags[0], L.flags[1], nullptr, 0, kPassQuiet, L.near[0], L.near[1], d.ctl, r,
+                              segs);
 }
 template <class S, class R, bool FAST>
 __global__ void __launch_bounds__(kLbmBlock) lbm_list_batch_k(const BatchDesc* descs, const int* start, int nj) {

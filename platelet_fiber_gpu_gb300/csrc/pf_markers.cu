@@ -2616,7 +2616,7 @@ __global__ void __launch_bounds__(kFlagThreads) flag_batch_k(const BatchDesc* de
   cta_copy(s_lk, d.L.k);
   __syncthreads();
   flag_k_body(s_lk, d.L.mark, d.L.flags[0], d.L.flags[1], d.L.list[0], d.L.list[1], nullptr, nullptr,
-              kFlagR - 1, d.ctl, bid, nblk);
+              kFlagR - 1, d.ctl, bid, nblk, true);
 }
 
 __global__ void __launch_bounds__(kMem32Threads, 1) membrane_batch_k(const BatchDesc* descs, const int* start,
