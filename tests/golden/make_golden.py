@@ -157,6 +157,11 @@ CASES = {
     # the FEM bending chain the reference comments out (semLB.cu:518-520),
     # launched in its slot on top of the membrane chain it runs
     "ref_fembend": dict(seed=13, nx=16, ny=20, nz=10, level=1, R=2, nsteps=20, mem=MEM_ALL | MEM_FEMBEND),
+    # the same chain on the reference's own 958-vertex mesh; four steps: the
+    # chain makes this mesh's motion grow step by step (0.04 um in the first
+    # step, 15 um by the eighth), after which rounding differences grow with it
+    "ref_fembend958": dict(seed=17, nx=16, ny=16, nz=8, level=1, R=1, nsteps=4, mesh="958", gap=0.02,
+                           kr0=0.0, mem=MEM_ALL | MEM_FEMBEND),
 }
 
 

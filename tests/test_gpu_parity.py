@@ -41,7 +41,7 @@ def golden(name):
     return scene_from_dict(d), int(d["nsteps"]), d
 
 
-@pytest.mark.parametrize("name", ["ref_wall", "ref_edges", "ref_mesh958", "ref_fembend"])
+@pytest.mark.parametrize("name", ["ref_wall", "ref_edges", "ref_mesh958", "ref_fembend", "ref_fembend958"])
 def test_fp64_matches_reference_kernels(gpu, name):
     sc, n, d = golden(name)
     j = gpu.Job(sc, 0)
@@ -79,22 +79,23 @@ def test_reduced_precision_vs_reference_kernels(gpu, prec, tol, name):
     j.close()
 
 
+@pytest.mark.parametrize("name", ["ref_fembend", "ref_fembend958"])
 @pytest.mark.parametrize("prec", [1, 2])
-def test_fem_bending_reduced_precision(gpu, prec):
+def test_fem_bending_reduced_precision(gpu, prec, name):
     """The reference's disabled FEM bending chain (sem_kernel.cu:1129-1497,
     launched in the slot of semLB.cu:518-520) in the FP32 per-vertex
     membrane kernel, against the reference kernels run with it: the chain
     dominates the membrane force of this case, so its FP32 rounding shows in
     the positions (tolerance written here), while bond states stay exact."""
-    sc, n, d = golden("ref_fembend")
+    sc, n, d = golden(name)
     j = gpu.Job(sc, prec, 0.0)
     j.step(n)
     E, B = j.elements(), j.bonds()
     pos = np.stack([E["X"], E["Y"], E["Z"]])
     pos_ref = np.stack([d["out.X"], d["out.Y"], d["out.Z"]])
     err = rel_l2(pos, pos_ref)
-    print(f"fem prec {prec}: position rel L2 {err:.3e}")
-    assert err < (1e-7 if prec == 1 else 2e-6)
+    print(f"fem {name} prec {prec}: position rel L2 {err:.3e}")
+    assert err < (1e-7 if prec == 1 else 5e-6)
     np.testing.assert_array_equal(B["rec_state"], d["out.rec_state"])
     j.close()
 
