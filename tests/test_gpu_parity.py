@@ -230,6 +230,43 @@ def test_graph_and_direct_stepping_agree(gpu):
     assert a.steps == b.steps == 7
 
 
+@pytest.mark.parametrize("prec,tol", [(0, 1e-13), (1, 1e-5), (2, 1e-3)], ids=["fp64", "fp32", "fp16"])
+def test_quiet_pass_schedules_agree(gpu, prec, tol, monkeypatch):
+    """The quiet lattice pass at the fork, run ahead with one-step graphs, run
+    ahead with four- and eight-step graphs, and run ahead while stepping
+    directly give the same job, over step counts that leave remainders and
+    across calls (the prologue of each call), a snapshot restore and a
+    profiled step in between."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small()
+    variants = [dict(PFGPU_QUIET_AHEAD="0"), dict(PFGPU_GRAPH_STEPS="1"), dict(PFGPU_GRAPH_STEPS="4"),
+                dict(PFGPU_GRAPH_STEPS="8"), dict(direct=True)]
+    out = []
+    for v in variants:
+        for key in ("PFGPU_QUIET_AHEAD", "PFGPU_GRAPH_STEPS"):
+            monkeypatch.delenv(key, raising=False)
+        for key, val in v.items():
+            if key != "direct":
+                monkeypatch.setenv(key, val)
+        j = gpu.Job(sc, prec, 0.0)
+        g = not v.get("direct", False)
+        j.step(5, graph=g)
+        snap = j.save()
+        j.step(9, graph=g)
+        j.restore(snap)  # back to step 5: the next call runs its own prologue
+        j.step(3, graph=g)
+        j.profile(1)
+        j.step(8, graph=g)
+        assert j.steps == 17
+        out.append((j.lattice()["fIN"], j.elements()["Z"], j.bonds()["rec_state"]))
+        j.close()
+    ref = out[0]
+    for f, z, rs in out[1:]:
+        assert rel_max(f, ref[0]) < tol
+        assert np.abs(z - ref[1]).max() < (1e-12 if prec == 0 else 1e-6)
+        np.testing.assert_array_equal(rs, ref[2])
+
+
 @pytest.mark.parametrize("prec,tol", [(0, 1e-14), (1, 1e-6)], ids=["fp64", "fp32"])
 def test_pipelined_and_serial_schedules_agree(gpu, prec, tol, monkeypatch):
     """The pipelined schedule updates the far region of step t+1 (bricks
