@@ -371,10 +371,13 @@ __device__ __forceinline__ void node_q(const LatticeConst& k, float q[Q], int z,
     const float jx = s1 * (q[1] - q[2]) + s2 * ((q[7] + q[8] + q[9] + q[10]) - (q[11] + q[12] + q[13] + q[14]));
     const float jy = s1 * (q[3] - q[4]) + s2 * ((q[7] + q[11] + q[15] + q[16]) - (q[8] + q[12] + q[17] + q[18]));
     const float jz = s1 * (q[5] - q[6]) + s2 * ((q[9] + q[13] + q[15] + q[17]) - (q[10] + q[14] + q[16] + q[18]));
-    const float hk = 0.5f * k.kmom_f, rho = 1.0f + drho;
-    ux = (jx + hk * px) / rho;
-    uy = (jy + hk * py) / rho;
-    uz = (jz + hk * pz) / rho;
+    // one correctly rounded reciprocal instead of three divisions: the
+    // FP16 pass is bound by its instruction issue, and the difference (an
+    // ulp of FP32) is far below the store's FP16 rounding
+    const float hk = 0.5f * k.kmom_f, irho = __frcp_rn(1.0f + drho);
+    ux = (jx + hk * px) * irho;
+    uy = (jy + hk * py) * irho;
+    uz = (jz + hk * pz) * irho;
   }
   const float rho = 1.0f + drho;
   const float usq = ux * ux + uy * uy + uz * uz;
