@@ -63,6 +63,7 @@ struct LatticeConst {
   // kernels read these instead of converting from double per thread (FP64
   // conversions use the narrow FP64 pipe of this GPU)
   float omega_f, kcoll_f, kmom_f, body_f[3], uw_f;
+  int nobody;  // the body force is zero (in its float rounding)
 };
 
 struct Lattice {

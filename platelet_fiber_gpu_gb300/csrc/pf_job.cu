@@ -234,6 +234,7 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
   k.kcoll_f = (float)k.kcoll;
   k.kmom_f = (float)k.kmom;
   for (int a = 0; a < 3; ++a) k.body_f[a] = (float)k.body[a];
+  k.nobody = k.body_f[0] == 0.f && k.body_f[1] == 0.f && k.body_f[2] == 0.f;
   k.uw_f = (float)k.uw;
   return k;
 }

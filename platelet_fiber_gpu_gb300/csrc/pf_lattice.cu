@@ -328,6 +328,46 @@ __device__ __forceinline__ void collide(R g[Q], R drho, R ux, R uy, R uz, R Fx, 
   }
 }
 
+// FP32 collision of a node without any force: collide's regrouped
+// polynomial without the force terms (exact zeros there).
+__device__ __forceinline__ void collide_noforce(float g[Q], float drho, float ux, float uy, float uz, float om) {
+  const float rho = 1.0f + drho;
+  const float usq = ux * ux + uy * uy + uz * uz;
+  const float omr = om * rho;
+  const float A = om * drho - 1.5f * omr * usq;
+  const float B = 3.0f * omr, C = 4.5f * omr;
+  const float omc = 1.0f - om;
+  g[0] = omc * g[0] + (float)wgt(0) * A;
+#pragma unroll
+  for (int d = 1; d < Q; ++d) {
+    if (opp(d) < d) continue;
+    const int o = opp(d);
+    const float cu = cdot<float>(d, ux, uy, uz);
+    const float even = A + cu * (C * cu);
+    const float odd = B * cu;
+    const float w = (float)wgt(d);
+    g[d] = omc * g[d] + w * (even + odd);
+    g[o] = omc * g[o] + w * (even - odd);
+  }
+}
+
+// The collision of one node with the step's force F = body + Fc.  FP32 nodes
+// without any (no marker force, no body force) take collide_noforce; every
+// FP32 kernel makes the same choice, so that they stay equal bit for bit.
+template <typename R>
+__device__ __forceinline__ void collide_node(const LatticeConst& k, R g[Q], R drho, R ux, R uy, R uz,
+                                             const R4<R>* Fc, size_t n, unsigned fc, R kc, R om) {
+  if constexpr (sizeof(R) == 4) {
+    if (!fc && k.nobody) {
+      collide_noforce(g, drho, ux, uy, uz, om);
+      return;
+    }
+  }
+  R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
+  if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
+  collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
+}
+
 // One node of the step on the FP16 store's own values q = g / (w_c sigma)
 // (c: the weight class), in place.  Interior nodes: the moments from
 // per-class sums (g = w_c sigma q) and the FP32 collision's polynomial with
@@ -357,6 +397,36 @@ __device__ __forceinline__ void node_q(const LatticeConst& k, float q[Q], int z,
     collide<float>(g, drho, ux, uy, uz, Fx, Fy, Fz, om, sf);
 #pragma unroll
     for (int d = 0; d < Q; ++d) q[d] = g[d] * k.hinv[wcls(d)];
+    return;
+  }
+  if (!fc && !fp && !first && k.nobody) {
+    // interior node without any force (the quiet pass: most of the
+    // lattice): the moments and the collision polynomial without their
+    // force terms, which are exact zeros in the general form below
+    const float s1 = k.hs[1], s2 = k.hs[2];
+    const float ax = q[1] + q[2] + q[3] + q[4] + q[5] + q[6];
+    const float dg = q[7] + q[8] + q[9] + q[10] + q[11] + q[12] + q[13] + q[14] + q[15] + q[16] + q[17] + q[18];
+    const float drh = k.hs[0] * q[0] + s1 * ax + s2 * dg;
+    const float jx = s1 * (q[1] - q[2]) + s2 * ((q[7] + q[8] + q[9] + q[10]) - (q[11] + q[12] + q[13] + q[14]));
+    const float jy = s1 * (q[3] - q[4]) + s2 * ((q[7] + q[11] + q[15] + q[16]) - (q[8] + q[12] + q[17] + q[18]));
+    const float jz = s1 * (q[5] - q[6]) + s2 * ((q[9] + q[13] + q[15] + q[17]) - (q[10] + q[14] + q[16] + q[18]));
+    const float irho = __frcp_rn(1.0f + drh);
+    const float vx = jx * irho, vy = jy * irho, vz = jz * irho;
+    const float omr = om * (1.0f + drh), is = k.isig;
+    const float A = (om * drh - 1.5f * omr * (vx * vx + vy * vy + vz * vz)) * is;
+    const float B = 3.0f * omr * is, C = 4.5f * omr * is;
+    const float omc = 1.0f - om;
+    q[0] = omc * q[0] + A;
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+      if (opp(d) < d) continue;
+      const int o = opp(d);
+      const float cu = cdot<float>(d, vx, vy, vz);
+      const float even = A + cu * (C * cu);
+      const float odd = B * cu;
+      q[d] = omc * q[d] + (even + odd);
+      q[o] = omc * q[o] + (even - odd);
+    }
     return;
   }
   if (first) {
@@ -436,11 +506,7 @@ __device__ __forceinline__ void lbm_node(const LatticeConst& k, const S* __restr
     if (fp) ld_force<R>(Fp, n, px, py, pz);
     node_state<R>(k, g, z, n, true, px, py, pz, drho, ux, uy, uz);
   }
-  R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
-  if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
-  const R kc = kv<R>(k.kcoll, k.kcoll_f);
-  const R om = kv<R>(k.omega, k.omega_f);
-  collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, (R)1 - (R)0.5 * om);
+  collide_node<R>(k, g, drho, ux, uy, uz, Fc, n, fc, kv<R>(k.kcoll, k.kcoll_f), kv<R>(k.omega, k.omega_f));
   // one pointer stepped by N: a 64-bit add per store instead of forming
   // each direction's index (16 % fewer instructions in the FP32 pass)
   S* p = gout + n;
@@ -709,9 +775,7 @@ __device__ __forceinline__ void vec_collide_store(const LatticeConst& k, S* __re
         if (fp) ld_force<float>(Fp, n, px, py, pz);
         node_state<float>(k, g, (int)z, (size_t)n, true, px, py, pz, drho, ux, uy, uz);
       }
-      float Fx = k.body_f[0], Fy = k.body_f[1], Fz = k.body_f[2];
-      if (fc) ld_force<float>(Fc, n, Fx, Fy, Fz);
-      collide<float>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, 1.0f - 0.5f * om);
+      collide_node<float>(k, g, drho, ux, uy, uz, Fc, n, fc, kc, om);
 #pragma unroll
       for (int d = 0; d < Q; ++d) IO::put(w[d], i, g[d]);
       if (fp) zero_force<float>(Fp, n);
@@ -1043,7 +1107,6 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
 
   const R kc = kv<R>(k.kcoll, k.kcoll_f);
   const R om = kv<R>(k.omega, k.omega_f);
-  const R sf = (R)1 - (R)0.5 * om;
   // One node; p points at the node's column in direction 0 of its staged row.
   // Called by whole warps (a warp's 32 nodes are one force brick, whose
   // previous-force flag the warp clears).
@@ -1083,9 +1146,7 @@ __global__ void __launch_bounds__(kRowThreads, sizeof(R) == 8 ? 1 : 3) lbm_rows_
       if (fp) ld_force<R>(Fp, n, px, py, pz);
       node_state<R>(k, g, z, n, true, px, py, pz, drho, ux, uy, uz);
     }
-    R Fx = kv<R>(k.body[0], k.body_f[0]), Fy = kv<R>(k.body[1], k.body_f[1]), Fz = kv<R>(k.body[2], k.body_f[2]);
-    if (fc) ld_force<R>(Fc, n, Fx, Fy, Fz);
-    collide<R>(g, drho, ux, uy, uz, Fx * kc, Fy * kc, Fz * kc, om, sf);
+    collide_node<R>(k, g, drho, ux, uy, uz, Fc, n, fc, kc, om);
     S* o = gout + n;
 #pragma unroll
     for (int d = 0; d < Q; ++d)
