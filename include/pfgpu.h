@@ -216,7 +216,9 @@ size_t pfgpu_job_device_bytes(const pfgpu_job *job);
 size_t pfgpu_job_state_bytes(const pfgpu_job *job);
 int pfgpu_job_save(pfgpu_job *job, void *buf, size_t bytes);
 int pfgpu_job_restore(pfgpu_job *job, const void *buf, size_t bytes);
-/* Kernel launches one coupled step issues (graph nodes). */
+/* Kernel launches one coupled step issues: after a graph step, the kernel
+ * nodes of the captured step graph per step; after a direct step, the
+ * launches that step made. */
 int pfgpu_job_launches_per_step(const pfgpu_job *job);
 /* Which collide-stream kernels the job runs: "lbm_rows_k" (rows staged
  * through shared memory by bulk asynchronous copies; needs nx *

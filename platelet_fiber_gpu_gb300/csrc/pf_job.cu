@@ -555,7 +555,7 @@ static int enqueue_step(pfgpu_job* j) {
   CK(flag_markers(j->L, Pl, Fb, j->ctl, j->s0, pipe, quiet));
   CK(cudaEventRecord(j->ev_flag, j->s0));
   CK(cudaStreamWaitEvent(j->sL, quiet ? j->ev_fork : j->ev_flag, 0));
-  launches += 2;
+  launches++;
   if (pipe) {
     CK(cudaStreamWaitEvent(j->sF, j->ev_flag, 0));
     CK(lattice_near(j->L, j->ctl, 0, j->sF));
@@ -622,6 +622,7 @@ static int enqueue_step(pfgpu_job* j) {
     launches++;
   }
   CK(lattice_step_part(j->L, j->ctl, 2, bins, ncells, j->s0));
+  launches++;
   if (ahead) {
     // the next step's quiet pass: it needs this step's output only
     CK(cudaEventRecord(j->ev_list, j->s0));
@@ -631,12 +632,13 @@ static int enqueue_step(pfgpu_job* j) {
     launches++;
   }
   CK(lattice_moments_active(j->L, j->ctl, j->s0));
+  launches++;
   if (Fb && Fb->coupling == PF_FIBCPL_PENALTY) {
     CK(fibrin_penalty_step(j->L, *Fb, j->precision, Pl ? (double)Pl->k.f0 : 1.0, j->ctl, j->s0));
     launches += 4;
   }
   CK(interp_advance(j->L, Pl, marker_fibrin(Fb), j->ctl, j->detach_rate, j->seed, j->done_blocks, j->s0));
-  launches += 3;
+  launches++;
   if (pipe) CK(cudaStreamWaitEvent(j->s0, j->ev_far, 0));
   if (ahead) j->q_pending = true;
   j->launches_per_step = launches;
@@ -969,6 +971,24 @@ static int capture_steps(pfgpu_job* j, int k, cudaGraphExec_t* out) {
     return rc;
   }
   CK(e);
+  // the kernels of one step, counted from the captured graph itself
+  size_t nn = 0;
+  e = cudaGraphGetNodes(g, nullptr, &nn);
+  if (e == cudaSuccess && nn > 0) {
+    std::vector<cudaGraphNode_t> nodes(nn);
+    e = cudaGraphGetNodes(g, nodes.data(), &nn);
+    int kernels = 0;
+    for (size_t i = 0; e == cudaSuccess && i < nn; ++i) {
+      cudaGraphNodeType t;
+      e = cudaGraphNodeGetType(nodes[i], &t);
+      if (e == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+    }
+    if (e == cudaSuccess) j->launches_per_step = kernels / k;
+  }
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    CK(e);
+  }
   e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   CK(e);

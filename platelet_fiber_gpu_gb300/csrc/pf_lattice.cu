@@ -824,8 +824,19 @@ __device__ __forceinline__ void lbm_vec_body(const LatticeConst& k, S* gA, S* gB
   if (fp && (x0 % kBrickX) == 0) flp[brick] = 0;
 }
 
+// CTAs per SM the vector kernel is compiled for: FP32 with two nodes per
+// thread at 72 registers (7 CTAs, no spills), FP16 with four at 96 (5 CTAs,
+// 80 bytes spilled).  The extra resident warps hide more of the pass's
+// memory latency: 0.2002 -> 0.1968 ms (FP32) and 0.1690 -> 0.1667 ms (FP16)
+// per coupled step of the 256x128x128 channel against the compiler's own
+// 78 and 124 registers; 64 registers (8 CTAs) spill and were slower.
 template <class S, int V>
-__global__ void __launch_bounds__(kLbmBlock) lbm_vec_k(LatticeConst k, S* gA, S* gB, float4* FA, float4* FB,
+constexpr int vec_min_ctas() {
+  return (sizeof(S) == 4 && V == 2) ? 7 : ((sizeof(S) == 2 && V == 4) ? 5 : 1);
+}
+
+template <class S, int V>
+__global__ void __launch_bounds__(kLbmBlock, vec_min_ctas<S, V>()) lbm_vec_k(LatticeConst k, S* gA, S* gB, float4* FA, float4* FB,
                                                        float4* ubuf, unsigned* flA, unsigned* flB, int* bin_count,
                                                        int ncells, int mode, Control* ctl) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
