@@ -85,6 +85,7 @@ struct Lattice {
   // reduced precision: spread/interpolate platelet elements through shared
   // per-platelet node boxes (1) or per marker with global atomics (0)
   int ibm_box = 0;
+  int spread_lanes = 4;  // reduced-precision spreading: threads per marker (1 or 4)
   size_t bytes = 0;
   // row-staged step: rows per tile, tiles in flight per CTA, persistent grid
   // (rows_stages == 0: the direct-gather kernel is used)

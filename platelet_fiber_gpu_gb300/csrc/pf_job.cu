@@ -828,6 +828,10 @@ int pfgpu_job_create(const pf_scene* s, int precision, double fp16_scale, pfgpu_
     // which measured faster on the 50-platelet channel)
     const char* ibm = getenv("PFGPU_IBM");
     L.ibm_box = ibm && strcmp(ibm, "boxes") == 0;
+    // PFGPU_SPREAD_LANES=1: one thread per marker in the reduced-precision
+    // spreading (default four lanes per marker, measured faster)
+    const char* sl = getenv("PFGPU_SPREAD_LANES");
+    L.spread_lanes = sl && atoi(sl) == 1 ? 1 : 4;
   }
   const size_t N = (size_t)L.k.N;
   const size_t sb = store_bytes(precision), rb = real_bytes(precision);
