@@ -234,63 +234,74 @@ __global__ void __launch_bounds__(128) spread_k(LatticeConst lk, R4<R>* FA, R4<R
 }
 
 // FP32 spreading of one force part as soon as it exists: n markers at
-// (X, Y, Z) with force Fa (float, may be null) + Fd / div (double, may be
+// (X, Y, Z) with force Fa (float, may be null) + Fd * rdiv (double, may be
 // null), components n apart; markers whose part is zero add nothing.
 __device__ __forceinline__ void spread_part_k_body(const LatticeConst& lk, float4* FA, float4* FB, int n,
                                                      const double* X, const double* Y, const double* Z,
-                                                     const float* Fa, const double* Fd, double div, Control* ctl, int bid, int nblk) {
+                                                     const float* Fa, const double* Fd, double rdiv, Control* ctl, int bid, int nblk) {
   if (ctl->done) return;
   const int i = bid * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double fx = 0, fy = 0, fz = 0;
   if (Fa) { fx = (double)Fa[i]; fy = (double)Fa[n + i]; fz = (double)Fa[2 * n + i]; }
-  // div: F0 for fibrin forces (a product with its FP64 reciprocal; FP64
-  // division is slow on this GPU)
-  if (Fd) {
-    const double r = 1.0 / div;
-    fx += Fd[i] * r; fy += Fd[n + i] * r; fz += Fd[2 * n + i] * r;
-  }
+  // rdiv: 1/F0 for fibrin forces, formed once by the caller (FP64 division
+  // is slow on this GPU)
+  if (Fd) { fx += Fd[i] * rdiv; fy += Fd[n + i] * rdiv; fz += Fd[2 * n + i] * rdiv; }
   if (fx == 0 && fy == 0 && fz == 0) return;
   spread_one<float>(lk, (ctl->step & 1) ? FB : FA, X[i], Y[i], Z[i], (float)fx, (float)fy, (float)fz);
 }
 __global__ void __launch_bounds__(128) spread_part_k(LatticeConst lk, float4* FA, float4* FB, int n,
                                                      const double* X, const double* Y, const double* Z,
-                                                     const float* Fa, const double* Fd, double div, Control* ctl) {
-  spread_part_k_body(lk, FA, FB, n, X, Y, Z, Fa, Fd, div, ctl, blockIdx.x, gridDim.x);
+                                                     const float* Fa, const double* Fd, double rdiv, Control* ctl) {
+  spread_part_k_body(lk, FA, FB, n, X, Y, Z, Fa, Fd, rdiv, ctl, blockIdx.x, gridDim.x);
 }
 
 // The same spreading with four lanes per marker: lane a of a marker's group
 // takes the stencil's x slot a, so the 32 atomics of one warp instruction
 // fall on 8 markers x 4 consecutive nodes (16 sectors of 32 bytes) instead
-// of 32 scattered nodes.  Each node receives the same product as from
-// spread_one; only the order of the atomic additions changes.
+// of 32 scattered nodes.  The FP64 work is done once per marker (FP64 issues
+// at a small fraction of the FP32 rate on this GPU): lane l < 3 forms force
+// component l and the stencil base of axis l and the group shares them by
+// shuffles.  Each node receives the same product as from spread_one; only
+// the order of the atomic additions changes.  rdiv: the reciprocal of the
+// divisor of Fd (1/F0 for fibrin forces), formed once by the caller.
 constexpr int kSpreadLanes = 4;
 __device__ __forceinline__ void spread4_body(const LatticeConst& lk, float4* FA, float4* FB, int n,
                                              const double* X, const double* Y, const double* Z, const float* Fa,
-                                             const double* Fd, double div, Control* ctl, int bid) {
+                                             const double* Fd, double rdiv, Control* ctl, int bid) {
   if (ctl->done) return;
   const long long t = (long long)bid * blockDim.x + threadIdx.x;
   const int i = (int)(t / kSpreadLanes), a = (int)(t % kSpreadLanes);
-  if (i >= n) return;
-  double fx = 0, fy = 0, fz = 0;
-  if (Fa) { fx = (double)Fa[i]; fy = (double)Fa[n + i]; fz = (double)Fa[2 * n + i]; }
-  if (Fd) {
-    const double r = 1.0 / div;
-    fx += Fd[i] * r; fy += Fd[n + i] * r; fz += Fd[2 * n + i] * r;
-  }
-  if (fx == 0 && fy == 0 && fz == 0) return;
-  const float Fx = (float)fx, Fy = (float)fy, Fz = (float)fz;
+  const bool in = i < n;
+  // groups are whole: every lane of an active group is in `act`
+  const unsigned act = __ballot_sync(0xffffffffu, in);
+  if (!in) return;
+  const int l = a < 3 ? a : 2;
+  double f = 0;
+  if (Fa) f = (double)Fa[(size_t)l * n + i];
+  if (Fd) f += Fd[(size_t)l * n + i] * rdiv;
+  int base;
+  float fr;
+  axis_base(l == 0 ? X[i] : (l == 1 ? Y[i] : Z[i]), lk.inv_dx, base, fr);
+  const unsigned nz = __ballot_sync(act, f != 0);
+  const int g0 = (int)(threadIdx.x & 31u) & ~(kSpreadLanes - 1);
+  const float fl = (float)f;
+  const float Fx = __shfl_sync(act, fl, g0), Fy = __shfl_sync(act, fl, g0 + 1), Fz = __shfl_sync(act, fl, g0 + 2);
+  const int bx = __shfl_sync(act, base, g0), by = __shfl_sync(act, base, g0 + 1), bz = __shfl_sync(act, base, g0 + 2);
+  const float frx = __shfl_sync(act, fr, g0), fry = __shfl_sync(act, fr, g0 + 1), frz = __shfl_sync(act, fr, g0 + 2);
+  if (((nz >> g0) & 7u) == 0u) return;  // no force in this part: nothing to add
   float4* Fc = (ctl->step & 1) ? FB : FA;
-  const double inv = lk.inv_dx;
-  int bx, nxa;
-  float frx, wxa;
-  axis_base(X[i], inv, bx, frx);
+  int nxa;
+  float wxa;
   axis_slot(bx, frx, lk.nx, lk.ibm_wrap[0], a, nxa, wxa);
   if (wxa == 0.f) return;
   int nya[4], nza[4];
   float wy[4], wz[4];
-  axis4(Y[i], inv, lk.ny, lk.ibm_wrap[1], nya, wy);
-  axis4(Z[i], inv, lk.nz, 0, nza, wz);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    axis_slot(by, fry, lk.ny, lk.ibm_wrap[1], q, nya[q], wy[q]);
+    axis_slot(bz, frz, lk.nz, 0, q, nza[q], wz[q]);
+  }
 #pragma unroll
   for (int c = 0; c < 4; ++c)
 #pragma unroll
@@ -302,8 +313,8 @@ __device__ __forceinline__ void spread4_body(const LatticeConst& lk, float4* FA,
 }
 __global__ void __launch_bounds__(128) spread4_k(LatticeConst lk, float4* FA, float4* FB, int n, const double* X,
                                                  const double* Y, const double* Z, const float* Fa,
-                                                 const double* Fd, double div, Control* ctl) {
-  spread4_body(lk, FA, FB, n, X, Y, Z, Fa, Fd, div, ctl, blockIdx.x);
+                                                 const double* Fd, double rdiv, Control* ctl) {
+  spread4_body(lk, FA, FB, n, X, Y, Z, Fa, Fd, rdiv, ctl, blockIdx.x);
 }
 
 // Force bricks of this step: every brick holding a lattice node that the
@@ -2752,15 +2763,16 @@ template <int PART>
 __global__ void __launch_bounds__(kMarkerThreadsMax) spread_batch_k(const BatchDesc* descs, const int* start, int nj) {
   PF_BATCH_PROLOGUE
   __shared__ LatticeConst s_lk;
+  __shared__ double s_rdiv;
   cta_copy(s_lk, d.L.k);
+  if (threadIdx.x == 0) s_rdiv = 1.0 / (d.has_pl ? (double)d.Pl.k.f0 : 1.0);
   __syncthreads();
   float4* FA = (float4*)d.L.F[0];
   float4* FB = (float4*)d.L.F[1];
   (void)nblk;
   if constexpr (PART == 2) {
     const Fibrin& Fb = d.Fb;
-    spread4_body(s_lk, FA, FB, Fb.M, Fb.X, Fb.Y, Fb.Z, nullptr, Fb.F, d.has_pl ? (double)d.Pl.k.f0 : 1.0, d.ctl,
-                 bid);
+    spread4_body(s_lk, FA, FB, Fb.M, Fb.X, Fb.Y, Fb.Z, nullptr, Fb.F, s_rdiv, d.ctl, bid);
   } else {
     const Platelets& Pl = d.Pl;
     const int PE = Pl.k.P * Pl.k.E;
@@ -3144,13 +3156,14 @@ bool spread_split(const Lattice& L) { return L.precision != PF_PREC_FP64 && !L.i
 // double divided by div), one thread or four lanes per marker.
 static cudaError_t launch_spread(const Lattice& L, int n, const double* X, const double* Y, const double* Z,
                                  const float* Fa, const double* Fd, double div, Control* ctl, cudaStream_t st) {
+  const double rdiv = 1.0 / div;  // the device's FP64 quotient, rounded the same (IEEE)
   if (L.spread_lanes == kSpreadLanes) {
     const long long threads = (long long)n * kSpreadLanes;
     spread4_k<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(L.k, (float4*)L.F[0], (float4*)L.F[1], n, X, Y, Z,
-                                                                  Fa, Fd, div, ctl);
+                                                                  Fa, Fd, rdiv, ctl);
   } else {
     spread_part_k<<<(n + marker_block() - 1) / marker_block(), marker_block(), 0, st>>>(
-        L.k, (float4*)L.F[0], (float4*)L.F[1], n, X, Y, Z, Fa, Fd, div, ctl);
+        L.k, (float4*)L.F[0], (float4*)L.F[1], n, X, Y, Z, Fa, Fd, rdiv, ctl);
   }
   return cudaGetLastError();
 }
