@@ -48,6 +48,7 @@ struct LatticeConst {
   int ibm_wrap[3];
   float dxf, dtf;
   double inv_dx;      // 1 / (double)dxf, so kernels divide by no double per thread
+  double Lx, Ly;      // (double)nx * dxf, (double)ny * dxf: periodic lengths of the position update
   double C;           // float-rounded dx/dt/UMAX
   double omega;       // 1/tau
   double kcoll;       // F0/rho0/UMAX*UNIT (double chain) * dt / C

@@ -224,6 +224,8 @@ static LatticeConst lattice_const(const pf_scene* s, double fp16_scale, int prec
   }
   k.isig = (float)(1.0 / k.fp16_scale);
   k.inv_dx = 1.0 / (double)k.dxf;
+  k.Lx = (double)k.nx * (double)k.dxf;
+  k.Ly = (double)k.ny * (double)k.dxf;
   // bounded device waits give up after 1 s; PFGPU_WAIT_LIMIT_NS shortens
   // the limit (0: give up at the first unfinished wait) so that tests can
   // run the give-up path

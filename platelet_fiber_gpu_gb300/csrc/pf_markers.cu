@@ -336,8 +336,10 @@ __device__ __forceinline__ void mark_node(const LatticeConst& lk, unsigned* mark
                                           bool fp64) {
   const double dxd = (double)lk.dxf, inv = lk.inv_dx;
   auto node = [&](double v, int n, int wrap) {
-    const double f = floor(fp64 ? v / dxd : v * inv);
-    const int i = f < -1e9 ? -1000000000 : (f > 1e9 ? 1000000000 : (int)f);
+    // floor and conversion in one saturating instruction (NaN: 0), then
+    // within +-1e9 so that the index arithmetic below cannot overflow
+    int i = __double2int_rd(fp64 ? v / dxd : v * inv);
+    i = i < -1000000000 ? -1000000000 : (i > 1000000000 ? 1000000000 : i);
     if (wrap) return wrapi(i, n);
     return i < 0 ? 0 : (i >= n ? n - 1 : i);
   };
@@ -531,7 +533,7 @@ __device__ __forceinline__ void advance_marker(const LatticeConst& lk, const Pla
                                                bool fp64) {
   const double vx = ax * lk.C, vy = ay * lk.C, vz = az * lk.C;
   const float dtT = lk.dtT;
-  const double Lx = (double)lk.nx * (double)lk.dxf, Ly = (double)lk.ny * (double)lk.dxf;
+  const double Lx = lk.Lx, Ly = lk.Ly;
   if (idx < PE) {
     V[idx] = vx; V[PE + idx] = vy; V[2 * PE + idx] = vz;
     x += vx * dtT;
@@ -3023,7 +3025,7 @@ __global__ void __launch_bounds__(128) fibrin_kick_k(LatticeConst lk, int M, int
   if (phase == 0) {
     if (fx) return;
     const float dtT = lk.dtT;
-    const double Lx = (double)lk.nx * (double)lk.dxf, Ly = (double)lk.ny * (double)lk.dxf;
+    const double Lx = lk.Lx, Ly = lk.Ly;
     x += v[0] * dtT;
     if (lk.ibm_wrap[0]) { if (x > Lx) x -= Lx; else if (x < 0) x += Lx; }
     y += v[1] * dtT;
