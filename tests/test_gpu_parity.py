@@ -332,6 +332,34 @@ def test_row_staged_and_direct_lbm_kernels_agree(gpu, scene, prec, tol, monkeypa
 
 
 @pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-4)], ids=["fp32", "fp16"])
+def test_one_thread_spreading_matches_four_lanes(gpu, prec, tol, monkeypatch):
+    """The reduced-precision spreading with one thread per marker
+    (PFGPU_SPREAD_LANES=1) and with four lanes per marker (the default) add
+    the same product to the same nodes; only the order of the float atomics
+    differs, so the two agree to that rounding (platelets, bonds and fibrin,
+    all three force parts)."""
+    from platelet_fiber_gpu_gb300 import workloads as W
+    sc = W.mixed_small()
+    monkeypatch.setenv("PFGPU_SPREAD_LANES", "1")
+    a = gpu.Job(sc, prec)
+    monkeypatch.delenv("PFGPU_SPREAD_LANES")
+    b = gpu.Job(sc, prec)
+    a.step(5)
+    b.step(5)
+    La, Lb = a.lattice(), b.lattice()
+    assert rel_l2(La["u"], Lb["u"]) < tol
+    assert rel_l2(La["F"], Lb["F"]) < 10 * tol
+    Ea, Eb = a.elements(), b.elements()
+    for k in ("X", "Y", "Z"):
+        assert np.abs(Ea[k] - Eb[k]).max() < 1e-3 * tol
+    Fa, Fb = a.fibrin(), b.fibrin()
+    assert np.abs(Fa["X"] - Fb["X"]).max() < 1e-3 * tol
+    np.testing.assert_array_equal(a.bonds()["rec_state"], b.bonds()["rec_state"])
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-4)], ids=["fp32", "fp16"])
 def test_platelet_box_ibm_matches_per_marker(gpu, prec, tol, monkeypatch):
     """Reduced precision spreads and interpolates platelet elements through a
     shared-memory node box per platelet; the per-marker kernels use the same
