@@ -1323,11 +1323,15 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
     }
     __syncthreads();
   }
+  __shared__ double s_sglob, s_vglob;
   if (threadIdx.x == 0) {
     s_Sall = s_a[0];
     s_V = s_b[0];
     SV[2 * p] = s_a[0];
     SV[2 * p + 1] = s_b[0];
+    // the relative area and volume errors, formed once per platelet
+    s_sglob = (s_a[0] - S0_all[p]) / S0_all[p];
+    s_vglob = (s_b[0] - V0[p]) / V0[p];
   }
   __syncthreads();
   // nodal normals: mean of the element normals of the node's triangles
@@ -1414,7 +1418,6 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
   }
   // area/volume penalty (sem_kernel.cu:1640-1749) and bending
   // (:1499-1638) at each vertex
-  const double Sall = s_Sall, Vol = s_V;
   for (int v = threadIdx.x; v < Em; v += blockDim.x) {
     R fx = Fmem[base + v], fy = Fmem[PE + base + v], fz = Fmem[2 * PE + base + v];
     const int cnt = node_ntri[v];
@@ -1432,8 +1435,7 @@ __global__ void __launch_bounds__(512) membrane_k(PlateletConst k, const double*
     }
     if (k.mask & PF_MEM_AREAVOL) {
       const R Ks = (R)k.ks, Kv = (R)k.kv;
-      const R sglob = (R)((Sall - S0_all[p]) / S0_all[p]);
-      const R vglob = (R)((Vol - V0[p]) / V0[p]);
+      const R sglob = (R)s_sglob, vglob = (R)s_vglob;
       for (int j = 0; j < cnt; ++j) {
         const int t = node_tri[10 * v + j];
         const int i = vert_local[10 * v + j];
@@ -1641,6 +1643,7 @@ __device__ __forceinline__ void membrane32_k_body(const PlateletConst& k, const 
   __shared__ int s_wall_idx, s_total;
   __shared__ float s_wall_f;
   __shared__ double s_Sall, s_V;
+  __shared__ float s_sglob, s_vglob;
 
   // phase 0: positions relative to element 0, the lowest element, node
   // triangle counts and triangles staged, per-thread sums of the vertex
@@ -1783,6 +1786,10 @@ __device__ __forceinline__ void membrane32_k_body(const PlateletConst& k, const 
     s_V = b;
     SV[2 * p] = a;
     SV[2 * p + 1] = b;
+    // the relative area and volume errors, formed once: FP64 divisions in
+    // every thread would hold the SM's narrow FP64 pipe for microseconds
+    s_sglob = (float)((a - S0_all[p]) / S0_all[p]);
+    s_vglob = (float)((b - V0[p]) / V0[p]);
   }
   for (int q = tid; q < NN; q += NT) {
     const int cnt = s_cnt[q];
@@ -1803,8 +1810,7 @@ __device__ __forceinline__ void membrane32_k_body(const PlateletConst& k, const 
   // phase 3: items -- curvature trace, area/volume gradient
   // (sem_kernel.cu:1640-1749), bending geometry (:1499-1638)
   const int total = s_total;
-  const float sglob = (float)((s_Sall - S0_all[p]) / S0_all[p]);
-  const float vglob = (float)((s_V - V0[p]) / V0[p]);
+  const float sglob = s_sglob, vglob = s_vglob;
   for (int it = tid; it < 3 * total; it += NT) {
     const int kind = it >= total ? (it >= 2 * total ? 2 : 1) : 0;
     const int i = it - kind * total;
